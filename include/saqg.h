@@ -1,0 +1,127 @@
+/*
+ * saqg.h -- C ABI of the GB300-native SAQ search / encode path.
+ *
+ * Every entry point replaces a call on the reference's header-only C++ API
+ * (howarlii/SAQ, saqlib/); the citation beside each one names it.  The ABI uses
+ * plain pointers and sizes only: no C++ or torch types cross it, errors are
+ * returned as status codes (never thrown), and saqg_last_error() gives the
+ * message of the last failure on the calling thread.
+ *
+ * Memory: pointers named *_host are host memory; functions taking a `mem`
+ * argument accept either host (SAQG_MEM_HOST: the library stages the copies,
+ * host<->device transfers included) or device pointers (SAQG_MEM_DEVICE: the
+ * caller's buffers are used in place, nothing is copied).  `stream` is a
+ * cudaStream_t passed as void* (NULL = the legacy default stream).
+ *
+ * Threading: an index handle is read-only after load/construct; concurrent
+ * searches on one handle are serialised by a per-handle lock around its
+ * device scratch arena.
+ */
+#ifndef SAQG_H
+#define SAQG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SAQG_OK 0
+#define SAQG_ERR_INVALID 1  /* bad argument (sizes, nprobe > K, unsupported dim ...) */
+#define SAQG_ERR_IO 2       /* unreadable / truncated / malformed index file */
+#define SAQG_ERR_CUDA 3     /* a CUDA runtime call failed */
+#define SAQG_ERR_NOMEM 4    /* device or host allocation failed */
+#define SAQG_ERR_INTERNAL 5 /* a device-side consistency check failed */
+
+#define SAQG_MEM_HOST 0
+#define SAQG_MEM_DEVICE 1
+
+#define SAQG_DIST_L2 1 /* DistType::L2Sqr (defines.hpp); the only type the search supports */
+
+/* QuantizeConfig + QuantSingleConfig (quantization/config.h:12-74), field for field. */
+typedef struct saqg_quantize_config {
+    float avg_bits;          /* QuantizeConfig::avg_bits */
+    int seg_eqseg;           /* QuantizeConfig::seg_eqseg */
+    int enable_segmentation; /* QuantizeConfig::enable_segmentation (default 1) */
+    int use_compact_layout;  /* QuantizeConfig::use_compact_layout (default 0) */
+    int random_rotation;     /* QuantSingleConfig::random_rotation (default 1) */
+    int caq_adj_rd_lmt;      /* QuantSingleConfig::caq_adj_rd_lmt (default 6) */
+    float caq_adj_eps;       /* QuantSingleConfig::caq_adj_eps (default 1e-8) */
+} saqg_quantize_config;
+
+/* SearcherConfig (quantization/config.h:76-79). */
+typedef struct saqg_searcher_config {
+    float searcher_vars_bound_m; /* default 4 */
+    int dist_type;               /* SAQG_DIST_L2 */
+} saqg_searcher_config;
+
+typedef struct saqg_index saqg_index;
+
+typedef struct saqg_index_info {
+    int64_t num_data, num_dim, num_clusters;
+    int32_t num_segments;
+    int32_t seg_dim[16];
+    int32_t seg_bits[16];
+    int64_t device_bytes; /* bytes of device memory held by the index */
+} saqg_index_info;
+
+/* ---- library ---------------------------------------------------------- */
+int saqg_version(void);
+const char *saqg_last_error(void);
+/* Number of kernels this library launched on the calling process so far. */
+int64_t saqg_kernel_launches(void);
+
+/* ---- index lifecycle -------------------------------------------------- */
+/* IVF::load (index/ivf.hpp:230-264): reads the reference's binary .index file
+ * and uploads it to the current CUDA device. */
+int saqg_index_load(const char *path, saqg_index **out);
+/* IVF::save (index/ivf.hpp:197-228): writes the reference's binary format. */
+int saqg_index_save(const saqg_index *index, const char *path);
+int saqg_index_free(saqg_index *index);
+int saqg_index_get_info(const saqg_index *index, saqg_index_info *out);
+
+/* IVF::construct (index/ivf.hpp:130-184) with IVF::set_variance (ivf.hpp:104-107):
+ * builds the index on the GPU from `data` (n x dim, row-major), `centroids`
+ * (k x dim) and `cluster_ids` (n).  `variance` (dim, may be NULL -> computed
+ * from the data as SaqDataMaker::compute_variance does) and `rotations`
+ * (concatenated row-major D_s x D_s matrices of the planned segments, may be
+ * NULL -> random orthogonal matrices drawn from `seed`; ignored when
+ * cfg->random_rotation is 0).  Inputs are host memory. */
+int saqg_index_construct(const float *data, int64_t n, int64_t dim, const float *centroids, int64_t k,
+                         const uint32_t *cluster_ids, const saqg_quantize_config *cfg, const float *variance,
+                         const float *rotations, uint64_t seed, saqg_index **out);
+
+/* ---- search ------------------------------------------------------------ */
+/* IVF::search<L2Sqr> (index/ivf.hpp:275-311) for `nq` queries (nq x dim), each
+ * as an independent call of the reference: probe the `nprobe` nearest
+ * centroids, scan them in order with the reference's pruning, keep `topk`.
+ * ids: nq x topk (unfilled slots are 0, as ResultPool leaves them);
+ * dists: nq x topk estimated distances (may be NULL; FLT_MAX when unfilled). */
+int saqg_search(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
+                const saqg_searcher_config *cfg, uint32_t *ids, float *dists, int mem, void *stream);
+
+/* IVF::estimate<L2Sqr> (index/ivf.hpp:313-362) for one query: every vector of
+ * the `nprobe` probed clusters, in probe order, with its accurate, fast and
+ * variance-bound estimates.  Host outputs of capacity `cap`; *count receives
+ * the number of vectors (may exceed cap: then only cap are written). */
+int saqg_estimate(const saqg_index *index, const float *query_host, int64_t nprobe, const saqg_searcher_config *cfg,
+                  uint32_t *ids, float *acc, float *fast, float *vars, int64_t cap, int64_t *count);
+
+/* ---- encode primitives ------------------------------------------------- */
+/* SaqDataMaker::analyze_plan (quantization/saq_data.hpp:119-227): segment bit
+ * plan for a padded dimension.  Writes up to `cap` (dim, bits) pairs. */
+int saqg_plan(const float *variance_host, int64_t dim_padded, float avg_bits, int enable_segmentation, int seg_eqseg,
+              int64_t *dims, int64_t *bits, int cap, int *num_segments);
+
+/* CAQEncoder::encode_and_fac (quantization/caq/caq_encoder.hpp:172-247) for n
+ * residual vectors of one segment: codes (n x dim int32) and factors
+ * (n x 4: o_l2norm, ip_cent_oa, fac_rescale, fac_error).  `centroid` is the
+ * un-rotated centroid used for ip_cent_oa (may be NULL). */
+int saqg_caq_encode(const float *resid, int64_t n, int64_t dim, int bits, const float *centroid, int rd_lmt,
+                    float eps, int32_t *codes, float *factors, int mem, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SAQG_H */

@@ -1,0 +1,89 @@
+"""ctypes binding of the C ABI in include/saqg.h.
+
+The library is loaded from the package's own _lib/ directory (built by
+saq_gb300/build.py).  There is no fallback: if the shared library or a CUDA
+device is missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from .build import LIB
+
+SAQG_MEM_HOST = 0
+SAQG_MEM_DEVICE = 1
+SAQG_DIST_L2 = 1
+
+I64 = C.c_int64
+
+
+class QuantizeConfig(C.Structure):
+    _fields_ = [("avg_bits", C.c_float), ("seg_eqseg", C.c_int), ("enable_segmentation", C.c_int),
+                ("use_compact_layout", C.c_int), ("random_rotation", C.c_int), ("caq_adj_rd_lmt", C.c_int),
+                ("caq_adj_eps", C.c_float)]
+
+
+class SearcherConfig(C.Structure):
+    _fields_ = [("searcher_vars_bound_m", C.c_float), ("dist_type", C.c_int)]
+
+
+class IndexInfo(C.Structure):
+    _fields_ = [("num_data", I64), ("num_dim", I64), ("num_clusters", I64), ("num_segments", C.c_int32),
+                ("seg_dim", C.c_int32 * 16), ("seg_bits", C.c_int32 * 16), ("device_bytes", I64)]
+
+
+class SaqgError(RuntimeError):
+    pass
+
+
+_lib = None
+
+EXPORTS = {
+    "saqg_version": (C.c_int, []),
+    "saqg_last_error": (C.c_char_p, []),
+    "saqg_kernel_launches": (I64, []),
+    "saqg_index_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    "saqg_index_save": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "saqg_index_free": (C.c_int, [C.c_void_p]),
+    "saqg_index_get_info": (C.c_int, [C.c_void_p, C.POINTER(IndexInfo)]),
+    "saqg_index_construct": (C.c_int, [C.c_void_p, I64, I64, C.c_void_p, I64, C.c_void_p, C.POINTER(QuantizeConfig),
+                                       C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "saqg_search": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig), C.c_void_p,
+                              C.c_void_p, C.c_int, C.c_void_p]),
+    "saqg_estimate": (C.c_int, [C.c_void_p, C.c_void_p, I64, C.POINTER(SearcherConfig), C.c_void_p, C.c_void_p,
+                                C.c_void_p, C.c_void_p, I64, C.POINTER(I64)]),
+    "saqg_plan": (C.c_int, [C.c_void_p, I64, C.c_float, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                            C.POINTER(C.c_int)]),
+    "saqg_caq_encode": (C.c_int, [C.c_void_p, I64, I64, C.c_int, C.c_void_p, C.c_int, C.c_float, C.c_void_p,
+                                  C.c_void_p, C.c_int, C.c_void_p]),
+}
+
+
+def lib_path() -> str:
+    return LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load libsaqg.so (optionally building it first); raises if unavailable."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB):
+        if not build_if_missing:
+            raise SaqgError(f"native library {LIB} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        from .build import build
+        build()
+    l = C.CDLL(LIB)
+    for name, (res, args) in EXPORTS.items():
+        fn = getattr(l, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = l
+    return l
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        msg = _lib.saqg_last_error().decode(errors="replace") if _lib else "unknown"
+        raise SaqgError(f"saqg error {rc}: {msg}")

@@ -1,0 +1,155 @@
+// extern "C" entry points (include/saqg.h).  Every call catches its errors and
+// turns them into a status code plus a thread-local message.
+#include <atomic>
+#include <cstring>
+#include <string>
+
+#include "saqg_internal.h"
+
+namespace saqg {
+
+namespace {
+thread_local std::string g_last_error;
+std::atomic<int64_t> g_launches{0};
+}  // namespace
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+void count_launch(int n) { g_launches += n; }
+
+template <class F>
+int guarded(F &&f) {
+    try {
+        f();
+        return SAQG_OK;
+    } catch (const Error &e) {
+        set_error(e.msg);
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        set_error("host allocation failed");
+        return SAQG_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return SAQG_ERR_INTERNAL;
+    }
+}
+
+}  // namespace saqg
+
+using namespace saqg;
+
+struct saqg_index {
+    Index *impl;
+};
+
+extern "C" {
+
+int saqg_version(void) { return 1; }
+
+const char *saqg_last_error(void) { return g_last_error.c_str(); }
+
+int64_t saqg_kernel_launches(void) { return g_launches.load(); }
+
+int saqg_index_load(const char *path, saqg_index **out) {
+    return guarded([&] {
+        SAQG_REQUIRE(path && out, "null argument");
+        *out = nullptr;
+        Index *I = load_index_file(path);
+        *out = new saqg_index{I};
+    });
+}
+
+int saqg_index_save(const saqg_index *index, const char *path) {
+    return guarded([&] {
+        SAQG_REQUIRE(index && path, "null argument");
+        save_index_file(*index->impl, path);
+    });
+}
+
+int saqg_index_free(saqg_index *index) {
+    return guarded([&] {
+        if (!index) return;
+        delete index->impl;
+        delete index;
+    });
+}
+
+int saqg_index_get_info(const saqg_index *index, saqg_index_info *out) {
+    return guarded([&] {
+        SAQG_REQUIRE(index && out, "null argument");
+        const Index &I = *index->impl;
+        std::memset(out, 0, sizeof(*out));
+        out->num_data = I.N;
+        out->num_dim = I.D;
+        out->num_clusters = I.K;
+        out->num_segments = (int32_t)I.segs.size();
+        for (size_t s = 0; s < I.segs.size() && s < 16; ++s) {
+            out->seg_dim[s] = (int32_t)I.segs[s].dim;
+            out->seg_bits[s] = (int32_t)I.segs[s].bits;
+        }
+        out->device_bytes = I.device_bytes;
+    });
+}
+
+int saqg_index_construct(const float *data, int64_t n, int64_t dim, const float *centroids, int64_t k,
+                         const uint32_t *cluster_ids, const saqg_quantize_config *cfg, const float *variance,
+                         const float *rotations, uint64_t seed, saqg_index **out) {
+    return guarded([&] {
+        SAQG_REQUIRE(data && centroids && cluster_ids && cfg && out, "null argument");
+        SAQG_REQUIRE(n > 0 && dim > 0 && k > 0, "empty input");
+        *out = nullptr;
+        Index *I = construct_index(data, n, dim, centroids, k, cluster_ids, *cfg, variance, rotations, seed);
+        *out = new saqg_index{I};
+    });
+}
+
+int saqg_search(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
+                const saqg_searcher_config *cfg, uint32_t *ids, float *dists, int mem, void *stream) {
+    return guarded([&] {
+        SAQG_REQUIRE(index && queries && ids, "null argument");
+        SAQG_REQUIRE(mem == SAQG_MEM_HOST || mem == SAQG_MEM_DEVICE, "mem must be SAQG_MEM_HOST or SAQG_MEM_DEVICE");
+        const float m = cfg ? cfg->searcher_vars_bound_m : 4.0f;
+        SAQG_REQUIRE(!cfg || cfg->dist_type == SAQG_DIST_L2, "only L2 search is supported (the reference's IP search "
+                                                              "never inserts a result)");
+        run_search(*index->impl, queries, nq, topk, nprobe, m, ids, dists, mem, (cudaStream_t)stream);
+    });
+}
+
+int saqg_estimate(const saqg_index *index, const float *query_host, int64_t nprobe, const saqg_searcher_config *cfg,
+                  uint32_t *ids, float *acc, float *fast, float *vars, int64_t cap, int64_t *count) {
+    return guarded([&] {
+        SAQG_REQUIRE(index && query_host && count, "null argument");
+        SAQG_REQUIRE(cap == 0 || (ids && acc && fast && vars), "null output buffer");
+        SAQG_REQUIRE(!cfg || cfg->dist_type == SAQG_DIST_L2, "only L2 estimation is supported");
+        const float m = cfg ? cfg->searcher_vars_bound_m : 4.0f;
+        *count = run_estimate(*index->impl, query_host, nprobe, m, ids, acc, fast, vars, cap);
+    });
+}
+
+int saqg_plan(const float *variance_host, int64_t dim_padded, float avg_bits, int enable_segmentation, int seg_eqseg,
+              int64_t *dims, int64_t *bits, int cap, int *num_segments) {
+    return guarded([&] {
+        SAQG_REQUIRE(num_segments && (cap == 0 || (dims && bits)), "null argument");
+        SAQG_REQUIRE(dim_padded > 0 && dim_padded % 64 == 0, "dim_padded must be a positive multiple of 64");
+        SAQG_REQUIRE(avg_bits >= 0 && avg_bits <= kMaxBits, "avg_bits out of range");
+        SAQG_REQUIRE(!enable_segmentation || seg_eqseg > 0 || variance_host, "variance required for the DP planner");
+        auto p = make_plan(variance_host, dim_padded, avg_bits, enable_segmentation != 0, seg_eqseg);
+        *num_segments = (int)p.size();
+        for (int i = 0; i < (int)p.size() && i < cap; ++i) {
+            dims[i] = p[i].first;
+            bits[i] = p[i].second;
+        }
+    });
+}
+
+int saqg_caq_encode(const float *resid, int64_t n, int64_t dim, int bits, const float *centroid, int rd_lmt, float eps,
+                    int32_t *codes, float *factors, int mem, void *stream) {
+    return guarded([&] {
+        SAQG_REQUIRE(resid && codes && factors, "null argument");
+        SAQG_REQUIRE(n >= 0 && dim > 1 && dim % 64 == 0, "dim must be a multiple of 64");
+        SAQG_REQUIRE(bits >= 0 && bits <= kMaxBits, "bits must be in [0, 13]");
+        SAQG_REQUIRE(mem == SAQG_MEM_HOST || mem == SAQG_MEM_DEVICE, "bad mem flag");
+        run_caq_encode(resid, n, dim, bits, centroid, rd_lmt, eps, codes, factors, mem, (cudaStream_t)stream);
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,130 @@
+// Internal host-side definitions shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/saqg.h"
+
+namespace saqg {
+
+constexpr int kBlock = 32;     // vectors per FastScan block (defines.hpp KFastScanSize)
+constexpr int kMaxSeg = 16;    // segments per index
+constexpr int kMaxBits = 13;   // KMaxQuantizeBits (defines.hpp)
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string &msg);
+struct Error {
+    int code;
+    std::string msg;
+};
+#define SAQG_CUDA_TRY(expr)                                                                           \
+    do {                                                                                              \
+        cudaError_t e__ = (expr);                                                                     \
+        if (e__ != cudaSuccess)                                                                       \
+            throw ::saqg::Error{SAQG_ERR_CUDA, std::string(#expr " failed: ") + cudaGetErrorString(e__)}; \
+    } while (0)
+#define SAQG_REQUIRE(cond, msg)                                         \
+    do {                                                                \
+        if (!(cond)) throw ::saqg::Error{SAQG_ERR_INVALID, (msg)};      \
+    } while (0)
+
+void count_launch(int n = 1);
+
+// ---------------------------------------------------------------- device layout
+// One segment of the plan, laid out for the GPU.  All clusters are
+// concatenated: cluster c owns blocks [blk_off[c], blk_off[c] + nb_c) and
+// vectors [vec_off[c], vec_off[c] + n_c).
+//
+//   codes  : [block][dim/64][32 lanes] of 8 bytes -- the vector's own 1-bit
+//            code (MSB-first per 8 dims, as ClusterPacker::pack_short_codes
+//            writes it before FastScan packing), interleaved so that lane v of
+//            a warp reads vector v of the block with one coalesced 8-byte load.
+//   onorm  : [block][32] |o| (including the file's tail lanes)
+//   ipcent : [block][32] ip_cent_oa
+//   lcode  : [vector][lstride] ex-code in the reference's compacted layout,
+//            row padded to 16 bytes
+//   exfac  : [vector] (rescale, error)
+//   cent   : [cluster][dim] rotated centroid
+struct SegDev {
+    int dim = 0, bits = 0, pv = 0, lstride = 0, qoff = 0;
+    float *P = nullptr;
+    uint2 *codes = nullptr;
+    float *onorm = nullptr;
+    float *ipcent = nullptr;
+    uint8_t *lcode = nullptr;
+    float2 *exfac = nullptr;
+    float *cent = nullptr;
+};
+
+struct DevIndexView {  // passed to kernels by value
+    int S = 0;
+    int K = 0;
+    int D = 0;       // original dimension
+    int Dtot = 0;    // sum of segment dims (padded)
+    const float *centroids = nullptr;  // [K][D]
+    const float *var = nullptr;        // [Dtot] (zero beyond the stored variance)
+    const uint32_t *ids = nullptr;     // [N]
+    const int64_t *blk_off = nullptr;  // [K+1]
+    const int64_t *vec_off = nullptr;  // [K+1]
+    SegDev seg[kMaxSeg];
+};
+
+struct Index {
+    // metadata
+    int64_t N = 0, D = 0, K = 0;
+    uint8_t qcfg_raw[32] = {0};
+    std::vector<float> var;  // as stored in the file
+    struct SegHost {
+        int64_t dim, bits;
+        uint8_t cfg_raw[20];
+        bool rotated;
+        std::vector<float> P;
+    };
+    std::vector<SegHost> segs;
+    bool compact = false;
+    std::vector<int64_t> sizes, blk_off, vec_off;
+    int64_t total_blocks = 0;
+    // device
+    DevIndexView view;
+    std::vector<void *> allocations;
+    int64_t device_bytes = 0;
+    int device = 0;
+    // scratch arena for searches (guarded)
+    mutable std::mutex mu;
+    mutable void *scratch = nullptr;
+    mutable size_t scratch_bytes = 0;
+
+    ~Index();
+    void *dalloc(size_t bytes);
+    void upload(void *dst, const void *src, size_t bytes);
+    void *scratch_get(size_t bytes) const;
+};
+
+// index_io.cpp
+Index *load_index_file(const std::string &path);
+void save_index_file(const Index &idx, const std::string &path);
+void finalize_view(Index &idx);
+
+// search.cu
+void run_search(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,
+                float *dists, int mem, cudaStream_t st);
+int64_t run_estimate(const Index &idx, const float *q_host, int64_t nprobe, float m, uint32_t *ids, float *acc,
+                     float *fast, float *vars, int64_t cap);
+
+// encode.cu
+void run_caq_encode(const float *resid, int64_t n, int64_t dim, int bits, const float *cent, int rdlmt, float eps,
+                    int32_t *codes, float *facs, int mem, cudaStream_t st);
+Index *construct_index(const float *data, int64_t n, int64_t dim, const float *centroids, int64_t k,
+                       const uint32_t *cids, const saqg_quantize_config &cfg, const float *variance,
+                       const float *rotations, uint64_t seed);
+
+// plan.cpp
+std::vector<std::pair<int64_t, int64_t>> make_plan(const float *var, int64_t dpad, float avg_bits, bool seg,
+                                                   int eqseg);
+
+}  // namespace saqg

@@ -1,0 +1,815 @@
+// Search hot path: IVF::search / IVF::estimate (index/ivf.hpp:275-362) on the GPU.
+//
+// Pipeline for a batch of nq independent queries (nq = 1 is the plain
+// single-query drop-in):
+//   k_probe_dist   L2 from every query to every centroid, in Eigen's order
+//                  (FlatInitializer::centroids_distances, initializer.hpp:52-76)
+//   k_probe_select the nprobe nearest in std::partial_sort order: radix select
+//                  + sort; on any tie the exact libstdc++ heap algorithm runs
+//   k_qprep        per segment: zero-padded query slice, prune bound
+//                  sqrt(sum var*q^2)*m and the rotated query q_s*P_s in Eigen's
+//                  GEMV order (saq_estimator.hpp:28-48, caq_estimator.hpp:56-68)
+//   k_scan         one CTA per query walks its probes in order.  Per cluster:
+//                  LUTs (Lut::prepare, lut.hpp:60-87); per tile of blocks
+//                  (one warp = one 32-vector block): FastScan sums and fast /
+//                  variance estimates, the block's pruning stages, accurate
+//                  distances of every lane that can pass under the tile-start
+//                  distk (distk only shrinks, so this is a superset), then one
+//                  thread replays SAQSearcher::searchCluster / scanCluster
+//                  (saq_searcher.hpp:68-214) and the ResultPool inserts
+//                  (utils/pool.hpp:17-30) exactly in the reference's order.
+#include <cfloat>
+#include <cstdio>
+
+#include "device_common.cuh"
+#include "saqg_internal.h"
+
+namespace saqg {
+
+namespace {
+
+constexpr int kScanWarps = 8;
+constexpr int kScanThreads = kScanWarps * 32;
+constexpr int kMaxTopK = 4096;
+
+struct SegScal {
+    float delta, sum_vl, sum_q, q_l2sqr, q_l2norm, c1, c2, vfac;
+};
+
+__device__ __forceinline__ uint32_t fkey(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// ------------------------------------------------------------------ probe
+__global__ void k_probe_dist(DevIndexView ix, const float *__restrict__ q, float *__restrict__ dist) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = blockIdx.x * (blockDim.x >> 5) + warp;
+    const int qi = blockIdx.y;
+    if (c >= ix.K) return;
+    const float *cr = ix.centroids + (size_t)c * ix.D;
+    const float *qq = q + (size_t)qi * ix.D;
+    float d = warp_eigen_sum(ix.D, [&](int i) {
+        const float t = __fsub_rn(cr[i], qq[i]);
+        return __fmul_rn(t, t);
+    });
+    if (lane == 0) dist[(size_t)qi * ix.K + c] = d;
+}
+
+struct Cand {
+    uint32_t id;
+    float d;
+};
+
+// libstdc++ std::partial_sort (stl_algo.h __heap_select + __sort_heap,
+// stl_heap.h __adjust_heap / __push_heap / __pop_heap), comp = operator< on
+// the distance (Candidate::operator<, defines.hpp:48).
+__device__ void heap_adjust(Cand *a, long hole, long len, Cand val) {
+    const long top = hole;
+    long sc = hole;
+    while (sc < (len - 1) / 2) {
+        sc = 2 * (sc + 1);
+        if (a[sc].d < a[sc - 1].d) sc--;
+        a[hole] = a[sc];
+        hole = sc;
+    }
+    if ((len & 1) == 0 && sc == (len - 2) / 2) {
+        sc = 2 * (sc + 1);
+        a[hole] = a[sc - 1];
+        hole = sc - 1;
+    }
+    long parent = (hole - 1) / 2;
+    while (hole > top && a[parent].d < val.d) {
+        a[hole] = a[parent];
+        hole = parent;
+        parent = (hole - 1) / 2;
+    }
+    a[hole] = val;
+}
+
+__device__ void exact_partial_sort(Cand *a, long mid, long len) {
+    if (mid >= 2)
+        for (long parent = (mid - 2) / 2;; --parent) {
+            heap_adjust(a, parent, mid, a[parent]);
+            if (parent == 0) break;
+        }
+    for (long i = mid; i < len; ++i)
+        if (a[i].d < a[0].d) {
+            Cand v = a[i];
+            a[i] = a[0];
+            heap_adjust(a, 0, mid, v);
+        }
+    for (long last = mid; last > 1;) {
+        --last;
+        Cand v = a[last];
+        a[last] = a[0];
+        heap_adjust(a, 0, last, v);
+    }
+}
+
+constexpr int kSelThreads = 1024;
+constexpr int kSelMax = 1024;  // fast path handles nprobe <= 1024
+
+__global__ void __launch_bounds__(kSelThreads) k_probe_select(const float *__restrict__ dist, int K, int nprobe,
+                                                              uint32_t *__restrict__ probe, Cand *__restrict__ work,
+                                                              int *__restrict__ fallback_count) {
+    __shared__ uint32_t hist[256];
+    __shared__ uint32_t s_prefix, s_mask, s_rem, s_eq, s_n;
+    __shared__ unsigned long long sel[kSelMax];
+    const int qi = blockIdx.x, tid = threadIdx.x;
+    const float *dq = dist + (size_t)qi * K;
+    if (tid == 0) {
+        s_prefix = 0;
+        s_mask = 0;
+        s_rem = (uint32_t)(nprobe - 1);
+    }
+    __syncthreads();
+    for (int pass = 0; pass < 4; ++pass) {
+        const int shift = 24 - 8 * pass;
+        for (int i = tid; i < 256; i += kSelThreads) hist[i] = 0;
+        __syncthreads();
+        const uint32_t prefix = s_prefix, mask = s_mask;
+        for (int i = tid; i < K; i += kSelThreads) {
+            const uint32_t k = fkey(dq[i]);
+            if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t cum = 0, rem = s_rem;
+            int b = 0;
+            for (; b < 256; ++b) {
+                if (cum + hist[b] > rem) break;
+                cum += hist[b];
+            }
+            s_rem = rem - cum;
+            s_prefix = prefix | ((uint32_t)b << shift);
+            s_mask = mask | (255u << shift);
+            s_eq = hist[b];
+            s_n = 0;
+        }
+        __syncthreads();
+    }
+    const uint32_t T = s_prefix;
+    const uint32_t count_lt = (uint32_t)(nprobe - 1) - s_rem;
+    bool need_exact = (s_eq != 1) || nprobe > kSelMax;
+    if (!need_exact) {
+        for (int i = tid; i < K; i += kSelThreads) {
+            const uint32_t k = fkey(dq[i]);
+            if (k <= T) {
+                const uint32_t pos = atomicAdd(&s_n, 1u);
+                if (pos < kSelMax) sel[pos] = ((unsigned long long)k << 32) | (uint32_t)i;
+            }
+        }
+        __syncthreads();
+        const int n = (int)s_n;
+        int P = 1;
+        while (P < n) P <<= 1;
+        for (int i = n + tid; i < P; i += kSelThreads) sel[i] = ~0ull;
+        __syncthreads();
+        for (int k = 2; k <= P; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = tid; i < P; i += kSelThreads) {
+                    const int ixj = i ^ j;
+                    if (ixj > i) {
+                        const unsigned long long a = sel[i], b = sel[ixj];
+                        const bool up = (i & k) == 0;
+                        if ((a > b) == up) {
+                            sel[i] = b;
+                            sel[ixj] = a;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        // equal keys inside the selection make the heap order matter
+        __shared__ int s_dup;
+        if (tid == 0) s_dup = (n != nprobe) || (count_lt + 1 != (uint32_t)nprobe);
+        __syncthreads();
+        for (int i = tid; i + 1 < n; i += kSelThreads)
+            if ((sel[i] >> 32) == (sel[i + 1] >> 32)) s_dup = 1;
+        __syncthreads();
+        if (!s_dup) {
+            for (int i = tid; i < nprobe; i += kSelThreads) probe[(size_t)qi * nprobe + i] = (uint32_t)(sel[i] & 0xffffffffu);
+            return;
+        }
+        need_exact = true;
+    }
+    // exact fallback: the standard library's algorithm, sequentially
+    if (tid == 0) {
+        atomicAdd(fallback_count, 1);
+        Cand *a = work + (size_t)qi * K;
+        for (int i = 0; i < K; ++i) a[i] = Cand{(uint32_t)i, dq[i]};
+        exact_partial_sort(a, nprobe, K);
+        for (int i = 0; i < nprobe; ++i) probe[(size_t)qi * nprobe + i] = a[i].id;
+    }
+}
+
+// ------------------------------------------------------------------ query prep
+__global__ void k_qprep(DevIndexView ix, const float *__restrict__ q, float m, float *__restrict__ qrot,
+                        float *__restrict__ prune) {
+    extern __shared__ float cq[];
+    const int s = blockIdx.x, qi = blockIdx.y;
+    const SegDev &g = ix.seg[s];
+    const int dim = g.dim, qoff = g.qoff;
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) {
+        const int gi = qoff + i;
+        cq[i] = gi < ix.D ? q[(size_t)qi * ix.D + gi] : 0.0f;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const float *var = ix.var + qoff;
+        const float v2 = warp_eigen_sum(dim, [&](int i) { return __fmul_rn(var[i], __fmul_rn(cq[i], cq[i])); });
+        if (threadIdx.x == 0) prune[(size_t)qi * ix.S + s] = __fmul_rn(sqrtf(v2), m);
+    }
+    float *out = qrot + (size_t)qi * ix.Dtot + qoff;
+    if (!g.P) {
+        for (int i = threadIdx.x; i < dim; i += blockDim.x) out[i] = cq[i];
+        return;
+    }
+    // Eigen general_matrix_vector_product<ColMajor> (GeneralMatrixVector.h:108-300):
+    // per output, FMA chains over blocks of 16 inputs (one block if dim < 128).
+    const int bc = dim < 128 ? dim : 16;
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) {
+        float res = 0.0f;
+        for (int j2 = 0; j2 < dim; j2 += bc) {
+            float c = 0.0f;
+            const int je = min(j2 + bc, dim);
+            for (int j = j2; j < je; ++j) c = fmaf(g.P[(size_t)j * dim + i], cq[j], c);
+            res = fmaf(c, 1.0f, res);
+        }
+        out[i] = res;
+    }
+}
+
+// ------------------------------------------------------------------ LUT
+// Lut::prepare for one segment, by one warp (lut.hpp:60-87, fastscan.hpp:236-248).
+__device__ void build_lut(const float *__restrict__ qres, int dim, uint16_t *__restrict__ lut, SegScal &sc, float prune) {
+    const int lane = threadIdx.x & 31;
+    const float sum_q = warp_eigen_sum(dim, [&](int i) { return qres[i]; });
+    const float q2 = warp_eigen_sum(dim, [&](int i) { return __fmul_rn(qres[i], qres[i]); });
+    const int ncb = dim / 4;
+    float vl = FLT_MAX, vr = -FLT_MAX;
+    for (int cb = lane; cb < ncb; cb += 32) {
+        const float *qq = qres + cb * 4;
+        float t[16];
+        t[0] = 0.0f;
+#pragma unroll
+        for (int j = 1; j < 16; ++j) {
+            const int lb = j & -j, pos = lb == 1 ? 3 : lb == 2 ? 2 : lb == 4 ? 1 : 0;  // kPos[j] (fastscan.hpp:22-39)
+            t[j] = __fadd_rn(t[j - (j & -j)], qq[pos]);
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            vl = fminf(vl, t[j]);
+            vr = fmaxf(vr, t[j]);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        vl = fminf(vl, __shfl_xor_sync(kFull, vl, o));
+        vr = fmaxf(vr, __shfl_xor_sync(kFull, vr, o));
+    }
+    const float delta = (float)__ddiv_rn((double)__fsub_rn(vr, vl), 65536.0 - 0.01);
+    for (int cb = lane; cb < ncb; cb += 32) {
+        const float *qq = qres + cb * 4;
+        float t[16];
+        t[0] = 0.0f;
+#pragma unroll
+        for (int j = 1; j < 16; ++j) {
+            const int lb = j & -j, pos = lb == 1 ? 3 : lb == 2 ? 2 : lb == 4 ? 1 : 0;
+            t[j] = __fadd_rn(t[j - (j & -j)], qq[pos]);
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) lut[cb * 16 + j] = (uint16_t)(int)__fdiv_rn(__fsub_rn(t[j], vl), delta);
+    }
+    if (lane == 0) {
+        sc.delta = delta;
+        sc.sum_vl = (float)__dmul_rn(__dadd_rn((double)vl, __dmul_rn(0.5, (double)delta)), (double)(float)ncb);
+        sc.sum_q = sum_q;
+        sc.q_l2sqr = q2;
+        sc.q_l2norm = sqrtf(q2);
+        sc.c1 = (float)__dsub_rn(__dmul_rn(0.5, (double)sum_q), (double)__fmul_rn(0.58f, sc.q_l2norm));
+        const float one_over_sqrtD = (float)__ddiv_rn(1.0, (double)sqrtf((float)dim));
+        sc.c2 = __fmul_rn(__fdiv_rn(4.0f, 0.8f), one_over_sqrtD);
+        sc.vfac = __fsub_rn(q2, __fmul_rn(2.0f, prune));
+    }
+}
+
+// FastScan sum of one vector (this lane) of block gb: sum over codebooks of
+// LUT_u16[cb][nibble] (accumulate_hacc, fastscan_highacc.hpp:66-139, exact
+// for dim <= 2048), then Lut::compFastIP's float epilogue and the L2 form of
+// CaqCluEstimator::compFastDist (caq_estimator.hpp:148-179).
+__device__ __forceinline__ float fast_est(const SegDev &g, const uint16_t *__restrict__ lut, const SegScal &sc,
+                                          int64_t gb, int lane, float onorm, float &ipx) {
+    const int nc = g.dim / 64;
+    const uint2 *cp = g.codes + (size_t)gb * nc * 32 + lane;
+    int sum = 0;
+#pragma unroll 4
+    for (int c8 = 0; c8 < nc; ++c8) {
+        const uint2 w = cp[(size_t)c8 * 32];
+        const uint16_t *L = lut + c8 * 256;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t b = (w.x >> (8 * j)) & 255u;
+            sum += L[(2 * j) * 16 + (b >> 4)] + L[(2 * j + 1) * 16 + (b & 15u)];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t b = (w.y >> (8 * j)) & 255u;
+            sum += L[(8 + 2 * j) * 16 + (b >> 4)] + L[(8 + 2 * j + 1) * 16 + (b & 15u)];
+        }
+    }
+    float t = __fmul_rn((float)sum, sc.delta);
+    t = __fadd_rn(t, sc.sum_vl);
+    ipx = t;
+    float f = __fmul_rn(__fsub_rn(t, sc.c1), sc.c2);
+    f = __fmul_rn(f, onorm);
+    return maxps(0.0f, __fadd_rn(__fmul_rn(onorm, onorm), __fsub_rn(sc.q_l2sqr, f)));
+}
+
+__device__ __forceinline__ float vars_est(const SegScal &sc, float onorm) {
+    return maxps(0.0f, __fadd_rn(__fmul_rn(onorm, onorm), sc.vfac));
+}
+
+// ResultPool::insert / distk (utils/pool.hpp:17-49), L2
+__device__ __forceinline__ void pool_insert(uint32_t *ids, float *d, int &size, int cap, uint32_t u, float dist) {
+    if (size == cap && dist > d[size - 1]) return;
+    int lo = 0, len = size;
+    while (len > 1) {
+        const int half = len >> 1;
+        len -= half;
+        lo += (d[lo + half - 1] < dist) * half;
+    }
+    if (lo < size && d[lo] < dist) lo++;
+    for (int i = size; i > lo; --i) {
+        ids[i] = ids[i - 1];
+        d[i] = d[i - 1];
+    }
+    ids[lo] = u;
+    d[lo] = dist;
+    size += (size < cap);
+}
+
+// ------------------------------------------------------------------ scan
+struct ScanSmem {
+    // laid out in dynamic shared memory by scan_smem_layout()
+    uint16_t *lut;
+    float *qres;
+    SegScal *scal;
+    float *cd, *ipx, *part, *cur, *stage;
+    uint32_t *cmask;
+    int *nstage;
+    uint32_t *pool_id;
+    float *pool_d;
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+__host__ __device__ inline size_t scan_smem_bytes(int Dtot, int S, int topk) {
+    size_t b = 0;
+    b += align16(sizeof(uint16_t) * 4 * (size_t)Dtot);
+    b += align16(sizeof(float) * Dtot);
+    b += align16(sizeof(SegScal) * S);
+    b += 3 * align16(sizeof(float) * kScanWarps * S * 32);  // cd, ipx, part
+    b += align16(sizeof(float) * kScanWarps * 32);          // cur
+    b += align16(sizeof(float) * kScanWarps * (S + 1));     // stage minima
+    b += align16(sizeof(uint32_t) * kScanWarps);
+    b += align16(sizeof(int) * kScanWarps);
+    b += align16(sizeof(uint32_t) * (topk + 1));
+    b += align16(sizeof(float) * (topk + 1));
+    return b;
+}
+
+__device__ ScanSmem scan_smem_layout(char *base, int Dtot, int S, int topk) {
+    ScanSmem s;
+    size_t o = 0;
+    s.lut = (uint16_t *)(base + o);
+    o += align16(sizeof(uint16_t) * 4 * (size_t)Dtot);
+    s.qres = (float *)(base + o);
+    o += align16(sizeof(float) * Dtot);
+    s.scal = (SegScal *)(base + o);
+    o += align16(sizeof(SegScal) * S);
+    s.cd = (float *)(base + o);
+    o += align16(sizeof(float) * kScanWarps * S * 32);
+    s.ipx = (float *)(base + o);
+    o += align16(sizeof(float) * kScanWarps * S * 32);
+    s.part = (float *)(base + o);
+    o += align16(sizeof(float) * kScanWarps * S * 32);
+    s.cur = (float *)(base + o);
+    o += align16(sizeof(float) * kScanWarps * 32);
+    s.stage = (float *)(base + o);
+    o += align16(sizeof(float) * kScanWarps * (S + 1));
+    s.cmask = (uint32_t *)(base + o);
+    o += align16(sizeof(uint32_t) * kScanWarps);
+    s.nstage = (int *)(base + o);
+    o += align16(sizeof(int) * kScanWarps);
+    s.pool_id = (uint32_t *)(base + o);
+    o += align16(sizeof(uint32_t) * (topk + 1));
+    s.pool_d = (float *)(base + o);
+    return s;
+}
+
+// Prepares the LUTs and scalars of every segment for cluster c.
+__device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict__ qrot, const float *__restrict__ prune,
+                                int c, ScanSmem &sm) {
+    for (int i = threadIdx.x; i < ix.Dtot; i += blockDim.x) {
+        int s = 0;
+        while (s + 1 < ix.S && i >= ix.seg[s + 1].qoff) ++s;
+        const SegDev &g = ix.seg[s];
+        sm.qres[i] = __fsub_rn(qrot[i], g.cent[(size_t)c * g.dim + (i - g.qoff)]);
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5;
+    for (int s = warp; s < ix.S; s += kScanWarps)
+        build_lut(sm.qres + ix.seg[s].qoff, ix.seg[s].dim, sm.lut + 4 * ix.seg[s].qoff, sm.scal[s], prune[s]);
+    __syncthreads();
+}
+
+// Estimates of one block (this warp, lane = vector).  Fills cd/ipx for every
+// segment and, for several segments, the running sum and the pruning-stage
+// minima of SAQSearcher::searchCluster steps 1-2 (saq_searcher.hpp:87-132).
+__device__ void block_estimates(const DevIndexView &ix, int64_t gb, ScanSmem &sm, int w, int lane) {
+    const int S = ix.S;
+    if (S == 1) {
+        const SegDev &g = ix.seg[0];
+        const float on = g.onorm[gb * 32 + lane];
+        float ipx = 0.0f, est;
+        if (g.bits) est = fast_est(g, sm.lut, sm.scal[0], gb, lane, on, ipx);
+        else est = vars_est(sm.scal[0], on);
+        sm.cd[w * 32 + lane] = est;
+        sm.ipx[w * 32 + lane] = ipx;
+        sm.cur[w * 32 + lane] = est;
+        return;
+    }
+    float cur = 0.0f;
+    for (int s = 0; s < S; ++s) {
+        const float v = vars_est(sm.scal[s], ix.seg[s].onorm[gb * 32 + lane]);
+        sm.cd[(w * S + s) * 32 + lane] = v;
+        sm.ipx[(w * S + s) * 32 + lane] = 0.0f;
+        cur = __fadd_rn(cur, v);
+    }
+    int k = 0;
+    float mi = warp_min_tree(cur);
+    if (lane == 0) sm.stage[w * (S + 1) + k] = mi;
+    ++k;
+    for (int s = 0; s < S; ++s) {
+        const SegDev &g = ix.seg[s];
+        if (!g.bits) continue;
+        const float on = g.onorm[gb * 32 + lane];
+        cur = __fsub_rn(cur, sm.cd[(w * S + s) * 32 + lane]);
+        float ipx;
+        const float f = fast_est(g, sm.lut + 4 * g.qoff, sm.scal[s], gb, lane, on, ipx);
+        sm.cd[(w * S + s) * 32 + lane] = f;
+        sm.ipx[(w * S + s) * 32 + lane] = ipx;
+        cur = __fadd_rn(cur, f);
+        mi = warp_min_tree(cur);
+        if (lane == 0) sm.stage[w * (S + 1) + k] = mi;
+        ++k;
+    }
+    if (lane == 0) sm.nstage[w] = k;
+    sm.cur[w * 32 + lane] = cur;
+}
+
+__device__ __forceinline__ bool stages_pass(const float *st, int n, float tau) {
+    for (int i = 0; i < n; ++i)
+        if (st[i] > tau) return false;
+    return true;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const uint32_t *__restrict__ probe, int nprobe,
+                                                       const float *__restrict__ qrot_all,
+                                                       const float *__restrict__ prune_all, int topk,
+                                                       uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
+                                                       int *__restrict__ err) {
+    extern __shared__ __align__(16) char smem_raw[];
+    const int S = ix.S;
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, topk);
+    __shared__ int pool_size;
+    __shared__ float distk;
+    const int qi = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const float *qrot = qrot_all + (size_t)qi * ix.Dtot;
+    const float *prune = prune_all + (size_t)qi * S;
+    for (int i = tid; i <= topk; i += kScanThreads) {
+        sm.pool_id[i] = 0;
+        sm.pool_d[i] = 0.0f;
+    }
+    if (tid == 0) {
+        pool_size = 0;
+        distk = FLT_MAX;
+    }
+    __syncthreads();
+    for (int p = 0; p < nprobe; ++p) {
+        const int c = (int)probe[(size_t)qi * nprobe + p];
+        prepare_cluster(ix, qrot, prune, c, sm);
+        const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
+        const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
+        for (int t0 = 0; t0 < nb; t0 += kScanWarps) {
+            const int b = t0 + w;
+            const bool active = b < nb;
+            if (active) block_estimates(ix, b0 + b, sm, w, lane);
+            __syncthreads();
+            const float tau = distk;
+            if (active) {
+                bool cand;
+                if (S == 1) {
+                    const int cnp = (b == nb - 1) ? (n % 32) : 32;  // scanCluster's last-block count (saq_searcher.hpp:186)
+                    cand = lane < cnp && sm.cd[w * 32 + lane] < tau;
+                } else {
+                    cand = stages_pass(sm.stage + w * (S + 1), sm.nstage[w], tau) && sm.cur[w * 32 + lane] < tau &&
+                           (b * 32 + lane) < n;
+                }
+                const uint32_t m = __ballot_sync(kFull, cand);
+                if (lane == 0) sm.cmask[w] = m;
+            } else if (lane == 0) {
+                sm.cmask[w] = 0;
+            }
+            __syncthreads();
+            // accurate distances of candidate lanes: one half-warp per (vector, segment)
+            {
+                int total = 0;
+                for (int i = 0; i < kScanWarps; ++i) total += __popc(sm.cmask[i]) * S;
+                const int hw = tid >> 4, l = tid & 15;
+                const unsigned hmask = (lane < 16) ? 0x0000ffffu : 0xffff0000u;
+                for (int t = hw; t < total; t += 2 * kScanWarps) {
+                    int r = t / S, s = t - r * S, ww = 0;
+                    while (r >= __popc(sm.cmask[ww])) {
+                        r -= __popc(sm.cmask[ww]);
+                        ++ww;
+                    }
+                    uint32_t mk = sm.cmask[ww];
+                    for (int i = 0; i < r; ++i) mk &= mk - 1;
+                    const int j = __ffs(mk) - 1;
+                    const int64_t gb = b0 + t0 + ww, gv = v0 + (int64_t)(t0 + ww) * 32 + j;
+                    const SegDev &g = ix.seg[s];
+                    const float on = g.onorm[gb * 32 + j];
+                    float ex = 0.0f;
+                    if (g.bits > 1)
+                        ex = excode_ip_half(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim, g.bits - 1, l, hmask);
+                    if (l == 0) {
+                        const SegScal &sc = sm.scal[s];
+                        const float acc = accurate_dist(on, sm.ipx[(ww * S + s) * 32 + j], ex, g.exfac[gv].x, g.bits,
+                                                        sc.sum_q, sc.q_l2sqr);
+                        sm.part[(ww * S + s) * 32 + j] = S == 1 ? acc : __fsub_rn(acc, sm.cd[(ww * S + s) * 32 + j]);
+                    }
+                }
+            }
+            __syncthreads();
+            // exact replay of the reference's sequential decisions
+            if (tid == 0) {
+                float dk = distk;
+                int sz = pool_size;
+                for (int ww = 0; ww < kScanWarps && t0 + ww < nb; ++ww) {
+                    const int bb = t0 + ww;
+                    const uint32_t cm = sm.cmask[ww];
+                    if (S == 1) {
+                        const int cnp = (bb == nb - 1) ? (n % 32) : 32;
+                        uint32_t mask = 0;
+                        for (int j = 0; j < cnp; ++j) mask |= (uint32_t)(sm.cd[ww * 32 + j] < dk) << j;
+                        while (mask) {
+                            const int j = __ffs(mask) - 1;
+                            mask &= mask - 1;
+                            if (!((cm >> j) & 1u)) *err = 1;
+                            pool_insert(sm.pool_id, sm.pool_d, sz, topk, ix.ids[v0 + (int64_t)bb * 32 + j],
+                                        sm.part[ww * 32 + j]);
+                            dk = sz == topk ? sm.pool_d[sz - 1] : FLT_MAX;
+                        }
+                    } else {
+                        if (!stages_pass(sm.stage + ww * (S + 1), sm.nstage[ww], dk)) continue;
+                        for (int j = 0; j < 32; ++j) {
+                            if (!(sm.cur[ww * 32 + j] < dk)) continue;
+                            if (bb * 32 + j >= n) break;
+                            if (!((cm >> j) & 1u)) *err = 1;
+                            float acc = sm.cur[ww * 32 + j];
+                            for (int s = 0; s < S; ++s) {
+                                acc = __fadd_rn(acc, sm.part[(ww * S + s) * 32 + j]);
+                                if (acc >= dk) break;
+                            }
+                            pool_insert(sm.pool_id, sm.pool_d, sz, topk, ix.ids[v0 + (int64_t)bb * 32 + j], acc);
+                            dk = sz == topk ? sm.pool_d[sz - 1] : FLT_MAX;
+                        }
+                    }
+                }
+                distk = dk;
+                pool_size = sz;
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = tid; i < topk; i += kScanThreads) {
+        out_ids[(size_t)qi * topk + i] = sm.pool_id[i];
+        if (out_d) out_d[(size_t)qi * topk + i] = i < pool_size ? sm.pool_d[i] : FLT_MAX;
+    }
+}
+
+// ------------------------------------------------------------------ estimate
+// IVF::estimate: every vector of the probed clusters (no pruning); one CTA per
+// probed cluster, outputs at the cluster's offset in probe order.
+__global__ void __launch_bounds__(kScanThreads) k_estimate(DevIndexView ix, const uint32_t *__restrict__ probe,
+                                                           const int64_t *__restrict__ out_off,
+                                                           const float *__restrict__ qrot,
+                                                           const float *__restrict__ prune, uint32_t *__restrict__ o_ids,
+                                                           float *__restrict__ o_acc, float *__restrict__ o_fast,
+                                                           float *__restrict__ o_vars) {
+    extern __shared__ __align__(16) char smem_raw[];
+    const int S = ix.S;
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, 1);
+    const int p = blockIdx.x, c = (int)probe[p];
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    prepare_cluster(ix, qrot, prune, c, sm);
+    const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
+    const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
+    const int64_t base = out_off[p];
+    for (int b = w; b < nb; b += kScanWarps) {
+        const int64_t gb = b0 + b;
+        float fsum = 0.0f, vsum = 0.0f;
+        for (int s = 0; s < S; ++s) {
+            const SegDev &g = ix.seg[s];
+            const float on = g.onorm[gb * 32 + lane];
+            const float v = vars_est(sm.scal[s], on);
+            float ipx = 0.0f;
+            const float f = g.bits ? fast_est(g, sm.lut + 4 * g.qoff, sm.scal[s], gb, lane, on, ipx) : v;
+            sm.ipx[(w * S + s) * 32 + lane] = ipx;
+            fsum = __fadd_rn(fsum, f);
+            vsum = __fadd_rn(vsum, v);
+        }
+        __syncwarp();
+        const int nv = min(32, n - b * 32);
+        for (int j = 0; j < nv; ++j) {
+            const int64_t gv = v0 + (int64_t)b * 32 + j;
+            float acc = 0.0f;
+            for (int s = 0; s < S; ++s) {
+                const SegDev &g = ix.seg[s];
+                float ex = 0.0f;
+                if (g.bits > 1) {
+                    // whole warp: lanes 0-15 do the chain, 16-31 idle duplicates
+                    ex = excode_ip_half(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim, g.bits - 1, lane & 15,
+                                        (lane < 16) ? 0x0000ffffu : 0xffff0000u);
+                    ex = __shfl_sync(kFull, ex, 0);
+                }
+                const float on = g.onorm[gb * 32 + j];
+                acc = __fadd_rn(acc, accurate_dist(on, sm.ipx[(w * S + s) * 32 + j], ex, g.exfac[gv].x, g.bits,
+                                                   sm.scal[s].sum_q, sm.scal[s].q_l2sqr));
+            }
+            const float fj = __shfl_sync(kFull, fsum, j), vj = __shfl_sync(kFull, vsum, j);
+            if (lane == 0) {
+                const int64_t o = base + (int64_t)b * 32 + j;
+                o_ids[o] = ix.ids[gv];
+                o_acc[o] = acc;
+                o_fast[o] = fj;
+                o_vars[o] = vj;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+struct Bump {
+    char *base;
+    size_t off = 0;
+    template <class T>
+    T *take(size_t count) {
+        off = align16(off);
+        T *p = reinterpret_cast<T *>(base + off);
+        off += sizeof(T) * count;
+        return p;
+    }
+};
+
+size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t nprobe, bool host_io) {
+    size_t b = 0;
+    auto add = [&](size_t x) { b += align16(x); };
+    add(4 * (size_t)nq * I.D);                 // queries (host io)
+    add(4 * (size_t)nq * I.K);                 // centroid distances
+    add(8 * (size_t)nq * I.K);                 // exact-select work (fallback)
+    add(4 * (size_t)nq * nprobe);              // probe ids
+    add(4 * (size_t)nq * I.view.Dtot);         // rotated queries
+    add(4 * (size_t)nq * I.view.S);            // prune bounds
+    add(4 * (size_t)nq * topk * 2);            // outputs (host io)
+    add(64);                                   // flags
+    (void)host_io;
+    return b + 256;
+}
+
+void check_launch(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw Error{SAQG_ERR_CUDA, std::string(what) + " launch failed: " + cudaGetErrorString(e)};
+}
+
+}  // namespace
+
+void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,
+                float *dists, int mem, cudaStream_t st) {
+    SAQG_REQUIRE(nq >= 0 && topk >= 1 && topk <= kMaxTopK, "topk must be in [1, 4096]");
+    SAQG_REQUIRE(nprobe >= 1 && nprobe <= I.K, "nprobe must be in [1, number of clusters]");
+    if (nq == 0) return;
+    const DevIndexView &ix = I.view;
+    std::lock_guard<std::mutex> lock(I.mu);
+    const bool host = mem == SAQG_MEM_HOST;
+    Bump bp{(char *)I.scratch_get(search_scratch_bytes(I, nq, topk, nprobe, host))};
+    float *dq = bp.take<float>((size_t)nq * I.D);
+    float *dist = bp.take<float>((size_t)nq * I.K);
+    Cand *work = bp.take<Cand>((size_t)nq * I.K);
+    uint32_t *probe = bp.take<uint32_t>((size_t)nq * nprobe);
+    float *qrot = bp.take<float>((size_t)nq * ix.Dtot);
+    float *prune = bp.take<float>((size_t)nq * ix.S);
+    uint32_t *oid = bp.take<uint32_t>((size_t)nq * topk);
+    float *od = bp.take<float>((size_t)nq * topk);
+    int *flags = bp.take<int>(16);
+    const float *qin = q;
+    if (host) {
+        SAQG_CUDA_TRY(cudaMemcpyAsync(dq, q, 4 * (size_t)nq * I.D, cudaMemcpyHostToDevice, st));
+        qin = dq;
+    }
+    SAQG_CUDA_TRY(cudaMemsetAsync(flags, 0, 64, st));
+    {
+        const int wpb = 8;
+        dim3 grid((unsigned)((I.K + wpb - 1) / wpb), (unsigned)nq);
+        k_probe_dist<<<grid, wpb * 32, 0, st>>>(ix, qin, dist);
+        check_launch("k_probe_dist");
+        k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, work, flags);
+        check_launch("k_probe_select");
+        size_t qsm = 0;
+        for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
+        k_qprep<<<dim3((unsigned)ix.S, (unsigned)nq), 256, qsm, st>>>(ix, qin, m, qrot, prune);
+        check_launch("k_qprep");
+        const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, (int)topk);
+        SAQG_REQUIRE(smem <= 220 * 1024, "dimension / topk too large for the scan kernel's shared memory");
+        SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        uint32_t *ids_out = host ? oid : ids;
+        float *d_out = host ? od : dists;
+        k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ids_out,
+                                                          d_out, flags + 1);
+        check_launch("k_scan");
+        count_launch(4);
+    }
+    if (host) {
+        SAQG_CUDA_TRY(cudaMemcpyAsync(ids, oid, 4 * (size_t)nq * topk, cudaMemcpyDeviceToHost, st));
+        if (dists) SAQG_CUDA_TRY(cudaMemcpyAsync(dists, od, 4 * (size_t)nq * topk, cudaMemcpyDeviceToHost, st));
+        int hflags[2] = {0, 0};
+        SAQG_CUDA_TRY(cudaMemcpyAsync(hflags, flags, 8, cudaMemcpyDeviceToHost, st));
+        SAQG_CUDA_TRY(cudaStreamSynchronize(st));
+        if (hflags[1]) throw Error{SAQG_ERR_INTERNAL, "scan replay met a lane without a precomputed distance"};
+    }
+}
+
+int64_t run_estimate(const Index &I, const float *q_host, int64_t nprobe, float m, uint32_t *ids, float *acc,
+                     float *fast, float *vars, int64_t cap) {
+    SAQG_REQUIRE(nprobe >= 1 && nprobe <= I.K, "nprobe must be in [1, number of clusters]");
+    const DevIndexView &ix = I.view;
+    std::lock_guard<std::mutex> lock(I.mu);
+    cudaStream_t st = 0;
+    Bump bp{(char *)I.scratch_get(search_scratch_bytes(I, 1, 1, nprobe, true))};
+    float *dq = bp.take<float>(I.D);
+    float *dist = bp.take<float>(I.K);
+    Cand *work = bp.take<Cand>(I.K);
+    uint32_t *probe = bp.take<uint32_t>(nprobe);
+    float *qrot = bp.take<float>(ix.Dtot);
+    float *prune = bp.take<float>(ix.S);
+    bp.take<uint32_t>(2);
+    bp.take<float>(2);
+    int *flags = bp.take<int>(16);
+    SAQG_CUDA_TRY(cudaMemcpy(dq, q_host, 4 * I.D, cudaMemcpyHostToDevice));
+    SAQG_CUDA_TRY(cudaMemset(flags, 0, 64));
+    const int wpb = 8;
+    k_probe_dist<<<dim3((unsigned)((I.K + wpb - 1) / wpb), 1), wpb * 32, 0, st>>>(ix, dq, dist);
+    check_launch("k_probe_dist");
+    k_probe_select<<<1, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, work, flags);
+    check_launch("k_probe_select");
+    size_t qsm = 0;
+    for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
+    k_qprep<<<dim3((unsigned)ix.S, 1), 256, qsm, st>>>(ix, dq, m, qrot, prune);
+    check_launch("k_qprep");
+    std::vector<uint32_t> hprobe(nprobe);
+    SAQG_CUDA_TRY(cudaMemcpy(hprobe.data(), probe, 4 * nprobe, cudaMemcpyDeviceToHost));
+    std::vector<int64_t> off(nprobe + 1, 0);
+    for (int64_t p = 0; p < nprobe; ++p) off[p + 1] = off[p] + I.sizes[hprobe[p]];
+    const int64_t total = off[nprobe];
+    if (total > 0) {
+        int64_t *doff;
+        uint32_t *oids;
+        float *oacc, *ofast, *ovars;
+        SAQG_CUDA_TRY(cudaMalloc(&doff, 8 * (nprobe + 1)));
+        SAQG_CUDA_TRY(cudaMalloc(&oids, 4 * total));
+        SAQG_CUDA_TRY(cudaMalloc(&oacc, 4 * total));
+        SAQG_CUDA_TRY(cudaMalloc(&ofast, 4 * total));
+        SAQG_CUDA_TRY(cudaMalloc(&ovars, 4 * total));
+        SAQG_CUDA_TRY(cudaMemcpy(doff, off.data(), 8 * (nprobe + 1), cudaMemcpyHostToDevice));
+        const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, 1);
+        SAQG_CUDA_TRY(cudaFuncSetAttribute(k_estimate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_estimate<<<(unsigned)nprobe, kScanThreads, smem, st>>>(ix, probe, doff, qrot, prune, oids, oacc, ofast, ovars);
+        check_launch("k_estimate");
+        count_launch(4);
+        const int64_t nw = std::min(total, cap);
+        SAQG_CUDA_TRY(cudaMemcpy(ids, oids, 4 * nw, cudaMemcpyDeviceToHost));
+        SAQG_CUDA_TRY(cudaMemcpy(acc, oacc, 4 * nw, cudaMemcpyDeviceToHost));
+        SAQG_CUDA_TRY(cudaMemcpy(fast, ofast, 4 * nw, cudaMemcpyDeviceToHost));
+        SAQG_CUDA_TRY(cudaMemcpy(vars, ovars, 4 * nw, cudaMemcpyDeviceToHost));
+        cudaFree(doff);
+        cudaFree(oids);
+        cudaFree(oacc);
+        cudaFree(ofast);
+        cudaFree(ovars);
+    }
+    return total;
+}
+
+}  // namespace saqg

@@ -1,0 +1,178 @@
+"""Python mirror of the reference's IVF API (index/ivf.hpp) over the C ABI.
+
+    ivf = IVF(n, num_dim, k, QuantizeConfig(...))      # IVF(n, dim, k, cfg)
+    ivf.set_variance(vars)                              # IVF::set_variance
+    ivf.construct(data, centroids, cluster_ids)         # IVF::construct
+    ivf.save(path) / IVF.load(path)                     # IVF::save / IVF::load
+    ids = ivf.search(query, topk, nprobe, SearcherConfig())   # IVF::search<L2Sqr>
+    dist_list, fast, vars = ivf.estimate(query, nprobe)       # IVF::estimate<L2Sqr>
+
+`search` accepts one query (the reference's signature) or a batch (nq x dim),
+each answered exactly as an independent reference call.  Inputs may be numpy
+arrays (host memory; the copies are part of the call) or CUDA torch tensors
+(device memory, used in place).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N
+
+
+@dataclass
+class QuantizeConfig:
+    """quantization/config.h:21-74 (QuantizeConfig with its QuantSingleConfig)."""
+    avg_bits: float = 0.0
+    seg_eqseg: int = 0
+    enable_segmentation: bool = True
+    use_compact_layout: bool = False
+    random_rotation: bool = True
+    caq_adj_rd_lmt: int = 6
+    caq_adj_eps: float = 1e-8
+
+    def to_c(self):
+        return N.QuantizeConfig(self.avg_bits, self.seg_eqseg, int(self.enable_segmentation),
+                                int(self.use_compact_layout), int(self.random_rotation), self.caq_adj_rd_lmt,
+                                self.caq_adj_eps)
+
+
+@dataclass
+class SearcherConfig:
+    """quantization/config.h:76-79."""
+    searcher_vars_bound_m: float = 4.0
+    dist_type: int = N.SAQG_DIST_L2
+
+    def to_c(self):
+        return N.SearcherConfig(self.searcher_vars_bound_m, self.dist_type)
+
+
+def _is_cuda_tensor(x) -> bool:
+    return hasattr(x, "is_cuda") and bool(x.is_cuda)
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    return C.c_void_p(getattr(stream, "cuda_stream", stream))
+
+
+class IVF:
+    def __init__(self, n: int = 0, num_dim: int = 0, k: int = 0, cfg: QuantizeConfig | None = None):
+        self.lib = N.load()
+        self._h = C.c_void_p()
+        self.num_data, self.num_dim, self.num_cen = n, num_dim, k
+        self.cfg = cfg or QuantizeConfig()
+        self._variance = None
+
+    # -- lifecycle --------------------------------------------------------
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.lib.saqg_index_free(self._h)
+            self._h = C.c_void_p()
+
+    @classmethod
+    def load(cls, path: str) -> "IVF":
+        ivf = cls()
+        N.check(ivf.lib.saqg_index_load(path.encode(), C.byref(ivf._h)))
+        info = ivf.info()
+        ivf.num_data, ivf.num_dim, ivf.num_cen = info["num_data"], info["num_dim"], info["num_clusters"]
+        return ivf
+
+    def save(self, path: str) -> None:
+        N.check(self.lib.saqg_index_save(self._h, path.encode()))
+
+    def set_variance(self, vars_) -> None:
+        self._variance = np.ascontiguousarray(vars_, np.float32).reshape(-1)
+
+    def construct(self, data, centroids, cluster_ids, rotations=None, seed: int = 1) -> None:
+        data = np.ascontiguousarray(data, np.float32)
+        cent = np.ascontiguousarray(centroids, np.float32)
+        cids = np.ascontiguousarray(cluster_ids, np.uint32).reshape(-1)
+        n, d = data.shape
+        if self._h.value:
+            self.lib.saqg_index_free(self._h)
+            self._h = C.c_void_p()
+        cfg = self.cfg.to_c()
+        rot = None if rotations is None else np.ascontiguousarray(rotations, np.float32)
+        N.check(self.lib.saqg_index_construct(
+            data.ctypes.data, n, d, cent.ctypes.data, cent.shape[0], cids.ctypes.data, C.byref(cfg),
+            None if self._variance is None else self._variance.ctypes.data,
+            None if rot is None else rot.ctypes.data, seed, C.byref(self._h)))
+        self.num_data, self.num_dim, self.num_cen = n, d, cent.shape[0]
+
+    def info(self) -> dict:
+        inf = N.IndexInfo()
+        N.check(self.lib.saqg_index_get_info(self._h, C.byref(inf)))
+        S = inf.num_segments
+        return dict(num_data=inf.num_data, num_dim=inf.num_dim, num_clusters=inf.num_clusters,
+                    plan=[(inf.seg_dim[i], inf.seg_bits[i]) for i in range(S)], device_bytes=inf.device_bytes)
+
+    # -- search -----------------------------------------------------------
+    def search(self, query, topk: int, nprobe: int, searcher_cfg: SearcherConfig | None = None,
+               return_dists: bool = False, out=None, stream=None):
+        cfg = (searcher_cfg or SearcherConfig()).to_c()
+        if _is_cuda_tensor(query):
+            import torch
+            q = query.contiguous().view(-1, self.num_dim)
+            nq = q.shape[0]
+            ids, dists = out if out is not None else (
+                torch.empty((nq, topk), dtype=torch.int32, device=q.device),
+                torch.empty((nq, topk), dtype=torch.float32, device=q.device))
+            N.check(self.lib.saqg_search(self._h, q.data_ptr(), nq, topk, nprobe, C.byref(cfg), ids.data_ptr(),
+                                         dists.data_ptr() if dists is not None else None, N.SAQG_MEM_DEVICE,
+                                         _stream_ptr(stream)))
+            return (ids, dists) if return_dists else ids
+        q = np.ascontiguousarray(query, np.float32)
+        single = q.ndim == 1
+        q = q.reshape(-1, self.num_dim)
+        nq = q.shape[0]
+        ids = np.zeros((nq, topk), np.uint32)
+        dists = np.zeros((nq, topk), np.float32)
+        N.check(self.lib.saqg_search(self._h, q.ctypes.data, nq, topk, nprobe, C.byref(cfg), ids.ctypes.data,
+                                     dists.ctypes.data, N.SAQG_MEM_HOST, _stream_ptr(stream)))
+        if single:
+            ids, dists = ids[0], dists[0]
+        return (ids, dists) if return_dists else ids
+
+    def estimate(self, query, nprobe: int, searcher_cfg: SearcherConfig | None = None):
+        """IVF::estimate: ([(id, accurate)], fast list, vars list) for every vector of the probed clusters."""
+        cfg = (searcher_cfg or SearcherConfig()).to_c()
+        q = np.ascontiguousarray(query, np.float32).reshape(-1)
+        cap = max(1, self.num_data)
+        ids = np.zeros(cap, np.uint32)
+        acc = np.zeros(cap, np.float32)
+        fast = np.zeros(cap, np.float32)
+        var = np.zeros(cap, np.float32)
+        cnt = C.c_int64()
+        N.check(self.lib.saqg_estimate(self._h, q.ctypes.data, nprobe, C.byref(cfg), ids.ctypes.data,
+                                       acc.ctypes.data, fast.ctypes.data, var.ctypes.data, cap, C.byref(cnt)))
+        n = cnt.value
+        return ids[:n], acc[:n], fast[:n], var[:n]
+
+
+def plan(variance, avg_bits: float, enable_segmentation: bool = True, seg_eqseg: int = 0):
+    """SaqDataMaker::analyze_plan through the C ABI (host computation)."""
+    lib = N.load()
+    v = np.ascontiguousarray(variance, np.float32).reshape(-1)
+    dims = np.zeros(64, np.int64)
+    bits = np.zeros(64, np.int64)
+    ns = C.c_int()
+    N.check(lib.saqg_plan(v.ctypes.data, v.size, avg_bits, int(enable_segmentation), seg_eqseg, dims.ctypes.data,
+                          bits.ctypes.data, 64, C.byref(ns)))
+    return [(int(dims[i]), int(bits[i])) for i in range(ns.value)]
+
+
+def caq_encode(resid, bits: int, centroid=None, rd_lmt: int = 6, eps: float = 1e-8):
+    """CAQEncoder::encode_and_fac on the GPU for n residual vectors (host arrays)."""
+    lib = N.load()
+    r = np.ascontiguousarray(resid, np.float32)
+    n, d = r.shape
+    codes = np.zeros((n, d), np.int32)
+    facs = np.zeros((n, 4), np.float32)
+    c = None if centroid is None else np.ascontiguousarray(centroid, np.float32)
+    N.check(lib.saqg_caq_encode(r.ctypes.data, n, d, bits, None if c is None else c.ctypes.data, rd_lmt, eps,
+                                codes.ctypes.data, facs.ctypes.data, N.SAQG_MEM_HOST, None))
+    return codes, facs
