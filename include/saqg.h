@@ -87,10 +87,12 @@ int saqg_index_get_info(const saqg_index *index, saqg_index_info *out);
  * from the data as SaqDataMaker::compute_variance does) and `rotations`
  * (concatenated row-major D_s x D_s matrices of the planned segments, may be
  * NULL -> random orthogonal matrices drawn from `seed`; ignored when
- * cfg->random_rotation is 0).  Inputs are host memory. */
+ * cfg->random_rotation is 0).  `data` is host or device memory per
+ * `data_mem`; every other input is host memory.  Each vector is rotated with
+ * the reference's GEMV summation order. */
 int saqg_index_construct(const float *data, int64_t n, int64_t dim, const float *centroids, int64_t k,
                          const uint32_t *cluster_ids, const saqg_quantize_config *cfg, const float *variance,
-                         const float *rotations, uint64_t seed, saqg_index **out);
+                         const float *rotations, uint64_t seed, int data_mem, saqg_index **out);
 
 /* ---- search ------------------------------------------------------------ */
 /* IVF::search<L2Sqr> (index/ivf.hpp:275-311) for `nq` queries (nq x dim), each

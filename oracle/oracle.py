@@ -63,6 +63,9 @@ def lib():
         l.orc_search.argtypes = [C.c_void_p, f32p, L, L, L, C.c_float, u32p, C.c_void_p, C.c_int]
         l.orc_estimate.restype = L
         l.orc_estimate.argtypes = [C.c_void_p, f32p, L, C.c_float, u32p, f32p, f32p, f32p, L]
+        l.orc_build_index.restype = C.c_int
+        l.orc_build_index.argtypes = [f32p, L, L, f32p, L, u32p, C.c_float, C.c_int, C.c_int, C.c_int, C.c_float,
+                                      C.c_int, C.c_void_p, C.c_void_p, C.c_char_p]
         _lib = l
     return _lib
 
@@ -136,6 +139,21 @@ def caq_encode(resid, bits, cent_unrot=None, rdlmt=6, eps=1e-8):
     c = None if cent_unrot is None else _f32(cent_unrot)
     lib().orc_caq_encode(r, n, D, bits, None if c is None else c.ctypes.data, rdlmt, eps, codes, facs)
     return codes, facs
+
+
+def build_index(path, data, centroids, cids, avg_bits, enable_seg=True, eqseg=0, rotations=None, variance=None,
+                rdlmt=6, eps=1e-8):
+    """IVF::construct + IVF::save with the given rotations (concatenated per segment; None = no rotation)."""
+    x = _f32(data)
+    c = _f32(centroids)
+    v = None if variance is None else _f32(variance)
+    r = None if rotations is None else _f32(rotations)
+    rc = lib().orc_build_index(x, x.shape[0], x.shape[1], c, c.shape[0], np.ascontiguousarray(cids, np.uint32),
+                               avg_bits, int(enable_seg), eqseg, rdlmt, eps, int(r is not None),
+                               None if v is None else v.ctypes.data, None if r is None else r.ctypes.data,
+                               path.encode())
+    if rc != 0:
+        raise RuntimeError(f"oracle build failed ({rc})")
 
 
 class OracleIndex:

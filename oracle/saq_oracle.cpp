@@ -881,8 +881,11 @@ void search_one(const Index *idx, const float *q, long topk, long nprobe, float 
 
 // ------------------------------------------------------------------ build
 void colwise_mean_var(const float *x, long N, long D, std::vector<float> &var) {
-    // Eigen packetwise_redux_impl (PartialReduxEvaluator.h:102-128) per column,
-    // then / rows; variance = colwise mean of (x - mean)^2.
+    // SaqDataMaker::compute_variance (saq_data.hpp:95-100).  data.colwise().mean()
+    // is vectorised: Eigen packetwise_redux_impl (PartialReduxEvaluator.h:102-128),
+    // x0 + ((x1+x2)+(x3+x4)) + ... per column; the variance's argument is a
+    // rowwise() replicate expression without packet access, so its column sums
+    // run sequentially.  Both are divided by the row count.
     auto colsum = [&](auto f, long col) {
         float p = f(0, col);
         long size4 = (N - 1) & ~3L;
@@ -894,16 +897,151 @@ void colwise_mean_var(const float *x, long N, long D, std::vector<float> &var) {
     std::vector<float> mean(D);
     for (long c = 0; c < D; ++c) mean[c] = colsum([&](long r, long cc) { return x[r * D + cc]; }, c) / (float)N;
     var.resize(D);
-    for (long c = 0; c < D; ++c)
-        var[c] = colsum(
-                     [&](long r, long cc) {
-                         float d = x[r * D + cc] - mean[cc];
-                         return d * d;
-                     },
-                     c) /
-                 (float)N;
+    for (long c = 0; c < D; ++c) {
+        float p = 0.0f;
+        for (long r = 0; r < N; ++r) {
+            const float d = x[r * D + c] - mean[c];
+            p = r == 0 ? d * d : p + d * d;
+        }
+        var[c] = p / (float)N;
+    }
 }
 
+
+// ------------------------------------------------------------------ index build
+// IVF::construct (ivf.hpp:130-184) -> IVF::save layout.  Rotation of every
+// vector and centroid uses the GEMV order above (the reference's GEMM order for
+// whole clusters depends on the host's cache-blocking sizes; its GEMV order is
+// what it uses for the centroid and for single-vector clusters).
+struct BuildCfg {
+    float avg_bits;
+    int seg, eqseg, rdlmt, rotate;
+    float eps;
+};
+
+void put_cfg_bytes(const BuildCfg &c, uint8_t *q32, uint8_t *s20) {
+    std::memset(q32, 0, 32);
+    std::memset(s20, 0, 20);
+    // QuantSingleConfig (config.h:12-19): quant_type, random_rotation, use_fastscan, rd_lmt, eps, ori_qB
+    int32_t qt = 0, rd = c.rdlmt, ori = 0;
+    std::memcpy(s20 + 0, &qt, 4);
+    s20[4] = (uint8_t)(c.rotate != 0);
+    s20[5] = 1;
+    std::memcpy(s20 + 8, &rd, 4);
+    std::memcpy(s20 + 12, &c.eps, 4);
+    std::memcpy(s20 + 16, &ori, 4);
+    // QuantizeConfig (config.h:21-27)
+    int32_t eq = c.eqseg;
+    std::memcpy(q32 + 0, &c.avg_bits, 4);
+    std::memcpy(q32 + 4, &eq, 4);
+    q32[8] = (uint8_t)(c.seg != 0);
+    q32[9] = 0;
+    std::memcpy(q32 + 12, s20, 20);
+}
+
+int build_index(const float *data, long N, long D, const float *cent, long K, const uint32_t *cids, const BuildCfg &cfg,
+                const float *vars_in, const float *rots, const char *path) {
+    if (D % 64) return 1;
+    std::vector<float> var;
+    if (vars_in) var.assign(vars_in, vars_in + D);
+    else colwise_mean_var(data, N, D, var);
+    Plan plan = !cfg.seg ? plan_equal(D, cfg.avg_bits, 1)
+                         : (cfg.eqseg > 0 ? plan_equal(D, cfg.avg_bits, cfg.eqseg) : plan_dp(var.data(), D, cfg.avg_bits));
+    const long S = (long)plan.segs.size();
+    uint8_t q32[32], s20[20];
+    put_cfg_bytes(cfg, q32, s20);
+    std::vector<std::vector<uint32_t>> lists(K);
+    for (long i = 0; i < N; ++i) lists[cids[i]].push_back((uint32_t)i);
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return 2;
+    auto w = [&](const void *p, size_t n) { std::fwrite(p, 1, n, f); };
+    auto w64 = [&](uint64_t v) { w(&v, 8); };
+    w64(N);
+    w64(D);
+    w64(K);
+    w(cent, 4 * K * D);
+    w(q32, 32);
+    w64(D);
+    w64(D);
+    w(var.data(), 4 * D);
+    w64(S);
+    std::vector<long> roff(S, 0);
+    long ro = 0;
+    for (long s = 0; s < S; ++s) {
+        const long d = plan.segs[s].first;
+        w64(d);
+        w64(plan.segs[s].second);
+        w(s20, 20);
+        uint8_t flag = cfg.rotate ? 1 : 0;
+        w(&flag, 1);
+        if (cfg.rotate) w(rots + ro, 4 * d * d);
+        roff[s] = ro;
+        ro += d * d;
+    }
+    for (long c = 0; c < K; ++c) w64(lists[c].size());
+    Index meta;
+    for (long s = 0; s < S; ++s) meta.segs.push_back(Seg{plan.segs[s].first, plan.segs[s].second, {}});
+    std::memcpy(meta.qcfg, q32, 32);
+    meta.derive();
+    for (long c = 0; c < K; ++c) {
+        const long n = (long)lists[c].size(), nb = (n + kFS - 1) / kFS;
+        std::vector<float> sfac(S > 1 ? 64 * S * nb : 0, 0.0f);
+        std::vector<uint8_t> scode(meta.block_bytes * nb, 0), lc(meta.long_stride * n, 0);
+        std::vector<float> lfac(2 * S * n, 0.0f);
+        std::vector<std::vector<float>> rc(S);
+        long off = 0;
+        for (long s = 0; s < S; ++s) {
+            const long d = plan.segs[s].first, bits = plan.segs[s].second;
+            std::vector<float> cseg(d, 0.0f), xs(d), xr(d), o(d);
+            for (long i = 0; i < d && off + i < D; ++i) cseg[i] = cent[c * D + off + i];
+            rc[s].resize(d);
+            if (cfg.rotate) gemv_rowvec(cseg.data(), rots + roff[s], d, rc[s].data());
+            else rc[s] = cseg;
+            std::vector<uint8_t> shortc(nb * kFS * (d / 8), 0);
+            CaqOut out;
+            for (long v = 0; v < n; ++v) {
+                const float *x = data + (size_t)lists[c][v] * D;
+                for (long i = 0; i < d; ++i) xs[i] = off + i < D ? x[off + i] : 0.0f;
+                if (cfg.rotate) gemv_rowvec(xs.data(), rots + roff[s], d, xr.data());
+                else xr = xs;
+                for (long i = 0; i < d; ++i) o[i] = xr[i] - rc[s][i];
+                caq_encode(o.data(), d, (int)bits, cseg.data(), cfg.rdlmt, cfg.eps, out);
+                const long b = v / kFS, j = v % kFS;
+                float *fac = S == 1 ? reinterpret_cast<float *>(scode.data() + b * meta.block_bytes)
+                                    : sfac.data() + (b * S + s) * 64;
+                fac[j] = out.o_l2norm;
+                if (bits == 0) continue;
+                fac[kFS + j] = out.ip_cent_oa;
+                lfac[(v * S + s) * 2] = out.rescale;
+                lfac[(v * S + s) * 2 + 1] = out.error;
+                const int sb = 1 << (bits - 1);
+                uint8_t *sc = &shortc[v * (d / 8)];
+                for (long i = 0; i < d; ++i)
+                    if (out.code[i] & sb) sc[i / 8] |= (uint8_t)(0x80 >> (i % 8));
+                if (bits > 1) {
+                    std::vector<uint16_t> low(d);
+                    for (long i = 0; i < d; ++i) low[i] = (uint16_t)(out.code[i] & (sb - 1));
+                    uint8_t *dst = S == 1 ? lc.data() + v * meta.long_pv[0] : lc.data() + v * meta.long_stride + meta.long_off[s];
+                    pack_excode(low.data(), d, (int)bits - 1, dst);
+                }
+            }
+            if (bits)
+                for (long b = 0; b < nb; ++b) {
+                    uint8_t *blk = S == 1 ? scode.data() + b * meta.block_bytes + 256 : scode.data() + b * meta.block_bytes + meta.sc_off[s];
+                    pack_block(&shortc[b * kFS * (d / 8)], d, blk);
+                }
+            off += d;
+        }
+        if (S > 1) w(sfac.data(), 4 * sfac.size());
+        w(scode.data(), scode.size());
+        w(lc.data(), lc.size());
+        w(lfac.data(), 4 * lfac.size());
+        w(lists[c].data(), 4 * n);
+        for (long s = 0; s < S; ++s) w(rc[s].data(), 4 * rc[s].size());
+    }
+    std::fclose(f);
+    return 0;
+}
 }  // namespace
 
 // ============================================================== C interface
@@ -1057,6 +1195,13 @@ long orc_estimate(void *h, const float *q, long nprobe, float m, uint32_t *ids, 
         }
     }
     return w;
+}
+
+int orc_build_index(const float *data, long N, long D, const float *cent, long K, const uint32_t *cids, float avg_bits,
+                    int seg, int eqseg, int rdlmt, float eps, int rotate, const float *vars, const float *rots,
+                    const char *path) {
+    BuildCfg c{avg_bits, seg, eqseg, rdlmt, rotate, eps};
+    return build_index(data, N, D, cent, K, cids, c, vars, rots, path);
 }
 
 }  // extern "C"

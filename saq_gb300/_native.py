@@ -48,7 +48,7 @@ EXPORTS = {
     "saqg_index_free": (C.c_int, [C.c_void_p]),
     "saqg_index_get_info": (C.c_int, [C.c_void_p, C.POINTER(IndexInfo)]),
     "saqg_index_construct": (C.c_int, [C.c_void_p, I64, I64, C.c_void_p, I64, C.c_void_p, C.POINTER(QuantizeConfig),
-                                       C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+                                       C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.POINTER(C.c_void_p)]),
     "saqg_search": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig), C.c_void_p,
                               C.c_void_p, C.c_int, C.c_void_p]),
     "saqg_estimate": (C.c_int, [C.c_void_p, C.c_void_p, I64, C.POINTER(SearcherConfig), C.c_void_p, C.c_void_p,

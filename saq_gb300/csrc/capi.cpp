@@ -92,12 +92,13 @@ int saqg_index_get_info(const saqg_index *index, saqg_index_info *out) {
 
 int saqg_index_construct(const float *data, int64_t n, int64_t dim, const float *centroids, int64_t k,
                          const uint32_t *cluster_ids, const saqg_quantize_config *cfg, const float *variance,
-                         const float *rotations, uint64_t seed, saqg_index **out) {
+                         const float *rotations, uint64_t seed, int data_mem, saqg_index **out) {
     return guarded([&] {
         SAQG_REQUIRE(data && centroids && cluster_ids && cfg && out, "null argument");
         SAQG_REQUIRE(n > 0 && dim > 0 && k > 0, "empty input");
         *out = nullptr;
-        Index *I = construct_index(data, n, dim, centroids, k, cluster_ids, *cfg, variance, rotations, seed);
+        SAQG_REQUIRE(data_mem == SAQG_MEM_HOST || data_mem == SAQG_MEM_DEVICE, "bad mem flag");
+        Index *I = construct_index(data, n, dim, centroids, k, cluster_ids, *cfg, variance, rotations, seed, data_mem);
         *out = new saqg_index{I};
     });
 }

@@ -121,7 +121,7 @@ void run_caq_encode(const float *resid, int64_t n, int64_t dim, int bits, const 
                     int32_t *codes, float *facs, int mem, cudaStream_t st);
 Index *construct_index(const float *data, int64_t n, int64_t dim, const float *centroids, int64_t k,
                        const uint32_t *cids, const saqg_quantize_config &cfg, const float *variance,
-                       const float *rotations, uint64_t seed);
+                       const float *rotations, uint64_t seed, int data_mem);
 
 // plan.cpp
 std::vector<std::pair<int64_t, int64_t>> make_plan(const float *var, int64_t dpad, float avg_bits, bool seg,

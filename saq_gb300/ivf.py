@@ -88,19 +88,26 @@ class IVF:
         self._variance = np.ascontiguousarray(vars_, np.float32).reshape(-1)
 
     def construct(self, data, centroids, cluster_ids, rotations=None, seed: int = 1) -> None:
-        data = np.ascontiguousarray(data, np.float32)
+        """IVF::construct.  `data` may be a numpy array or a CUDA torch tensor (used in place)."""
+        if _is_cuda_tensor(data):
+            data_t = data.contiguous()
+            n, d = data_t.shape
+            data_ptr, mem = data_t.data_ptr(), N.SAQG_MEM_DEVICE
+        else:
+            data_t = np.ascontiguousarray(data, np.float32)
+            n, d = data_t.shape
+            data_ptr, mem = data_t.ctypes.data, N.SAQG_MEM_HOST
         cent = np.ascontiguousarray(centroids, np.float32)
         cids = np.ascontiguousarray(cluster_ids, np.uint32).reshape(-1)
-        n, d = data.shape
         if self._h.value:
             self.lib.saqg_index_free(self._h)
             self._h = C.c_void_p()
         cfg = self.cfg.to_c()
         rot = None if rotations is None else np.ascontiguousarray(rotations, np.float32)
         N.check(self.lib.saqg_index_construct(
-            data.ctypes.data, n, d, cent.ctypes.data, cent.shape[0], cids.ctypes.data, C.byref(cfg),
+            data_ptr, n, d, cent.ctypes.data, cent.shape[0], cids.ctypes.data, C.byref(cfg),
             None if self._variance is None else self._variance.ctypes.data,
-            None if rot is None else rot.ctypes.data, seed, C.byref(self._h)))
+            None if rot is None else rot.ctypes.data, seed, mem, C.byref(self._h)))
         self.num_data, self.num_dim, self.num_cen = n, d, cent.shape[0]
 
     def info(self) -> dict:

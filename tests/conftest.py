@@ -19,8 +19,9 @@ def pytest_configure(config):
 
 INDEX_CASES = sorted(
     os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-    if os.path.basename(p) not in ("encode.npz", "plan.npz")
+    if os.path.basename(p) not in ("encode.npz", "plan.npz") and not os.path.basename(p).startswith("construct_")
 )
+CONSTRUCT_CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "construct_*.npz")))
 
 
 class GoldenCase:

@@ -52,6 +52,14 @@ INDEX_CASES = {
     "aniso_b4_seg_top100": dict(gen="aniso", n=800, d=256, k=6, nq=6, bits=4, seg=1, eqseg=0, topk=100, nprobe=6, seed=19),
 }
 
+# IVF::construct without rotation: residuals are exact, so the whole index is
+# comparable (inputs are stored too)
+CONSTRUCT_CASES = {
+    "construct_norot_b4_seg": dict(gen="aniso", n=400, d=256, k=5, bits=4, seg=1, eqseg=0, seed=31),
+    "construct_norot_b15_seg": dict(gen="aniso", n=300, d=128, k=4, bits=1.5, seg=1, eqseg=0, seed=32),
+    "construct_norot_b9_noseg": dict(gen="mix", n=300, d=128, k=4, bits=9, seg=0, eqseg=0, seed=33),
+}
+
 ENCODE_BITS = [1, 2, 3, 4, 5, 6, 7, 8, 9, 13]
 PLAN_CASES = [(256, 4), (1024, 4), (1024, 1.5), (960, 4), (1536, 6), (1536, 8), (512, 2), (1024, 0.5)]
 
@@ -106,6 +114,25 @@ def index_case(name, p, tmp):
     print(name, info["plan"], "index bytes", out["index_bytes"].size)
 
 
+def construct_case(name, p, tmp):
+    pp = dict(p, nq=1)
+    x, _, cent, cids = make_data(pp)
+    N, D = x.shape
+    K = cent.shape[0]
+    f = lambda s: os.path.join(tmp, s)  # noqa: E731
+    x.tofile(f("x.f32"))
+    cent.astype(np.float32).tofile(f("c.f32"))
+    cids.astype(np.uint32).tofile(f("cid.u32"))
+    info = json.loads(O.run_ref("build", f("x.f32"), N, D, f("c.f32"), K, f("cid.u32"), f("a.index"), p["bits"],
+                                p["seg"], p["eqseg"], 0, 6, 1e-8, 2))
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), x=x, centroids=cent.astype(np.float32),
+                        cids=cids.astype(np.uint32),
+                        index_bytes=np.frombuffer(open(f("a.index"), "rb").read(), dtype=np.uint8),
+                        plan=np.array(info["plan"], dtype=np.int64),
+                        params=np.frombuffer(json.dumps(p).encode(), dtype=np.uint8))
+    print(name, info["plan"])
+
+
 def encode_case(tmp):
     rng = np.random.default_rng(21)
     D, n = 128, 40
@@ -150,6 +177,8 @@ def main():
     with tempfile.TemporaryDirectory() as tmp:
         for name, p in INDEX_CASES.items():
             index_case(name, p, tmp)
+        for name, p in CONSTRUCT_CASES.items():
+            construct_case(name, p, tmp)
         encode_case(tmp)
         plan_case(tmp)
 
