@@ -1,0 +1,399 @@
+"""Benchmark of the SAQ search hot path on one GB300 (or N replicas).
+
+Workload (default): 10M x 1024 unit-norm vectors, anisotropic spectrum, PCA,
+16,384 clusters with Zipf(1.1) sizes, SAQ B=4 with segmentation, k=10, the
+smallest nprobe that reaches recall@10 >= 0.95 against exact FP64 ground truth.
+
+  value   batched QPS: one search call answers a batch of 4096 queries that are
+          already in HBM (each query answered exactly as an independent
+          IVF::search call); the L2 cache is flushed between timed steps.
+  e2e     the same batch through the C ABI with host buffers: host->device copy
+          of the queries and device->host copy of ids + distances inside the
+          timed region.
+  plain   the plain single-query drop-in: one query per call (QPS, p50, p99).
+  roofline  the scan kernel's algorithmic bytes / its CUDA-event duration.
+  cpu_baseline  the CPU oracle (a port of the reference's search) on the host
+          cores, on a bounded sample of the same queries and index.
+
+--impl reference times the CPU implementation alone (same index, same
+queries, all host threads) and prints its line with "impl": "reference".
+Multi-GPU (--gpus N via torchrun) runs N independent replicas (the search
+has no exchange step): value = all ranks' queries / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "QPS at recall@10≥0.95 (10M×1024, B=4): batched vs plain GPU; p99 ms; HBM %"
+NPROBE_GRID = [16, 24, 32, 48, 64, 96, 128, 160, 192, 256]
+CACHE_VERSION = 3
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=10_000_000)
+    ap.add_argument("--dim", type=int, default=1024)
+    ap.add_argument("--clusters", type=int, default=16384)
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--topk", type=int, default=10)
+    ap.add_argument("--bits", type=float, default=4.0)
+    ap.add_argument("--gt-queries", type=int, default=1000)
+    ap.add_argument("--plain-queries", type=int, default=256)
+    ap.add_argument("--target-recall", type=float, default=0.95)
+    ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "saqg_bench_cache"))
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for row in csv.reader(io.StringIO(getattr(self, "out", ""))):
+            if len(row) < 9:
+                continue
+            try:
+                sm.append(float(row[1]))
+                smax.append(float(row[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, row[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        load = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": float(np.median(load)), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cache_paths(a):
+    key = f"v{CACHE_VERSION}_n{a.n}_d{a.dim}_k{a.clusters}_b{a.bits}_seed0"
+    d = os.path.join(a.cache, key)
+    os.makedirs(d, exist_ok=True)
+    return d, os.path.join(d, "index.saq"), os.path.join(d, "meta.json")
+
+
+def build_workload(a, torch):
+    from saq_gb300 import workloads
+    return workloads.zipf_aniso(a.n, a.dim, a.clusters, nq=max(a.batch, a.gt_queries, a.plain_queries), seed=0)
+
+
+def get_index_and_meta(a, torch, wl, log):
+    """Index built on the GPU (or loaded from this box's cache), ground truth and the tuned nprobe."""
+    from saq_gb300 import ivf, workloads
+    cdir, ipath, mpath = cache_paths(a)
+    meta = json.load(open(mpath)) if os.path.exists(mpath) and os.path.exists(ipath) else None
+    t0 = time.time()
+    if meta:
+        index = ivf.IVF.load(ipath)
+        log(f"index loaded from cache in {time.time() - t0:.1f}s")
+    else:
+        cfg = ivf.QuantizeConfig(avg_bits=a.bits, enable_segmentation=True)
+        index = ivf.IVF(a.n, a.dim, a.clusters, cfg)
+        index.set_variance(wl.variance)
+        index.construct(wl.x, wl.centroids.cpu().numpy(), wl.cids.cpu().numpy().astype(np.uint32), seed=1)
+        torch.cuda.synchronize()
+        build_s = time.time() - t0
+        log(f"index built on the GPU in {build_s:.1f}s plan={index.info()['plan']}")
+        gt = workloads.ground_truth(wl.x, wl.q[: a.gt_queries], a.topk)
+        np.save(os.path.join(cdir, "gt.npy"), gt)
+        # nprobe: smallest on the grid reaching the target recall@10
+        nprobe, rec, curve = None, None, {}
+        qg = wl.q[: a.gt_queries].contiguous()
+        for npb in NPROBE_GRID:
+            if npb > a.clusters:
+                break
+            ids = index.search(qg, a.topk, npb).cpu().numpy().view(np.uint32)
+            r = workloads.recall_at(ids, gt, a.topk)
+            curve[npb] = r
+            if r >= a.target_recall:
+                nprobe, rec = npb, r
+                break
+        if nprobe is None:
+            nprobe, rec = max(curve), curve[max(curve)]
+        index.save(ipath)
+        meta = dict(nprobe=nprobe, recall=rec, curve=curve, build_s=build_s, plan=index.info()["plan"])
+        json.dump(meta, open(mpath, "w"))
+        log(f"nprobe={nprobe} recall@{a.topk}={rec:.4f} curve={curve}")
+    meta["gt"] = np.load(os.path.join(cdir, "gt.npy"))
+    return index, ipath, meta
+
+
+def cpu_search_rate(ipath, q, topk, nprobe, seconds, threads):
+    """Oracle (CPU port of the reference search) QPS on a bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    oi = O.OracleIndex(ipath)
+    probe = q[:threads]
+    t0 = time.time()
+    oi.search(probe, topk, nprobe, threads=threads)
+    per_q = (time.time() - t0) / len(probe)
+    nsamp = int(min(len(q), max(threads, seconds / max(per_q, 1e-6))))
+    sample = q[:nsamp]
+    t0 = time.time()
+    ids = oi.search(sample, topk, nprobe, threads=threads)
+    dt = time.time() - t0
+    return nsamp / dt, nsamp, dt, ids, oi
+
+
+def main():
+    a = parse()
+    rank, world, local = dist_env()
+    if a.impl == "reference" and rank != 0:
+        return
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    log = (lambda m: print(f"[bench] {m}", file=sys.stderr, flush=True)) if rank == 0 else (lambda m: None)
+    t_start = time.time()
+    wl = build_workload(a, torch)
+    log(f"workload {wl.name} generated in {time.time() - t_start:.1f}s")
+    index, ipath, meta = get_index_and_meta(a, torch, wl, log)
+    nprobe = meta["nprobe"]
+    threads = os.cpu_count() or 1
+    config = {"workload": f"{a.n // 1_000_000}M x {a.dim}, B={a.bits:g} SAQ (segmented), {a.clusters} clusters "
+                          f"Zipf(1.1), PCA, k={a.topk}, batch {a.batch}",
+              "nprobe": nprobe, f"recall@{a.topk}": round(meta["recall"], 4), "plan": meta["plan"],
+              "l2": "flushed between timed steps (256 MiB write)", "queries": "same distribution as the base set"}
+
+    if a.impl == "reference":
+        qh = wl.q.cpu().numpy()
+        rates = []
+        for _ in range(a.warmup):
+            cpu_search_rate(ipath, qh, a.topk, nprobe, 2.0, threads)
+        step_q = None
+        times = []
+        for _ in range(a.steps):
+            r, ns, dt, _, _ = cpu_search_rate(ipath, qh, a.topk, nprobe, 3.0, threads)
+            rates.append(r)
+            times.append(dt)
+            step_q = ns
+        v = float(sum(step_q for _ in rates) / sum(times))
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "queries/s", "n_gpus": world,
+                "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32",
+                "data": "synthetic (seeded, generated on the GPU)", "config": config,
+                "cpu_baseline": {"value": v, "unit": "queries/s", "cores": threads, "kind": "port",
+                                 "sample": f"{step_q} queries per step on the same 10M index"},
+                "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    from saq_gb300 import _native as N, ivf
+    import ctypes as C
+    lib = index.lib
+    stream = torch.cuda.current_stream()
+    sptr = C.c_void_p(stream.cuda_stream)
+    scfg = ivf.SearcherConfig().to_c()
+    B = a.batch
+    qdev = wl.q[:B].contiguous()
+    ids = torch.empty((B, a.topk), dtype=torch.int32, device="cuda")
+    dd = torch.empty((B, a.topk), dtype=torch.float32, device="cuda")
+    probes = torch.empty((B, nprobe), dtype=torch.int32, device="cuda")
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    stats = N.SearchStats()
+
+    def batched(with_stats):
+        N.check(lib.saqg_search_ex(index._h, qdev.data_ptr(), B, a.topk, nprobe, C.byref(scfg), ids.data_ptr(),
+                                   dd.data_ptr(), N.SAQG_MEM_DEVICE, sptr,
+                                   C.byref(stats) if with_stats else None,
+                                   probes.data_ptr() if with_stats else None))
+
+    # ---- batched, device-resident (value) ----
+    for _ in range(a.warmup):
+        batched(True)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms, scan_ms, fast_b, rr_b, spec, rr = [], [], [], [], [], []
+    launches0 = lib.saqg_kernel_launches()
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        for _ in range(a.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            batched(True)
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            scan_ms.append(stats.ms_scan)
+            fast_b.append(stats.fast_bytes)
+            rr_b.append(stats.rerank_bytes)
+            spec.append(stats.speculative)
+            rr.append(stats.reranked)
+        torch.cuda.synchronize()
+    launches = lib.saqg_kernel_launches() - launches0
+    tot_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([tot_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    value = world * B * a.steps / (tot_ms / 1e3)
+    got = ids.cpu().numpy().view(np.uint32)
+    from saq_gb300 import workloads
+    gt = meta["gt"]
+    ng = min(len(gt), B)
+    batch_recall = workloads.recall_at(got[:ng], gt[:ng], a.topk)
+
+    # compulsory bytes: each distinct probed cluster once + every re-rank
+    info = index.info()
+    sizes = np.bincount(wl.cids.cpu().numpy(), minlength=a.clusters)
+    nblk = (sizes + 31) // 32
+    per_lane = sum(4 + (d // 8 if b else 0) for d, b in info["plan"])
+    distinct = np.unique(probes.cpu().numpy())
+    compulsory = int((nblk[distinct] * 32 * per_lane).sum() + len(distinct) * 4 * a.dim + rr_b[-1])
+    effective = fast_b[-1] + rr_b[-1]
+    mean_scan = float(np.mean(scan_ms))
+    hbm, peak_kind = peaks()
+    achieved = compulsory / (mean_scan / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "k_scan_traffic.json")
+    if os.path.exists(tf):
+        tj = json.load(open(tf))
+        if tj.get("workload") == config["workload"] and tj.get("nprobe") == nprobe:
+            traffic = tj.get("dram_bytes_per_launch")
+
+    # ---- e2e: host buffers through the C ABI ----
+    qh = torch.empty((B, a.dim), dtype=torch.float32).pin_memory()
+    qh.copy_(qdev.cpu())
+    ih = torch.empty((B, a.topk), dtype=torch.int32).pin_memory()
+    dh = torch.empty((B, a.topk), dtype=torch.float32).pin_memory()
+    for _ in range(max(1, a.warmup)):
+        N.check(lib.saqg_search(index._h, qh.data_ptr(), B, a.topk, nprobe, C.byref(scfg), ih.data_ptr(),
+                                dh.data_ptr(), N.SAQG_MEM_HOST, sptr))
+    e2e_ms = []
+    for _ in range(a.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        N.check(lib.saqg_search(index._h, qh.data_ptr(), B, a.topk, nprobe, C.byref(scfg), ih.data_ptr(),
+                                dh.data_ptr(), N.SAQG_MEM_HOST, sptr))
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_v = world * B * a.steps / (sum(e2e_ms) / 1e3)
+
+    # ---- plain single-query drop-in ----
+    P = a.plain_queries
+    qp = wl.q[:P].contiguous()
+    lat = []
+    for i in range(min(8, P)):
+        N.check(lib.saqg_search(index._h, qp[i].data_ptr(), 1, a.topk, nprobe, C.byref(scfg), ids.data_ptr(),
+                                dd.data_ptr(), N.SAQG_MEM_DEVICE, sptr))
+    torch.cuda.synchronize()
+    for i in range(P):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        N.check(lib.saqg_search(index._h, qp[i].data_ptr(), 1, a.topk, nprobe, C.byref(scfg), ids.data_ptr(),
+                                dd.data_ptr(), N.SAQG_MEM_DEVICE, sptr))
+        e1.record(stream)
+        e1.synchronize()
+        lat.append(e0.elapsed_time(e1))
+    lat = np.array(lat)
+    plain_qps = P / (lat.sum() / 1e3)
+
+    # ---- CPU baseline (oracle port) on a bounded sample ----
+    cpu = None
+    if rank == 0:
+        qnp = wl.q.cpu().numpy()
+        r, ns, dt, cids_cpu, _ = cpu_search_rate(ipath, qnp, a.topk, nprobe, a.cpu_seconds, threads)
+        same = bool(np.array_equal(cids_cpu[:min(ns, B)], got[:min(ns, B)]))
+        cpu = {"value": r, "unit": "queries/s", "cores": threads, "kind": "port",
+               "sample": f"{ns} queries of the batch on the same index ({dt:.1f}s, {threads} threads)",
+               "ids_equal_gpu": same}
+
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": tot_ms / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic (seeded, generated on the GPU)",
+        "config": config,
+        "batched": {"qps": value, "batch": B, "p50_ms": float(np.median(step_ms)),
+                    "p99_ms": float(np.percentile(step_ms, 99)), f"recall@{a.topk}": round(batch_recall, 4)},
+        "plain": {"qps": plain_qps, "queries": P, "p50_ms": float(np.median(lat)),
+                  "p99_ms": float(np.percentile(lat, 99))},
+        "batched_over_plain": value / world / plain_qps,
+        "p99_ms": float(np.percentile(lat, 99)),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "kernel": "k_scan", "peak_kind": peak_kind,
+                     "bytes_per_launch": compulsory, "effective_bytes_per_launch": effective,
+                     "effective_gbs": effective / (mean_scan / 1e3) / 1e9, "scan_ms": mean_scan,
+                     "reranked_per_query": float(np.mean(rr)) / B, "speculative_per_query": float(np.mean(spec)) / B},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_v, "unit": "queries/s", "h2d_bytes_per_step": B * a.dim * 4,
+                "d2h_bytes_per_step": B * a.topk * 8},
+        "clocks": clocks,
+        "gpu_launches": int(launches),
+        "wall_s": time.time() - t_start,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -103,6 +103,30 @@ int saqg_index_construct(const float *data, int64_t n, int64_t dim, const float 
 int saqg_search(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
                 const saqg_searcher_config *cfg, uint32_t *ids, float *dists, int mem, void *stream);
 
+/* Measurements of one saqg_search_ex call (the counterpart of the reference's
+ * QueryRuntimeMetrics, caq_estimator.hpp:21-25, summed over the batch).
+ * Kernel times come from CUDA events on the call's stream. */
+typedef struct saqg_search_stats {
+    float ms_probe;        /* centroid distances + nprobe selection */
+    float ms_qprep;        /* prune bounds + query rotation */
+    float ms_scan;         /* the cluster scan (FastScan + re-rank + top-k) */
+    float ms_total;        /* first to last kernel */
+    int64_t probes;        /* (query, cluster) pairs scanned */
+    int64_t blocks;        /* 32-vector blocks scanned */
+    int64_t vectors;       /* vectors scanned */
+    int64_t reranked;      /* vectors whose accurate distance the reference evaluates */
+    int64_t speculative;   /* accurate distances evaluated (a superset of `reranked`) */
+    int64_t fast_bytes;    /* algorithmic bytes of the scan: 1-bit codes, |o| factors, centroids */
+    int64_t rerank_bytes;  /* algorithmic bytes of the re-rank: ex-codes, ex factors, ids */
+} saqg_search_stats;
+
+/* saqg_search plus measurements: `stats` (may be NULL) and `probes` (may be
+ * NULL; nq x nprobe probed cluster ids in probe order, memory per `mem`).
+ * With stats the call synchronises its stream before returning. */
+int saqg_search_ex(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
+                   const saqg_searcher_config *cfg, uint32_t *ids, float *dists, int mem, void *stream,
+                   saqg_search_stats *stats, uint32_t *probes);
+
 /* IVF::estimate<L2Sqr> (index/ivf.hpp:313-362) for one query: every vector of
  * the `nprobe` probed clusters, in probe order, with its accurate, fast and
  * variance-bound estimates.  Host outputs of capacity `cap`; *count receives

@@ -33,6 +33,15 @@ class IndexInfo(C.Structure):
                 ("seg_dim", C.c_int32 * 16), ("seg_bits", C.c_int32 * 16), ("device_bytes", I64)]
 
 
+class SearchStats(C.Structure):
+    _fields_ = [("ms_probe", C.c_float), ("ms_qprep", C.c_float), ("ms_scan", C.c_float), ("ms_total", C.c_float),
+                ("probes", I64), ("blocks", I64), ("vectors", I64), ("reranked", I64), ("speculative", I64),
+                ("fast_bytes", I64), ("rerank_bytes", I64)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class SaqgError(RuntimeError):
     pass
 
@@ -51,6 +60,8 @@ EXPORTS = {
                                        C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.POINTER(C.c_void_p)]),
     "saqg_search": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig), C.c_void_p,
                               C.c_void_p, C.c_int, C.c_void_p]),
+    "saqg_search_ex": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig), C.c_void_p,
+                                 C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "saqg_estimate": (C.c_int, [C.c_void_p, C.c_void_p, I64, C.POINTER(SearcherConfig), C.c_void_p, C.c_void_p,
                                 C.c_void_p, C.c_void_p, I64, C.POINTER(I64)]),
     "saqg_plan": (C.c_int, [C.c_void_p, I64, C.c_float, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,

@@ -115,6 +115,18 @@ int saqg_search(const saqg_index *index, const float *queries, int64_t nq, int64
     });
 }
 
+int saqg_search_ex(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
+                   const saqg_searcher_config *cfg, uint32_t *ids, float *dists, int mem, void *stream,
+                   saqg_search_stats *stats, uint32_t *probes) {
+    return guarded([&] {
+        SAQG_REQUIRE(index && queries && ids, "null argument");
+        SAQG_REQUIRE(mem == SAQG_MEM_HOST || mem == SAQG_MEM_DEVICE, "mem must be SAQG_MEM_HOST or SAQG_MEM_DEVICE");
+        SAQG_REQUIRE(!cfg || cfg->dist_type == SAQG_DIST_L2, "only L2 search is supported");
+        const float m = cfg ? cfg->searcher_vars_bound_m : 4.0f;
+        run_search(*index->impl, queries, nq, topk, nprobe, m, ids, dists, mem, (cudaStream_t)stream, stats, probes);
+    });
+}
+
 int saqg_estimate(const saqg_index *index, const float *query_host, int64_t nprobe, const saqg_searcher_config *cfg,
                   uint32_t *ids, float *acc, float *fast, float *vars, int64_t cap, int64_t *count) {
     return guarded([&] {

@@ -479,13 +479,14 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
                                                        const float *__restrict__ qrot_all,
                                                        const float *__restrict__ prune_all, int topk,
                                                        uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
-                                                       int *__restrict__ err) {
+                                                       int *__restrict__ err, unsigned long long *__restrict__ counters) {
     extern __shared__ __align__(16) char smem_raw[];
     const int S = ix.S;
     ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, topk);
     __shared__ int pool_size;
     __shared__ float distk;
     const int qi = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    unsigned long long c_blocks = 0, c_vecs = 0, c_rr = 0, c_spec = 0;  // thread 0's tallies
     const float *qrot = qrot_all + (size_t)qi * ix.Dtot;
     const float *prune = prune_all + (size_t)qi * S;
     for (int i = tid; i <= topk; i += kScanThreads) {
@@ -502,6 +503,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
         prepare_cluster(ix, qrot, prune, c, sm);
         const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
         const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
+        c_blocks += nb;
+        c_vecs += n;
         for (int t0 = 0; t0 < nb; t0 += kScanWarps) {
             const int b = t0 + w;
             const bool active = b < nb;
@@ -555,6 +558,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
             __syncthreads();
             // exact replay of the reference's sequential decisions
             if (tid == 0) {
+                for (int i = 0; i < kScanWarps; ++i) c_spec += __popc(sm.cmask[i]);
                 float dk = distk;
                 int sz = pool_size;
                 for (int ww = 0; ww < kScanWarps && t0 + ww < nb; ++ww) {
@@ -568,6 +572,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
                             const int j = __ffs(mask) - 1;
                             mask &= mask - 1;
                             if (!((cm >> j) & 1u)) *err = 1;
+                            ++c_rr;
                             pool_insert(sm.pool_id, sm.pool_d, sz, topk, ix.ids[v0 + (int64_t)bb * 32 + j],
                                         sm.part[ww * 32 + j]);
                             dk = sz == topk ? sm.pool_d[sz - 1] : FLT_MAX;
@@ -578,6 +583,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
                             if (!(sm.cur[ww * 32 + j] < dk)) continue;
                             if (bb * 32 + j >= n) break;
                             if (!((cm >> j) & 1u)) *err = 1;
+                            ++c_rr;
                             float acc = sm.cur[ww * 32 + j];
                             for (int s = 0; s < S; ++s) {
                                 acc = __fadd_rn(acc, sm.part[(ww * S + s) * 32 + j]);
@@ -593,6 +599,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
             }
             __syncthreads();
         }
+    }
+    if (tid == 0 && counters) {
+        atomicAdd(counters + 0, c_blocks);
+        atomicAdd(counters + 1, c_vecs);
+        atomicAdd(counters + 2, c_rr);
+        atomicAdd(counters + 3, c_spec);
     }
     for (int i = tid; i < topk; i += kScanThreads) {
         out_ids[(size_t)qi * topk + i] = sm.pool_id[i];
@@ -697,7 +709,7 @@ void check_launch(const char *what) {
 }  // namespace
 
 void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,
-                float *dists, int mem, cudaStream_t st) {
+                float *dists, int mem, cudaStream_t st, saqg_search_stats *stats, uint32_t *probes_out) {
     SAQG_REQUIRE(nq >= 0 && topk >= 1 && topk <= kMaxTopK, "topk must be in [1, 4096]");
     SAQG_REQUIRE(nprobe >= 1 && nprobe <= I.K, "nprobe must be in [1, number of clusters]");
     if (nq == 0) return;
@@ -714,33 +726,52 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
     uint32_t *oid = bp.take<uint32_t>((size_t)nq * topk);
     float *od = bp.take<float>((size_t)nq * topk);
     int *flags = bp.take<int>(16);
+    unsigned long long *counters = bp.take<unsigned long long>(8);
+    cudaEvent_t ev[5] = {};
+    if (stats)
+        for (auto &e : ev) SAQG_CUDA_TRY(cudaEventCreate(&e));
+    struct EvGuard {
+        cudaEvent_t *e;
+        ~EvGuard() {
+            for (int i = 0; i < 5; ++i)
+                if (e[i]) cudaEventDestroy(e[i]);
+        }
+    } evg{ev};
     const float *qin = q;
     if (host) {
         SAQG_CUDA_TRY(cudaMemcpyAsync(dq, q, 4 * (size_t)nq * I.D, cudaMemcpyHostToDevice, st));
         qin = dq;
     }
     SAQG_CUDA_TRY(cudaMemsetAsync(flags, 0, 64, st));
+    if (stats) SAQG_CUDA_TRY(cudaMemsetAsync(counters, 0, 64, st));
     {
         const int wpb = 8;
         dim3 grid((unsigned)((I.K + wpb - 1) / wpb), (unsigned)nq);
+        if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[0], st));
         k_probe_dist<<<grid, wpb * 32, 0, st>>>(ix, qin, dist);
         check_launch("k_probe_dist");
         k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, work, flags);
         check_launch("k_probe_select");
+        if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[1], st));
         size_t qsm = 0;
         for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
         k_qprep<<<dim3((unsigned)ix.S, (unsigned)nq), 256, qsm, st>>>(ix, qin, m, qrot, prune);
         check_launch("k_qprep");
+        if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[2], st));
         const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, (int)topk);
         SAQG_REQUIRE(smem <= 220 * 1024, "dimension / topk too large for the scan kernel's shared memory");
         SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         uint32_t *ids_out = host ? oid : ids;
         float *d_out = host ? od : dists;
         k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ids_out,
-                                                          d_out, flags + 1);
+                                                          d_out, flags + 1, stats ? counters : nullptr);
         check_launch("k_scan");
+        if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[3], st));
         count_launch(4);
     }
+    if (probes_out)
+        SAQG_CUDA_TRY(cudaMemcpyAsync(probes_out, probe, 4 * (size_t)nq * nprobe,
+                                      host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
     if (host) {
         SAQG_CUDA_TRY(cudaMemcpyAsync(ids, oid, 4 * (size_t)nq * topk, cudaMemcpyDeviceToHost, st));
         if (dists) SAQG_CUDA_TRY(cudaMemcpyAsync(dists, od, 4 * (size_t)nq * topk, cudaMemcpyDeviceToHost, st));
@@ -748,6 +779,35 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         SAQG_CUDA_TRY(cudaMemcpyAsync(hflags, flags, 8, cudaMemcpyDeviceToHost, st));
         SAQG_CUDA_TRY(cudaStreamSynchronize(st));
         if (hflags[1]) throw Error{SAQG_ERR_INTERNAL, "scan replay met a lane without a precomputed distance"};
+    }
+    if (stats) {
+        unsigned long long hc[4] = {0, 0, 0, 0};
+        SAQG_CUDA_TRY(cudaMemcpyAsync(hc, counters, 32, cudaMemcpyDeviceToHost, st));
+        SAQG_CUDA_TRY(cudaStreamSynchronize(st));
+        float t01 = 0, t12 = 0, t23 = 0, t03 = 0;
+        SAQG_CUDA_TRY(cudaEventElapsedTime(&t01, ev[0], ev[1]));
+        SAQG_CUDA_TRY(cudaEventElapsedTime(&t12, ev[1], ev[2]));
+        SAQG_CUDA_TRY(cudaEventElapsedTime(&t23, ev[2], ev[3]));
+        SAQG_CUDA_TRY(cudaEventElapsedTime(&t03, ev[0], ev[3]));
+        stats->ms_probe = t01;
+        stats->ms_qprep = t12;
+        stats->ms_scan = t23;
+        stats->ms_total = t03;
+        stats->probes = nq * nprobe;
+        stats->blocks = (int64_t)hc[0];
+        stats->vectors = (int64_t)hc[1];
+        stats->reranked = (int64_t)hc[2];
+        stats->speculative = (int64_t)hc[3];
+        // SURVEY-style algorithmic bytes: per scanned block 32 lanes of 1-bit codes of
+        // every coded segment and |o| of every segment; per probe the rotated centroid;
+        // per re-ranked vector its ex-codes, ex factors and id.
+        int64_t per_lane = 0, per_rr = 4;
+        for (int s = 0; s < ix.S; ++s) {
+            per_lane += 4 + (ix.seg[s].bits ? ix.seg[s].dim / 8 : 0);
+            per_rr += ix.seg[s].pv + 8;
+        }
+        stats->fast_bytes = stats->blocks * 32 * per_lane + stats->probes * 4 * (int64_t)ix.Dtot;
+        stats->rerank_bytes = stats->reranked * per_rr;
     }
 }
 

@@ -1,0 +1,130 @@
+"""Seeded synthetic workloads with the shapes of the SAQ benchmark configurations,
+generated on the GPU (torch), plus exact ground truth.
+
+Public datasets are not available, so each workload is a seeded stand-in with
+the configuration's sizes and value distributions:
+
+  zipf_aniso (10M x 1024, 16,384 clusters): unit-norm vectors with an
+      anisotropic spectrum (random orthogonal basis, per-axis variance ~
+      i^-alpha); cluster centres from the same spectrum, cluster sizes
+      ~ rank^-1.1 (Zipf); point = normalise(centre + sigma * noise).  The
+      cluster index is the IVF cluster id; centroids are the cluster means.
+  PCA: mean-centred, components by descending eigenvalue (the reference's
+      python/pca.py workflow), applied to base, queries and centroids.
+
+Queries follow the base distribution (their clusters drawn with the same
+Zipf weights).  Ground truth is exact: an FP32 shortlist followed by an FP64
+re-rank.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from .data import zipf_sizes
+
+
+@dataclass
+class Workload:
+    name: str
+    x: torch.Tensor          # n x d float32, cuda (PCA-transformed)
+    q: torch.Tensor          # nq x d float32, cuda (PCA-transformed)
+    centroids: torch.Tensor  # k x d float32, cuda
+    cids: torch.Tensor       # n int64, cuda
+    variance: np.ndarray     # d float32 (column variance of x)
+    sizes: np.ndarray        # k cluster sizes
+
+
+def _spectrum(d, alpha, dev):
+    return torch.arange(1, d + 1, device=dev, dtype=torch.float64).pow(-alpha / 2).float()
+
+
+def zipf_aniso(n: int, d: int, k: int, nq: int, s: float = 1.1, alpha: float = 0.8, sigma: float = 0.2,
+               seed: int = 0, device: str = "cuda", chunk: int = 1 << 20) -> Workload:
+    torch.backends.cuda.matmul.allow_tf32 = False
+    dev = torch.device(device)
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    basis, _ = torch.linalg.qr(torch.randn(d, d, generator=g, device=dev, dtype=torch.float64))
+    basis = basis.float()
+    scale = _spectrum(d, alpha, dev)
+    centers = (torch.randn(k, d, generator=g, device=dev) * scale) @ basis.T
+    centers = centers / centers.norm(dim=1, keepdim=True)
+    sizes = zipf_sizes(n, k, s)
+    labels = torch.repeat_interleave(torch.arange(k, device=dev), torch.as_tensor(sizes, device=dev))
+    labels = labels[torch.randperm(n, generator=g, device=dev)]
+
+    def draw(lab):
+        out = torch.empty(lab.numel(), d, device=dev)
+        for a in range(0, lab.numel(), chunk):
+            b = min(lab.numel(), a + chunk)
+            z = (torch.randn(b - a, d, generator=g, device=dev) * scale) @ basis.T
+            v = centers[lab[a:b]] + sigma * z
+            out[a:b] = v / v.norm(dim=1, keepdim=True)
+        return out
+
+    x = draw(labels)
+    w = torch.as_tensor(sizes / sizes.sum(), device=dev, dtype=torch.float64)
+    qlab = torch.multinomial(w, nq, replacement=True, generator=g)
+    q = draw(qlab)
+    # PCA over (a sample of) the base set
+    samp = x[torch.randperm(n, generator=g, device=dev)[: min(n, 1 << 20)]].double()
+    mean = samp.mean(0)
+    xc = samp - mean
+    cov = xc.T @ xc / samp.shape[0]
+    evals, evecs = torch.linalg.eigh(cov)
+    comp = evecs[:, torch.argsort(evals, descending=True)].T.float().contiguous()
+    meanf = mean.float()
+    del samp, xc, cov
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        x[a:b] = (x[a:b] - meanf) @ comp.T
+    q = (q - meanf) @ comp.T
+    # centroids: cluster means; variance: column variance of the base set
+    sums = torch.zeros(k, d, device=dev, dtype=torch.float64)
+    sumsq = torch.zeros(d, device=dev, dtype=torch.float64)
+    colsum = torch.zeros(d, device=dev, dtype=torch.float64)
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        xb = x[a:b].double()
+        sums.index_add_(0, labels[a:b], xb)
+        colsum += xb.sum(0)
+        sumsq += (xb * xb).sum(0)
+    cnt = torch.as_tensor(sizes, device=dev, dtype=torch.float64).clamp(min=1).unsqueeze(1)
+    cent = (sums / cnt).float()
+    var = (sumsq / n - (colsum / n) ** 2).float().cpu().numpy()
+    return Workload(f"zipf_aniso_{n}x{d}_k{k}", x, q.contiguous(), cent, labels, var, sizes)
+
+
+@torch.no_grad()
+def ground_truth(x: torch.Tensor, q: torch.Tensor, k: int, shortlist: int = 200, chunk: int = 1 << 21):
+    """Exact FP64 top-k (L2) for each query: FP32 shortlist, FP64 re-rank."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = x.shape[0]
+    best_d = torch.full((q.shape[0], shortlist), math.inf, device=q.device)
+    best_i = torch.zeros((q.shape[0], shortlist), dtype=torch.int64, device=q.device)
+    qn = (q * q).sum(1, keepdim=True)
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        xb = x[a:b]
+        d = qn - 2.0 * q @ xb.T + (xb * xb).sum(1)[None, :]
+        vals, idx = torch.topk(d, min(shortlist, b - a), dim=1, largest=False)
+        cat_d = torch.cat([best_d, vals], 1)
+        cat_i = torch.cat([best_i, idx + a], 1)
+        o = torch.topk(cat_d, shortlist, dim=1, largest=False).indices
+        best_d = torch.gather(cat_d, 1, o)
+        best_i = torch.gather(cat_i, 1, o)
+    cand = x[best_i.reshape(-1)].double().reshape(q.shape[0], shortlist, -1)
+    d64 = ((cand - q.double()[:, None, :]) ** 2).sum(-1)
+    order = torch.argsort(d64, dim=1, stable=True)[:, :k]
+    return torch.gather(best_i, 1, order).cpu().numpy()
+
+
+def recall_at(found: np.ndarray, gt: np.ndarray, k: int) -> float:
+    hit = 0
+    for f, g_ in zip(found, gt):
+        hit += len(set(f[:k].tolist()) & set(g_[:k].tolist()))
+    return hit / (k * len(gt))
