@@ -33,7 +33,7 @@ constexpr int kScanThreads = kScanWarps * 32;
 constexpr int kMaxTopK = 4096;
 
 struct SegScal {
-    float delta, sum_vl, sum_q, q_l2sqr, q_l2norm, c1, c2, vfac;
+    float delta, vl, sum_vl, sum_q, q_l2sqr, q_l2norm, c1, c2, vfac;
 };
 
 __device__ __forceinline__ uint32_t fkey(float f) {
@@ -242,55 +242,18 @@ __global__ void k_qprep(DevIndexView ix, const float *__restrict__ q, float m, f
 }
 
 // ------------------------------------------------------------------ LUT
-// Lut::prepare for one segment, by one warp (lut.hpp:60-87, fastscan.hpp:236-248).
-__device__ void build_lut(const float *__restrict__ qres, int dim, uint16_t *__restrict__ lut, SegScal &sc, float prune) {
-    const int lane = threadIdx.x & 31;
-    const float sum_q = warp_eigen_sum(dim, [&](int i) { return qres[i]; });
-    const float q2 = warp_eigen_sum(dim, [&](int i) { return __fmul_rn(qres[i], qres[i]); });
-    const int ncb = dim / 4;
-    float vl = FLT_MAX, vr = -FLT_MAX;
-    for (int cb = lane; cb < ncb; cb += 32) {
-        const float *qq = qres + cb * 4;
-        float t[16];
-        t[0] = 0.0f;
+__device__ __forceinline__ float key_to_float(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// 16 float LUT entries of one 4-dim codebook: fastscan::pack_lut (fastscan.hpp:236-248),
+// entry j = entry[j - lowbit(j)] + q[kPos[j]].
+__device__ __forceinline__ void lut_entries(const float *__restrict__ qq, float *t) {
+    t[0] = 0.0f;
 #pragma unroll
-        for (int j = 1; j < 16; ++j) {
-            const int lb = j & -j, pos = lb == 1 ? 3 : lb == 2 ? 2 : lb == 4 ? 1 : 0;  // kPos[j] (fastscan.hpp:22-39)
-            t[j] = __fadd_rn(t[j - (j & -j)], qq[pos]);
-        }
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            vl = fminf(vl, t[j]);
-            vr = fmaxf(vr, t[j]);
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        vl = fminf(vl, __shfl_xor_sync(kFull, vl, o));
-        vr = fmaxf(vr, __shfl_xor_sync(kFull, vr, o));
-    }
-    const float delta = (float)__ddiv_rn((double)__fsub_rn(vr, vl), 65536.0 - 0.01);
-    for (int cb = lane; cb < ncb; cb += 32) {
-        const float *qq = qres + cb * 4;
-        float t[16];
-        t[0] = 0.0f;
-#pragma unroll
-        for (int j = 1; j < 16; ++j) {
-            const int lb = j & -j, pos = lb == 1 ? 3 : lb == 2 ? 2 : lb == 4 ? 1 : 0;
-            t[j] = __fadd_rn(t[j - (j & -j)], qq[pos]);
-        }
-#pragma unroll
-        for (int j = 0; j < 16; ++j) lut[cb * 16 + j] = (uint16_t)(int)__fdiv_rn(__fsub_rn(t[j], vl), delta);
-    }
-    if (lane == 0) {
-        sc.delta = delta;
-        sc.sum_vl = (float)__dmul_rn(__dadd_rn((double)vl, __dmul_rn(0.5, (double)delta)), (double)(float)ncb);
-        sc.sum_q = sum_q;
-        sc.q_l2sqr = q2;
-        sc.q_l2norm = sqrtf(q2);
-        sc.c1 = (float)__dsub_rn(__dmul_rn(0.5, (double)sum_q), (double)__fmul_rn(0.58f, sc.q_l2norm));
-        const float one_over_sqrtD = (float)__ddiv_rn(1.0, (double)sqrtf((float)dim));
-        sc.c2 = __fmul_rn(__fdiv_rn(4.0f, 0.8f), one_over_sqrtD);
-        sc.vfac = __fsub_rn(q2, __fmul_rn(2.0f, prune));
+    for (int j = 1; j < 16; ++j) {
+        const int lb = j & -j, pos = lb == 1 ? 3 : lb == 2 ? 2 : lb == 4 ? 1 : 0;  // kPos[j] (fastscan.hpp:22-39)
+        t[j] = __fadd_rn(t[j - lb], qq[pos]);
     }
 }
 
@@ -349,6 +312,14 @@ __device__ __forceinline__ void pool_insert(uint32_t *ids, float *d, int &size, 
     size += (size < cap);
 }
 
+// Copies one vector's ex-code (lstride bytes, 16-byte aligned rows) into a
+// half-warp's shared buffer with coalesced 16-byte loads.
+__device__ __forceinline__ void stage_excode(const uint8_t *__restrict__ src, int lstride, uint8_t *dst, int l) {
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+    for (int o = l; o < lstride / 16; o += 16) d4[o] = __ldg(s4 + o);
+}
+
 // ------------------------------------------------------------------ scan
 struct ScanSmem {
     // laid out in dynamic shared memory by scan_smem_layout()
@@ -360,12 +331,17 @@ struct ScanSmem {
     int *nstage;
     uint32_t *pool_id;
     float *pool_d;
+    uint32_t *mm;     // per segment LUT min / max keys
+    uint8_t *xbuf;    // per half-warp ex-code staging
+    int xstride;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
-__host__ __device__ inline size_t scan_smem_bytes(int Dtot, int S, int topk) {
+__host__ __device__ inline size_t scan_smem_bytes(int Dtot, int S, int topk, int xstride) {
     size_t b = 0;
+    b += align16(sizeof(uint32_t) * 2 * S);
+    b += align16((size_t)2 * kScanWarps * xstride);
     b += align16(sizeof(uint16_t) * 4 * (size_t)Dtot);
     b += align16(sizeof(float) * Dtot);
     b += align16(sizeof(SegScal) * S);
@@ -379,9 +355,14 @@ __host__ __device__ inline size_t scan_smem_bytes(int Dtot, int S, int topk) {
     return b;
 }
 
-__device__ ScanSmem scan_smem_layout(char *base, int Dtot, int S, int topk) {
+__device__ ScanSmem scan_smem_layout(char *base, int Dtot, int S, int topk, int xstride) {
     ScanSmem s;
     size_t o = 0;
+    s.mm = (uint32_t *)(base + o);
+    o += align16(sizeof(uint32_t) * 2 * S);
+    s.xbuf = (uint8_t *)(base + o);
+    s.xstride = xstride;
+    o += align16((size_t)2 * kScanWarps * xstride);
     s.lut = (uint16_t *)(base + o);
     o += align16(sizeof(uint16_t) * 4 * (size_t)Dtot);
     s.qres = (float *)(base + o);
@@ -408,19 +389,83 @@ __device__ ScanSmem scan_smem_layout(char *base, int Dtot, int S, int topk) {
     return s;
 }
 
-// Prepares the LUTs and scalars of every segment for cluster c.
+// Lut::prepare (lut.hpp:60-87) for every segment of cluster c, spread over the
+// whole CTA: residual query, its Eigen-order sum and squared norm, the float
+// LUT's min / max, delta = (max-min)/(65536-0.01) in double, the u16 LUT
+// trunc((entry-min)/delta), and the epilogue constants of compFastIP.
 __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict__ qrot, const float *__restrict__ prune,
                                 int c, ScanSmem &sm) {
-    for (int i = threadIdx.x; i < ix.Dtot; i += blockDim.x) {
+    const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
+    const int S = ix.S;
+    for (int i = tid; i < ix.Dtot; i += nt) {
         int s = 0;
-        while (s + 1 < ix.S && i >= ix.seg[s + 1].qoff) ++s;
+        while (s + 1 < S && i >= ix.seg[s + 1].qoff) ++s;
         const SegDev &g = ix.seg[s];
         sm.qres[i] = __fsub_rn(qrot[i], g.cent[(size_t)c * g.dim + (i - g.qoff)]);
     }
+    if (tid < S) {
+        sm.mm[2 * tid] = 0xffffffffu;  // min key
+        sm.mm[2 * tid + 1] = 0u;       // max key
+    }
     __syncthreads();
-    const int warp = threadIdx.x >> 5;
-    for (int s = warp; s < ix.S; s += kScanWarps)
-        build_lut(sm.qres + ix.seg[s].qoff, ix.seg[s].dim, sm.lut + 4 * ix.seg[s].qoff, sm.scal[s], prune[s]);
+    for (int t = warp; t < 2 * S; t += nt / 32) {
+        const int s = t >> 1;
+        const float *qr = sm.qres + ix.seg[s].qoff;
+        const float r = (t & 1) ? warp_eigen_sum(ix.seg[s].dim, [&](int i) { return __fmul_rn(qr[i], qr[i]); })
+                                : warp_eigen_sum(ix.seg[s].dim, [&](int i) { return qr[i]; });
+        if (lane == 0) {
+            if (t & 1) sm.scal[s].q_l2sqr = r;
+            else sm.scal[s].sum_q = r;
+        }
+    }
+    const int ncb_all = ix.Dtot / 4;
+    for (int cb = tid; cb < ncb_all; cb += nt) {
+        int s = 0;
+        while (s + 1 < S && cb * 4 >= ix.seg[s + 1].qoff) ++s;
+        float t[16];
+        lut_entries(sm.qres + cb * 4, t);
+        float lo = t[0], hi = t[0];
+#pragma unroll
+        for (int j = 1; j < 16; ++j) {
+            lo = fminf(lo, t[j]);
+            hi = fmaxf(hi, t[j]);
+        }
+        atomicMin(&sm.mm[2 * s], fkey(lo));
+        atomicMax(&sm.mm[2 * s + 1], fkey(hi));
+    }
+    __syncthreads();
+    if (tid < S) {
+        SegScal &sc = sm.scal[tid];
+        const int dim = ix.seg[tid].dim, ncb = dim / 4;
+        const float vl = key_to_float(sm.mm[2 * tid]), vr = key_to_float(sm.mm[2 * tid + 1]);
+        const float delta = (float)__ddiv_rn((double)__fsub_rn(vr, vl), 65536.0 - 0.01);
+        sc.delta = delta;
+        sc.vl = vl;
+        sc.sum_vl = (float)__dmul_rn(__dadd_rn((double)vl, __dmul_rn(0.5, (double)delta)), (double)(float)ncb);
+        sc.q_l2norm = sqrtf(sc.q_l2sqr);
+        sc.c1 = (float)__dsub_rn(__dmul_rn(0.5, (double)sc.sum_q), (double)__fmul_rn(0.58f, sc.q_l2norm));
+        const float one_over_sqrtD = (float)__ddiv_rn(1.0, (double)sqrtf((float)dim));
+        sc.c2 = __fmul_rn(__fdiv_rn(4.0f, 0.8f), one_over_sqrtD);
+        sc.vfac = __fsub_rn(sc.q_l2sqr, __fmul_rn(2.0f, prune[tid]));
+    }
+    __syncthreads();
+    for (int cb = tid; cb < ncb_all; cb += nt) {
+        int s = 0;
+        while (s + 1 < S && cb * 4 >= ix.seg[s + 1].qoff) ++s;
+        const float vl = sm.scal[s].vl, delta = sm.scal[s].delta;
+        float t[16];
+        lut_entries(sm.qres + cb * 4, t);
+        uint32_t packed[8];
+#pragma unroll
+        for (int j = 0; j < 16; j += 2) {
+            const uint32_t a = (uint16_t)(int)__fdiv_rn(__fsub_rn(t[j], vl), delta);
+            const uint32_t b = (uint16_t)(int)__fdiv_rn(__fsub_rn(t[j + 1], vl), delta);
+            packed[j / 2] = a | (b << 16);
+        }
+        uint4 *dst = reinterpret_cast<uint4 *>(sm.lut + cb * 16);
+        dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+    }
     __syncthreads();
 }
 
@@ -479,10 +524,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
                                                        const float *__restrict__ qrot_all,
                                                        const float *__restrict__ prune_all, int topk,
                                                        uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
-                                                       int *__restrict__ err, unsigned long long *__restrict__ counters) {
+                                                       int *__restrict__ err, unsigned long long *__restrict__ counters,
+                                                       int xstride) {
     extern __shared__ __align__(16) char smem_raw[];
     const int S = ix.S;
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, topk);
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, topk, xstride);
     __shared__ int pool_size;
     __shared__ float distk;
     const int qi = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
@@ -545,8 +591,13 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
                     const SegDev &g = ix.seg[s];
                     const float on = g.onorm[gb * 32 + j];
                     float ex = 0.0f;
-                    if (g.bits > 1)
-                        ex = excode_ip_half(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim, g.bits - 1, l, hmask);
+                    if (g.bits > 1) {
+                        uint8_t *xb = sm.xbuf + hw * sm.xstride;
+                        stage_excode(g.lcode + (size_t)gv * g.lstride, g.lstride, xb, l);
+                        __syncwarp(hmask);
+                        ex = excode_ip_half(sm.qres + g.qoff, xb, g.dim, g.bits - 1, l, hmask);
+                        __syncwarp(hmask);
+                    }
                     if (l == 0) {
                         const SegScal &sc = sm.scal[s];
                         const float acc = accurate_dist(on, sm.ipx[(ww * S + s) * 32 + j], ex, g.exfac[gv].x, g.bits,
@@ -620,10 +671,10 @@ __global__ void __launch_bounds__(kScanThreads) k_estimate(DevIndexView ix, cons
                                                            const float *__restrict__ qrot,
                                                            const float *__restrict__ prune, uint32_t *__restrict__ o_ids,
                                                            float *__restrict__ o_acc, float *__restrict__ o_fast,
-                                                           float *__restrict__ o_vars) {
+                                                           float *__restrict__ o_vars, int xstride) {
     extern __shared__ __align__(16) char smem_raw[];
     const int S = ix.S;
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, 1);
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, 1, xstride);
     const int p = blockIdx.x, c = (int)probe[p];
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     prepare_cluster(ix, qrot, prune, c, sm);
@@ -653,8 +704,12 @@ __global__ void __launch_bounds__(kScanThreads) k_estimate(DevIndexView ix, cons
                 float ex = 0.0f;
                 if (g.bits > 1) {
                     // whole warp: lanes 0-15 do the chain, 16-31 idle duplicates
-                    ex = excode_ip_half(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim, g.bits - 1, lane & 15,
-                                        (lane < 16) ? 0x0000ffffu : 0xffff0000u);
+                    const unsigned hm = (lane < 16) ? 0x0000ffffu : 0xffff0000u;
+                    uint8_t *xb = sm.xbuf + (tid >> 4) * sm.xstride;
+                    stage_excode(g.lcode + (size_t)gv * g.lstride, g.lstride, xb, lane & 15);
+                    __syncwarp(hm);
+                    ex = excode_ip_half(sm.qres + g.qoff, xb, g.dim, g.bits - 1, lane & 15, hm);
+                    __syncwarp(hm);
                     ex = __shfl_sync(kFull, ex, 0);
                 }
                 const float on = g.onorm[gb * 32 + j];
@@ -699,6 +754,12 @@ size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t np
     add(64);                                   // flags
     (void)host_io;
     return b + 256;
+}
+
+int xstride_of(const DevIndexView &ix) {
+    int m = 16;
+    for (int s = 0; s < ix.S; ++s) m = std::max(m, ix.seg[s].lstride);
+    return m;
 }
 
 void check_launch(const char *what) {
@@ -758,13 +819,14 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         k_qprep<<<dim3((unsigned)ix.S, (unsigned)nq), 256, qsm, st>>>(ix, qin, m, qrot, prune);
         check_launch("k_qprep");
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[2], st));
-        const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, (int)topk);
+        const int xs = xstride_of(ix);
+        const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs);
         SAQG_REQUIRE(smem <= 220 * 1024, "dimension / topk too large for the scan kernel's shared memory");
         SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         uint32_t *ids_out = host ? oid : ids;
         float *d_out = host ? od : dists;
         k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ids_out,
-                                                          d_out, flags + 1, stats ? counters : nullptr);
+                                                          d_out, flags + 1, stats ? counters : nullptr, xs);
         check_launch("k_scan");
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[3], st));
         count_launch(4);
@@ -853,9 +915,11 @@ int64_t run_estimate(const Index &I, const float *q_host, int64_t nprobe, float 
         SAQG_CUDA_TRY(cudaMalloc(&ofast, 4 * total));
         SAQG_CUDA_TRY(cudaMalloc(&ovars, 4 * total));
         SAQG_CUDA_TRY(cudaMemcpy(doff, off.data(), 8 * (nprobe + 1), cudaMemcpyHostToDevice));
-        const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, 1);
+        const int xs = xstride_of(ix);
+        const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
         SAQG_CUDA_TRY(cudaFuncSetAttribute(k_estimate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_estimate<<<(unsigned)nprobe, kScanThreads, smem, st>>>(ix, probe, doff, qrot, prune, oids, oacc, ofast, ovars);
+        k_estimate<<<(unsigned)nprobe, kScanThreads, smem, st>>>(ix, probe, doff, qrot, prune, oids, oacc, ofast, ovars,
+                                                                 xs);
         check_launch("k_estimate");
         count_launch(4);
         const int64_t nw = std::min(total, cap);

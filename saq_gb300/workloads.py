@@ -43,14 +43,21 @@ def _spectrum(d, alpha, dev):
 
 
 def zipf_aniso(n: int, d: int, k: int, nq: int, s: float = 1.1, alpha: float = 0.8, sigma: float = 0.2,
-               seed: int = 0, device: str = "cuda", chunk: int = 1 << 20) -> Workload:
+               noise_alpha: float | None = None, seed: int = 0, device: str = "cuda",
+               chunk: int = 1 << 20) -> Workload:
+    """Zipf-sized clusters of unit-norm vectors.  Centres follow the per-axis
+    spectrum i^-alpha; the within-cluster noise follows i^-noise_alpha
+    (default: the same spectrum)."""
     torch.backends.cuda.matmul.allow_tf32 = False
     dev = torch.device(device)
+    rng = np.random.default_rng(seed)
     g = torch.Generator(device=dev)
     g.manual_seed(seed)
-    basis, _ = torch.linalg.qr(torch.randn(d, d, generator=g, device=dev, dtype=torch.float64))
-    basis = basis.float()
+    q_, r_ = np.linalg.qr(rng.standard_normal((d, d)))
+    basis = torch.as_tensor((q_ * np.sign(np.diag(r_))[None, :]).astype(np.float32), device=dev)
     scale = _spectrum(d, alpha, dev)
+    nscale = _spectrum(d, alpha if noise_alpha is None else noise_alpha, dev)
+    nscale = nscale * (scale.norm() / nscale.norm())
     centers = (torch.randn(k, d, generator=g, device=dev) * scale) @ basis.T
     centers = centers / centers.norm(dim=1, keepdim=True)
     sizes = zipf_sizes(n, k, s)
@@ -61,40 +68,35 @@ def zipf_aniso(n: int, d: int, k: int, nq: int, s: float = 1.1, alpha: float = 0
         out = torch.empty(lab.numel(), d, device=dev)
         for a in range(0, lab.numel(), chunk):
             b = min(lab.numel(), a + chunk)
-            z = (torch.randn(b - a, d, generator=g, device=dev) * scale) @ basis.T
+            z = (torch.randn(b - a, d, generator=g, device=dev) * nscale) @ basis.T
             v = centers[lab[a:b]] + sigma * z
             out[a:b] = v / v.norm(dim=1, keepdim=True)
         return out
 
     x = draw(labels)
-    w = torch.as_tensor(sizes / sizes.sum(), device=dev, dtype=torch.float64)
+    w = torch.as_tensor(sizes / sizes.sum(), device=dev, dtype=torch.float32)
     qlab = torch.multinomial(w, nq, replacement=True, generator=g)
     q = draw(qlab)
-    # PCA over (a sample of) the base set
-    samp = x[torch.randperm(n, generator=g, device=dev)[: min(n, 1 << 20)]].double()
+    # PCA (python/pca.py): covariance of a sample in FP32 GEMMs, eigendecomposition on the host in FP64
+    samp = x[torch.randperm(n, generator=g, device=dev)[: min(n, 1 << 20)]]
     mean = samp.mean(0)
     xc = samp - mean
-    cov = xc.T @ xc / samp.shape[0]
-    evals, evecs = torch.linalg.eigh(cov)
-    comp = evecs[:, torch.argsort(evals, descending=True)].T.float().contiguous()
-    meanf = mean.float()
-    del samp, xc, cov
+    cov = (xc.T @ xc / samp.shape[0]).double().cpu().numpy()
+    evals, evecs = np.linalg.eigh(cov)
+    comp = torch.as_tensor(evecs[:, np.argsort(-evals, kind="stable")].T.astype(np.float32), device=dev)
+    del samp, xc
     for a in range(0, n, chunk):
         b = min(n, a + chunk)
-        x[a:b] = (x[a:b] - meanf) @ comp.T
-    q = (q - meanf) @ comp.T
-    # centroids: cluster means; variance: column variance of the base set
-    sums = torch.zeros(k, d, device=dev, dtype=torch.float64)
-    sumsq = torch.zeros(d, device=dev, dtype=torch.float64)
+        x[a:b] = (x[a:b] - mean) @ comp.T
+    q = (q - mean) @ comp.T
+    # IVF centroids: the generating centres in PCA coordinates
+    cent = ((centers - mean) @ comp.T).contiguous()
     colsum = torch.zeros(d, device=dev, dtype=torch.float64)
+    sumsq = torch.zeros(d, device=dev, dtype=torch.float64)
     for a in range(0, n, chunk):
         b = min(n, a + chunk)
-        xb = x[a:b].double()
-        sums.index_add_(0, labels[a:b], xb)
-        colsum += xb.sum(0)
-        sumsq += (xb * xb).sum(0)
-    cnt = torch.as_tensor(sizes, device=dev, dtype=torch.float64).clamp(min=1).unsqueeze(1)
-    cent = (sums / cnt).float()
+        colsum += x[a:b].sum(0, dtype=torch.float64)
+        sumsq += (x[a:b] * x[a:b]).sum(0, dtype=torch.float64)
     var = (sumsq / n - (colsum / n) ** 2).float().cpu().numpy()
     return Workload(f"zipf_aniso_{n}x{d}_k{k}", x, q.contiguous(), cent, labels, var, sizes)
 
