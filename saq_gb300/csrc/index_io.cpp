@@ -75,6 +75,7 @@ Index::~Index() {
     cudaSetDevice(device);
     for (void *p : allocations) cudaFree(p);
     if (scratch) cudaFree(scratch);
+    if (split_scratch) cudaFree(split_scratch);
     cudaSetDevice(cur);
 }
 
@@ -92,8 +93,26 @@ void Index::upload(void *dst, const void *src, size_t bytes) {
     if (bytes) SAQG_CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
 }
 
+static void *grow(void *&buf, size_t &have, size_t bytes) {
+    if (bytes > have) {
+        // previous work on this buffer may still be in flight on any stream
+        SAQG_CUDA_TRY(cudaDeviceSynchronize());
+        if (buf) SAQG_CUDA_TRY(cudaFree(buf));
+        buf = nullptr;
+        have = 0;
+        const size_t want = bytes + bytes / 4 + (1 << 20);
+        cudaError_t e = cudaMalloc(&buf, want);
+        if (e != cudaSuccess) throw Error{SAQG_ERR_NOMEM, std::string("scratch cudaMalloc failed: ") + cudaGetErrorString(e)};
+        have = want;
+    }
+    return buf;
+}
+
+void *Index::split_scratch_get(size_t bytes) const { return grow(split_scratch, split_scratch_bytes, bytes); }
+
 void *Index::scratch_get(size_t bytes) const {
     if (bytes > scratch_bytes) {
+        SAQG_CUDA_TRY(cudaDeviceSynchronize());
         if (scratch) SAQG_CUDA_TRY(cudaFree(scratch));
         scratch = nullptr;
         scratch_bytes = 0;

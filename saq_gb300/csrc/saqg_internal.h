@@ -98,11 +98,14 @@ struct Index {
     mutable std::mutex mu;
     mutable void *scratch = nullptr;
     mutable size_t scratch_bytes = 0;
+    mutable void *split_scratch = nullptr;
+    mutable size_t split_scratch_bytes = 0;
 
     ~Index();
     void *dalloc(size_t bytes);
     void upload(void *dst, const void *src, size_t bytes);
     void *scratch_get(size_t bytes) const;
+    void *split_scratch_get(size_t bytes) const;
 };
 
 // index_io.cpp

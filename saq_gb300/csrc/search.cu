@@ -20,6 +20,8 @@
 //                  (utils/pool.hpp:17-30) exactly in the reference's order.
 #include <cfloat>
 #include <cstdio>
+#include <cstdlib>
+#include <string>
 
 #include "device_common.cuh"
 #include "saqg_internal.h"
@@ -520,6 +522,168 @@ __device__ __forceinline__ bool stages_pass(const float *st, int n, float tau) {
     return true;
 }
 
+// Steps 1-3 of a tile of up to kScanWarps blocks (warp w <-> block t0 + w of
+// cluster c): estimates, candidate masks under `tau`, and the accurate
+// distances (multi-segment: accurate - estimate per segment) of every
+// candidate lane.  Ends with the partials in sm.part and the masks in sm.cmask.
+__device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0, int64_t v0, int nb, int n, int t0,
+                                int t_end, float tau) {
+    const int S = ix.S, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int b = t0 + w;
+    const bool active = b < t_end;
+    if (active) block_estimates(ix, b0 + b, sm, w, lane);
+    __syncthreads();
+    if (active) {
+        bool cand;
+        if (S == 1) {
+            const int cnp = (b == nb - 1) ? (n % 32) : 32;  // scanCluster's last-block count (saq_searcher.hpp:186)
+            cand = lane < cnp && sm.cd[w * 32 + lane] < tau;
+        } else {
+            cand = stages_pass(sm.stage + w * (S + 1), sm.nstage[w], tau) && sm.cur[w * 32 + lane] < tau &&
+                   (b * 32 + lane) < n;
+        }
+        const uint32_t m = __ballot_sync(kFull, cand);
+        if (lane == 0) sm.cmask[w] = m;
+    } else if (lane == 0) {
+        sm.cmask[w] = 0;
+    }
+    __syncthreads();
+    int total = 0;
+    for (int i = 0; i < kScanWarps; ++i) total += __popc(sm.cmask[i]) * S;
+    const int hw = tid >> 4, l = tid & 15;
+    const unsigned hmask = (lane < 16) ? 0x0000ffffu : 0xffff0000u;
+    for (int t = hw; t < total; t += 2 * kScanWarps) {
+        int r = t / S, s = t - r * S, ww = 0;
+        while (r >= __popc(sm.cmask[ww])) {
+            r -= __popc(sm.cmask[ww]);
+            ++ww;
+        }
+        uint32_t mk = sm.cmask[ww];
+        for (int i = 0; i < r; ++i) mk &= mk - 1;
+        const int j = __ffs(mk) - 1;
+        const int64_t gb = b0 + t0 + ww, gv = v0 + (int64_t)(t0 + ww) * 32 + j;
+        const SegDev &g = ix.seg[s];
+        const float on = g.onorm[gb * 32 + j];
+        float ex = 0.0f;
+        if (g.bits > 1) {
+            uint8_t *xb = sm.xbuf + hw * sm.xstride;
+            stage_excode(g.lcode + (size_t)gv * g.lstride, g.lstride, xb, l);
+            __syncwarp(hmask);
+            ex = excode_ip_half(sm.qres + g.qoff, xb, g.dim, g.bits - 1, l, hmask);
+            __syncwarp(hmask);
+        }
+        if (l == 0) {
+            const SegScal &sc = sm.scal[s];
+            const float acc = accurate_dist(on, sm.ipx[(ww * S + s) * 32 + j], ex, g.exfac[gv].x, g.bits, sc.sum_q,
+                                            sc.q_l2sqr);
+            sm.part[(ww * S + s) * 32 + j] = S == 1 ? acc : __fsub_rn(acc, sm.cd[(ww * S + s) * 32 + j]);
+        }
+    }
+    __syncthreads();
+}
+
+// The reference's sequential decisions for one block (single thread):
+// scanCluster's mask-then-insert (saq_searcher.hpp:185-208) or
+// searchCluster's stage checks and per-lane partial sums (saq_searcher.hpp:87-160).
+// cur: fast estimate (one segment) or running sum; part: [S][32] partials.
+__device__ __forceinline__ void replay_block(int S, int n, int nb, int bb, const float *cur, const float *stage,
+                                             int nstage, const float *part, uint32_t cm, const uint32_t *ids_v0,
+                                             uint32_t *pid, float *pd, int &sz, int topk, float &dk, int *err,
+                                             unsigned long long &c_rr) {
+    if (S == 1) {
+        const int cnp = (bb == nb - 1) ? (n % 32) : 32;
+        uint32_t mask = 0;
+        for (int j = 0; j < cnp; ++j) mask |= (uint32_t)(cur[j] < dk) << j;
+        while (mask) {
+            const int j = __ffs(mask) - 1;
+            mask &= mask - 1;
+            if (!((cm >> j) & 1u)) *err = 1;
+            ++c_rr;
+            pool_insert(pid, pd, sz, topk, ids_v0[(int64_t)bb * 32 + j], part[j]);
+            dk = sz == topk ? pd[sz - 1] : FLT_MAX;
+        }
+        return;
+    }
+    if (!stages_pass(stage, nstage, dk)) return;
+    for (int j = 0; j < 32; ++j) {
+        if (!(cur[j] < dk)) continue;
+        if (bb * 32 + j >= n) break;
+        if (!((cm >> j) & 1u)) *err = 1;
+        ++c_rr;
+        float acc = cur[j];
+        for (int s = 0; s < S; ++s) {
+            acc = __fadd_rn(acc, part[s * 32 + j]);
+            if (acc >= dk) break;
+        }
+        pool_insert(pid, pd, sz, topk, ids_v0[(int64_t)bb * 32 + j], acc);
+        dk = sz == topk ? pd[sz - 1] : FLT_MAX;
+    }
+}
+
+struct ScanTally {
+    unsigned long long blocks = 0, vecs = 0, rr = 0, spec = 0;
+};
+
+// Exact sequential scan of probes [p_begin, p_end) of one query, continuing
+// the pool held in shared memory (pool_size / distk in shared memory).
+__device__ void scan_probes(const DevIndexView &ix, const uint32_t *__restrict__ probe, int p_begin, int p_end,
+                            const float *__restrict__ qrot, const float *__restrict__ prune, int topk, ScanSmem &sm,
+                            int &pool_size, float &distk, int *err, ScanTally &tl) {
+    const int S = ix.S, tid = threadIdx.x;
+    for (int p = p_begin; p < p_end; ++p) {
+        const int c = (int)probe[p];
+        prepare_cluster(ix, qrot, prune, c, sm);
+        const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
+        const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
+        tl.blocks += nb;
+        tl.vecs += n;
+        for (int t0 = 0; t0 < nb; t0 += kScanWarps) {
+            tile_candidates(ix, sm, b0, v0, nb, n, t0, nb, distk);
+            if (tid == 0) {
+                for (int i = 0; i < kScanWarps; ++i) tl.spec += __popc(sm.cmask[i]);
+                float dk = distk;
+                int sz = pool_size;
+                for (int ww = 0; ww < kScanWarps && t0 + ww < nb; ++ww)
+                    replay_block(S, n, nb, t0 + ww, sm.cur + ww * 32, sm.stage + ww * (S + 1), sm.nstage[ww],
+                                 S == 1 ? sm.part + ww * 32 : sm.part + ww * S * 32, sm.cmask[ww], ix.ids + v0,
+                                 sm.pool_id, sm.pool_d, sz, topk, dk, err, tl.rr);
+                distk = dk;
+                pool_size = sz;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__device__ void init_pool(ScanSmem &sm, int topk, int &pool_size, float &distk) {
+    for (int i = threadIdx.x; i <= topk; i += blockDim.x) {
+        sm.pool_id[i] = 0;
+        sm.pool_d[i] = 0.0f;
+    }
+    if (threadIdx.x == 0) {
+        pool_size = 0;
+        distk = FLT_MAX;
+    }
+    __syncthreads();
+}
+
+__device__ void flush_tally(const ScanTally &tl, unsigned long long *counters) {
+    if (threadIdx.x == 0 && counters) {
+        atomicAdd(counters + 0, tl.blocks);
+        atomicAdd(counters + 1, tl.vecs);
+        atomicAdd(counters + 2, tl.rr);
+        atomicAdd(counters + 3, tl.spec);
+    }
+}
+
+__device__ void write_results(const ScanSmem &sm, int pool_size, int topk, uint32_t *out_ids, float *out_d) {
+    for (int i = threadIdx.x; i < topk; i += blockDim.x) {
+        out_ids[i] = sm.pool_id[i];
+        if (out_d) out_d[i] = i < pool_size ? sm.pool_d[i] : FLT_MAX;
+    }
+}
+
+// One CTA per query: the whole probe list sequentially.
 __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const uint32_t *__restrict__ probe, int nprobe,
                                                        const float *__restrict__ qrot_all,
                                                        const float *__restrict__ prune_all, int topk,
@@ -527,140 +691,243 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
                                                        int *__restrict__ err, unsigned long long *__restrict__ counters,
                                                        int xstride) {
     extern __shared__ __align__(16) char smem_raw[];
-    const int S = ix.S;
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, topk, xstride);
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, topk, xstride);
     __shared__ int pool_size;
     __shared__ float distk;
-    const int qi = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    unsigned long long c_blocks = 0, c_vecs = 0, c_rr = 0, c_spec = 0;  // thread 0's tallies
-    const float *qrot = qrot_all + (size_t)qi * ix.Dtot;
-    const float *prune = prune_all + (size_t)qi * S;
-    for (int i = tid; i <= topk; i += kScanThreads) {
-        sm.pool_id[i] = 0;
-        sm.pool_d[i] = 0.0f;
+    const int qi = blockIdx.x;
+    ScanTally tl;
+    init_pool(sm, topk, pool_size, distk);
+    scan_probes(ix, probe + (size_t)qi * nprobe, 0, nprobe, qrot_all + (size_t)qi * ix.Dtot, prune_all + (size_t)qi * ix.S,
+                topk, sm, pool_size, distk, err, tl);
+    flush_tally(tl, counters);
+    write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
+}
+
+// ------------------------------------------------------------------ split scan
+// For latency (one query, or a few): the nearest cluster is scanned exactly
+// first; its distk, tau1, bounds distk for the rest of the scan.  Every other
+// (probe, tile) is then processed in parallel across the GPU under tau1 and
+// leaves a record for each block with a lane that can pass; a final pass per
+// query sorts the records into scan order and replays the reference's
+// decisions.  Blocks without a record cannot insert anything (no lane is below
+// tau1 >= distk), so the replay is exact.  If a query overflows its record
+// space, its replay falls back to the full sequential scan.
+constexpr int kTileBlocks = 64;
+
+struct SplitState {
+    uint32_t *pool_id;   // [nq][topk]
+    float *pool_d;       // [nq][topk]
+    int *pool_size;      // [nq]
+    float *tau;          // [nq]
+    int *tile_off;       // [nq][nprobe + 1] tiles before probe p (probe 0 has none)
+    int *blk_base;       // [nq][nprobe] scan-order position of the probe's first block
+    int *q_tile_off;     // [nq + 1]
+    int *rec_count;      // [nq]
+    int *overflow;       // [nq]
+    float *rec;          // [nq][cap][rec_words]
+    int cap, rec_words;
+};
+
+__host__ __device__ inline int rec_words_of(int S) { return (8 + (S + 1) + 32 + 32 * S + 3) & ~3; }
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, const uint32_t *__restrict__ probe,
+                                                             int nprobe, const float *__restrict__ qrot_all,
+                                                             const float *__restrict__ prune_all, int topk,
+                                                             SplitState st, int *__restrict__ err,
+                                                             unsigned long long *__restrict__ counters, int xstride) {
+    extern __shared__ __align__(16) char smem_raw[];
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, topk, xstride);
+    __shared__ int pool_size;
+    __shared__ float distk;
+    const int qi = blockIdx.x;
+    ScanTally tl;
+    init_pool(sm, topk, pool_size, distk);
+    scan_probes(ix, probe + (size_t)qi * nprobe, 0, 1, qrot_all + (size_t)qi * ix.Dtot, prune_all + (size_t)qi * ix.S,
+                topk, sm, pool_size, distk, err, tl);
+    flush_tally(tl, counters);
+    for (int i = threadIdx.x; i < topk; i += blockDim.x) {
+        st.pool_id[(size_t)qi * topk + i] = sm.pool_id[i];
+        st.pool_d[(size_t)qi * topk + i] = sm.pool_d[i];
     }
-    if (tid == 0) {
-        pool_size = 0;
-        distk = FLT_MAX;
+    if (threadIdx.x == 0) {
+        st.pool_size[qi] = pool_size;
+        st.tau[qi] = distk;
+        st.rec_count[qi] = 0;
+        st.overflow[qi] = 0;
+        // tiles and scan-order block positions of this query's probes
+        const uint32_t *pr = probe + (size_t)qi * nprobe;
+        int tiles = 0, pos = 0;
+        for (int p = 0; p < nprobe; ++p) {
+            const int c = (int)pr[p];
+            const int nb = (int)(ix.blk_off[c + 1] - ix.blk_off[c]);
+            st.tile_off[(size_t)qi * (nprobe + 1) + p] = tiles;
+            st.blk_base[(size_t)qi * nprobe + p] = pos;
+            if (p > 0) tiles += (nb + kTileBlocks - 1) / kTileBlocks;
+            pos += nb;
+        }
+        st.tile_off[(size_t)qi * (nprobe + 1) + nprobe] = tiles;
     }
-    __syncthreads();
-    for (int p = 0; p < nprobe; ++p) {
-        const int c = (int)probe[(size_t)qi * nprobe + p];
-        prepare_cluster(ix, qrot, prune, c, sm);
+}
+
+__global__ void k_tile_prefix(SplitState st, int nq, int nprobe) {
+    // one thread: nq is small on this path (the split scan serves latency-bound calls)
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int acc = 0;
+    for (int q = 0; q < nq; ++q) {
+        st.q_tile_off[q] = acc;
+        acc += st.tile_off[(size_t)q * (nprobe + 1) + nprobe];
+    }
+    st.q_tile_off[nq] = acc;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, const uint32_t *__restrict__ probe,
+                                                            int nprobe, int nq, const float *__restrict__ qrot_all,
+                                                            const float *__restrict__ prune_all, SplitState st,
+                                                            unsigned long long *__restrict__ counters, int xstride) {
+    extern __shared__ __align__(16) char smem_raw[];
+    const int S = ix.S, tid = threadIdx.x;
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, 1, xstride);
+    ScanTally tl;
+    const int total = st.q_tile_off[nq];
+    for (int wi = blockIdx.x; wi < total; wi += gridDim.x) {
+        int lo = 0, hi = nq;  // query: last q with q_tile_off[q] <= wi
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (st.q_tile_off[mid] <= wi) lo = mid;
+            else hi = mid;
+        }
+        const int q = lo;
+        const int local = wi - st.q_tile_off[q];
+        const int *to = st.tile_off + (size_t)q * (nprobe + 1);
+        int plo = 1, phi = nprobe;  // probe: last p >= 1 with to[p] <= local
+        while (phi - plo > 1) {
+            const int mid = (plo + phi) >> 1;
+            if (to[mid] <= local) plo = mid;
+            else phi = mid;
+        }
+        const int p = plo, tile = local - to[p];
+        const int c = (int)probe[(size_t)q * nprobe + p];
+        const float *qrot = qrot_all + (size_t)q * ix.Dtot;
+        prepare_cluster(ix, qrot, prune_all + (size_t)q * S, c, sm);
         const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
         const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
-        c_blocks += nb;
-        c_vecs += n;
-        for (int t0 = 0; t0 < nb; t0 += kScanWarps) {
-            const int b = t0 + w;
-            const bool active = b < nb;
-            if (active) block_estimates(ix, b0 + b, sm, w, lane);
-            __syncthreads();
-            const float tau = distk;
-            if (active) {
-                bool cand;
-                if (S == 1) {
-                    const int cnp = (b == nb - 1) ? (n % 32) : 32;  // scanCluster's last-block count (saq_searcher.hpp:186)
-                    cand = lane < cnp && sm.cd[w * 32 + lane] < tau;
-                } else {
-                    cand = stages_pass(sm.stage + w * (S + 1), sm.nstage[w], tau) && sm.cur[w * 32 + lane] < tau &&
-                           (b * 32 + lane) < n;
-                }
-                const uint32_t m = __ballot_sync(kFull, cand);
-                if (lane == 0) sm.cmask[w] = m;
-            } else if (lane == 0) {
-                sm.cmask[w] = 0;
-            }
-            __syncthreads();
-            // accurate distances of candidate lanes: one half-warp per (vector, segment)
-            {
-                int total = 0;
-                for (int i = 0; i < kScanWarps; ++i) total += __popc(sm.cmask[i]) * S;
-                const int hw = tid >> 4, l = tid & 15;
-                const unsigned hmask = (lane < 16) ? 0x0000ffffu : 0xffff0000u;
-                for (int t = hw; t < total; t += 2 * kScanWarps) {
-                    int r = t / S, s = t - r * S, ww = 0;
-                    while (r >= __popc(sm.cmask[ww])) {
-                        r -= __popc(sm.cmask[ww]);
-                        ++ww;
-                    }
-                    uint32_t mk = sm.cmask[ww];
-                    for (int i = 0; i < r; ++i) mk &= mk - 1;
-                    const int j = __ffs(mk) - 1;
-                    const int64_t gb = b0 + t0 + ww, gv = v0 + (int64_t)(t0 + ww) * 32 + j;
-                    const SegDev &g = ix.seg[s];
-                    const float on = g.onorm[gb * 32 + j];
-                    float ex = 0.0f;
-                    if (g.bits > 1) {
-                        uint8_t *xb = sm.xbuf + hw * sm.xstride;
-                        stage_excode(g.lcode + (size_t)gv * g.lstride, g.lstride, xb, l);
-                        __syncwarp(hmask);
-                        ex = excode_ip_half(sm.qres + g.qoff, xb, g.dim, g.bits - 1, l, hmask);
-                        __syncwarp(hmask);
-                    }
-                    if (l == 0) {
-                        const SegScal &sc = sm.scal[s];
-                        const float acc = accurate_dist(on, sm.ipx[(ww * S + s) * 32 + j], ex, g.exfac[gv].x, g.bits,
-                                                        sc.sum_q, sc.q_l2sqr);
-                        sm.part[(ww * S + s) * 32 + j] = S == 1 ? acc : __fsub_rn(acc, sm.cd[(ww * S + s) * 32 + j]);
-                    }
-                }
-            }
-            __syncthreads();
-            // exact replay of the reference's sequential decisions
-            if (tid == 0) {
-                for (int i = 0; i < kScanWarps; ++i) c_spec += __popc(sm.cmask[i]);
-                float dk = distk;
-                int sz = pool_size;
-                for (int ww = 0; ww < kScanWarps && t0 + ww < nb; ++ww) {
-                    const int bb = t0 + ww;
-                    const uint32_t cm = sm.cmask[ww];
-                    if (S == 1) {
-                        const int cnp = (bb == nb - 1) ? (n % 32) : 32;
-                        uint32_t mask = 0;
-                        for (int j = 0; j < cnp; ++j) mask |= (uint32_t)(sm.cd[ww * 32 + j] < dk) << j;
-                        while (mask) {
-                            const int j = __ffs(mask) - 1;
-                            mask &= mask - 1;
-                            if (!((cm >> j) & 1u)) *err = 1;
-                            ++c_rr;
-                            pool_insert(sm.pool_id, sm.pool_d, sz, topk, ix.ids[v0 + (int64_t)bb * 32 + j],
-                                        sm.part[ww * 32 + j]);
-                            dk = sz == topk ? sm.pool_d[sz - 1] : FLT_MAX;
-                        }
+        const int bstart = tile * kTileBlocks, bend = min(nb, bstart + kTileBlocks);
+        if (tid == 0) {
+            tl.blocks += bend - bstart;
+            tl.vecs += min(n, bend * 32) - bstart * 32;
+        }
+        const float tau = st.tau[q];
+        const int base = st.blk_base[(size_t)q * nprobe + p];
+        for (int t0 = bstart; t0 < bend; t0 += kScanWarps) {
+            tile_candidates(ix, sm, b0, v0, nb, n, t0, bend, tau);
+            const int w = tid >> 5, lane = tid & 31, b = t0 + w;
+            if (b < bend) {
+                const uint32_t cm = sm.cmask[w];
+                if (cm) {
+                    int slot = 0;
+                    if (lane == 0) slot = atomicAdd(st.rec_count + q, 1);
+                    slot = __shfl_sync(kFull, slot, 0);
+                    if (slot >= st.cap) {
+                        if (lane == 0) st.overflow[q] = 1;
                     } else {
-                        if (!stages_pass(sm.stage + ww * (S + 1), sm.nstage[ww], dk)) continue;
-                        for (int j = 0; j < 32; ++j) {
-                            if (!(sm.cur[ww * 32 + j] < dk)) continue;
-                            if (bb * 32 + j >= n) break;
-                            if (!((cm >> j) & 1u)) *err = 1;
-                            ++c_rr;
-                            float acc = sm.cur[ww * 32 + j];
-                            for (int s = 0; s < S; ++s) {
-                                acc = __fadd_rn(acc, sm.part[(ww * S + s) * 32 + j]);
-                                if (acc >= dk) break;
-                            }
-                            pool_insert(sm.pool_id, sm.pool_d, sz, topk, ix.ids[v0 + (int64_t)bb * 32 + j], acc);
-                            dk = sz == topk ? sm.pool_d[sz - 1] : FLT_MAX;
+                        float *r = st.rec + ((size_t)q * st.cap + slot) * st.rec_words;
+                        uint32_t *ri = reinterpret_cast<uint32_t *>(r);
+                        if (lane == 0) {
+                            ri[0] = (uint32_t)(base + b);
+                            ri[1] = cm;
+                            ri[2] = (uint32_t)(S == 1 ? 0 : sm.nstage[w]);
+                            ri[3] = (uint32_t)c;
+                            ri[4] = (uint32_t)b;
+                            tl.spec += __popc(cm);
                         }
+                        if (S > 1 && lane <= S) r[8 + lane] = sm.stage[w * (S + 1) + lane];
+                        r[8 + (S + 1) + lane] = sm.cur[w * 32 + lane];
+                        for (int s = 0; s < S; ++s)
+                            r[8 + (S + 1) + 32 + s * 32 + lane] = sm.part[(w * S + s) * 32 + lane];
                     }
                 }
-                distk = dk;
-                pool_size = sz;
             }
             __syncthreads();
         }
     }
     if (tid == 0 && counters) {
-        atomicAdd(counters + 0, c_blocks);
-        atomicAdd(counters + 1, c_vecs);
-        atomicAdd(counters + 2, c_rr);
-        atomicAdd(counters + 3, c_spec);
+        atomicAdd(counters + 0, tl.blocks);
+        atomicAdd(counters + 1, tl.vecs);
+        atomicAdd(counters + 3, tl.spec);
     }
-    for (int i = tid; i < topk; i += kScanThreads) {
-        out_ids[(size_t)qi * topk + i] = sm.pool_id[i];
-        if (out_d) out_d[(size_t)qi * topk + i] = i < pool_size ? sm.pool_d[i] : FLT_MAX;
+}
+
+constexpr int kSplitCap = 2048;
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, const uint32_t *__restrict__ probe,
+                                                              int nprobe, const float *__restrict__ qrot_all,
+                                                              const float *__restrict__ prune_all, int topk,
+                                                              SplitState st, uint32_t *__restrict__ out_ids,
+                                                              float *__restrict__ out_d, int *__restrict__ err,
+                                                              unsigned long long *__restrict__ counters, int xstride) {
+    extern __shared__ __align__(16) char smem_raw[];
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, topk, xstride);
+    __shared__ int pool_size;
+    __shared__ float distk;
+    __shared__ unsigned long long keys[kSplitCap];
+    const int qi = blockIdx.x, tid = threadIdx.x, S = ix.S;
+    ScanTally tl;
+    if (st.overflow[qi]) {  // exact sequential scan from scratch
+        init_pool(sm, topk, pool_size, distk);
+        scan_probes(ix, probe + (size_t)qi * nprobe, 0, nprobe, qrot_all + (size_t)qi * ix.Dtot,
+                    prune_all + (size_t)qi * S, topk, sm, pool_size, distk, err, tl);
+        flush_tally(tl, counters);
+        write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
+        return;
     }
+    for (int i = tid; i < topk; i += blockDim.x) {
+        sm.pool_id[i] = st.pool_id[(size_t)qi * topk + i];
+        sm.pool_d[i] = st.pool_d[(size_t)qi * topk + i];
+    }
+    const int n = min(st.rec_count[qi], st.cap);
+    int P = 1;
+    while (P < n) P <<= 1;
+    const float *rq = st.rec + (size_t)qi * st.cap * st.rec_words;
+    for (int i = tid; i < P; i += blockDim.x)
+        keys[i] = i < n ? (((unsigned long long)reinterpret_cast<const uint32_t *>(rq + (size_t)i * st.rec_words)[0]
+                            << 32) | (uint32_t)i)
+                        : ~0ull;
+    if (tid == 0) {
+        pool_size = st.pool_size[qi];
+        distk = st.tau[qi];
+    }
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < P; i += blockDim.x) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long a = keys[i], b = keys[ixj];
+                    if ((a > b) == ((i & k) == 0)) {
+                        keys[i] = b;
+                        keys[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    if (tid == 0) {
+        float dk = distk;
+        int sz = pool_size;
+        for (int i = 0; i < n; ++i) {
+            const float *r = rq + (size_t)(keys[i] & 0xffffffffu) * st.rec_words;
+            const uint32_t *ri = reinterpret_cast<const uint32_t *>(r);
+            const int c = (int)ri[3], bb = (int)ri[4];
+            const int64_t v0 = ix.vec_off[c];
+            const int nb = (int)(ix.blk_off[c + 1] - ix.blk_off[c]), nv = (int)(ix.vec_off[c + 1] - v0);
+            replay_block(S, nv, nb, bb, r + 8 + (S + 1), r + 8, (int)ri[2], r + 8 + (S + 1) + 32, ri[1], ix.ids + v0,
+                         sm.pool_id, sm.pool_d, sz, topk, dk, err, tl.rr);
+        }
+        pool_size = sz;
+        if (counters) atomicAdd(counters + 2, tl.rr);
+    }
+    __syncthreads();
+    write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
 }
 
 // ------------------------------------------------------------------ estimate
@@ -752,8 +1019,34 @@ size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t np
     add(4 * (size_t)nq * I.view.S);            // prune bounds
     add(4 * (size_t)nq * topk * 2);            // outputs (host io)
     add(64);                                   // flags
+    add(64);                                   // counters
     (void)host_io;
     return b + 256;
+}
+
+size_t split_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t nprobe) {
+    size_t b = 0;
+    auto add = [&](size_t x) { b += align16(x); };
+    add(4 * (size_t)nq * topk);
+    add(4 * (size_t)nq * topk);
+    add(4 * (size_t)nq);
+    add(4 * (size_t)nq);
+    add(4 * (size_t)nq * (nprobe + 1));
+    add(4 * (size_t)nq * nprobe);
+    add(4 * (size_t)(nq + 1));
+    add(4 * (size_t)nq);
+    add(4 * (size_t)nq);
+    add(4 * (size_t)nq * kSplitCap * rec_words_of(I.view.S));
+    return b + 256;
+}
+
+// Which exact scan serves a call: the split scan for latency-bound calls (few
+// queries), one CTA per query for batches.  SAQG_SCAN_MODE=seq|split forces one.
+bool use_split(int64_t nq) {
+    const char *m = std::getenv("SAQG_SCAN_MODE");
+    if (m && std::string(m) == "seq") return false;
+    if (m && std::string(m) == "split") return nq <= 4096;
+    return nq <= 64;
 }
 
 int xstride_of(const DevIndexView &ix) {
@@ -821,15 +1114,53 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[2], st));
         const int xs = xstride_of(ix);
         const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs);
-        SAQG_REQUIRE(smem <= 220 * 1024, "dimension / topk too large for the scan kernel's shared memory");
-        SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        SAQG_REQUIRE(smem <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
         uint32_t *ids_out = host ? oid : ids;
         float *d_out = host ? od : dists;
-        k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ids_out,
-                                                          d_out, flags + 1, stats ? counters : nullptr, xs);
-        check_launch("k_scan");
+        unsigned long long *cnt = stats ? counters : nullptr;
+        if (!use_split(nq)) {
+            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ids_out,
+                                                              d_out, flags + 1, cnt, xs);
+            check_launch("k_scan");
+            count_launch(4);
+        } else {
+            Bump sb{(char *)I.split_scratch_get(split_scratch_bytes(I, nq, topk, nprobe))};
+            SplitState ss;
+            ss.pool_id = sb.take<uint32_t>((size_t)nq * topk);
+            ss.pool_d = sb.take<float>((size_t)nq * topk);
+            ss.pool_size = sb.take<int>(nq);
+            ss.tau = sb.take<float>(nq);
+            ss.tile_off = sb.take<int>((size_t)nq * (nprobe + 1));
+            ss.blk_base = sb.take<int>((size_t)nq * nprobe);
+            ss.q_tile_off = sb.take<int>(nq + 1);
+            ss.rec_count = sb.take<int>(nq);
+            ss.overflow = sb.take<int>(nq);
+            ss.cap = kSplitCap;
+            ss.rec_words = rec_words_of(ix.S);
+            ss.rec = sb.take<float>((size_t)nq * kSplitCap * ss.rec_words);
+            const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
+            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_first, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_spec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
+            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_scan_first<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ss,
+                                                                    flags + 1, cnt, xs);
+            check_launch("k_scan_first");
+            k_tile_prefix<<<1, 32, 0, st>>>(ss, (int)nq, (int)nprobe);
+            check_launch("k_tile_prefix");
+            int dev = 0, sms = 0, per_sm = 0;
+            SAQG_CUDA_TRY(cudaGetDevice(&dev));
+            SAQG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            SAQG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scan_spec, kScanThreads, smem1));
+            const unsigned grid = (unsigned)std::max(1, sms * std::max(1, per_sm));
+            k_scan_spec<<<grid, kScanThreads, smem1, st>>>(ix, probe, (int)nprobe, (int)nq, qrot, prune, ss, cnt, xs);
+            check_launch("k_scan_spec");
+            k_scan_replay<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ss,
+                                                                     ids_out, d_out, flags + 1, cnt, xs);
+            check_launch("k_scan_replay");
+            count_launch(7);
+        }
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[3], st));
-        count_launch(4);
     }
     if (probes_out)
         SAQG_CUDA_TRY(cudaMemcpyAsync(probes_out, probe, 4 * (size_t)nq * nprobe,

@@ -126,7 +126,12 @@ def test_gpu_construct_matches_oracle_and_searches(case, tmp_path):
     index.save(gpath)
     O.build_index(opath, x, cent, cids, bits, seg, eqseg, rots)
     assert open(gpath, "rb").read() == open(opath, "rb").read()
-    ids, d = index.search(q, 10, 5, return_dists=True)
     oids, od = O.OracleIndex(opath).search(q, 10, 5, with_dists=True)
-    assert np.array_equal(ids, oids)
-    assert np.array_equal(d.view(np.uint32), od.view(np.uint32))
+    for mode in ("seq", "split"):
+        os.environ["SAQG_SCAN_MODE"] = mode
+        try:
+            ids, d = index.search(q, 10, 5, return_dists=True)
+        finally:
+            del os.environ["SAQG_SCAN_MODE"]
+        assert np.array_equal(ids, oids), mode
+        assert np.array_equal(d.view(np.uint32), od.view(np.uint32)), mode

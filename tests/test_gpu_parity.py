@@ -26,7 +26,14 @@ def saqg():
     return ivf
 
 
-def test_search_matches_reference(golden_case, saqg):
+@pytest.fixture(params=["seq", "split"])
+def scan_mode(request, monkeypatch):
+    """Both exact scan implementations: one CTA per query, and the split scan."""
+    monkeypatch.setenv("SAQG_SCAN_MODE", request.param)
+    return request.param
+
+
+def test_search_matches_reference(golden_case, saqg, scan_mode):
     idx = saqg.IVF.load(golden_case.index_path)
     ids, dists = idx.search(golden_case.q, golden_case.topk, golden_case.nprobe, return_dists=True)
     assert np.array_equal(ids, golden_case.z["search_ids"])
@@ -36,7 +43,7 @@ def test_search_matches_reference(golden_case, saqg):
     assert bits_eq(dists, od)
 
 
-def test_single_query_signature(golden_case, saqg):
+def test_single_query_signature(golden_case, saqg, scan_mode):
     idx = saqg.IVF.load(golden_case.index_path)
     for i in range(min(3, golden_case.q.shape[0])):
         ids = idx.search(golden_case.q[i], golden_case.topk, golden_case.nprobe)
