@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--target-recall", type=float, default=0.95)
     ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "saqg_bench_cache"))
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--sigma", type=float, default=0.35)
+    ap.add_argument("--noise-alpha", type=float, default=1.2)
     return ap.parse_args()
 
 
@@ -129,7 +131,7 @@ def dist_env():
 
 
 def cache_paths(a):
-    key = f"v{CACHE_VERSION}_n{a.n}_d{a.dim}_k{a.clusters}_b{a.bits}_seed0"
+    key = f"v{CACHE_VERSION}_n{a.n}_d{a.dim}_k{a.clusters}_b{a.bits}_s{a.sigma}_na{a.noise_alpha}_seed0"
     d = os.path.join(a.cache, key)
     os.makedirs(d, exist_ok=True)
     return d, os.path.join(d, "index.saq"), os.path.join(d, "meta.json")
@@ -137,7 +139,8 @@ def cache_paths(a):
 
 def build_workload(a, torch):
     from saq_gb300 import workloads
-    return workloads.zipf_aniso(a.n, a.dim, a.clusters, nq=max(a.batch, a.gt_queries, a.plain_queries), seed=0)
+    return workloads.zipf_aniso(a.n, a.dim, a.clusters, nq=max(a.batch, a.gt_queries, a.plain_queries), seed=0,
+                                sigma=a.sigma, noise_alpha=a.noise_alpha)
 
 
 def get_index_and_meta(a, torch, wl, log):
@@ -218,7 +221,9 @@ def main():
     config = {"workload": f"{a.n // 1_000_000}M x {a.dim}, B={a.bits:g} SAQ (segmented), {a.clusters} clusters "
                           f"Zipf(1.1), PCA, k={a.topk}, batch {a.batch}",
               "nprobe": nprobe, f"recall@{a.topk}": round(meta["recall"], 4), "plan": meta["plan"],
-              "l2": "flushed between timed steps (256 MiB write)", "queries": "same distribution as the base set"}
+              "l2": "flushed between timed steps (256 MiB write)", "queries": "same distribution as the base set",
+              "data_model": f"unit-norm; centre spectrum i^-0.8, within-cluster spectrum i^-{a.noise_alpha:g}, "
+                            f"sigma {a.sigma:g}"}
 
     if a.impl == "reference":
         qh = wl.q.cpu().numpy()
