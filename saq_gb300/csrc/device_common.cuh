@@ -83,56 +83,130 @@ __device__ __forceinline__ float warp_min_tree(float x) {
 }
 
 // --------------------------------------------------------------- ex-codes
-// Value of dimension d in the reference's compacted ex-code layouts
-// (utils/code_helper.hpp CodeHelper<B>::compacted_code8, B <= 8).
-__device__ __forceinline__ uint32_t excode_get8(const uint8_t *__restrict__ y, int d, int bits) {
-    switch (bits) {
-    case 1:
-        return (y[d >> 3] >> (d & 7)) & 1u;
-    case 2: {
-        const int g = d >> 6, k = d & 63;
-        return (y[g * 16 + (k & 15)] >> (2 * (k >> 4))) & 3u;
-    }
-    case 3: {
-        const int g = d >> 6, k = d & 63;
-        const uint8_t *b = y + g * 24;
-        return ((b[k & 15] >> (2 * (k >> 4))) & 3u) | (((b[16 + (k & 7)] >> (k >> 3)) & 1u) << 2);
-    }
-    case 4: {
-        const int g = d >> 5, k = d & 31;
-        const uint8_t byte = y[g * 16 + (k & 15)];
-        return k < 16 ? (byte & 15u) : (uint32_t)(byte >> 4);
-    }
-    case 6:
-    case 7: {
-        const int g = d >> 6, k = d & 63, r = k & 15;
-        const uint8_t *b = y + g * (bits == 6 ? 48 : 56);
-        uint32_t v;
-        if (k < 16) v = b[r] & 63u;
-        else if (k < 32) v = b[16 + r] & 63u;
-        else if (k < 48) v = ((uint32_t)(b[r] >> 6) << 4) | (b[32 + r] & 15u);
-        else v = ((uint32_t)(b[16 + r] >> 6) << 4) | (uint32_t)(b[32 + r] >> 4);
-        if (bits == 7) v |= ((b[48 + (k & 7)] >> (k >> 3)) & 1u) << 6;
-        return v;
-    }
-    case 8:
-        return y[d];
-    default:
-        return 0;
-    }
-}
+// One 16-lane chain of CodeHelper<B>::compute_ip, lane l of a half-warp
+// accumulating dims l, l+16, l+32, ... in increasing order.  The reference's
+// compacted layouts were designed for 16-lane SIMD, so lane l reads the same
+// byte positions in every group of dims; the chains read them straight from
+// global memory (L1/L2), 16 consecutive bytes per half-warp load.
+template <int B>
+__device__ __forceinline__ float chain_bits(const float *__restrict__ q, const uint8_t *__restrict__ y, int D, int l);
 
-// One 16-lane chain of CodeHelper<bits>::compute_ip for bits in 1..8 except 5,
-// run by half-warp lane l (dims l, l+16, ...).  Returns this lane's accumulator.
-__device__ __forceinline__ float excode_lane_chain(const float *__restrict__ q, const uint8_t *__restrict__ y, int D,
-                                                   int bits, int l) {
+template <>
+__device__ __forceinline__ float chain_bits<1>(const float *__restrict__ q, const uint8_t *__restrict__ y, int D, int l) {
+    // CodeHelper<1>: bit d of the little-endian bit string; masked adds
     float acc = 0.0f;
-    if (bits == 1) {
-        for (int d = l; d < D; d += 16) acc = __fadd_rn(acc, excode_get8(y, d, 1) ? q[d] : 0.0f);
-    } else {
-        for (int d = l; d < D; d += 16) acc = fmaf((float)excode_get8(y, d, bits), q[d], acc);
+    for (int g = 0; g < D; g += 16) {
+        const uint32_t m = (uint32_t)y[g / 8] | ((uint32_t)y[g / 8 + 1] << 8);
+        acc = __fadd_rn(acc, ((m >> l) & 1u) ? q[g + l] : 0.0f);
     }
     return acc;
+}
+
+template <>
+__device__ __forceinline__ float chain_bits<2>(const float *__restrict__ q, const uint8_t *__restrict__ y, int D, int l) {
+    float acc = 0.0f;
+    for (int g = 0; g < D; g += 64) {
+        const uint32_t b = y[(g / 64) * 16 + l];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc = fmaf((float)((b >> (2 * k)) & 3u), q[g + 16 * k + l], acc);
+    }
+    return acc;
+}
+
+template <>
+__device__ __forceinline__ float chain_bits<3>(const float *__restrict__ q, const uint8_t *__restrict__ y, int D, int l) {
+    float acc = 0.0f;
+    for (int g = 0; g < D; g += 64) {
+        const uint8_t *gp = y + (g / 64) * 24;
+        const uint32_t b = gp[l];
+        // top bit of dim (16k + l) sits in byte 16 + (l & 7), bit 2k + (l >> 3)
+        const uint32_t t = gp[16 + (l & 7)];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t v = ((b >> (2 * k)) & 3u) | (((t >> (2 * k + (l >> 3))) & 1u) << 2);
+            acc = fmaf((float)v, q[g + 16 * k + l], acc);
+        }
+    }
+    return acc;
+}
+
+template <>
+__device__ __forceinline__ float chain_bits<4>(const float *__restrict__ q, const uint8_t *__restrict__ y, int D, int l) {
+    float acc = 0.0f;
+    for (int g = 0; g < D; g += 32) {
+        const uint32_t b = y[(g / 32) * 16 + l];
+        acc = fmaf((float)(b & 15u), q[g + l], acc);
+        acc = fmaf((float)(b >> 4), q[g + 16 + l], acc);
+    }
+    return acc;
+}
+
+template <int B>  // 6 or 7
+__device__ __forceinline__ float chain_67(const float *__restrict__ q, const uint8_t *__restrict__ y, int D, int l) {
+    float acc = 0.0f;
+    for (int g = 0; g < D; g += 64) {
+        const uint8_t *gp = y + (g / 64) * (B == 6 ? 48 : 56);
+        const uint32_t b0 = gp[l], b1 = gp[16 + l], b2 = gp[32 + l];
+        uint32_t v0 = b0 & 63u, v1 = b1 & 63u;
+        uint32_t v2 = ((b0 >> 6) << 4) | (b2 & 15u), v3 = ((b1 >> 6) << 4) | (b2 >> 4);
+        if (B == 7) {
+            const uint32_t t = gp[48 + (l & 7)];
+            const int sh = l >> 3;
+            v0 |= ((t >> (0 + sh)) & 1u) << 6;
+            v1 |= ((t >> (2 + sh)) & 1u) << 6;
+            v2 |= ((t >> (4 + sh)) & 1u) << 6;
+            v3 |= ((t >> (6 + sh)) & 1u) << 6;
+        }
+        acc = fmaf((float)v0, q[g + l], acc);
+        acc = fmaf((float)v1, q[g + 16 + l], acc);
+        acc = fmaf((float)v2, q[g + 32 + l], acc);
+        acc = fmaf((float)v3, q[g + 48 + l], acc);
+    }
+    return acc;
+}
+
+template <>
+__device__ __forceinline__ float chain_bits<6>(const float *__restrict__ q, const uint8_t *__restrict__ y, int D, int l) {
+    return chain_67<6>(q, y, D, l);
+}
+template <>
+__device__ __forceinline__ float chain_bits<7>(const float *__restrict__ q, const uint8_t *__restrict__ y, int D, int l) {
+    return chain_67<7>(q, y, D, l);
+}
+
+template <>
+__device__ __forceinline__ float chain_bits<8>(const float *__restrict__ q, const uint8_t *__restrict__ y, int D, int l) {
+    float acc = 0.0f;
+    for (int d = l; d < D; d += 16) acc = fmaf((float)y[d], q[d], acc);
+    return acc;
+}
+
+// IP of a code of at most 8 bits, reduced over the half-warp (valid in lane 0).
+__device__ __forceinline__ float ip8_half(const float *__restrict__ q, const uint8_t *__restrict__ y, int D, int bits,
+                                          int l, unsigned mask) {
+    switch (bits) {
+    case 1:
+        return half_reduce16(chain_bits<1>(q, y, D, l), mask);
+    case 2:
+        return half_reduce16(chain_bits<2>(q, y, D, l), mask);
+    case 3:
+        return half_reduce16(chain_bits<3>(q, y, D, l), mask);
+    case 4:
+        return half_reduce16(chain_bits<4>(q, y, D, l), mask);
+    case 5: {  // CodeHelper<5>::compute_ip = 2 * IP4(top 4 bits) + IP1(low bit)
+        const float a = half_reduce16(chain_bits<4>(q, y, D, l), mask);
+        const float b = half_reduce16(chain_bits<1>(q, y + D / 2, D, l), mask);
+        return __fadd_rn(2.0f * a, b);
+    }
+    case 6:
+        return half_reduce16(chain_bits<6>(q, y, D, l), mask);
+    case 7:
+        return half_reduce16(chain_bits<7>(q, y, D, l), mask);
+    case 8:
+        return half_reduce16(chain_bits<8>(q, y, D, l), mask);
+    default:
+        return 0.0f;
+    }
 }
 
 // get_IP_FUNC(ex_bits)(q, y, D) (code_helper.hpp:599-640) computed by a
@@ -141,24 +215,11 @@ __device__ __forceinline__ float excode_ip_half(const float *__restrict__ q, con
                                                 int exb, int l, unsigned mask) {
     if (exb == 0) return 0.0f;
     if (exb > 8) {  // CodeHelper<B>::compute_ip, B > 8: IP8(low bytes) + 256 * IP(rest)
-        float lo = half_reduce16(excode_lane_chain(q, y, D, 8, l), mask);
-        float hi;
-        const int hb = exb - 8;
-        if (hb == 5) {
-            float a = half_reduce16(excode_lane_chain(q, y + D, D, 4, l), mask);
-            float b = half_reduce16(excode_lane_chain(q, y + D + D / 2, D, 1, l), mask);
-            hi = __fadd_rn(2.0f * a, b);
-        } else {
-            hi = half_reduce16(excode_lane_chain(q, y + D, D, hb, l), mask);
-        }
+        const float lo = ip8_half(q, y, D, 8, l, mask);
+        const float hi = ip8_half(q, y + D, D, exb - 8, l, mask);
         return __fadd_rn(lo, 256.0f * hi);
     }
-    if (exb == 5) {  // CodeHelper<5>::compute_ip = 2 * IP4(top 4 bits) + IP1(low bit)
-        float a = half_reduce16(excode_lane_chain(q, y, D, 4, l), mask);
-        float b = half_reduce16(excode_lane_chain(q, y + D / 2, D, 1, l), mask);
-        return __fadd_rn(2.0f * a, b);
-    }
-    return half_reduce16(excode_lane_chain(q, y, D, exb, l), mask);
+    return ip8_half(q, y, D, exb, l, mask);
 }
 
 // CaqCluEstimator::compAccurateDist + Lut::getExtIP, L2 (caq_estimator.hpp:190-217, lut.hpp:121-126)

@@ -10,8 +10,10 @@
 //   short code blocks, long codes, long factors, ids, rotated centroids.
 // IVF::load reads every cluster K times in a nested loop (ivf.hpp:256-260,
 // harmless only because reads past EOF are no-ops); here each is read once.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <memory>
 
 #include "saqg_internal.h"
@@ -124,7 +126,19 @@ void *Index::scratch_get(size_t bytes) const {
     return scratch;
 }
 
+int64_t Index::max_blocks_of_probes(int64_t nprobe) const {
+    if (top_blocks_prefix.empty()) return 1;
+    return std::max<int64_t>(1, top_blocks_prefix[std::min<int64_t>(nprobe, (int64_t)top_blocks_prefix.size() - 1)]);
+}
+
 void finalize_view(Index &idx) {
+    {
+        std::vector<int64_t> nb(idx.K);
+        for (int64_t c = 0; c < idx.K; ++c) nb[c] = idx.blk_off[c + 1] - idx.blk_off[c];
+        std::sort(nb.begin(), nb.end(), std::greater<int64_t>());
+        idx.top_blocks_prefix.assign(idx.K + 1, 0);
+        for (int64_t c = 0; c < idx.K; ++c) idx.top_blocks_prefix[c + 1] = idx.top_blocks_prefix[c] + nb[c];
+    }
     DevIndexView &v = idx.view;
     v.S = (int)idx.segs.size();
     v.K = (int)idx.K;

@@ -106,6 +106,9 @@ struct Index {
     void upload(void *dst, const void *src, size_t bytes);
     void *scratch_get(size_t bytes) const;
     void *split_scratch_get(size_t bytes) const;
+    // most blocks any nprobe clusters can hold (sizes of the largest clusters)
+    std::vector<int64_t> top_blocks_prefix;
+    int64_t max_blocks_of_probes(int64_t nprobe) const;
 };
 
 // index_io.cpp

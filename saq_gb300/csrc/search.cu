@@ -314,14 +314,6 @@ __device__ __forceinline__ void pool_insert(uint32_t *ids, float *d, int &size, 
     size += (size < cap);
 }
 
-// Copies one vector's ex-code (lstride bytes, 16-byte aligned rows) into a
-// half-warp's shared buffer with coalesced 16-byte loads.
-__device__ __forceinline__ void stage_excode(const uint8_t *__restrict__ src, int lstride, uint8_t *dst, int l) {
-    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
-    uint4 *d4 = reinterpret_cast<uint4 *>(dst);
-    for (int o = l; o < lstride / 16; o += 16) d4[o] = __ldg(s4 + o);
-}
-
 // ------------------------------------------------------------------ scan
 struct ScanSmem {
     // laid out in dynamic shared memory by scan_smem_layout()
@@ -565,13 +557,7 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
         const SegDev &g = ix.seg[s];
         const float on = g.onorm[gb * 32 + j];
         float ex = 0.0f;
-        if (g.bits > 1) {
-            uint8_t *xb = sm.xbuf + hw * sm.xstride;
-            stage_excode(g.lcode + (size_t)gv * g.lstride, g.lstride, xb, l);
-            __syncwarp(hmask);
-            ex = excode_ip_half(sm.qres + g.qoff, xb, g.dim, g.bits - 1, l, hmask);
-            __syncwarp(hmask);
-        }
+        if (g.bits > 1) ex = excode_ip_half(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim, g.bits - 1, l, hmask);
         if (l == 0) {
             const SegScal &sc = sm.scal[s];
             const float acc = accurate_dist(on, sm.ipx[(ww * S + s) * 32 + j], ex, g.exfac[gv].x, g.bits, sc.sum_q,
@@ -704,28 +690,30 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
 }
 
 // ------------------------------------------------------------------ split scan
-// For latency (one query, or a few): the nearest cluster is scanned exactly
-// first; its distk, tau1, bounds distk for the rest of the scan.  Every other
-// (probe, tile) is then processed in parallel across the GPU under tau1 and
-// leaves a record for each block with a lane that can pass; a final pass per
-// query sorts the records into scan order and replays the reference's
-// decisions.  Blocks without a record cannot insert anything (no lane is below
-// tau1 >= distk), so the replay is exact.  If a query overflows its record
-// space, its replay falls back to the full sequential scan.
+// For latency-bound calls (one query, or a few).  The first tile of the
+// nearest cluster is scanned exactly; the pool's distk afterwards, tau1, bounds
+// distk for the rest of the scan (distk never grows).  Every remaining (probe,
+// tile) is processed in parallel across the GPU under tau1; each block with a
+// lane below tau1 leaves a record in a slot indexed by its position in scan
+// order.  A final pass per query walks the positions in order and replays the
+// reference's decisions on the records.  Blocks without a record cannot insert
+// anything (none of their lanes is below tau1 >= distk), so the replay is exact.
 constexpr int kTileBlocks = 64;
+constexpr int kFirstBlocks = 16;
 
 struct SplitState {
     uint32_t *pool_id;   // [nq][topk]
     float *pool_d;       // [nq][topk]
     int *pool_size;      // [nq]
     float *tau;          // [nq]
-    int *tile_off;       // [nq][nprobe + 1] tiles before probe p (probe 0 has none)
+    int *tile_off;       // [nq][nprobe + 1] tiles before probe p
     int *blk_base;       // [nq][nprobe] scan-order position of the probe's first block
     int *q_tile_off;     // [nq + 1]
-    int *rec_count;      // [nq]
-    int *overflow;       // [nq]
-    float *rec;          // [nq][cap][rec_words]
-    int cap, rec_words;
+    int *npos;           // [nq] scan positions of the query
+    uint8_t *flag;       // [nq][max_pos]
+    float *rec;          // [nq][max_pos][rec_words]
+    int64_t max_pos;
+    int rec_words;
 };
 
 __host__ __device__ inline int rec_words_of(int S) { return (8 + (S + 1) + 32 + 32 * S + 3) & ~3; }
@@ -736,41 +724,64 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
                                                              SplitState st, int *__restrict__ err,
                                                              unsigned long long *__restrict__ counters, int xstride) {
     extern __shared__ __align__(16) char smem_raw[];
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, topk, xstride);
+    const int S = ix.S, tid = threadIdx.x;
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, topk, xstride);
     __shared__ int pool_size;
     __shared__ float distk;
     const int qi = blockIdx.x;
     ScanTally tl;
     init_pool(sm, topk, pool_size, distk);
-    scan_probes(ix, probe + (size_t)qi * nprobe, 0, 1, qrot_all + (size_t)qi * ix.Dtot, prune_all + (size_t)qi * ix.S,
-                topk, sm, pool_size, distk, err, tl);
+    const uint32_t *pr = probe + (size_t)qi * nprobe;
+    const float *qrot = qrot_all + (size_t)qi * ix.Dtot, *prune = prune_all + (size_t)qi * S;
+    {  // the first kFirstBlocks blocks of the nearest cluster, exactly as scan_probes does
+        const int c = (int)pr[0];
+        prepare_cluster(ix, qrot, prune, c, sm);
+        const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
+        const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
+        const int fe = min(nb, kFirstBlocks);
+        tl.blocks += fe;
+        tl.vecs += min(n, fe * 32);
+        for (int t0 = 0; t0 < fe; t0 += kScanWarps) {
+            tile_candidates(ix, sm, b0, v0, nb, n, t0, fe, distk);
+            if (tid == 0) {
+                for (int i = 0; i < kScanWarps; ++i) tl.spec += __popc(sm.cmask[i]);
+                float dk = distk;
+                int sz = pool_size;
+                for (int ww = 0; ww < kScanWarps && t0 + ww < fe; ++ww)
+                    replay_block(S, n, nb, t0 + ww, sm.cur + ww * 32, sm.stage + ww * (S + 1), sm.nstage[ww],
+                                 S == 1 ? sm.part + ww * 32 : sm.part + ww * S * 32, sm.cmask[ww], ix.ids + v0,
+                                 sm.pool_id, sm.pool_d, sz, topk, dk, err, tl.rr);
+                distk = dk;
+                pool_size = sz;
+            }
+            __syncthreads();
+        }
+    }
     flush_tally(tl, counters);
-    for (int i = threadIdx.x; i < topk; i += blockDim.x) {
+    for (int i = tid; i < topk; i += blockDim.x) {
         st.pool_id[(size_t)qi * topk + i] = sm.pool_id[i];
         st.pool_d[(size_t)qi * topk + i] = sm.pool_d[i];
     }
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         st.pool_size[qi] = pool_size;
         st.tau[qi] = distk;
-        st.rec_count[qi] = 0;
-        st.overflow[qi] = 0;
-        // tiles and scan-order block positions of this query's probes
-        const uint32_t *pr = probe + (size_t)qi * nprobe;
         int tiles = 0, pos = 0;
         for (int p = 0; p < nprobe; ++p) {
             const int c = (int)pr[p];
             const int nb = (int)(ix.blk_off[c + 1] - ix.blk_off[c]);
             st.tile_off[(size_t)qi * (nprobe + 1) + p] = tiles;
             st.blk_base[(size_t)qi * nprobe + p] = pos;
-            if (p > 0) tiles += (nb + kTileBlocks - 1) / kTileBlocks;
+            const int rest = p == 0 ? max(0, nb - kFirstBlocks) : nb;
+            tiles += (rest + kTileBlocks - 1) / kTileBlocks;
             pos += nb;
         }
         st.tile_off[(size_t)qi * (nprobe + 1) + nprobe] = tiles;
+        st.npos[qi] = min((int64_t)pos, st.max_pos);
+        if (pos > st.max_pos) *err = 2;
     }
 }
 
 __global__ void k_tile_prefix(SplitState st, int nq, int nprobe) {
-    // one thread: nq is small on this path (the split scan serves latency-bound calls)
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     int acc = 0;
     for (int q = 0; q < nq; ++q) {
@@ -789,6 +800,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
     ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, 1, xstride);
     ScanTally tl;
     const int total = st.q_tile_off[nq];
+    int last_q = -1, last_c = -1;
     for (int wi = blockIdx.x; wi < total; wi += gridDim.x) {
         int lo = 0, hi = nq;  // query: last q with q_tile_off[q] <= wi
         while (hi - lo > 1) {
@@ -799,7 +811,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
         const int q = lo;
         const int local = wi - st.q_tile_off[q];
         const int *to = st.tile_off + (size_t)q * (nprobe + 1);
-        int plo = 1, phi = nprobe;  // probe: last p >= 1 with to[p] <= local
+        int plo = 0, phi = nprobe;  // probe: last p with to[p] <= local
         while (phi - plo > 1) {
             const int mid = (plo + phi) >> 1;
             if (to[mid] <= local) plo = mid;
@@ -807,44 +819,42 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
         }
         const int p = plo, tile = local - to[p];
         const int c = (int)probe[(size_t)q * nprobe + p];
-        const float *qrot = qrot_all + (size_t)q * ix.Dtot;
-        prepare_cluster(ix, qrot, prune_all + (size_t)q * S, c, sm);
+        if (q != last_q || c != last_c) {  // LUTs survive across tiles of one cluster
+            prepare_cluster(ix, qrot_all + (size_t)q * ix.Dtot, prune_all + (size_t)q * S, c, sm);
+            last_q = q;
+            last_c = c;
+        }
         const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
         const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
-        const int bstart = tile * kTileBlocks, bend = min(nb, bstart + kTileBlocks);
+        const int first = p == 0 ? kFirstBlocks : 0;
+        const int bstart = first + tile * kTileBlocks, bend = min(nb, bstart + kTileBlocks);
         if (tid == 0) {
             tl.blocks += bend - bstart;
             tl.vecs += min(n, bend * 32) - bstart * 32;
         }
         const float tau = st.tau[q];
-        const int base = st.blk_base[(size_t)q * nprobe + p];
+        const int64_t base = st.blk_base[(size_t)q * nprobe + p];
         for (int t0 = bstart; t0 < bend; t0 += kScanWarps) {
             tile_candidates(ix, sm, b0, v0, nb, n, t0, bend, tau);
             const int w = tid >> 5, lane = tid & 31, b = t0 + w;
             if (b < bend) {
                 const uint32_t cm = sm.cmask[w];
-                if (cm) {
-                    int slot = 0;
-                    if (lane == 0) slot = atomicAdd(st.rec_count + q, 1);
-                    slot = __shfl_sync(kFull, slot, 0);
-                    if (slot >= st.cap) {
-                        if (lane == 0) st.overflow[q] = 1;
-                    } else {
-                        float *r = st.rec + ((size_t)q * st.cap + slot) * st.rec_words;
-                        uint32_t *ri = reinterpret_cast<uint32_t *>(r);
-                        if (lane == 0) {
-                            ri[0] = (uint32_t)(base + b);
-                            ri[1] = cm;
-                            ri[2] = (uint32_t)(S == 1 ? 0 : sm.nstage[w]);
-                            ri[3] = (uint32_t)c;
-                            ri[4] = (uint32_t)b;
-                            tl.spec += __popc(cm);
-                        }
-                        if (S > 1 && lane <= S) r[8 + lane] = sm.stage[w * (S + 1) + lane];
-                        r[8 + (S + 1) + lane] = sm.cur[w * 32 + lane];
-                        for (int s = 0; s < S; ++s)
-                            r[8 + (S + 1) + 32 + s * 32 + lane] = sm.part[(w * S + s) * 32 + lane];
+                const int64_t pos = base + b;
+                if (cm && pos < st.max_pos) {
+                    float *r = st.rec + ((size_t)q * st.max_pos + pos) * st.rec_words;
+                    uint32_t *ri = reinterpret_cast<uint32_t *>(r);
+                    if (lane == 0) {
+                        ri[0] = (uint32_t)pos;
+                        ri[1] = cm;
+                        ri[2] = (uint32_t)(S == 1 ? 0 : sm.nstage[w]);
+                        ri[3] = (uint32_t)c;
+                        ri[4] = (uint32_t)b;
+                        st.flag[(size_t)q * st.max_pos + pos] = 1;
+                        tl.spec += __popc(cm);
                     }
+                    if (S > 1 && lane <= S) r[8 + lane] = sm.stage[w * (S + 1) + lane];
+                    r[8 + (S + 1) + lane] = sm.cur[w * 32 + lane];
+                    for (int s = 0; s < S; ++s) r[8 + (S + 1) + 32 + s * 32 + lane] = sm.part[(w * S + s) * 32 + lane];
                 }
             }
             __syncthreads();
@@ -857,76 +867,62 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
     }
 }
 
-constexpr int kSplitCap = 2048;
-
 __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, const uint32_t *__restrict__ probe,
-                                                              int nprobe, const float *__restrict__ qrot_all,
-                                                              const float *__restrict__ prune_all, int topk,
-                                                              SplitState st, uint32_t *__restrict__ out_ids,
-                                                              float *__restrict__ out_d, int *__restrict__ err,
+                                                              int nprobe, int topk, SplitState st,
+                                                              uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
+                                                              int *__restrict__ err,
                                                               unsigned long long *__restrict__ counters, int xstride) {
     extern __shared__ __align__(16) char smem_raw[];
     ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, topk, xstride);
     __shared__ int pool_size;
     __shared__ float distk;
-    __shared__ unsigned long long keys[kSplitCap];
-    const int qi = blockIdx.x, tid = threadIdx.x, S = ix.S;
-    ScanTally tl;
-    if (st.overflow[qi]) {  // exact sequential scan from scratch
-        init_pool(sm, topk, pool_size, distk);
-        scan_probes(ix, probe + (size_t)qi * nprobe, 0, nprobe, qrot_all + (size_t)qi * ix.Dtot,
-                    prune_all + (size_t)qi * S, topk, sm, pool_size, distk, err, tl);
-        flush_tally(tl, counters);
-        write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
-        return;
-    }
+    __shared__ int list[kScanThreads];
+    __shared__ int warp_cnt[kScanWarps];
+    const int qi = blockIdx.x, tid = threadIdx.x, S = ix.S, w = tid >> 5, lane = tid & 31;
     for (int i = tid; i < topk; i += blockDim.x) {
         sm.pool_id[i] = st.pool_id[(size_t)qi * topk + i];
         sm.pool_d[i] = st.pool_d[(size_t)qi * topk + i];
     }
-    const int n = min(st.rec_count[qi], st.cap);
-    int P = 1;
-    while (P < n) P <<= 1;
-    const float *rq = st.rec + (size_t)qi * st.cap * st.rec_words;
-    for (int i = tid; i < P; i += blockDim.x)
-        keys[i] = i < n ? (((unsigned long long)reinterpret_cast<const uint32_t *>(rq + (size_t)i * st.rec_words)[0]
-                            << 32) | (uint32_t)i)
-                        : ~0ull;
     if (tid == 0) {
         pool_size = st.pool_size[qi];
         distk = st.tau[qi];
     }
+    const int np = st.npos[qi];
+    const uint8_t *fl = st.flag + (size_t)qi * st.max_pos;
+    const float *rq = st.rec + (size_t)qi * st.max_pos * st.rec_words;
+    unsigned long long rr = 0;
     __syncthreads();
-    for (int k = 2; k <= P; k <<= 1)
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = tid; i < P; i += blockDim.x) {
-                const int ixj = i ^ j;
-                if (ixj > i) {
-                    const unsigned long long a = keys[i], b = keys[ixj];
-                    if ((a > b) == ((i & k) == 0)) {
-                        keys[i] = b;
-                        keys[ixj] = a;
-                    }
-                }
+    for (int base = 0; base < np; base += kScanThreads) {
+        const int pos = base + tid;
+        const bool f = pos < np && fl[pos];
+        const uint32_t bal = __ballot_sync(kFull, f);
+        if (lane == 0) warp_cnt[w] = __popc(bal);
+        __syncthreads();
+        int off = 0, total = 0;
+        for (int i = 0; i < kScanWarps; ++i) {
+            if (i < w) off += warp_cnt[i];
+            total += warp_cnt[i];
+        }
+        if (f) list[off + __popc(bal & ((1u << lane) - 1))] = pos;
+        __syncthreads();
+        if (tid == 0 && total) {
+            float dk = distk;
+            int sz = pool_size;
+            for (int i = 0; i < total; ++i) {
+                const float *r = rq + (size_t)list[i] * st.rec_words;
+                const uint32_t *ri = reinterpret_cast<const uint32_t *>(r);
+                const int c = (int)ri[3], bb = (int)ri[4];
+                const int64_t v0 = ix.vec_off[c];
+                const int nb = (int)(ix.blk_off[c + 1] - ix.blk_off[c]), nv = (int)(ix.vec_off[c + 1] - v0);
+                replay_block(S, nv, nb, bb, r + 8 + (S + 1), r + 8, (int)ri[2], r + 8 + (S + 1) + 32, ri[1],
+                             ix.ids + v0, sm.pool_id, sm.pool_d, sz, topk, dk, err, rr);
             }
-            __syncthreads();
+            distk = dk;
+            pool_size = sz;
         }
-    if (tid == 0) {
-        float dk = distk;
-        int sz = pool_size;
-        for (int i = 0; i < n; ++i) {
-            const float *r = rq + (size_t)(keys[i] & 0xffffffffu) * st.rec_words;
-            const uint32_t *ri = reinterpret_cast<const uint32_t *>(r);
-            const int c = (int)ri[3], bb = (int)ri[4];
-            const int64_t v0 = ix.vec_off[c];
-            const int nb = (int)(ix.blk_off[c + 1] - ix.blk_off[c]), nv = (int)(ix.vec_off[c + 1] - v0);
-            replay_block(S, nv, nb, bb, r + 8 + (S + 1), r + 8, (int)ri[2], r + 8 + (S + 1) + 32, ri[1], ix.ids + v0,
-                         sm.pool_id, sm.pool_d, sz, topk, dk, err, tl.rr);
-        }
-        pool_size = sz;
-        if (counters) atomicAdd(counters + 2, tl.rr);
+        __syncthreads();
     }
-    __syncthreads();
+    if (tid == 0 && counters) atomicAdd(counters + 2, rr);
     write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
 }
 
@@ -972,11 +968,8 @@ __global__ void __launch_bounds__(kScanThreads) k_estimate(DevIndexView ix, cons
                 if (g.bits > 1) {
                     // whole warp: lanes 0-15 do the chain, 16-31 idle duplicates
                     const unsigned hm = (lane < 16) ? 0x0000ffffu : 0xffff0000u;
-                    uint8_t *xb = sm.xbuf + (tid >> 4) * sm.xstride;
-                    stage_excode(g.lcode + (size_t)gv * g.lstride, g.lstride, xb, lane & 15);
-                    __syncwarp(hm);
-                    ex = excode_ip_half(sm.qres + g.qoff, xb, g.dim, g.bits - 1, lane & 15, hm);
-                    __syncwarp(hm);
+                    ex = excode_ip_half(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim, g.bits - 1,
+                                        lane & 15, hm);
                     ex = __shfl_sync(kFull, ex, 0);
                 }
                 const float on = g.onorm[gb * 32 + j];
@@ -1024,7 +1017,7 @@ size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t np
     return b + 256;
 }
 
-size_t split_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t nprobe) {
+size_t split_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t nprobe, int64_t max_pos) {
     size_t b = 0;
     auto add = [&](size_t x) { b += align16(x); };
     add(4 * (size_t)nq * topk);
@@ -1035,8 +1028,8 @@ size_t split_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t npr
     add(4 * (size_t)nq * nprobe);
     add(4 * (size_t)(nq + 1));
     add(4 * (size_t)nq);
-    add(4 * (size_t)nq);
-    add(4 * (size_t)nq * kSplitCap * rec_words_of(I.view.S));
+    add((size_t)nq * max_pos);
+    add(4 * (size_t)nq * max_pos * rec_words_of(I.view.S));
     return b + 256;
 }
 
@@ -1045,15 +1038,11 @@ size_t split_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t npr
 bool use_split(int64_t nq) {
     const char *m = std::getenv("SAQG_SCAN_MODE");
     if (m && std::string(m) == "seq") return false;
-    if (m && std::string(m) == "split") return nq <= 4096;
-    return nq <= 64;
+    if (m && std::string(m) == "split") return true;
+    return nq <= 16;
 }
 
-int xstride_of(const DevIndexView &ix) {
-    int m = 16;
-    for (int s = 0; s < ix.S; ++s) m = std::max(m, ix.seg[s].lstride);
-    return m;
-}
+int xstride_of(const DevIndexView &) { return 0; }
 
 void check_launch(const char *what) {
     cudaError_t e = cudaGetLastError();
@@ -1125,7 +1114,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             check_launch("k_scan");
             count_launch(4);
         } else {
-            Bump sb{(char *)I.split_scratch_get(split_scratch_bytes(I, nq, topk, nprobe))};
+            const int64_t max_pos = I.max_blocks_of_probes(nprobe);
+            Bump sb{(char *)I.split_scratch_get(split_scratch_bytes(I, nq, topk, nprobe, max_pos))};
             SplitState ss;
             ss.pool_id = sb.take<uint32_t>((size_t)nq * topk);
             ss.pool_d = sb.take<float>((size_t)nq * topk);
@@ -1134,11 +1124,12 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             ss.tile_off = sb.take<int>((size_t)nq * (nprobe + 1));
             ss.blk_base = sb.take<int>((size_t)nq * nprobe);
             ss.q_tile_off = sb.take<int>(nq + 1);
-            ss.rec_count = sb.take<int>(nq);
-            ss.overflow = sb.take<int>(nq);
-            ss.cap = kSplitCap;
+            ss.npos = sb.take<int>(nq);
+            ss.flag = sb.take<uint8_t>((size_t)nq * max_pos);
+            ss.max_pos = max_pos;
             ss.rec_words = rec_words_of(ix.S);
-            ss.rec = sb.take<float>((size_t)nq * kSplitCap * ss.rec_words);
+            ss.rec = sb.take<float>((size_t)nq * max_pos * ss.rec_words);
+            SAQG_CUDA_TRY(cudaMemsetAsync(ss.flag, 0, (size_t)nq * max_pos, st));
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_first, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_spec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
@@ -1155,8 +1146,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             const unsigned grid = (unsigned)std::max(1, sms * std::max(1, per_sm));
             k_scan_spec<<<grid, kScanThreads, smem1, st>>>(ix, probe, (int)nprobe, (int)nq, qrot, prune, ss, cnt, xs);
             check_launch("k_scan_spec");
-            k_scan_replay<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ss,
-                                                                     ids_out, d_out, flags + 1, cnt, xs);
+            k_scan_replay<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, (int)topk, ss, ids_out,
+                                                                     d_out, flags + 1, cnt, xs);
             check_launch("k_scan_replay");
             count_launch(7);
         }
