@@ -557,7 +557,14 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
         const SegDev &g = ix.seg[s];
         const float on = g.onorm[gb * 32 + j];
         float ex = 0.0f;
-        if (g.bits > 1) ex = excode_ip_half(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim, g.bits - 1, l, hmask);
+        if (g.bits > 1) {  // one coalesced round trip for the whole ex-code, then decode from shared memory
+            uint8_t *xb = sm.xbuf + hw * sm.xstride;
+            const uint4 *src = reinterpret_cast<const uint4 *>(g.lcode + (size_t)gv * g.lstride);
+            for (int o = l; o < g.lstride / 16; o += 16) reinterpret_cast<uint4 *>(xb)[o] = __ldg(src + o);
+            __syncwarp(hmask);
+            ex = excode_ip_half(sm.qres + g.qoff, xb, g.dim, g.bits - 1, l, hmask);
+            __syncwarp(hmask);
+        }
         if (l == 0) {
             const SegScal &sc = sm.scal[s];
             const float acc = accurate_dist(on, sm.ipx[(ww * S + s) * 32 + j], ex, g.exfac[gv].x, g.bits, sc.sum_q,
@@ -698,7 +705,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
 // order.  A final pass per query walks the positions in order and replays the
 // reference's decisions on the records.  Blocks without a record cannot insert
 // anything (none of their lanes is below tau1 >= distk), so the replay is exact.
-constexpr int kTileBlocks = 64;
+constexpr int kTileBlocks = 8;
 constexpr int kFirstBlocks = 16;
 
 struct SplitState {
@@ -850,7 +857,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
                         ri[3] = (uint32_t)c;
                         ri[4] = (uint32_t)b;
                         st.flag[(size_t)q * st.max_pos + pos] = 1;
-                        tl.spec += __popc(cm);
+                        if (counters) atomicAdd(counters + 3, (unsigned long long)__popc(cm));
                     }
                     if (S > 1 && lane <= S) r[8 + lane] = sm.stage[w * (S + 1) + lane];
                     r[8 + (S + 1) + lane] = sm.cur[w * 32 + lane];
@@ -863,7 +870,6 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
     if (tid == 0 && counters) {
         atomicAdd(counters + 0, tl.blocks);
         atomicAdd(counters + 1, tl.vecs);
-        atomicAdd(counters + 3, tl.spec);
     }
 }
 
@@ -1042,7 +1048,11 @@ bool use_split(int64_t nq) {
     return nq <= 16;
 }
 
-int xstride_of(const DevIndexView &) { return 0; }
+int xstride_of(const DevIndexView &ix) {
+    int m = 16;
+    for (int s = 0; s < ix.S; ++s) m = std::max(m, ix.seg[s].lstride);
+    return m;
+}
 
 void check_launch(const char *what) {
     cudaError_t e = cudaGetLastError();
