@@ -222,6 +222,133 @@ __device__ __forceinline__ float excode_ip_half(const float *__restrict__ q, con
     return ip8_half(q, y, D, exb, l, mask);
 }
 
+// ---- the same inner products computed by ONE thread: the 16 SIMD lanes of
+// CodeHelper<B>::compute_ip become 16 independent accumulators (lane l takes
+// dims l, l+16, ... in increasing order), reduced with the same 16->1 tree.
+// Bit-identical to the half-warp form; used where many candidate vectors are
+// re-ranked at once (one thread per vector and segment).
+__device__ __forceinline__ float tree16(const float *a) {
+    float x[8], y[4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = __fadd_rn(a[i], a[i + 8]);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) y[i] = __fadd_rn(x[i], x[i + 4]);
+    return __fadd_rn(__fadd_rn(y[0], y[2]), __fadd_rn(y[1], y[3]));
+}
+
+template <int B>
+__device__ __forceinline__ float ip_thread_bits(const float *__restrict__ q, const uint8_t *__restrict__ y, int D) {
+    float acc[16];
+#pragma unroll
+    for (int l = 0; l < 16; ++l) acc[l] = 0.0f;
+    if (B == 1) {
+        for (int g = 0; g < D; g += 16) {
+            const uint32_t m = (uint32_t)y[g / 8] | ((uint32_t)y[g / 8 + 1] << 8);
+#pragma unroll
+            for (int l = 0; l < 16; ++l) acc[l] = __fadd_rn(acc[l], ((m >> l) & 1u) ? q[g + l] : 0.0f);
+        }
+    } else if (B == 2 || B == 3) {
+        for (int g = 0; g < D; g += 64) {
+            const uint8_t *gp = y + (g / 64) * (B == 2 ? 16 : 24);
+            // 16 low-bit bytes; 3-bit groups are 24 bytes, so only 8-byte alignment is guaranteed
+            const uint2 w0 = *reinterpret_cast<const uint2 *>(gp), w1 = *reinterpret_cast<const uint2 *>(gp + 8);
+            const uint32_t wv[4] = {w0.x, w0.y, w1.x, w1.y};
+            uint2 tt = make_uint2(0, 0);
+            if (B == 3) tt = *reinterpret_cast<const uint2 *>(gp + 16);
+            const uint32_t tv[2] = {tt.x, tt.y};
+#pragma unroll
+            for (int l = 0; l < 16; ++l) {
+                const uint32_t b = (wv[l >> 2] >> (8 * (l & 3))) & 255u;
+                const uint32_t t = (tv[(l & 7) >> 2] >> (8 * (l & 3))) & 255u;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    uint32_t v = (b >> (2 * k)) & 3u;
+                    if (B == 3) v |= ((t >> (2 * k + (l >> 3))) & 1u) << 2;
+                    acc[l] = fmaf((float)v, q[g + 16 * k + l], acc[l]);
+                }
+            }
+        }
+    } else if (B == 4) {
+        for (int g = 0; g < D; g += 32) {
+            const uint4 w = *reinterpret_cast<const uint4 *>(y + (g / 32) * 16);
+            const uint32_t wv[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int l = 0; l < 16; ++l) {
+                const uint32_t b = (wv[l >> 2] >> (8 * (l & 3))) & 255u;
+                acc[l] = fmaf((float)(b & 15u), q[g + l], acc[l]);
+                acc[l] = fmaf((float)(b >> 4), q[g + 16 + l], acc[l]);
+            }
+        }
+    } else if (B == 6 || B == 7) {
+        for (int g = 0; g < D; g += 64) {
+            const uint8_t *gp = y + (g / 64) * (B == 6 ? 48 : 56);
+            uint32_t tv[2] = {0, 0};
+            if (B == 7) {
+                const uint2 tt = *reinterpret_cast<const uint2 *>(gp + 48);
+                tv[0] = tt.x;
+                tv[1] = tt.y;
+            }
+#pragma unroll
+            for (int l = 0; l < 16; ++l) {
+                const uint32_t b0 = gp[l], b1 = gp[16 + l], b2 = gp[32 + l];
+                uint32_t v0 = b0 & 63u, v1 = b1 & 63u;
+                uint32_t v2 = ((b0 >> 6) << 4) | (b2 & 15u), v3 = ((b1 >> 6) << 4) | (b2 >> 4);
+                if (B == 7) {
+                    const uint32_t t = (tv[(l & 7) >> 2] >> (8 * (l & 3))) & 255u;
+                    const int sh = l >> 3;
+                    v0 |= ((t >> (0 + sh)) & 1u) << 6;
+                    v1 |= ((t >> (2 + sh)) & 1u) << 6;
+                    v2 |= ((t >> (4 + sh)) & 1u) << 6;
+                    v3 |= ((t >> (6 + sh)) & 1u) << 6;
+                }
+                acc[l] = fmaf((float)v0, q[g + l], acc[l]);
+                acc[l] = fmaf((float)v1, q[g + 16 + l], acc[l]);
+                acc[l] = fmaf((float)v2, q[g + 32 + l], acc[l]);
+                acc[l] = fmaf((float)v3, q[g + 48 + l], acc[l]);
+            }
+        }
+    } else {  // 8
+        for (int g = 0; g < D; g += 16) {
+            const uint4 w = *reinterpret_cast<const uint4 *>(y + g);
+            const uint32_t wv[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int l = 0; l < 16; ++l) acc[l] = fmaf((float)((wv[l >> 2] >> (8 * (l & 3))) & 255u), q[g + l], acc[l]);
+        }
+    }
+    return tree16(acc);
+}
+
+__device__ __forceinline__ float ip8_thread(const float *__restrict__ q, const uint8_t *__restrict__ y, int D, int bits) {
+    switch (bits) {
+    case 1:
+        return ip_thread_bits<1>(q, y, D);
+    case 2:
+        return ip_thread_bits<2>(q, y, D);
+    case 3:
+        return ip_thread_bits<3>(q, y, D);
+    case 4:
+        return ip_thread_bits<4>(q, y, D);
+    case 5:
+        return __fadd_rn(2.0f * ip_thread_bits<4>(q, y, D), ip_thread_bits<1>(q, y + D / 2, D));
+    case 6:
+        return ip_thread_bits<6>(q, y, D);
+    case 7:
+        return ip_thread_bits<7>(q, y, D);
+    case 8:
+        return ip_thread_bits<8>(q, y, D);
+    default:
+        return 0.0f;
+    }
+}
+
+// get_IP_FUNC(ex_bits)(q, y, D) by one thread.
+__device__ __forceinline__ float excode_ip_thread(const float *__restrict__ q, const uint8_t *__restrict__ y, int D,
+                                                  int exb) {
+    if (exb == 0) return 0.0f;
+    if (exb > 8) return __fadd_rn(ip8_thread(q, y, D, 8), 256.0f * ip8_thread(q, y + D, D, exb - 8));
+    return ip8_thread(q, y, D, exb);
+}
+
 // CaqCluEstimator::compAccurateDist + Lut::getExtIP, L2 (caq_estimator.hpp:190-217, lut.hpp:121-126)
 __device__ __forceinline__ float accurate_dist(float onorm, float ipx, float ex_ip, float rescale, int bits, float sum_q,
                                                float q_l2sqr) {

@@ -540,11 +540,11 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
         sm.cmask[w] = 0;
     }
     __syncthreads();
+    // accurate distances: one thread per (candidate vector, segment)
     int total = 0;
-    for (int i = 0; i < kScanWarps; ++i) total += __popc(sm.cmask[i]) * S;
-    const int hw = tid >> 4, l = tid & 15;
-    const unsigned hmask = (lane < 16) ? 0x0000ffffu : 0xffff0000u;
-    for (int t = hw; t < total; t += 2 * kScanWarps) {
+    for (int i = 0; i < kScanWarps; ++i) total += __popc(sm.cmask[i]);
+    total *= S;
+    for (int t = tid; t < total; t += blockDim.x) {
         int r = t / S, s = t - r * S, ww = 0;
         while (r >= __popc(sm.cmask[ww])) {
             r -= __popc(sm.cmask[ww]);
@@ -555,22 +555,12 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
         const int j = __ffs(mk) - 1;
         const int64_t gb = b0 + t0 + ww, gv = v0 + (int64_t)(t0 + ww) * 32 + j;
         const SegDev &g = ix.seg[s];
-        const float on = g.onorm[gb * 32 + j];
-        float ex = 0.0f;
-        if (g.bits > 1) {  // one coalesced round trip for the whole ex-code, then decode from shared memory
-            uint8_t *xb = sm.xbuf + hw * sm.xstride;
-            const uint4 *src = reinterpret_cast<const uint4 *>(g.lcode + (size_t)gv * g.lstride);
-            for (int o = l; o < g.lstride / 16; o += 16) reinterpret_cast<uint4 *>(xb)[o] = __ldg(src + o);
-            __syncwarp(hmask);
-            ex = excode_ip_half(sm.qres + g.qoff, xb, g.dim, g.bits - 1, l, hmask);
-            __syncwarp(hmask);
-        }
-        if (l == 0) {
-            const SegScal &sc = sm.scal[s];
-            const float acc = accurate_dist(on, sm.ipx[(ww * S + s) * 32 + j], ex, g.exfac[gv].x, g.bits, sc.sum_q,
-                                            sc.q_l2sqr);
-            sm.part[(ww * S + s) * 32 + j] = S == 1 ? acc : __fsub_rn(acc, sm.cd[(ww * S + s) * 32 + j]);
-        }
+        const float ex =
+            g.bits > 1 ? excode_ip_thread(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim, g.bits - 1) : 0.0f;
+        const SegScal &sc = sm.scal[s];
+        const float acc = accurate_dist(g.onorm[gb * 32 + j], sm.ipx[(ww * S + s) * 32 + j], ex, g.exfac[gv].x, g.bits,
+                                        sc.sum_q, sc.q_l2sqr);
+        sm.part[(ww * S + s) * 32 + j] = S == 1 ? acc : __fsub_rn(acc, sm.cd[(ww * S + s) * 32 + j]);
     }
     __syncthreads();
 }
@@ -583,25 +573,30 @@ __device__ __forceinline__ void replay_block(int S, int n, int nb, int bb, const
                                              int nstage, const float *part, uint32_t cm, const uint32_t *ids_v0,
                                              uint32_t *pid, float *pd, int &sz, int topk, float &dk, int *err,
                                              unsigned long long &c_rr) {
+    // Only candidate lanes (cm) can pass: every other lane's estimate is >= the
+    // tile-start distk >= dk, or lies past the cluster's end.
+    (void)n;
+    (void)nb;
+    (void)err;
     if (S == 1) {
-        const int cnp = (bb == nb - 1) ? (n % 32) : 32;
-        uint32_t mask = 0;
-        for (int j = 0; j < cnp; ++j) mask |= (uint32_t)(cur[j] < dk) << j;
+        uint32_t mask = 0;  // scanCluster computes the mask once, at the block's start
+        for (uint32_t m = cm; m; m &= m - 1) {
+            const int j = __ffs(m) - 1;
+            mask |= (uint32_t)(cur[j] < dk) << j;
+        }
         while (mask) {
             const int j = __ffs(mask) - 1;
             mask &= mask - 1;
-            if (!((cm >> j) & 1u)) *err = 1;
             ++c_rr;
             pool_insert(pid, pd, sz, topk, ids_v0[(int64_t)bb * 32 + j], part[j]);
             dk = sz == topk ? pd[sz - 1] : FLT_MAX;
         }
         return;
     }
-    if (!stages_pass(stage, nstage, dk)) return;
-    for (int j = 0; j < 32; ++j) {
+    if (!cm || !stages_pass(stage, nstage, dk)) return;
+    for (uint32_t m = cm; m; m &= m - 1) {
+        const int j = __ffs(m) - 1;
         if (!(cur[j] < dk)) continue;
-        if (bb * 32 + j >= n) break;
-        if (!((cm >> j) & 1u)) *err = 1;
         ++c_rr;
         float acc = cur[j];
         for (int s = 0; s < S; ++s) {
@@ -965,31 +960,22 @@ __global__ void __launch_bounds__(kScanThreads) k_estimate(DevIndexView ix, cons
         }
         __syncwarp();
         const int nv = min(32, n - b * 32);
-        for (int j = 0; j < nv; ++j) {
-            const int64_t gv = v0 + (int64_t)b * 32 + j;
+        if (lane < nv) {  // one thread per vector, all segments in order
+            const int64_t gv = v0 + (int64_t)b * 32 + lane;
             float acc = 0.0f;
             for (int s = 0; s < S; ++s) {
                 const SegDev &g = ix.seg[s];
-                float ex = 0.0f;
-                if (g.bits > 1) {
-                    // whole warp: lanes 0-15 do the chain, 16-31 idle duplicates
-                    const unsigned hm = (lane < 16) ? 0x0000ffffu : 0xffff0000u;
-                    ex = excode_ip_half(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim, g.bits - 1,
-                                        lane & 15, hm);
-                    ex = __shfl_sync(kFull, ex, 0);
-                }
-                const float on = g.onorm[gb * 32 + j];
-                acc = __fadd_rn(acc, accurate_dist(on, sm.ipx[(w * S + s) * 32 + j], ex, g.exfac[gv].x, g.bits,
-                                                   sm.scal[s].sum_q, sm.scal[s].q_l2sqr));
+                const float ex = g.bits > 1 ? excode_ip_thread(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride,
+                                                               g.dim, g.bits - 1)
+                                            : 0.0f;
+                acc = __fadd_rn(acc, accurate_dist(g.onorm[gb * 32 + lane], sm.ipx[(w * S + s) * 32 + lane], ex,
+                                                   g.exfac[gv].x, g.bits, sm.scal[s].sum_q, sm.scal[s].q_l2sqr));
             }
-            const float fj = __shfl_sync(kFull, fsum, j), vj = __shfl_sync(kFull, vsum, j);
-            if (lane == 0) {
-                const int64_t o = base + (int64_t)b * 32 + j;
-                o_ids[o] = ix.ids[gv];
-                o_acc[o] = acc;
-                o_fast[o] = fj;
-                o_vars[o] = vj;
-            }
+            const int64_t o = base + (int64_t)b * 32 + lane;
+            o_ids[o] = ix.ids[gv];
+            o_acc[o] = acc;
+            o_fast[o] = fsum;
+            o_vars[o] = vsum;
         }
         __syncwarp();
     }
