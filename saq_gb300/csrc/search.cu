@@ -691,6 +691,235 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
     write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
 }
 
+// ------------------------------------------------------------------ warp scan
+// Throughput form for batches: one WARP per query, no CTA barriers.  The warp
+// walks its probes and blocks in the reference's order with the exact current
+// distk (no speculation): lane v estimates vector v of the block, the lanes
+// that pass re-rank themselves (thread-level chains, all segments), and lane 0
+// applies the reference's insert sequence.  Each warp owns its LUTs and pool
+// in shared memory.
+constexpr int kWarpsPerCta = 4;
+
+struct WarpSmem {
+    uint16_t *lut;   // 4 * Dtot
+    float *qres;     // Dtot
+    SegScal *scal;   // S
+    float *cd, *ipx, *part;  // S * 32 each
+    float *cur;      // 32
+    float *stage;    // S + 1
+    uint32_t *pool_id;
+    float *pool_d;   // topk + 1 each
+};
+
+__host__ __device__ inline size_t warp_smem_bytes(int Dtot, int S, int topk) {
+    return align16(2 * 4 * (size_t)Dtot) + align16(4 * (size_t)Dtot) + align16(sizeof(SegScal) * S) +
+           3 * align16(4 * 32 * (size_t)S) + align16(4 * 32) + align16(4 * (size_t)(S + 1)) +
+           2 * align16(4 * (size_t)(topk + 1));
+}
+
+__device__ WarpSmem warp_smem_layout(char *base, int Dtot, int S, int topk) {
+    WarpSmem w;
+    size_t o = 0;
+    w.lut = (uint16_t *)(base + o);
+    o += align16(2 * 4 * (size_t)Dtot);
+    w.qres = (float *)(base + o);
+    o += align16(4 * (size_t)Dtot);
+    w.scal = (SegScal *)(base + o);
+    o += align16(sizeof(SegScal) * S);
+    w.cd = (float *)(base + o);
+    o += align16(4 * 32 * (size_t)S);
+    w.ipx = (float *)(base + o);
+    o += align16(4 * 32 * (size_t)S);
+    w.part = (float *)(base + o);
+    o += align16(4 * 32 * (size_t)S);
+    w.cur = (float *)(base + o);
+    o += align16(4 * 32);
+    w.stage = (float *)(base + o);
+    o += align16(4 * (size_t)(S + 1));
+    w.pool_id = (uint32_t *)(base + o);
+    o += align16(4 * (size_t)(topk + 1));
+    w.pool_d = (float *)(base + o);
+    return w;
+}
+
+// Lut::prepare for every segment of cluster c, by one warp.
+__device__ void prepare_cluster_warp(const DevIndexView &ix, const float *__restrict__ qrot,
+                                     const float *__restrict__ prune, int c, WarpSmem &ws) {
+    const int lane = threadIdx.x & 31, S = ix.S;
+    for (int i = lane; i < ix.Dtot; i += 32) {
+        int s = 0;
+        while (s + 1 < S && i >= ix.seg[s + 1].qoff) ++s;
+        const SegDev &g = ix.seg[s];
+        ws.qres[i] = __fsub_rn(qrot[i], g.cent[(size_t)c * g.dim + (i - g.qoff)]);
+    }
+    __syncwarp();
+    for (int s = 0; s < S; ++s) {
+        const SegDev &g = ix.seg[s];
+        const float *qr = ws.qres + g.qoff;
+        const float sum_q = warp_eigen_sum(g.dim, [&](int i) { return qr[i]; });
+        const float q2 = warp_eigen_sum(g.dim, [&](int i) { return __fmul_rn(qr[i], qr[i]); });
+        const int ncb = g.dim / 4;
+        float lo = FLT_MAX, hi = -FLT_MAX;
+        for (int cb = lane; cb < ncb; cb += 32) {
+            float t[16];
+            lut_entries(qr + cb * 4, t);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                lo = fminf(lo, t[j]);
+                hi = fmaxf(hi, t[j]);
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(kFull, lo, o));
+            hi = fmaxf(hi, __shfl_xor_sync(kFull, hi, o));
+        }
+        const float delta = (float)__ddiv_rn((double)__fsub_rn(hi, lo), 65536.0 - 0.01);
+        uint16_t *lut = ws.lut + 4 * g.qoff;
+        for (int cb = lane; cb < ncb; cb += 32) {
+            float t[16];
+            lut_entries(qr + cb * 4, t);
+            uint32_t packed[8];
+#pragma unroll
+            for (int j = 0; j < 16; j += 2) {
+                const uint32_t a = (uint16_t)(int)__fdiv_rn(__fsub_rn(t[j], lo), delta);
+                const uint32_t b = (uint16_t)(int)__fdiv_rn(__fsub_rn(t[j + 1], lo), delta);
+                packed[j / 2] = a | (b << 16);
+            }
+            uint4 *dst = reinterpret_cast<uint4 *>(lut + cb * 16);
+            dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+            dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+        }
+        if (lane == 0) {
+            SegScal &sc = ws.scal[s];
+            sc.delta = delta;
+            sc.vl = lo;
+            sc.sum_vl = (float)__dmul_rn(__dadd_rn((double)lo, __dmul_rn(0.5, (double)delta)), (double)(float)ncb);
+            sc.sum_q = sum_q;
+            sc.q_l2sqr = q2;
+            sc.q_l2norm = sqrtf(q2);
+            sc.c1 = (float)__dsub_rn(__dmul_rn(0.5, (double)sum_q), (double)__fmul_rn(0.58f, sc.q_l2norm));
+            const float one_over_sqrtD = (float)__ddiv_rn(1.0, (double)sqrtf((float)g.dim));
+            sc.c2 = __fmul_rn(__fdiv_rn(4.0f, 0.8f), one_over_sqrtD);
+            sc.vfac = __fsub_rn(q2, __fmul_rn(2.0f, prune[s]));
+        }
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(kWarpsPerCta * 32) k_scan_warp(DevIndexView ix, const uint32_t *__restrict__ probe,
+                                                                 int nprobe, int nq, const float *__restrict__ qrot_all,
+                                                                 const float *__restrict__ prune_all, int topk,
+                                                                 uint32_t *__restrict__ out_ids,
+                                                                 float *__restrict__ out_d,
+                                                                 unsigned long long *__restrict__ counters,
+                                                                 size_t per_warp) {
+    extern __shared__ __align__(16) char smem_raw[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, S = ix.S;
+    const int qi = blockIdx.x * kWarpsPerCta + w;
+    if (qi >= nq) return;
+    WarpSmem ws = warp_smem_layout(smem_raw + w * per_warp, ix.Dtot, S, topk);
+    for (int i = lane; i <= topk; i += 32) {
+        ws.pool_id[i] = 0;
+        ws.pool_d[i] = 0.0f;
+    }
+    int sz = 0;
+    float dk = FLT_MAX;
+    unsigned long long c_blocks = 0, c_vecs = 0, c_rr = 0, c_spec = 0;
+    const uint32_t *pr = probe + (size_t)qi * nprobe;
+    const float *qrot = qrot_all + (size_t)qi * ix.Dtot, *prune = prune_all + (size_t)qi * S;
+    for (int p = 0; p < nprobe; ++p) {
+        const int c = (int)pr[p];
+        prepare_cluster_warp(ix, qrot, prune, c, ws);
+        const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
+        const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
+        c_blocks += nb;
+        c_vecs += n;
+        for (int b = 0; b < nb; ++b) {
+            const int64_t gb = b0 + b;
+            // estimates (saq_searcher.hpp:87-132 / 185-195), lane = vector
+            float cur = 0.0f;
+            int nst = 0;
+            bool pass = true;
+            if (S == 1) {
+                const SegDev &g = ix.seg[0];
+                const float on = g.onorm[gb * 32 + lane];
+                float ipx = 0.0f;
+                const float est = g.bits ? fast_est(g, ws.lut, ws.scal[0], gb, lane, on, ipx) : vars_est(ws.scal[0], on);
+                ws.cd[lane] = est;
+                ws.ipx[lane] = ipx;
+                cur = est;
+            } else {
+                float cdv[kMaxSeg];
+                for (int s = 0; s < S; ++s) {
+                    cdv[s] = vars_est(ws.scal[s], ix.seg[s].onorm[gb * 32 + lane]);
+                    cur = __fadd_rn(cur, cdv[s]);
+                }
+                float mi = warp_min_tree(cur);
+                pass = !(mi > dk);
+                ws.stage[0] = mi;  // all lanes write the same value
+                nst = 1;
+                for (int s = 0; s < S && pass; ++s) {
+                    const SegDev &g = ix.seg[s];
+                    if (!g.bits) continue;
+                    const float on = g.onorm[gb * 32 + lane];
+                    cur = __fsub_rn(cur, cdv[s]);
+                    float ipx;
+                    cdv[s] = fast_est(g, ws.lut + 4 * g.qoff, ws.scal[s], gb, lane, on, ipx);
+                    ws.ipx[s * 32 + lane] = ipx;
+                    cur = __fadd_rn(cur, cdv[s]);
+                    mi = warp_min_tree(cur);
+                    pass = !(mi > dk);
+                    ++nst;
+                }
+                for (int s = 0; s < S; ++s) ws.cd[s * 32 + lane] = cdv[s];
+            }
+            // candidates under the exact distk at the block's start
+            bool cand;
+            if (S == 1) {
+                const int cnp = (b == nb - 1) ? (n % 32) : 32;  // scanCluster's last-block count
+                cand = lane < cnp && cur < dk;
+            } else {
+                cand = pass && cur < dk && (b * 32 + lane) < n;
+            }
+            const uint32_t cm = __ballot_sync(kFull, cand);
+            if (!cm) continue;
+            if (cand) {  // re-rank this lane's vector: every segment, thread-level chains
+                const int64_t gv = v0 + (int64_t)b * 32 + lane;
+                for (int s = 0; s < S; ++s) {
+                    const SegDev &g = ix.seg[s];
+                    const float ex = g.bits > 1 ? excode_ip_thread(ws.qres + g.qoff, g.lcode + (size_t)gv * g.lstride,
+                                                                   g.dim, g.bits - 1)
+                                                : 0.0f;
+                    const float acc = accurate_dist(g.onorm[gb * 32 + lane], ws.ipx[s * 32 + lane], ex, g.exfac[gv].x,
+                                                    g.bits, ws.scal[s].sum_q, ws.scal[s].q_l2sqr);
+                    ws.part[s * 32 + lane] = S == 1 ? acc : __fsub_rn(acc, ws.cd[s * 32 + lane]);
+                }
+            }
+            ws.cur[lane] = cur;
+            __syncwarp();
+            if (lane == 0) {
+                c_spec += __popc(cm);
+                replay_block(S, n, nb, b, ws.cur, ws.stage, 0, ws.part, cm, ix.ids + v0, ws.pool_id, ws.pool_d, sz,
+                             topk, dk, nullptr, c_rr);
+            }
+            dk = __shfl_sync(kFull, dk, 0);
+            sz = __shfl_sync(kFull, sz, 0);
+            __syncwarp();
+        }
+    }
+    if (lane == 0 && counters) {
+        atomicAdd(counters + 0, c_blocks);
+        atomicAdd(counters + 1, c_vecs);
+        atomicAdd(counters + 2, c_rr);
+        atomicAdd(counters + 3, c_spec);
+    }
+    __syncwarp();
+    for (int i = lane; i < topk; i += 32) {
+        out_ids[(size_t)qi * topk + i] = ws.pool_id[i];
+        if (out_d) out_d[(size_t)qi * topk + i] = i < sz ? ws.pool_d[i] : FLT_MAX;
+    }
+}
+
 // ------------------------------------------------------------------ split scan
 // For latency-bound calls (one query, or a few).  The first tile of the
 // nearest cluster is scanned exactly; the pool's distk afterwards, tau1, bounds
@@ -1026,12 +1255,15 @@ size_t split_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t npr
 }
 
 // Which exact scan serves a call: the split scan for latency-bound calls (few
-// queries), one CTA per query for batches.  SAQG_SCAN_MODE=seq|split forces one.
-bool use_split(int64_t nq) {
+// queries), one warp per query for batches.  SAQG_SCAN_MODE=seq|split|warp forces one.
+// 0: one CTA per query, 1: split scan, 2: one warp per query.
+int scan_mode(int64_t nq, int64_t topk) {
     const char *m = std::getenv("SAQG_SCAN_MODE");
-    if (m && std::string(m) == "seq") return false;
-    if (m && std::string(m) == "split") return true;
-    return nq <= 16;
+    if (m && std::string(m) == "seq") return 0;
+    if (m && std::string(m) == "split") return 1;
+    if (m && std::string(m) == "warp") return topk <= 256 ? 2 : 0;
+    if (nq <= 16) return 1;
+    return topk <= 256 ? 2 : 0;
 }
 
 int xstride_of(const DevIndexView &ix) {
@@ -1103,7 +1335,16 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         uint32_t *ids_out = host ? oid : ids;
         float *d_out = host ? od : dists;
         unsigned long long *cnt = stats ? counters : nullptr;
-        if (!use_split(nq)) {
+        const int mode = scan_mode(nq, topk);
+        if (mode == 2) {
+            const size_t per_warp = align16(warp_smem_bytes(ix.Dtot, ix.S, (int)topk));
+            const size_t wsm = per_warp * kWarpsPerCta;
+            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+            k_scan_warp<<<(unsigned)((nq + kWarpsPerCta - 1) / kWarpsPerCta), kWarpsPerCta * 32, wsm, st>>>(
+                ix, probe, (int)nprobe, (int)nq, qrot, prune, (int)topk, ids_out, d_out, cnt, per_warp);
+            check_launch("k_scan_warp");
+            count_launch(4);
+        } else if (mode == 0) {
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ids_out,
                                                               d_out, flags + 1, cnt, xs);

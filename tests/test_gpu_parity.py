@@ -26,9 +26,9 @@ def saqg():
     return ivf
 
 
-@pytest.fixture(params=["seq", "split"])
+@pytest.fixture(params=["seq", "split", "warp"])
 def scan_mode(request, monkeypatch):
-    """Both exact scan implementations: one CTA per query, and the split scan."""
+    """The three exact scan implementations: CTA per query, split scan, warp per query."""
     monkeypatch.setenv("SAQG_SCAN_MODE", request.param)
     return request.param
 
