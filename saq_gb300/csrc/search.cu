@@ -32,6 +32,8 @@ namespace {
 
 constexpr int kScanWarps = 8;
 constexpr int kScanThreads = kScanWarps * 32;
+constexpr int kBlocksPerWarp = 2;
+constexpr int kTileB = kScanWarps * kBlocksPerWarp;  // blocks per tile
 constexpr int kMaxTopK = 4096;
 
 struct SegScal {
@@ -339,11 +341,11 @@ __host__ __device__ inline size_t scan_smem_bytes(int Dtot, int S, int topk, int
     b += align16(sizeof(uint16_t) * 4 * (size_t)Dtot);
     b += align16(sizeof(float) * Dtot);
     b += align16(sizeof(SegScal) * S);
-    b += 3 * align16(sizeof(float) * kScanWarps * S * 32);  // cd, ipx, part
-    b += align16(sizeof(float) * kScanWarps * 32);          // cur
-    b += align16(sizeof(float) * kScanWarps * (S + 1));     // stage minima
-    b += align16(sizeof(uint32_t) * kScanWarps);
-    b += align16(sizeof(int) * kScanWarps);
+    b += 3 * align16(sizeof(float) * kTileB * S * 32);  // cd, ipx, part
+    b += align16(sizeof(float) * kTileB * 32);          // cur
+    b += align16(sizeof(float) * kTileB * (S + 1));     // stage minima
+    b += align16(sizeof(uint32_t) * kTileB);
+    b += align16(sizeof(int) * kTileB);
     b += align16(sizeof(uint32_t) * (topk + 1));
     b += align16(sizeof(float) * (topk + 1));
     return b;
@@ -364,19 +366,19 @@ __device__ ScanSmem scan_smem_layout(char *base, int Dtot, int S, int topk, int 
     s.scal = (SegScal *)(base + o);
     o += align16(sizeof(SegScal) * S);
     s.cd = (float *)(base + o);
-    o += align16(sizeof(float) * kScanWarps * S * 32);
+    o += align16(sizeof(float) * kTileB * S * 32);
     s.ipx = (float *)(base + o);
-    o += align16(sizeof(float) * kScanWarps * S * 32);
+    o += align16(sizeof(float) * kTileB * S * 32);
     s.part = (float *)(base + o);
-    o += align16(sizeof(float) * kScanWarps * S * 32);
+    o += align16(sizeof(float) * kTileB * S * 32);
     s.cur = (float *)(base + o);
-    o += align16(sizeof(float) * kScanWarps * 32);
+    o += align16(sizeof(float) * kTileB * 32);
     s.stage = (float *)(base + o);
-    o += align16(sizeof(float) * kScanWarps * (S + 1));
+    o += align16(sizeof(float) * kTileB * (S + 1));
     s.cmask = (uint32_t *)(base + o);
-    o += align16(sizeof(uint32_t) * kScanWarps);
+    o += align16(sizeof(uint32_t) * kTileB);
     s.nstage = (int *)(base + o);
-    o += align16(sizeof(int) * kScanWarps);
+    o += align16(sizeof(int) * kTileB);
     s.pool_id = (uint32_t *)(base + o);
     o += align16(sizeof(uint32_t) * (topk + 1));
     s.pool_d = (float *)(base + o);
@@ -514,35 +516,41 @@ __device__ __forceinline__ bool stages_pass(const float *st, int n, float tau) {
     return true;
 }
 
-// Steps 1-3 of a tile of up to kScanWarps blocks (warp w <-> block t0 + w of
-// cluster c): estimates, candidate masks under `tau`, and the accurate
+// Steps 1-3 of a tile of up to kTileB blocks (warp w <-> blocks t0 + w + k * kScanWarps
+// of the cluster): estimates, candidate masks under `tau`, and the accurate
 // distances (multi-segment: accurate - estimate per segment) of every
 // candidate lane.  Ends with the partials in sm.part and the masks in sm.cmask.
 __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0, int64_t v0, int nb, int n, int t0,
                                 int t_end, float tau) {
     const int S = ix.S, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    const int b = t0 + w;
-    const bool active = b < t_end;
-    if (active) block_estimates(ix, b0 + b, sm, w, lane);
+#pragma unroll
+    for (int k = 0; k < kBlocksPerWarp; ++k) {
+        const int slot = w + k * kScanWarps, b = t0 + slot;
+        if (b < t_end) block_estimates(ix, b0 + b, sm, slot, lane);
+    }
     __syncthreads();
-    if (active) {
-        bool cand;
-        if (S == 1) {
-            const int cnp = (b == nb - 1) ? (n % 32) : 32;  // scanCluster's last-block count (saq_searcher.hpp:186)
-            cand = lane < cnp && sm.cd[w * 32 + lane] < tau;
-        } else {
-            cand = stages_pass(sm.stage + w * (S + 1), sm.nstage[w], tau) && sm.cur[w * 32 + lane] < tau &&
-                   (b * 32 + lane) < n;
+#pragma unroll
+    for (int k = 0; k < kBlocksPerWarp; ++k) {
+        const int slot = w + k * kScanWarps, b = t0 + slot;
+        if (b < t_end) {
+            bool cand;
+            if (S == 1) {
+                const int cnp = (b == nb - 1) ? (n % 32) : 32;  // scanCluster's last-block count (saq_searcher.hpp:186)
+                cand = lane < cnp && sm.cd[slot * 32 + lane] < tau;
+            } else {
+                cand = stages_pass(sm.stage + slot * (S + 1), sm.nstage[slot], tau) && sm.cur[slot * 32 + lane] < tau &&
+                       (b * 32 + lane) < n;
+            }
+            const uint32_t m = __ballot_sync(kFull, cand);
+            if (lane == 0) sm.cmask[slot] = m;
+        } else if (lane == 0) {
+            sm.cmask[slot] = 0;
         }
-        const uint32_t m = __ballot_sync(kFull, cand);
-        if (lane == 0) sm.cmask[w] = m;
-    } else if (lane == 0) {
-        sm.cmask[w] = 0;
     }
     __syncthreads();
     // accurate distances: one thread per (candidate vector, segment)
     int total = 0;
-    for (int i = 0; i < kScanWarps; ++i) total += __popc(sm.cmask[i]);
+    for (int i = 0; i < kTileB; ++i) total += __popc(sm.cmask[i]);
     total *= S;
     for (int t = tid; t < total; t += blockDim.x) {
         int r = t / S, s = t - r * S, ww = 0;
@@ -625,13 +633,13 @@ __device__ void scan_probes(const DevIndexView &ix, const uint32_t *__restrict__
         const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
         tl.blocks += nb;
         tl.vecs += n;
-        for (int t0 = 0; t0 < nb; t0 += kScanWarps) {
+        for (int t0 = 0; t0 < nb; t0 += kTileB) {
             tile_candidates(ix, sm, b0, v0, nb, n, t0, nb, distk);
             if (tid == 0) {
-                for (int i = 0; i < kScanWarps; ++i) tl.spec += __popc(sm.cmask[i]);
+                for (int i = 0; i < kTileB; ++i) tl.spec += __popc(sm.cmask[i]);
                 float dk = distk;
                 int sz = pool_size;
-                for (int ww = 0; ww < kScanWarps && t0 + ww < nb; ++ww)
+                for (int ww = 0; ww < kTileB && t0 + ww < nb; ++ww)
                     replay_block(S, n, nb, t0 + ww, sm.cur + ww * 32, sm.stage + ww * (S + 1), sm.nstage[ww],
                                  S == 1 ? sm.part + ww * 32 : sm.part + ww * S * 32, sm.cmask[ww], ix.ids + v0,
                                  sm.pool_id, sm.pool_d, sz, topk, dk, err, tl.rr);
@@ -929,7 +937,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_scan_warp(DevIndexView ix
 // order.  A final pass per query walks the positions in order and replays the
 // reference's decisions on the records.  Blocks without a record cannot insert
 // anything (none of their lanes is below tau1 >= distk), so the replay is exact.
-constexpr int kTileBlocks = 8;
+constexpr int kTileBlocks = 16;
 constexpr int kFirstBlocks = 16;
 
 struct SplitState {
@@ -972,13 +980,13 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
         const int fe = min(nb, kFirstBlocks);
         tl.blocks += fe;
         tl.vecs += min(n, fe * 32);
-        for (int t0 = 0; t0 < fe; t0 += kScanWarps) {
+        for (int t0 = 0; t0 < fe; t0 += kTileB) {
             tile_candidates(ix, sm, b0, v0, nb, n, t0, fe, distk);
             if (tid == 0) {
-                for (int i = 0; i < kScanWarps; ++i) tl.spec += __popc(sm.cmask[i]);
+                for (int i = 0; i < kTileB; ++i) tl.spec += __popc(sm.cmask[i]);
                 float dk = distk;
                 int sz = pool_size;
-                for (int ww = 0; ww < kScanWarps && t0 + ww < fe; ++ww)
+                for (int ww = 0; ww < kTileB && t0 + ww < fe; ++ww)
                     replay_block(S, n, nb, t0 + ww, sm.cur + ww * 32, sm.stage + ww * (S + 1), sm.nstage[ww],
                                  S == 1 ? sm.part + ww * 32 : sm.part + ww * S * 32, sm.cmask[ww], ix.ids + v0,
                                  sm.pool_id, sm.pool_d, sz, topk, dk, err, tl.rr);
@@ -1065,9 +1073,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
         }
         const float tau = st.tau[q];
         const int64_t base = st.blk_base[(size_t)q * nprobe + p];
-        for (int t0 = bstart; t0 < bend; t0 += kScanWarps) {
+        for (int t0 = bstart; t0 < bend; t0 += kTileB) {
             tile_candidates(ix, sm, b0, v0, nb, n, t0, bend, tau);
-            const int w = tid >> 5, lane = tid & 31, b = t0 + w;
+            const int lane = tid & 31;
+            for (int k = 0; k < kBlocksPerWarp; ++k) {
+            const int w = (tid >> 5) + k * kScanWarps, b = t0 + w;
             if (b < bend) {
                 const uint32_t cm = sm.cmask[w];
                 const int64_t pos = base + b;
@@ -1087,6 +1097,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
                     r[8 + (S + 1) + lane] = sm.cur[w * 32 + lane];
                     for (int s = 0; s < S; ++s) r[8 + (S + 1) + 32 + s * 32 + lane] = sm.part[(w * S + s) * 32 + lane];
                 }
+            }
             }
             __syncthreads();
         }
@@ -1255,7 +1266,7 @@ size_t split_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t npr
 }
 
 // Which exact scan serves a call: the split scan for latency-bound calls (few
-// queries), one warp per query for batches.  SAQG_SCAN_MODE=seq|split|warp forces one.
+// queries), one CTA per query for batches.  SAQG_SCAN_MODE=seq|split|warp forces one.
 // 0: one CTA per query, 1: split scan, 2: one warp per query.
 int scan_mode(int64_t nq, int64_t topk) {
     const char *m = std::getenv("SAQG_SCAN_MODE");
@@ -1263,14 +1274,10 @@ int scan_mode(int64_t nq, int64_t topk) {
     if (m && std::string(m) == "split") return 1;
     if (m && std::string(m) == "warp") return topk <= 256 ? 2 : 0;
     if (nq <= 16) return 1;
-    return topk <= 256 ? 2 : 0;
+    return 0;
 }
 
-int xstride_of(const DevIndexView &ix) {
-    int m = 16;
-    for (int s = 0; s < ix.S; ++s) m = std::max(m, ix.seg[s].lstride);
-    return m;
-}
+int xstride_of(const DevIndexView &) { return 0; }  // re-rank reads ex-codes in place (no staging buffer)
 
 void check_launch(const char *what) {
     cudaError_t e = cudaGetLastError();
