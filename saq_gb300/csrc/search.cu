@@ -552,6 +552,23 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
     int total = 0;
     for (int i = 0; i < kTileB; ++i) total += __popc(sm.cmask[i]);
     total *= S;
+    // first pull every task's ex-code row into L1, so the chains below do not
+    // wait on memory group by group
+    for (int t = tid; t < total; t += blockDim.x) {
+        int r = t / S, s = t - r * S, ww = 0;
+        while (r >= __popc(sm.cmask[ww])) {
+            r -= __popc(sm.cmask[ww]);
+            ++ww;
+        }
+        uint32_t mk = sm.cmask[ww];
+        for (int i = 0; i < r; ++i) mk &= mk - 1;
+        const int j = __ffs(mk) - 1;
+        const SegDev &g = ix.seg[s];
+        if (g.bits > 1) {
+            const uint8_t *row = g.lcode + (size_t)(v0 + (int64_t)(t0 + ww) * 32 + j) * g.lstride;
+            for (int o = 0; o < g.lstride; o += 128) asm volatile("prefetch.global.L1 [%0];" ::"l"(row + o));
+        }
+    }
     for (int t = tid; t < total; t += blockDim.x) {
         int r = t / S, s = t - r * S, ww = 0;
         while (r >= __popc(sm.cmask[ww])) {
@@ -616,6 +633,52 @@ __device__ __forceinline__ void replay_block(int S, int n, int nb, int bb, const
     }
 }
 
+// replay_block for a whole warp: the lanes first discard, in parallel, the
+// candidates that cannot change the pool (their insert would be rejected
+// whatever happens earlier in the block: the estimate is not below the
+// block-start distk, or the first partial distance already exceeds it), then
+// lane 0 replays the rest in order.  Same pool state as replay_block.
+__device__ __forceinline__ void replay_block_warp(int S, int bb, const float *cur, const float *stage, int nstage,
+                                                  const float *part, uint32_t cm, const uint32_t *ids_v0,
+                                                  uint32_t *pid, float *pd, int &sz, int topk, float &dk,
+                                                  unsigned long long &c_rr) {
+    const int lane = threadIdx.x & 31;
+    if (!cm) return;
+    if (S > 1 && !stages_pass(stage, nstage, dk)) return;
+    const bool in = (cm >> lane) & 1u;
+    const float c = in ? cur[lane] : FLT_MAX;
+    const uint32_t m = __ballot_sync(kFull, in && c < dk);  // lanes whose accurate distance the reference computes
+    const float first = in ? (S == 1 ? part[lane] : __fadd_rn(c, part[lane])) : FLT_MAX;
+    // while the pool is not full every candidate inserts (ResultPool rejects only when full)
+    uint32_t need = __ballot_sync(kFull, in && c < dk && (sz < topk || !(first > dk)));
+    if (lane == 0) {
+        c_rr += __popc(m);
+        if (S == 1) {
+            while (need) {
+                const int j = __ffs(need) - 1;
+                need &= need - 1;
+                pool_insert(pid, pd, sz, topk, ids_v0[(int64_t)bb * 32 + j], part[j]);
+                dk = sz == topk ? pd[sz - 1] : FLT_MAX;
+            }
+        } else {
+            while (need) {
+                const int j = __ffs(need) - 1;
+                need &= need - 1;
+                if (!(cur[j] < dk)) continue;
+                float acc = cur[j];
+                for (int s = 0; s < S; ++s) {
+                    acc = __fadd_rn(acc, part[s * 32 + j]);
+                    if (acc >= dk) break;
+                }
+                pool_insert(pid, pd, sz, topk, ids_v0[(int64_t)bb * 32 + j], acc);
+                dk = sz == topk ? pd[sz - 1] : FLT_MAX;
+            }
+        }
+    }
+    dk = __shfl_sync(kFull, dk, 0);
+    sz = __shfl_sync(kFull, sz, 0);
+}
+
 struct ScanTally {
     unsigned long long blocks = 0, vecs = 0, rr = 0, spec = 0;
 };
@@ -635,16 +698,19 @@ __device__ void scan_probes(const DevIndexView &ix, const uint32_t *__restrict__
         tl.vecs += n;
         for (int t0 = 0; t0 < nb; t0 += kTileB) {
             tile_candidates(ix, sm, b0, v0, nb, n, t0, nb, distk);
-            if (tid == 0) {
-                for (int i = 0; i < kTileB; ++i) tl.spec += __popc(sm.cmask[i]);
+            if (tid < 32) {
+                if (tid == 0)
+                    for (int i = 0; i < kTileB; ++i) tl.spec += __popc(sm.cmask[i]);
                 float dk = distk;
                 int sz = pool_size;
                 for (int ww = 0; ww < kTileB && t0 + ww < nb; ++ww)
-                    replay_block(S, n, nb, t0 + ww, sm.cur + ww * 32, sm.stage + ww * (S + 1), sm.nstage[ww],
-                                 S == 1 ? sm.part + ww * 32 : sm.part + ww * S * 32, sm.cmask[ww], ix.ids + v0,
-                                 sm.pool_id, sm.pool_d, sz, topk, dk, err, tl.rr);
-                distk = dk;
-                pool_size = sz;
+                    replay_block_warp(S, t0 + ww, sm.cur + ww * 32, sm.stage + ww * (S + 1), sm.nstage[ww],
+                                      S == 1 ? sm.part + ww * 32 : sm.part + ww * S * 32, sm.cmask[ww], ix.ids + v0,
+                                      sm.pool_id, sm.pool_d, sz, topk, dk, tl.rr);
+                if (tid == 0) {
+                    distk = dk;
+                    pool_size = sz;
+                }
             }
             __syncthreads();
         }
@@ -982,16 +1048,19 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
         tl.vecs += min(n, fe * 32);
         for (int t0 = 0; t0 < fe; t0 += kTileB) {
             tile_candidates(ix, sm, b0, v0, nb, n, t0, fe, distk);
-            if (tid == 0) {
-                for (int i = 0; i < kTileB; ++i) tl.spec += __popc(sm.cmask[i]);
+            if (tid < 32) {
+                if (tid == 0)
+                    for (int i = 0; i < kTileB; ++i) tl.spec += __popc(sm.cmask[i]);
                 float dk = distk;
                 int sz = pool_size;
                 for (int ww = 0; ww < kTileB && t0 + ww < fe; ++ww)
-                    replay_block(S, n, nb, t0 + ww, sm.cur + ww * 32, sm.stage + ww * (S + 1), sm.nstage[ww],
-                                 S == 1 ? sm.part + ww * 32 : sm.part + ww * S * 32, sm.cmask[ww], ix.ids + v0,
-                                 sm.pool_id, sm.pool_d, sz, topk, dk, err, tl.rr);
-                distk = dk;
-                pool_size = sz;
+                    replay_block_warp(S, t0 + ww, sm.cur + ww * 32, sm.stage + ww * (S + 1), sm.nstage[ww],
+                                      S == 1 ? sm.part + ww * 32 : sm.part + ww * S * 32, sm.cmask[ww], ix.ids + v0,
+                                      sm.pool_id, sm.pool_d, sz, topk, dk, tl.rr);
+                if (tid == 0) {
+                    distk = dk;
+                    pool_size = sz;
+                }
             }
             __syncthreads();
         }
