@@ -44,10 +44,11 @@ def _spectrum(d, alpha, dev):
 
 def zipf_aniso(n: int, d: int, k: int, nq: int, s: float = 1.1, alpha: float = 0.8, sigma: float = 0.2,
                noise_alpha: float | None = None, seed: int = 0, device: str = "cuda",
-               chunk: int = 1 << 20) -> Workload:
+               chunk: int = 1 << 20, query_clusters: str = "zipf") -> Workload:
     """Zipf-sized clusters of unit-norm vectors.  Centres follow the per-axis
     spectrum i^-alpha; the within-cluster noise follows i^-noise_alpha
-    (default: the same spectrum)."""
+    (default: the same spectrum).  Queries pick their cluster with the Zipf
+    weights ("zipf") or uniformly ("uniform")."""
     torch.backends.cuda.matmul.allow_tf32 = False
     dev = torch.device(device)
     rng = np.random.default_rng(seed)
@@ -74,7 +75,8 @@ def zipf_aniso(n: int, d: int, k: int, nq: int, s: float = 1.1, alpha: float = 0
         return out
 
     x = draw(labels)
-    w = torch.as_tensor(sizes / sizes.sum(), device=dev, dtype=torch.float32)
+    w = torch.as_tensor(sizes / sizes.sum() if query_clusters == "zipf" else np.full(k, 1.0 / k), device=dev,
+                        dtype=torch.float32)
     qlab = torch.multinomial(w, nq, replacement=True, generator=g)
     q = draw(qlab)
     # PCA (python/pca.py): covariance of a sample in FP32 GEMMs, eigendecomposition on the host in FP64
