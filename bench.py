@@ -59,8 +59,9 @@ def parse():
     ap.add_argument("--target-recall", type=float, default=0.95)
     ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "saqg_bench_cache"))
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--sigma", type=float, default=0.35)
-    ap.add_argument("--noise-alpha", type=float, default=1.2)
+    ap.add_argument("--sigma", type=float, default=0.2)
+    ap.add_argument("--noise-alpha", type=float, default=1.6)
+    ap.add_argument("--query-clusters", default="uniform", choices=["uniform", "zipf"])
     return ap.parse_args()
 
 
@@ -131,7 +132,8 @@ def dist_env():
 
 
 def cache_paths(a):
-    key = f"v{CACHE_VERSION}_n{a.n}_d{a.dim}_k{a.clusters}_b{a.bits}_s{a.sigma}_na{a.noise_alpha}_seed0"
+    key = (f"v{CACHE_VERSION}_n{a.n}_d{a.dim}_k{a.clusters}_b{a.bits}_s{a.sigma}_na{a.noise_alpha}"
+           f"_q{a.query_clusters}_seed0")
     d = os.path.join(a.cache, key)
     os.makedirs(d, exist_ok=True)
     return d, os.path.join(d, "index.saq"), os.path.join(d, "meta.json")
@@ -140,7 +142,7 @@ def cache_paths(a):
 def build_workload(a, torch):
     from saq_gb300 import workloads
     return workloads.zipf_aniso(a.n, a.dim, a.clusters, nq=max(a.batch, a.gt_queries, a.plain_queries), seed=0,
-                                sigma=a.sigma, noise_alpha=a.noise_alpha)
+                                sigma=a.sigma, noise_alpha=a.noise_alpha, query_clusters=a.query_clusters)
 
 
 def get_index_and_meta(a, torch, wl, log):
@@ -223,7 +225,7 @@ def main():
               "nprobe": nprobe, f"recall@{a.topk}": round(meta["recall"], 4), "plan": meta["plan"],
               "l2": "flushed between timed steps (256 MiB write)", "queries": "same distribution as the base set",
               "data_model": f"unit-norm; centre spectrum i^-0.8, within-cluster spectrum i^-{a.noise_alpha:g}, "
-                            f"sigma {a.sigma:g}"}
+                            f"sigma {a.sigma:g}; query clusters {a.query_clusters}"}
 
     if a.impl == "reference":
         qh = wl.q.cpu().numpy()
