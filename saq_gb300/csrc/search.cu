@@ -745,26 +745,6 @@ __device__ void write_results(const ScanSmem &sm, int pool_size, int topk, uint3
     }
 }
 
-// One CTA per query: the whole probe list sequentially.
-__global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const uint32_t *__restrict__ probe, int nprobe,
-                                                       const float *__restrict__ qrot_all,
-                                                       const float *__restrict__ prune_all, int topk,
-                                                       uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
-                                                       int *__restrict__ err, unsigned long long *__restrict__ counters,
-                                                       int xstride) {
-    extern __shared__ __align__(16) char smem_raw[];
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, topk, xstride);
-    __shared__ int pool_size;
-    __shared__ float distk;
-    const int qi = blockIdx.x;
-    ScanTally tl;
-    init_pool(sm, topk, pool_size, distk);
-    scan_probes(ix, probe + (size_t)qi * nprobe, 0, nprobe, qrot_all + (size_t)qi * ix.Dtot, prune_all + (size_t)qi * ix.S,
-                topk, sm, pool_size, distk, err, tl);
-    flush_tally(tl, counters);
-    write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
-}
-
 // ------------------------------------------------------------------ warp scan
 // Throughput form for batches: one WARP per query, no CTA barriers.  The warp
 // walks its probes and blocks in the reference's order with the exact current
@@ -1005,23 +985,31 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_scan_warp(DevIndexView ix
 // anything (none of their lanes is below tau1 >= distk), so the replay is exact.
 constexpr int kTileBlocks = 16;
 constexpr int kFirstBlocks = 16;
+constexpr int kDeferBlocks = 2048;  // a query scanning more blocks than this takes the split pass
+                                     // (SAQG_DEFER_BLOCKS overrides it; 0 disables deferral)
 
 struct SplitState {
-    uint32_t *pool_id;   // [nq][topk]
-    float *pool_d;       // [nq][topk]
-    int *pool_size;      // [nq]
-    float *tau;          // [nq]
-    int *tile_off;       // [nq][nprobe + 1] tiles before probe p
-    int *blk_base;       // [nq][nprobe] scan-order position of the probe's first block
-    int *q_tile_off;     // [nq + 1]
-    int *npos;           // [nq] scan positions of the query
-    uint8_t *flag;       // [nq][max_pos]
-    float *rec;          // [nq][max_pos][rec_words]
+    int *nlist;          // number of queries on the list (device)
+    int *qlist;          // [cap] slot -> query id
+    int cap;             // slots
+    uint32_t *pool_id;   // [cap][topk]
+    float *pool_d;       // [cap][topk]
+    int *pool_size;      // [cap]
+    float *tau;          // [cap]
+    int *tile_off;       // [cap][nprobe + 1] tiles before probe p
+    int *blk_base;       // [cap][nprobe] scan-order position of the probe's first block
+    int *q_tile_off;     // [cap + 1]
+    int *npos;           // [cap] scan positions of the query
+    uint8_t *flag;       // [cap][max_pos]
+    float *rec;          // [cap][max_pos][rec_words]
     int64_t max_pos;
     int rec_words;
 };
 
 __host__ __device__ inline int rec_words_of(int S) { return (8 + (S + 1) + 32 + 32 * S + 3) & ~3; }
+constexpr int kReplayChunk = 16;  // records staged in shared memory per replay step
+
+__device__ __forceinline__ int list_len(const SplitState &st) { return min(*st.nlist, st.cap); }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, const uint32_t *__restrict__ probe,
                                                              int nprobe, const float *__restrict__ qrot_all,
@@ -1029,11 +1017,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
                                                              SplitState st, int *__restrict__ err,
                                                              unsigned long long *__restrict__ counters, int xstride) {
     extern __shared__ __align__(16) char smem_raw[];
-    const int S = ix.S, tid = threadIdx.x;
+    const int S = ix.S, tid = threadIdx.x, slot = blockIdx.x;
+    if (slot >= list_len(st)) return;
+    const int qi = st.qlist[slot];
     ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, topk, xstride);
     __shared__ int pool_size;
     __shared__ float distk;
-    const int qi = blockIdx.x;
     ScanTally tl;
     init_pool(sm, topk, pool_size, distk);
     const uint32_t *pr = probe + (size_t)qi * nprobe;
@@ -1067,58 +1056,64 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
     }
     flush_tally(tl, counters);
     for (int i = tid; i < topk; i += blockDim.x) {
-        st.pool_id[(size_t)qi * topk + i] = sm.pool_id[i];
-        st.pool_d[(size_t)qi * topk + i] = sm.pool_d[i];
+        st.pool_id[(size_t)slot * topk + i] = sm.pool_id[i];
+        st.pool_d[(size_t)slot * topk + i] = sm.pool_d[i];
     }
     if (tid == 0) {
-        st.pool_size[qi] = pool_size;
-        st.tau[qi] = distk;
-        int tiles = 0, pos = 0;
+        st.pool_size[slot] = pool_size;
+        st.tau[slot] = distk;
+        int tiles = 0;
+        int64_t pos = 0;
         for (int p = 0; p < nprobe; ++p) {
             const int c = (int)pr[p];
             const int nb = (int)(ix.blk_off[c + 1] - ix.blk_off[c]);
-            st.tile_off[(size_t)qi * (nprobe + 1) + p] = tiles;
-            st.blk_base[(size_t)qi * nprobe + p] = pos;
+            st.tile_off[(size_t)slot * (nprobe + 1) + p] = tiles;
+            st.blk_base[(size_t)slot * nprobe + p] = (int)pos;
             const int rest = p == 0 ? max(0, nb - kFirstBlocks) : nb;
             tiles += (rest + kTileBlocks - 1) / kTileBlocks;
             pos += nb;
         }
-        st.tile_off[(size_t)qi * (nprobe + 1) + nprobe] = tiles;
-        st.npos[qi] = min((int64_t)pos, st.max_pos);
+        st.tile_off[(size_t)slot * (nprobe + 1) + nprobe] = tiles;
+        st.npos[slot] = (int)min(pos, st.max_pos);
         if (pos > st.max_pos) *err = 2;
     }
 }
 
-__global__ void k_tile_prefix(SplitState st, int nq, int nprobe) {
+__global__ void k_tile_prefix(SplitState st, int nprobe) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int n = list_len(st);
     int acc = 0;
-    for (int q = 0; q < nq; ++q) {
+    for (int q = 0; q < n; ++q) {
         st.q_tile_off[q] = acc;
         acc += st.tile_off[(size_t)q * (nprobe + 1) + nprobe];
     }
-    st.q_tile_off[nq] = acc;
+    st.q_tile_off[n] = acc;
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, const uint32_t *__restrict__ probe,
-                                                            int nprobe, int nq, const float *__restrict__ qrot_all,
+                                                            int nprobe, const float *__restrict__ qrot_all,
                                                             const float *__restrict__ prune_all, SplitState st,
                                                             unsigned long long *__restrict__ counters, int xstride) {
     extern __shared__ __align__(16) char smem_raw[];
     const int S = ix.S, tid = threadIdx.x;
     ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, 1, xstride);
     ScanTally tl;
-    const int total = st.q_tile_off[nq];
-    int last_q = -1, last_c = -1;
-    for (int wi = blockIdx.x; wi < total; wi += gridDim.x) {
-        int lo = 0, hi = nq;  // query: last q with q_tile_off[q] <= wi
+    const int nl = list_len(st);
+    const int total = st.q_tile_off[nl];
+    // contiguous work ranges per CTA keep the tiles of one cluster together (LUT reuse)
+    const int per = (total + gridDim.x - 1) / gridDim.x;
+    const int w_begin = blockIdx.x * per, w_end = min(total, w_begin + per);
+    int last_slot = -1, last_c = -1;
+    for (int wi = w_begin; wi < w_end; ++wi) {
+        int lo = 0, hi = nl;  // slot: last with q_tile_off[slot] <= wi
         while (hi - lo > 1) {
             const int mid = (lo + hi) >> 1;
             if (st.q_tile_off[mid] <= wi) lo = mid;
             else hi = mid;
         }
-        const int q = lo;
-        const int local = wi - st.q_tile_off[q];
-        const int *to = st.tile_off + (size_t)q * (nprobe + 1);
+        const int slot = lo, q = st.qlist[slot];
+        const int local = wi - st.q_tile_off[slot];
+        const int *to = st.tile_off + (size_t)slot * (nprobe + 1);
         int plo = 0, phi = nprobe;  // probe: last p with to[p] <= local
         while (phi - plo > 1) {
             const int mid = (plo + phi) >> 1;
@@ -1127,9 +1122,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
         }
         const int p = plo, tile = local - to[p];
         const int c = (int)probe[(size_t)q * nprobe + p];
-        if (q != last_q || c != last_c) {  // LUTs survive across tiles of one cluster
+        if (slot != last_slot || c != last_c) {  // LUTs survive across tiles of one cluster
             prepare_cluster(ix, qrot_all + (size_t)q * ix.Dtot, prune_all + (size_t)q * S, c, sm);
-            last_q = q;
+            last_slot = slot;
             last_c = c;
         }
         const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
@@ -1140,33 +1135,34 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
             tl.blocks += bend - bstart;
             tl.vecs += min(n, bend * 32) - bstart * 32;
         }
-        const float tau = st.tau[q];
-        const int64_t base = st.blk_base[(size_t)q * nprobe + p];
+        const float tau = st.tau[slot];
+        const int64_t base = st.blk_base[(size_t)slot * nprobe + p];
         for (int t0 = bstart; t0 < bend; t0 += kTileB) {
             tile_candidates(ix, sm, b0, v0, nb, n, t0, bend, tau);
             const int lane = tid & 31;
             for (int k = 0; k < kBlocksPerWarp; ++k) {
-            const int w = (tid >> 5) + k * kScanWarps, b = t0 + w;
-            if (b < bend) {
-                const uint32_t cm = sm.cmask[w];
-                const int64_t pos = base + b;
-                if (cm && pos < st.max_pos) {
-                    float *r = st.rec + ((size_t)q * st.max_pos + pos) * st.rec_words;
-                    uint32_t *ri = reinterpret_cast<uint32_t *>(r);
-                    if (lane == 0) {
-                        ri[0] = (uint32_t)pos;
-                        ri[1] = cm;
-                        ri[2] = (uint32_t)(S == 1 ? 0 : sm.nstage[w]);
-                        ri[3] = (uint32_t)c;
-                        ri[4] = (uint32_t)b;
-                        st.flag[(size_t)q * st.max_pos + pos] = 1;
-                        if (counters) atomicAdd(counters + 3, (unsigned long long)__popc(cm));
+                const int w = (tid >> 5) + k * kScanWarps, b = t0 + w;
+                if (b < bend) {
+                    const uint32_t cm = sm.cmask[w];
+                    const int64_t pos = base + b;
+                    if (cm && pos < st.max_pos) {
+                        float *r = st.rec + ((size_t)slot * st.max_pos + pos) * st.rec_words;
+                        uint32_t *ri = reinterpret_cast<uint32_t *>(r);
+                        if (lane == 0) {
+                            ri[0] = (uint32_t)pos;
+                            ri[1] = cm;
+                            ri[2] = (uint32_t)(S == 1 ? 0 : sm.nstage[w]);
+                            ri[3] = (uint32_t)c;
+                            ri[4] = (uint32_t)b;
+                            st.flag[(size_t)slot * st.max_pos + pos] = 1;
+                            if (counters) atomicAdd(counters + 3, (unsigned long long)__popc(cm));
+                        }
+                        if (S > 1 && lane <= S) r[8 + lane] = sm.stage[w * (S + 1) + lane];
+                        r[8 + (S + 1) + lane] = sm.cur[w * 32 + lane];
+                        for (int s = 0; s < S; ++s)
+                            r[8 + (S + 1) + 32 + s * 32 + lane] = sm.part[(w * S + s) * 32 + lane];
                     }
-                    if (S > 1 && lane <= S) r[8 + lane] = sm.stage[w * (S + 1) + lane];
-                    r[8 + (S + 1) + lane] = sm.cur[w * 32 + lane];
-                    for (int s = 0; s < S; ++s) r[8 + (S + 1) + 32 + s * 32 + lane] = sm.part[(w * S + s) * 32 + lane];
                 }
-            }
             }
             __syncthreads();
         }
@@ -1177,31 +1173,43 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
     }
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, const uint32_t *__restrict__ probe,
-                                                              int nprobe, int topk, SplitState st,
+// Per query on the list: walk its scan positions in order; flagged positions
+// are compacted CTA-wide, their records staged into shared memory by all warps
+// (kReplayChunk at a time), and warp 0 replays them.
+__global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, int topk, SplitState st,
                                                               uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
-                                                              int *__restrict__ err,
                                                               unsigned long long *__restrict__ counters, int xstride) {
     extern __shared__ __align__(16) char smem_raw[];
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, topk, xstride);
+    const int S = ix.S, slot = blockIdx.x;
+    if (slot >= list_len(st)) return;
+    const int qi = st.qlist[slot];
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, topk, xstride);
+    float *stage_buf = reinterpret_cast<float *>(smem_raw + scan_smem_bytes(ix.Dtot, S, topk, xstride));
     __shared__ int pool_size;
     __shared__ float distk;
     __shared__ int list[kScanThreads];
     __shared__ int warp_cnt[kScanWarps];
-    const int qi = blockIdx.x, tid = threadIdx.x, S = ix.S, w = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     for (int i = tid; i < topk; i += blockDim.x) {
-        sm.pool_id[i] = st.pool_id[(size_t)qi * topk + i];
-        sm.pool_d[i] = st.pool_d[(size_t)qi * topk + i];
+        sm.pool_id[i] = st.pool_id[(size_t)slot * topk + i];
+        sm.pool_d[i] = st.pool_d[(size_t)slot * topk + i];
     }
     if (tid == 0) {
-        pool_size = st.pool_size[qi];
-        distk = st.tau[qi];
+        pool_size = st.pool_size[slot];
+        distk = st.tau[slot];
     }
-    const int np = st.npos[qi];
-    const uint8_t *fl = st.flag + (size_t)qi * st.max_pos;
-    const float *rq = st.rec + (size_t)qi * st.max_pos * st.rec_words;
+    const int np = st.npos[slot];
+    const uint8_t *fl = st.flag + (size_t)slot * st.max_pos;
+    const float *rq = st.rec + (size_t)slot * st.max_pos * st.rec_words;
+    const int RW = st.rec_words;
     unsigned long long rr = 0;
+    float dk = FLT_MAX;
+    int sz = 0;
     __syncthreads();
+    if (w == 0) {
+        dk = distk;
+        sz = pool_size;
+    }
     for (int base = 0; base < np; base += kScanThreads) {
         const int pos = base + tid;
         const bool f = pos < np && fl[pos];
@@ -1215,25 +1223,75 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, c
         }
         if (f) list[off + __popc(bal & ((1u << lane) - 1))] = pos;
         __syncthreads();
-        if (tid == 0 && total) {
-            float dk = distk;
-            int sz = pool_size;
-            for (int i = 0; i < total; ++i) {
-                const float *r = rq + (size_t)list[i] * st.rec_words;
-                const uint32_t *ri = reinterpret_cast<const uint32_t *>(r);
-                const int c = (int)ri[3], bb = (int)ri[4];
-                const int64_t v0 = ix.vec_off[c];
-                const int nb = (int)(ix.blk_off[c + 1] - ix.blk_off[c]), nv = (int)(ix.vec_off[c + 1] - v0);
-                replay_block(S, nv, nb, bb, r + 8 + (S + 1), r + 8, (int)ri[2], r + 8 + (S + 1) + 32, ri[1],
-                             ix.ids + v0, sm.pool_id, sm.pool_d, sz, topk, dk, err, rr);
+        for (int c0 = 0; c0 < total; c0 += kReplayChunk) {
+            const int cn = min(kReplayChunk, total - c0);
+            for (int i = tid; i < cn * RW; i += blockDim.x) {
+                const int r = i / RW, k = i - r * RW;
+                stage_buf[i] = rq[(size_t)list[c0 + r] * RW + k];
             }
-            distk = dk;
-            pool_size = sz;
+            __syncthreads();
+            if (w == 0)
+                for (int r = 0; r < cn; ++r) {
+                    const float *rec = stage_buf + r * RW;
+                    const uint32_t *ri = reinterpret_cast<const uint32_t *>(rec);
+                    const int c = (int)ri[3], bb = (int)ri[4];
+                    replay_block_warp(S, bb, rec + 8 + (S + 1), rec + 8, (int)ri[2], rec + 8 + (S + 1) + 32, ri[1],
+                                      ix.ids + ix.vec_off[c], sm.pool_id, sm.pool_d, sz, topk, dk, rr);
+                }
+            __syncthreads();
         }
-        __syncthreads();
     }
+    if (tid == 0) pool_size = sz;
     if (tid == 0 && counters) atomicAdd(counters + 2, rr);
+    __syncthreads();
     write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
+}
+
+// One CTA per query: the whole probe list sequentially.  A query whose probes
+// hold more than `defer_blocks` blocks (a giant Zipf cluster) is put on the
+// split list instead, when it has room, and answered by the split pass.
+__global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const uint32_t *__restrict__ probe, int nprobe,
+                                                       const float *__restrict__ qrot_all,
+                                                       const float *__restrict__ prune_all, int topk,
+                                                       uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
+                                                       int *__restrict__ err, unsigned long long *__restrict__ counters,
+                                                       int xstride, int defer_blocks, SplitState st) {
+    extern __shared__ __align__(16) char smem_raw[];
+    __shared__ int defer;
+    const int qi = blockIdx.x;
+    if (threadIdx.x == 0) {
+        defer = 0;
+        if (defer_blocks > 0) {
+            int64_t total = 0;
+            for (int p = 0; p < nprobe; ++p) {
+                const int c = (int)probe[(size_t)qi * nprobe + p];
+                total += ix.blk_off[c + 1] - ix.blk_off[c];
+            }
+            if (total > defer_blocks) {
+                const int t = atomicAdd(st.nlist, 1);
+                if (t < st.cap) {
+                    st.qlist[t] = qi;
+                    defer = 1;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (defer) return;
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, topk, xstride);
+    __shared__ int pool_size;
+    __shared__ float distk;
+    ScanTally tl;
+    init_pool(sm, topk, pool_size, distk);
+    scan_probes(ix, probe + (size_t)qi * nprobe, 0, nprobe, qrot_all + (size_t)qi * ix.Dtot, prune_all + (size_t)qi * ix.S,
+                topk, sm, pool_size, distk, err, tl);
+    flush_tally(tl, counters);
+    write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
+}
+
+__global__ void k_iota(int *list, int *nlist, int n) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) list[i] = i;
+    if (threadIdx.x == 0) *nlist = n;
 }
 
 // ------------------------------------------------------------------ estimate
@@ -1318,20 +1376,29 @@ size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t np
     return b + 256;
 }
 
-size_t split_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t nprobe, int64_t max_pos) {
+size_t split_scratch_bytes(const Index &I, int64_t cap, int64_t topk, int64_t nprobe, int64_t max_pos) {
     size_t b = 0;
     auto add = [&](size_t x) { b += align16(x); };
-    add(4 * (size_t)nq * topk);
-    add(4 * (size_t)nq * topk);
-    add(4 * (size_t)nq);
-    add(4 * (size_t)nq);
-    add(4 * (size_t)nq * (nprobe + 1));
-    add(4 * (size_t)nq * nprobe);
-    add(4 * (size_t)(nq + 1));
-    add(4 * (size_t)nq);
-    add((size_t)nq * max_pos);
-    add(4 * (size_t)nq * max_pos * rec_words_of(I.view.S));
+    add(4 * 16);                                 // nlist
+    add(4 * (size_t)cap);                        // qlist
+    add(4 * (size_t)cap * topk);
+    add(4 * (size_t)cap * topk);
+    add(4 * (size_t)cap);
+    add(4 * (size_t)cap);
+    add(4 * (size_t)cap * (nprobe + 1));
+    add(4 * (size_t)cap * nprobe);
+    add(4 * (size_t)(cap + 1));
+    add(4 * (size_t)cap);
+    add((size_t)cap * max_pos);
+    add(4 * (size_t)cap * max_pos * rec_words_of(I.view.S));
     return b + 256;
+}
+
+// Slots of the split pass for a batch: bounded by scratch memory.
+int64_t split_slots(const Index &I, int64_t max_pos, int64_t want) {
+    const size_t per = (size_t)max_pos * (4 * rec_words_of(I.view.S) + 1);
+    const int64_t by_mem = (int64_t)((size_t)4 << 30) / (int64_t)std::max<size_t>(per, 1);
+    return std::max<int64_t>(1, std::min(want, by_mem));
 }
 
 // Which exact scan serves a call: the split scan for latency-bound calls (few
@@ -1420,49 +1487,61 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                 ix, probe, (int)nprobe, (int)nq, qrot, prune, (int)topk, ids_out, d_out, cnt, per_warp);
             check_launch("k_scan_warp");
             count_launch(4);
-        } else if (mode == 0) {
-            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ids_out,
-                                                              d_out, flags + 1, cnt, xs);
-            check_launch("k_scan");
-            count_launch(4);
         } else {
+            // split-pass state: every query (mode 1), or the deferred giant-cluster queries (mode 0)
             const int64_t max_pos = I.max_blocks_of_probes(nprobe);
-            Bump sb{(char *)I.split_scratch_get(split_scratch_bytes(I, nq, topk, nprobe, max_pos))};
+            const int64_t cap = mode == 1 ? nq : split_slots(I, max_pos, 32);
+            Bump sb{(char *)I.split_scratch_get(split_scratch_bytes(I, cap, topk, nprobe, max_pos))};
             SplitState ss;
-            ss.pool_id = sb.take<uint32_t>((size_t)nq * topk);
-            ss.pool_d = sb.take<float>((size_t)nq * topk);
-            ss.pool_size = sb.take<int>(nq);
-            ss.tau = sb.take<float>(nq);
-            ss.tile_off = sb.take<int>((size_t)nq * (nprobe + 1));
-            ss.blk_base = sb.take<int>((size_t)nq * nprobe);
-            ss.q_tile_off = sb.take<int>(nq + 1);
-            ss.npos = sb.take<int>(nq);
-            ss.flag = sb.take<uint8_t>((size_t)nq * max_pos);
+            ss.nlist = sb.take<int>(16);
+            ss.qlist = sb.take<int>(cap);
+            ss.cap = (int)cap;
+            ss.pool_id = sb.take<uint32_t>((size_t)cap * topk);
+            ss.pool_d = sb.take<float>((size_t)cap * topk);
+            ss.pool_size = sb.take<int>(cap);
+            ss.tau = sb.take<float>(cap);
+            ss.tile_off = sb.take<int>((size_t)cap * (nprobe + 1));
+            ss.blk_base = sb.take<int>((size_t)cap * nprobe);
+            ss.q_tile_off = sb.take<int>(cap + 1);
+            ss.npos = sb.take<int>(cap);
+            ss.flag = sb.take<uint8_t>((size_t)cap * max_pos);
             ss.max_pos = max_pos;
             ss.rec_words = rec_words_of(ix.S);
-            ss.rec = sb.take<float>((size_t)nq * max_pos * ss.rec_words);
-            SAQG_CUDA_TRY(cudaMemsetAsync(ss.flag, 0, (size_t)nq * max_pos, st));
+            ss.rec = sb.take<float>((size_t)cap * max_pos * ss.rec_words);
+            SAQG_CUDA_TRY(cudaMemsetAsync(ss.flag, 0, (size_t)cap * max_pos, st));
+            if (mode == 0) {
+                SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 4, st));
+                SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                int defer = kDeferBlocks;
+                if (const char *e = std::getenv("SAQG_DEFER_BLOCKS")) defer = std::atoi(e);
+                k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk,
+                                                                  ids_out, d_out, flags + 1, cnt, xs, defer, ss);
+                check_launch("k_scan");
+            } else {
+                k_iota<<<1, 256, 0, st>>>(ss.qlist, ss.nlist, (int)nq);
+                check_launch("k_iota");
+            }
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
+            const size_t smem_r = smem + 4 * (size_t)kReplayChunk * ss.rec_words;
+            SAQG_REQUIRE(smem_r <= 220 * 1024, "dimension / topk too large for the replay kernel's shared memory");
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_first, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_spec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
-            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_scan_first<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ss,
-                                                                    flags + 1, cnt, xs);
+            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
+            k_scan_first<<<(unsigned)cap, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ss,
+                                                                     flags + 1, cnt, xs);
             check_launch("k_scan_first");
-            k_tile_prefix<<<1, 32, 0, st>>>(ss, (int)nq, (int)nprobe);
+            k_tile_prefix<<<1, 32, 0, st>>>(ss, (int)nprobe);
             check_launch("k_tile_prefix");
             int dev = 0, sms = 0, per_sm = 0;
             SAQG_CUDA_TRY(cudaGetDevice(&dev));
             SAQG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
             SAQG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scan_spec, kScanThreads, smem1));
             const unsigned grid = (unsigned)std::max(1, sms * std::max(1, per_sm));
-            k_scan_spec<<<grid, kScanThreads, smem1, st>>>(ix, probe, (int)nprobe, (int)nq, qrot, prune, ss, cnt, xs);
+            k_scan_spec<<<grid, kScanThreads, smem1, st>>>(ix, probe, (int)nprobe, qrot, prune, ss, cnt, xs);
             check_launch("k_scan_spec");
-            k_scan_replay<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, (int)topk, ss, ids_out,
-                                                                     d_out, flags + 1, cnt, xs);
+            k_scan_replay<<<(unsigned)cap, kScanThreads, smem_r, st>>>(ix, (int)topk, ss, ids_out, d_out, cnt, xs);
             check_launch("k_scan_replay");
-            count_launch(7);
+            count_launch(mode == 0 ? 8 : 8);
         }
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[3], st));
     }

@@ -135,3 +135,30 @@ def test_gpu_construct_matches_oracle_and_searches(case, tmp_path):
             del os.environ["SAQG_SCAN_MODE"]
         assert np.array_equal(ids, oids), mode
         assert np.array_equal(d.view(np.uint32), od.view(np.uint32)), mode
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("defer", ["1", "0"])
+def test_batched_scan_with_deferred_queries(defer, tmp_path, monkeypatch):
+    """Batch path: queries over the block budget go to the split pass (only the
+    first 32 fit; the rest stay on the CTA scan).  Every answer must equal the
+    oracle's, whichever path served it."""
+    from saq_gb300 import ivf
+    x, q = data.anisotropic(4000, 256, 0.8, seed=8, n_query=48)
+    mean, comp, _ = data.pca_fit(x)
+    x, q = data.pca_apply(x, mean, comp), data.pca_apply(q, mean, comp)
+    cent, cids = data.kmeans(x, 10, iters=6, seed=3)
+    var = O.colwise_var(x)
+    plan = O.plan(var, 4.0, True, 0)
+    rots = _rotations(plan, 9)
+    index = ivf.IVF(x.shape[0], 256, 10, ivf.QuantizeConfig(avg_bits=4.0))
+    index.construct(x, cent, cids, rotations=rots)
+    opath = str(tmp_path / "o.index")
+    O.build_index(opath, x, cent, cids, 4.0, True, 0, rots)
+    monkeypatch.setenv("SAQG_SCAN_MODE", "seq")
+    monkeypatch.setenv("SAQG_DEFER_BLOCKS", defer)
+    for topk, nprobe in [(10, 4), (100, 10)]:
+        ids, d = index.search(q, topk, nprobe, return_dists=True)
+        oids, od = O.OracleIndex(opath).search(q, topk, nprobe, with_dists=True)
+        assert np.array_equal(ids, oids)
+        assert np.array_equal(d.view(np.uint32), od.view(np.uint32))
