@@ -78,6 +78,9 @@ Index::~Index() {
     for (void *p : allocations) cudaFree(p);
     if (scratch) cudaFree(scratch);
     if (split_scratch) cudaFree(split_scratch);
+    if (aux) cudaStreamDestroy(aux);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
     cudaSetDevice(cur);
 }
 
@@ -111,6 +114,19 @@ static void *grow(void *&buf, size_t &have, size_t bytes) {
 }
 
 void *Index::split_scratch_get(size_t bytes) const { return grow(split_scratch, split_scratch_bytes, bytes); }
+
+cudaStream_t Index::aux_stream() const {
+    if (!aux) SAQG_CUDA_TRY(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+    return aux;
+}
+cudaEvent_t Index::fork_event() const {
+    if (!ev_fork) SAQG_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    return ev_fork;
+}
+cudaEvent_t Index::join_event() const {
+    if (!ev_join) SAQG_CUDA_TRY(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    return ev_join;
+}
 
 void *Index::scratch_get(size_t bytes) const {
     if (bytes > scratch_bytes) {

@@ -100,6 +100,12 @@ struct Index {
     mutable size_t scratch_bytes = 0;
     mutable void *split_scratch = nullptr;
     mutable size_t split_scratch_bytes = 0;
+    // auxiliary stream and fork/join events (created on first use)
+    mutable cudaStream_t aux = nullptr;
+    mutable cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t aux_stream() const;
+    cudaEvent_t fork_event() const;
+    cudaEvent_t join_event() const;
 
     ~Index();
     void *dalloc(size_t bytes);

@@ -1247,37 +1247,17 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, i
     write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
 }
 
-// One CTA per query: the whole probe list sequentially.  A query whose probes
-// hold more than `defer_blocks` blocks (a giant Zipf cluster) is put on the
-// split list instead, when it has room, and answered by the split pass.
+// One CTA per query: the whole probe list sequentially (queries deferred to
+// the split pass are skipped).
 __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const uint32_t *__restrict__ probe, int nprobe,
                                                        const float *__restrict__ qrot_all,
                                                        const float *__restrict__ prune_all, int topk,
                                                        uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
                                                        int *__restrict__ err, unsigned long long *__restrict__ counters,
-                                                       int xstride, int defer_blocks, SplitState st) {
+                                                       int xstride, const uint8_t *__restrict__ deferred) {
     extern __shared__ __align__(16) char smem_raw[];
-    __shared__ int defer;
     const int qi = blockIdx.x;
-    if (threadIdx.x == 0) {
-        defer = 0;
-        if (defer_blocks > 0) {
-            int64_t total = 0;
-            for (int p = 0; p < nprobe; ++p) {
-                const int c = (int)probe[(size_t)qi * nprobe + p];
-                total += ix.blk_off[c + 1] - ix.blk_off[c];
-            }
-            if (total > defer_blocks) {
-                const int t = atomicAdd(st.nlist, 1);
-                if (t < st.cap) {
-                    st.qlist[t] = qi;
-                    defer = 1;
-                }
-            }
-        }
-    }
-    __syncthreads();
-    if (defer) return;
+    if (deferred && deferred[qi]) return;  // answered by the split pass
     ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, topk, xstride);
     __shared__ int pool_size;
     __shared__ float distk;
@@ -1287,6 +1267,28 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
                 topk, sm, pool_size, distk, err, tl);
     flush_tally(tl, counters);
     write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
+}
+
+// Puts every query whose probes hold more than `defer_blocks` blocks (a giant
+// Zipf cluster) on the split list, while it has room.
+__global__ void k_defer(DevIndexView ix, const uint32_t *__restrict__ probe, int nprobe, int nq, int defer_blocks,
+                        SplitState st, uint8_t *__restrict__ deferred) {
+    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= nq) return;
+    int64_t total = 0;
+    for (int p = 0; p < nprobe; ++p) {
+        const int c = (int)probe[(size_t)qi * nprobe + p];
+        total += ix.blk_off[c + 1] - ix.blk_off[c];
+    }
+    uint8_t d = 0;
+    if (defer_blocks > 0 && total > defer_blocks) {
+        const int t = atomicAdd(st.nlist, 1);
+        if (t < st.cap) {
+            st.qlist[t] = qi;
+            d = 1;
+        }
+    }
+    deferred[qi] = d;
 }
 
 __global__ void k_iota(int *list, int *nlist, int n) {
@@ -1376,7 +1378,7 @@ size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t np
     return b + 256;
 }
 
-size_t split_scratch_bytes(const Index &I, int64_t cap, int64_t topk, int64_t nprobe, int64_t max_pos) {
+size_t split_scratch_bytes(const Index &I, int64_t cap, int64_t topk, int64_t nprobe, int64_t max_pos, int64_t nq) {
     size_t b = 0;
     auto add = [&](size_t x) { b += align16(x); };
     add(4 * 16);                                 // nlist
@@ -1391,6 +1393,7 @@ size_t split_scratch_bytes(const Index &I, int64_t cap, int64_t topk, int64_t np
     add(4 * (size_t)cap);
     add((size_t)cap * max_pos);
     add(4 * (size_t)cap * max_pos * rec_words_of(I.view.S));
+    add((size_t)nq);  // deferred flags, one per query
     return b + 256;
 }
 
@@ -1490,8 +1493,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         } else {
             // split-pass state: every query (mode 1), or the deferred giant-cluster queries (mode 0)
             const int64_t max_pos = I.max_blocks_of_probes(nprobe);
-            const int64_t cap = mode == 1 ? nq : split_slots(I, max_pos, 32);
-            Bump sb{(char *)I.split_scratch_get(split_scratch_bytes(I, cap, topk, nprobe, max_pos))};
+            const int64_t cap = mode == 1 ? nq : split_slots(I, max_pos, nq);
+            Bump sb{(char *)I.split_scratch_get(split_scratch_bytes(I, cap, topk, nprobe, max_pos, nq))};
             SplitState ss;
             ss.nlist = sb.take<int>(16);
             ss.qlist = sb.take<int>(cap);
@@ -1508,14 +1511,23 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             ss.max_pos = max_pos;
             ss.rec_words = rec_words_of(ix.S);
             ss.rec = sb.take<float>((size_t)cap * max_pos * ss.rec_words);
+            uint8_t *deferred = sb.take<uint8_t>(nq);
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.flag, 0, (size_t)cap * max_pos, st));
+            cudaStream_t sp = st;  // stream of the split pass
             if (mode == 0) {
                 SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 4, st));
-                SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
                 int defer = kDeferBlocks;
                 if (const char *e = std::getenv("SAQG_DEFER_BLOCKS")) defer = std::atoi(e);
+                k_defer<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(ix, probe, (int)nprobe, (int)nq, defer, ss,
+                                                                       deferred);
+                check_launch("k_defer");
+                // the split pass runs beside the CTA scan on the index's auxiliary stream
+                sp = I.aux_stream();
+                SAQG_CUDA_TRY(cudaEventRecord(I.fork_event(), st));
+                SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, I.fork_event(), 0));
+                SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
                 k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk,
-                                                                  ids_out, d_out, flags + 1, cnt, xs, defer, ss);
+                                                                  ids_out, d_out, flags + 1, cnt, xs, deferred);
                 check_launch("k_scan");
             } else {
                 k_iota<<<1, 256, 0, st>>>(ss.qlist, ss.nlist, (int)nq);
@@ -1527,20 +1539,24 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_first, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_spec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
-            k_scan_first<<<(unsigned)cap, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ss,
+            k_scan_first<<<(unsigned)cap, kScanThreads, smem, sp>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ss,
                                                                      flags + 1, cnt, xs);
             check_launch("k_scan_first");
-            k_tile_prefix<<<1, 32, 0, st>>>(ss, (int)nprobe);
+            k_tile_prefix<<<1, 32, 0, sp>>>(ss, (int)nprobe);
             check_launch("k_tile_prefix");
             int dev = 0, sms = 0, per_sm = 0;
             SAQG_CUDA_TRY(cudaGetDevice(&dev));
             SAQG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
             SAQG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scan_spec, kScanThreads, smem1));
             const unsigned grid = (unsigned)std::max(1, sms * std::max(1, per_sm));
-            k_scan_spec<<<grid, kScanThreads, smem1, st>>>(ix, probe, (int)nprobe, qrot, prune, ss, cnt, xs);
+            k_scan_spec<<<grid, kScanThreads, smem1, sp>>>(ix, probe, (int)nprobe, qrot, prune, ss, cnt, xs);
             check_launch("k_scan_spec");
-            k_scan_replay<<<(unsigned)cap, kScanThreads, smem_r, st>>>(ix, (int)topk, ss, ids_out, d_out, cnt, xs);
+            k_scan_replay<<<(unsigned)cap, kScanThreads, smem_r, sp>>>(ix, (int)topk, ss, ids_out, d_out, cnt, xs);
             check_launch("k_scan_replay");
+            if (sp != st) {  // join
+                SAQG_CUDA_TRY(cudaEventRecord(I.join_event(), sp));
+                SAQG_CUDA_TRY(cudaStreamWaitEvent(st, I.join_event(), 0));
+            }
             count_launch(mode == 0 ? 8 : 8);
         }
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[3], st));
