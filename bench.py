@@ -276,7 +276,7 @@ def main():
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    step_ms, scan_ms, fast_b, rr_b, spec, rr = [], [], [], [], [], []
+    step_ms, scan_ms, fast_b, rr_b, spec, rr, probe_ms, qprep_ms, split_ms = [], [], [], [], [], [], [], [], []
     launches0 = lib.saqg_kernel_launches()
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
@@ -289,6 +289,9 @@ def main():
             e1.synchronize()
             step_ms.append(e0.elapsed_time(e1))
             scan_ms.append(stats.ms_scan)
+            probe_ms.append(stats.ms_probe)
+            qprep_ms.append(stats.ms_qprep)
+            split_ms.append(stats.ms_split)
             fast_b.append(stats.fast_bytes)
             rr_b.append(stats.rerank_bytes)
             spec.append(stats.speculative)
@@ -388,7 +391,9 @@ def main():
                      "traffic": traffic, "kernel": "k_scan", "peak_kind": peak_kind,
                      "bytes_per_launch": compulsory, "effective_bytes_per_launch": effective,
                      "effective_gbs": effective / (mean_scan / 1e3) / 1e9, "scan_ms": mean_scan,
-                     "reranked_per_query": float(np.mean(rr)) / B, "speculative_per_query": float(np.mean(spec)) / B},
+                     "reranked_per_query": float(np.mean(rr)) / B, "speculative_per_query": float(np.mean(spec)) / B,
+                     "probe_ms": float(np.mean(probe_ms)), "qprep_ms": float(np.mean(qprep_ms)),
+                     "split_pass_ms": float(np.mean(split_ms))},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_v, "unit": "queries/s", "h2d_bytes_per_step": B * a.dim * 4,
                 "d2h_bytes_per_step": B * a.topk * 8},

@@ -118,6 +118,7 @@ typedef struct saqg_search_stats {
     int64_t speculative;   /* accurate distances evaluated (a superset of `reranked`) */
     int64_t fast_bytes;    /* algorithmic bytes of the scan: 1-bit codes, |o| factors, centroids */
     int64_t rerank_bytes;  /* algorithmic bytes of the re-rank: ex-codes, ex factors, ids */
+    float ms_split;        /* the split pass for giant-cluster queries (auxiliary stream; 0 if unused) */
 } saqg_search_stats;
 
 /* saqg_search plus measurements: `stats` (may be NULL) and `probes` (may be

@@ -60,6 +60,45 @@ __global__ void k_probe_dist(DevIndexView ix, const float *__restrict__ q, float
     if (lane == 0) dist[(size_t)qi * ix.K + c] = d;
 }
 
+// Tiled form for batches: a CTA holds kProbeQT queries in shared memory; each
+// warp keeps one centroid in registers (lane (h, l) holds the elements of the
+// packets p = h, h+2, ... at offset l -- Eigen's two-accumulator assignment)
+// and evaluates it against every query of the tile.  Same reduction order as
+// k_probe_dist (dimension a multiple of 32, so no odd packet or scalar tail).
+constexpr int kProbeQT = 16, kProbeWarps = 8, kProbeRegs = 64;  // up to 64 floats per lane: dim <= 2048
+__global__ void __launch_bounds__(kProbeWarps * 32) k_probe_dist_tiled(DevIndexView ix, const float *__restrict__ q,
+                                                                        int nq, float *__restrict__ dist) {
+    extern __shared__ float qs[];  // kProbeQT x D
+    const int D = ix.D, warp = threadIdx.x >> 5, lane = threadIdx.x & 31, l = lane & 15, h = lane >> 4;
+    const int q0 = blockIdx.y * kProbeQT, nqt = min(kProbeQT, nq - q0);
+    for (int i = threadIdx.x; i < nqt * D; i += blockDim.x) qs[i] = q[(size_t)q0 * D + i];
+    __syncthreads();
+    const int npk = D / 32;  // packets per lane
+    for (int c = blockIdx.x * kProbeWarps + warp; c < ix.K; c += gridDim.x * kProbeWarps) {
+        const float *cr = ix.centroids + (size_t)c * D;
+        float cv[kProbeRegs];
+#pragma unroll
+        for (int k = 0; k < kProbeRegs; ++k)
+            if (k < npk) cv[k] = cr[16 * (h + 2 * k) + l];
+        for (int qi = 0; qi < nqt; ++qi) {
+            const float *qq = qs + qi * D;
+            float acc = 0.0f;
+#pragma unroll
+            for (int k = 0; k < kProbeRegs; ++k)
+                if (k < npk) {
+                    const float t = __fsub_rn(cv[k], qq[16 * (h + 2 * k) + l]);
+                    acc = k == 0 ? __fmul_rn(t, t) : __fadd_rn(acc, __fmul_rn(t, t));
+                }
+            acc = __fadd_rn(acc, __shfl_down_sync(kFull, acc, 16));
+            acc = __fadd_rn(acc, __shfl_down_sync(kFull, acc, 8));
+            acc = __fadd_rn(acc, __shfl_down_sync(kFull, acc, 4));
+            acc = __fadd_rn(acc, __shfl_down_sync(kFull, acc, 2));
+            acc = __fadd_rn(acc, __shfl_down_sync(kFull, acc, 1));
+            if (lane == 0) dist[(size_t)(q0 + qi) * ix.K + c] = acc;
+        }
+    }
+}
+
 struct Cand {
     uint32_t id;
     float d;
@@ -1465,8 +1504,17 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         const int wpb = 8;
         dim3 grid((unsigned)((I.K + wpb - 1) / wpb), (unsigned)nq);
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[0], st));
-        k_probe_dist<<<grid, wpb * 32, 0, st>>>(ix, qin, dist);
-        check_launch("k_probe_dist");
+        if (nq >= 8 && I.D % 32 == 0 && I.D <= 32 * kProbeRegs) {
+            const size_t qsm = 4 * (size_t)kProbeQT * I.D;
+            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_probe_dist_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm));
+            const unsigned gx = (unsigned)std::min<int64_t>((I.K + kProbeWarps - 1) / kProbeWarps, 304);
+            k_probe_dist_tiled<<<dim3(gx, (unsigned)((nq + kProbeQT - 1) / kProbeQT)), kProbeWarps * 32, qsm, st>>>(
+                ix, qin, (int)nq, dist);
+            check_launch("k_probe_dist_tiled");
+        } else {
+            k_probe_dist<<<grid, wpb * 32, 0, st>>>(ix, qin, dist);
+            check_launch("k_probe_dist");
+        }
         k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, work, flags);
         check_launch("k_probe_select");
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[1], st));
@@ -1554,6 +1602,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             k_scan_replay<<<(unsigned)cap, kScanThreads, smem_r, sp>>>(ix, (int)topk, ss, ids_out, d_out, cnt, xs);
             check_launch("k_scan_replay");
             if (sp != st) {  // join
+                if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[4], sp));
                 SAQG_CUDA_TRY(cudaEventRecord(I.join_event(), sp));
                 SAQG_CUDA_TRY(cudaStreamWaitEvent(st, I.join_event(), 0));
             }
@@ -1585,12 +1634,18 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         stats->ms_qprep = t12;
         stats->ms_scan = t23;
         stats->ms_total = t03;
+        stats->ms_split = 0.0f;
+        if (cudaEventQuery(ev[4]) == cudaSuccess) {
+            float t24 = 0;
+            if (cudaEventElapsedTime(&t24, ev[2], ev[4]) == cudaSuccess) stats->ms_split = t24;
+        }
+        cudaGetLastError();
         stats->probes = nq * nprobe;
         stats->blocks = (int64_t)hc[0];
         stats->vectors = (int64_t)hc[1];
         stats->reranked = (int64_t)hc[2];
         stats->speculative = (int64_t)hc[3];
-        // SURVEY-style algorithmic bytes: per scanned block 32 lanes of 1-bit codes of
+        // Algorithmic bytes: per scanned block 32 lanes of 1-bit codes of
         // every coded segment and |o| of every segment; per probe the rotated centroid;
         // per re-ranked vector its ex-codes, ex factors and id.
         int64_t per_lane = 0, per_rr = 4;
