@@ -128,6 +128,25 @@ int saqg_search_ex(const saqg_index *index, const float *queries, int64_t nq, in
                    const saqg_searcher_config *cfg, uint32_t *ids, float *dists, int mem, void *stream,
                    saqg_search_stats *stats, uint32_t *probes);
 
+/* ---- search without allocation ---------------------------------------- */
+/* No counterpart in the reference: saqg_search for callers that must not
+ * allocate device memory inside a call (a serving loop beside a framework
+ * whose caching allocator holds the device memory, where cudaMalloc fails or
+ * cudaFree stalls every stream of the device).  The call allocates nothing:
+ * its scratch is one static device array of SAQG_STATIC_SCRATCH_BYTES per
+ * device.  Queries (nq x dim), ids and dists (nq x topk; dists may be NULL)
+ * are device pointers on the index's device; results equal saqg_search's.
+ * A call needs nq * (12 * clusters + 4 * nprobe + 4 * padded dim + 4 * segments)
+ * bytes (each term rounded up to 16) + 64; larger calls fail with
+ * SAQG_ERR_INVALID before any work.  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress) and may make the driver load the
+ * kernels: make it before any stream capture.  Every call on a device shares
+ * the array, so calls that overlap on the GPU (other streams, other threads)
+ * race: order them on one stream. */
+#define SAQG_STATIC_SCRATCH_BYTES (16u << 20)
+int saqg_search_static(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
+                       const saqg_searcher_config *cfg, uint32_t *ids, float *dists, void *stream);
+
 /* IVF::estimate<L2Sqr> (index/ivf.hpp:313-362) for one query: every vector of
  * the `nprobe` probed clusters, in probe order, with its accurate, fast and
  * variance-bound estimates.  Host outputs of capacity `cap`; *count receives

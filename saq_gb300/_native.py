@@ -13,6 +13,7 @@ from .build import LIB
 
 SAQG_MEM_HOST = 0
 SAQG_MEM_DEVICE = 1
+SAQG_STATIC_SCRATCH_BYTES = 16 << 20
 SAQG_DIST_L2 = 1
 
 I64 = C.c_int64
@@ -62,6 +63,8 @@ EXPORTS = {
                               C.c_void_p, C.c_int, C.c_void_p]),
     "saqg_search_ex": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig), C.c_void_p,
                                  C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "saqg_search_static": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig), C.c_void_p,
+                                     C.c_void_p, C.c_void_p]),
     "saqg_estimate": (C.c_int, [C.c_void_p, C.c_void_p, I64, C.POINTER(SearcherConfig), C.c_void_p, C.c_void_p,
                                 C.c_void_p, C.c_void_p, I64, C.POINTER(I64)]),
     "saqg_plan": (C.c_int, [C.c_void_p, I64, C.c_float, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,

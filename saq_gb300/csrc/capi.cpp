@@ -127,6 +127,16 @@ int saqg_search_ex(const saqg_index *index, const float *queries, int64_t nq, in
     });
 }
 
+int saqg_search_static(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
+                       const saqg_searcher_config *cfg, uint32_t *ids, float *dists, void *stream) {
+    return guarded([&] {
+        SAQG_REQUIRE(index && queries && ids, "null argument");
+        SAQG_REQUIRE(!cfg || cfg->dist_type == SAQG_DIST_L2, "only L2 search is supported");
+        const float m = cfg ? cfg->searcher_vars_bound_m : 4.0f;
+        run_search_static(*index->impl, queries, nq, topk, nprobe, m, ids, dists, (cudaStream_t)stream);
+    });
+}
+
 int saqg_estimate(const saqg_index *index, const float *query_host, int64_t nprobe, const saqg_searcher_config *cfg,
                   uint32_t *ids, float *acc, float *fast, float *vars, int64_t cap, int64_t *count) {
     return guarded([&] {

@@ -126,6 +126,9 @@ void finalize_view(Index &idx);
 void run_search(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,
                 float *dists, int mem, cudaStream_t st, saqg_search_stats *stats = nullptr,
                 uint32_t *probes_out = nullptr);
+// saqg_search for device pointers with its scratch in a static device array.
+void run_search_static(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m,
+                       uint32_t *ids, float *dists, cudaStream_t stream);
 int64_t run_estimate(const Index &idx, const float *q_host, int64_t nprobe, float m, uint32_t *ids, float *acc,
                      float *fast, float *vars, int64_t cap);
 

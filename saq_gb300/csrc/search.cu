@@ -1721,4 +1721,103 @@ int64_t run_estimate(const Index &I, const float *q_host, int64_t nprobe, float 
     return total;
 }
 
+// ------------------------------------------------- search with static scratch
+// The scratch of saqg_search_static: one file-scope device array (one instance
+// per device, placed by the driver when it loads this file's kernels), shared by
+// every call on that device.  Nothing in it needs to start at zero except the
+// 64-byte flag words, which each call clears on its stream before its kernels.
+static __device__ __align__(256) unsigned char g_static_scratch[SAQG_STATIC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kMaxStaticDevices = 64;
+std::mutex g_static_mu;
+void *g_static_ptr[kMaxStaticDevices] = {};
+
+// Device address of the array on `dev` (current), looked up on the first call
+// on that device.
+void *static_scratch(int dev) {
+    SAQG_REQUIRE(dev >= 0 && dev < kMaxStaticDevices, "device ordinal out of range for the static scratch");
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess || !p)
+            throw Error{SAQG_ERR_CUDA, std::string("cudaGetSymbolAddress(static scratch) failed: ") +
+                                           cudaGetErrorString(e)};
+        g_static_ptr[dev] = p;
+    }
+    return g_static_ptr[dev];
+}
+
+}  // namespace
+
+size_t static_search_scratch_bytes(const Index &I, int64_t nq, int64_t nprobe) {
+    size_t b = 0;
+    auto add = [&](size_t x) { b += align16(x); };
+    add(4 * (size_t)nq * I.K);          // centroid distances
+    add(8 * (size_t)nq * I.K);          // exact-select work (fallback)
+    add(4 * (size_t)nq * nprobe);       // probe ids
+    add(4 * (size_t)nq * I.view.Dtot);  // rotated queries
+    add(4 * (size_t)nq * I.view.S);     // prune bounds
+    add(64);                            // flags
+    return b;
+}
+
+void run_search_static(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m,
+                       uint32_t *ids, float *dists, cudaStream_t st) {
+    SAQG_REQUIRE(nq >= 0 && topk >= 1 && topk <= kMaxTopK, "topk must be in [1, 4096]");
+    SAQG_REQUIRE(nprobe >= 1 && nprobe <= I.K, "nprobe must be in [1, number of clusters]");
+    if (nq == 0) return;
+    const size_t need = static_search_scratch_bytes(I, nq, nprobe);
+    SAQG_REQUIRE(need <= (size_t)SAQG_STATIC_SCRATCH_BYTES,
+                 "saqg_search_static: " + std::to_string(nq) + " queries with " + std::to_string(I.K) +
+                     " clusters and nprobe " + std::to_string(nprobe) + " need " + std::to_string(need) +
+                     " bytes of scratch, above the static maximum of " +
+                     std::to_string((size_t)SAQG_STATIC_SCRATCH_BYTES) + " bytes; split the batch");
+    const DevIndexView &ix = I.view;
+    const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xstride_of(ix));
+    SAQG_REQUIRE(smem <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
+    int prev = 0;
+    SAQG_CUDA_TRY(cudaGetDevice(&prev));
+    struct DevGuard {
+        int prev, cur;
+        ~DevGuard() {
+            if (prev != cur) cudaSetDevice(prev);
+        }
+    } dg{prev, I.device};
+    if (prev != I.device) SAQG_CUDA_TRY(cudaSetDevice(I.device));
+    Bump bp{(char *)static_scratch(I.device)};
+    float *dist = bp.take<float>((size_t)nq * I.K);
+    Cand *work = bp.take<Cand>((size_t)nq * I.K);
+    uint32_t *probe = bp.take<uint32_t>((size_t)nq * nprobe);
+    float *qrot = bp.take<float>((size_t)nq * ix.Dtot);
+    float *prune = bp.take<float>((size_t)nq * ix.S);
+    int *flags = bp.take<int>(16);
+    SAQG_CUDA_TRY(cudaMemsetAsync(flags, 0, 64, st));
+    if (nq >= 8 && I.D % 32 == 0 && I.D <= 32 * kProbeRegs) {
+        const size_t qsm = 4 * (size_t)kProbeQT * I.D;
+        SAQG_CUDA_TRY(cudaFuncSetAttribute(k_probe_dist_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm));
+        const unsigned gx = (unsigned)std::min<int64_t>((I.K + kProbeWarps - 1) / kProbeWarps, 304);
+        k_probe_dist_tiled<<<dim3(gx, (unsigned)((nq + kProbeQT - 1) / kProbeQT)), kProbeWarps * 32, qsm, st>>>(
+            ix, q, (int)nq, dist);
+        check_launch("k_probe_dist_tiled");
+    } else {
+        const int wpb = 8;
+        k_probe_dist<<<dim3((unsigned)((I.K + wpb - 1) / wpb), (unsigned)nq), wpb * 32, 0, st>>>(ix, q, dist);
+        check_launch("k_probe_dist");
+    }
+    k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, work, flags);
+    check_launch("k_probe_select");
+    size_t qsm = 0;
+    for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
+    k_qprep<<<dim3((unsigned)ix.S, (unsigned)nq), 256, qsm, st>>>(ix, q, m, qrot, prune);
+    check_launch("k_qprep");
+    SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ids, dists,
+                                                      flags + 1, nullptr, xstride_of(ix), nullptr);
+    check_launch("k_scan");
+    count_launch(4);
+}
+
 }  // namespace saqg
