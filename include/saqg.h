@@ -119,6 +119,9 @@ typedef struct saqg_search_stats {
     int64_t fast_bytes;    /* algorithmic bytes of the scan: 1-bit codes, |o| factors, centroids */
     int64_t rerank_bytes;  /* algorithmic bytes of the re-rank: ex-codes, ex factors, ids */
     float ms_split;        /* the split pass for giant-cluster queries (auxiliary stream; 0 if unused) */
+    float ms_split_first;  /* ... its exact prefix scans (the speculation bounds) */
+    float ms_split_spec;   /* ... its speculative tile estimates */
+    float ms_split_replay; /* ... its sequential replays */
 } saqg_search_stats;
 
 /* saqg_search plus measurements: `stats` (may be NULL) and `probes` (may be

@@ -115,8 +115,14 @@ static void *grow(void *&buf, size_t &have, size_t bytes) {
 
 void *Index::split_scratch_get(size_t bytes) const { return grow(split_scratch, split_scratch_bytes, bytes); }
 
+// The split pass is a batch's critical path: its stream gets the device's
+// highest priority, so its CTAs go first while the CTA scan beside it fills in.
 cudaStream_t Index::aux_stream() const {
-    if (!aux) SAQG_CUDA_TRY(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+    if (!aux) {
+        int least = 0, greatest = 0;
+        SAQG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        SAQG_CUDA_TRY(cudaStreamCreateWithPriority(&aux, cudaStreamNonBlocking, greatest));
+    }
     return aux;
 }
 cudaEvent_t Index::fork_event() const {

@@ -549,6 +549,14 @@ __device__ void block_estimates(const DevIndexView &ix, int64_t gb, ScanSmem &sm
     sm.cur[w * 32 + lane] = cur;
 }
 
+// Largest stage minimum (NaN-free ones; NaN when all are NaN or n == 0):
+// stages_pass(st, n, tau) == !(stage_max(st, n) > tau).
+__device__ __forceinline__ float stage_max(const float *st, int n) {
+    float m = __int_as_float(0x7fffffff);
+    for (int i = 0; i < n; ++i) m = fmaxf(m, st[i]);
+    return m;
+}
+
 __device__ __forceinline__ bool stages_pass(const float *st, int n, float tau) {
     for (int i = 0; i < n; ++i)
         if (st[i] > tau) return false;
@@ -672,50 +680,104 @@ __device__ __forceinline__ void replay_block(int S, int n, int nb, int bb, const
     }
 }
 
-// replay_block for a whole warp: the lanes first discard, in parallel, the
-// candidates that cannot change the pool (their insert would be rejected
-// whatever happens earlier in the block: the estimate is not below the
-// block-start distk, or the first partial distance already exceeds it), then
-// lane 0 replays the rest in order.  Same pool state as replay_block.
-__device__ __forceinline__ void replay_block_warp(int S, int bb, const float *cur, const float *stage, int nstage,
-                                                  const float *part, uint32_t cm, const uint32_t *ids_v0,
-                                                  uint32_t *pid, float *pd, int &sz, int topk, float &dk,
-                                                  unsigned long long &c_rr) {
+// ResultPool::insert (utils/pool.hpp:17-49) by a whole warp on the pool in
+// shared memory: the insert position is the number of entries below `dist`,
+// which is what the reference's lower-bound search returns on a sorted pool;
+// when `dist` or an entry is NaN (no order) lane 0 runs that search itself.
+__device__ __forceinline__ void pool_insert_warp(uint32_t *ids, float *d, int &size, int cap, uint32_t u, float dist) {
+    const int lane = threadIdx.x & 31;
+    if (size == cap && dist > d[size - 1]) return;
+    int lo = 0;
+    bool nan = dist != dist;
+    for (int i0 = 0; i0 < size; i0 += 32) {
+        const int i = i0 + lane;
+        const float v = i < size ? d[i] : 0.0f;
+        lo += __popc(__ballot_sync(kFull, i < size && v < dist));
+        nan = __any_sync(kFull, nan || v != v);
+    }
+    if (nan) {
+        int sz = size;
+        if (lane == 0) pool_insert(ids, d, sz, cap, u, dist);
+        __syncwarp();
+        size = __shfl_sync(kFull, sz, 0);
+        return;
+    }
+    // entries [lo, size) move up one (entry size - 1 lands in the spare slot when full), top chunk first
+    for (int i0 = (size >> 5) << 5; i0 >= ((lo + 1) >> 5) << 5; i0 -= 32) {
+        const int i = i0 + lane;
+        const bool mv = i > lo && i <= size;
+        uint32_t pi = 0;
+        float pv = 0.0f;
+        if (mv) {
+            pi = ids[i - 1];
+            pv = d[i - 1];
+        }
+        __syncwarp();
+        if (mv) {
+            ids[i] = pi;
+            d[i] = pv;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        ids[lo] = u;
+        d[lo] = dist;
+    }
+    __syncwarp();
+    size += size < cap;
+}
+
+// The reference's decisions for one block (saq_searcher.hpp:87-160 for several
+// segments, scanCluster's mask-then-insert, saq_searcher.hpp:185-208, for one),
+// taken by a whole warp.  distk changes only when an insert is accepted, so
+// every lane evaluates its own insert under the current distk at once; the
+// first accepted lane (in lane order) is inserted, the lanes before it were
+// rejected under that same distk, and the lanes after it are evaluated again.
+// Rejected inserts thus cost no serial steps.  c_rr counts the lanes whose
+// accurate distance the reference computes.
+// smax: stage_max of the block's stage minima (several segments).
+__device__ __forceinline__ void replay_block_warp(int S, int bb, const float *cur, float smax, const float *part,
+                                                  uint32_t cm, const uint32_t *ids_v0, uint32_t *pid, float *pd,
+                                                  int &sz, int topk, float &dk, unsigned long long &c_rr) {
     const int lane = threadIdx.x & 31;
     if (!cm) return;
-    if (S > 1 && !stages_pass(stage, nstage, dk)) return;
+    if (S > 1 && smax > dk) return;
     const bool in = (cm >> lane) & 1u;
     const float c = in ? cur[lane] : FLT_MAX;
-    const uint32_t m = __ballot_sync(kFull, in && c < dk);  // lanes whose accurate distance the reference computes
-    const float first = in ? (S == 1 ? part[lane] : __fadd_rn(c, part[lane])) : FLT_MAX;
-    // while the pool is not full every candidate inserts (ResultPool rejects only when full)
-    uint32_t need = __ballot_sync(kFull, in && c < dk && (sz < topk || !(first > dk)));
-    if (lane == 0) {
-        c_rr += __popc(m);
-        if (S == 1) {
-            while (need) {
-                const int j = __ffs(need) - 1;
-                need &= need - 1;
-                pool_insert(pid, pd, sz, topk, ids_v0[(int64_t)bb * 32 + j], part[j]);
-                dk = sz == topk ? pd[sz - 1] : FLT_MAX;
-            }
-        } else {
-            while (need) {
-                const int j = __ffs(need) - 1;
-                need &= need - 1;
-                if (!(cur[j] < dk)) continue;
-                float acc = cur[j];
-                for (int s = 0; s < S; ++s) {
-                    acc = __fadd_rn(acc, part[s * 32 + j]);
-                    if (acc >= dk) break;
-                }
-                pool_insert(pid, pd, sz, topk, ids_v0[(int64_t)bb * 32 + j], acc);
-                dk = sz == topk ? pd[sz - 1] : FLT_MAX;
-            }
+    if (S == 1) {
+        uint32_t rest = __ballot_sync(kFull, in && c < dk);  // the mask, at the block's start
+        c_rr += __popc(rest);
+        const float a = in ? part[lane] : FLT_MAX;
+        while (rest) {
+            const uint32_t ok = rest & __ballot_sync(kFull, !(sz == topk && a > dk));
+            if (!ok) break;
+            const int j = __ffs(ok) - 1;
+            pool_insert_warp(pid, pd, sz, topk, ids_v0[(int64_t)bb * 32 + j], __shfl_sync(kFull, a, j));
+            dk = sz == topk ? pd[sz - 1] : FLT_MAX;
+            rest &= ~((2u << j) - 1u);
         }
+        return;
     }
-    dk = __shfl_sync(kFull, dk, 0);
-    sz = __shfl_sync(kFull, sz, 0);
+    uint32_t rest = __ballot_sync(kFull, in);
+    while (rest) {
+        const uint32_t pass = rest & __ballot_sync(kFull, c < dk);
+        float acc = c;
+        if ((pass >> lane) & 1u)
+            for (int s = 0; s < S; ++s) {
+                acc = __fadd_rn(acc, part[s * 32 + lane]);
+                if (acc >= dk) break;
+            }
+        const uint32_t ok = pass & __ballot_sync(kFull, !(sz == topk && acc > dk));
+        if (!ok) {
+            c_rr += __popc(pass);
+            break;
+        }
+        const int j = __ffs(ok) - 1;
+        c_rr += __popc(pass & ((2u << j) - 1u));
+        pool_insert_warp(pid, pd, sz, topk, ids_v0[(int64_t)bb * 32 + j], __shfl_sync(kFull, acc, j));
+        dk = sz == topk ? pd[sz - 1] : FLT_MAX;
+        rest &= ~((2u << j) - 1u);
+    }
 }
 
 struct ScanTally {
@@ -743,7 +805,8 @@ __device__ void scan_probes(const DevIndexView &ix, const uint32_t *__restrict__
                 float dk = distk;
                 int sz = pool_size;
                 for (int ww = 0; ww < kTileB && t0 + ww < nb; ++ww)
-                    replay_block_warp(S, t0 + ww, sm.cur + ww * 32, sm.stage + ww * (S + 1), sm.nstage[ww],
+                    replay_block_warp(S, t0 + ww, sm.cur + ww * 32,
+                                      S == 1 ? 0.0f : stage_max(sm.stage + ww * (S + 1), sm.nstage[ww]),
                                       S == 1 ? sm.part + ww * 32 : sm.part + ww * S * 32, sm.cmask[ww], ix.ids + v0,
                                       sm.pool_id, sm.pool_d, sz, topk, dk, tl.rr);
                 if (tid == 0) {
@@ -1037,11 +1100,15 @@ struct SplitState {
     float *tau;          // [cap]
     int *tile_off;       // [cap][nprobe + 1] tiles before probe p
     int *blk_base;       // [cap][nprobe] scan-order position of the probe's first block
+    int *split_p;        // [cap] probe where the speculative part starts (nprobe: none)
+    int *split_b;        // [cap] block of that probe's cluster where it starts
     int *q_tile_off;     // [cap + 1]
-    int *npos;           // [cap] scan positions of the query
-    uint8_t *flag;       // [cap][max_pos]
-    float *rec;          // [cap][max_pos][rec_words]
-    int64_t max_pos;
+    int *npos;           // [cap] scan positions (blocks) of the query
+    int64_t *pos_off;    // [cap] first record position reserved for the slot
+    unsigned long long *pos_used;  // record positions handed out so far
+    float2 *summ;        // [pos_cap] per record: min candidate estimate, max stage minimum (NaN: none)
+    float *rec;          // [pos_cap][rec_words]
+    int64_t pos_cap;
     int rec_words;
 };
 
@@ -1066,23 +1133,37 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
     init_pool(sm, topk, pool_size, distk);
     const uint32_t *pr = probe + (size_t)qi * nprobe;
     const float *qrot = qrot_all + (size_t)qi * ix.Dtot, *prune = prune_all + (size_t)qi * S;
-    {  // the first kFirstBlocks blocks of the nearest cluster, exactly as scan_probes does
-        const int c = (int)pr[0];
-        prepare_cluster(ix, qrot, prune, c, sm);
+    // the exact prefix, as scan_probes does: whole tiles in scan order until at
+    // least kFirstBlocks blocks are done and the pool is full (its distk then
+    // bounds every later distk, so it can serve as the speculation bound)
+    int sp_p = nprobe, sp_b = 0;
+    for (int p = 0; p < nprobe && sp_p == nprobe; ++p) {
+        const int c = (int)pr[p];
         const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
         const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
-        const int fe = min(nb, kFirstBlocks);
-        tl.blocks += fe;
-        tl.vecs += min(n, fe * 32);
-        for (int t0 = 0; t0 < fe; t0 += kTileB) {
-            tile_candidates(ix, sm, b0, v0, nb, n, t0, fe, distk);
+        bool prepared = false;
+        for (int t0 = 0; t0 < nb; t0 += kTileB) {
+            if (tl.blocks >= kFirstBlocks && pool_size == topk) {
+                sp_p = p;
+                sp_b = t0;
+                break;
+            }
+            if (!prepared) {
+                prepare_cluster(ix, qrot, prune, c, sm);
+                prepared = true;
+            }
+            const int te = min(nb, t0 + kTileB);
+            tl.blocks += te - t0;
+            tl.vecs += min(n, te * 32) - t0 * 32;
+            tile_candidates(ix, sm, b0, v0, nb, n, t0, nb, distk);
             if (tid < 32) {
                 if (tid == 0)
                     for (int i = 0; i < kTileB; ++i) tl.spec += __popc(sm.cmask[i]);
                 float dk = distk;
                 int sz = pool_size;
-                for (int ww = 0; ww < kTileB && t0 + ww < fe; ++ww)
-                    replay_block_warp(S, t0 + ww, sm.cur + ww * 32, sm.stage + ww * (S + 1), sm.nstage[ww],
+                for (int ww = 0; ww < kTileB && t0 + ww < nb; ++ww)
+                    replay_block_warp(S, t0 + ww, sm.cur + ww * 32,
+                                      S == 1 ? 0.0f : stage_max(sm.stage + ww * (S + 1), sm.nstage[ww]),
                                       S == 1 ? sm.part + ww * 32 : sm.part + ww * S * 32, sm.cmask[ww], ix.ids + v0,
                                       sm.pool_id, sm.pool_d, sz, topk, dk, tl.rr);
                 if (tid == 0) {
@@ -1101,6 +1182,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
     if (tid == 0) {
         st.pool_size[slot] = pool_size;
         st.tau[slot] = distk;
+        st.split_p[slot] = sp_p;
+        st.split_b[slot] = sp_b;
         int tiles = 0;
         int64_t pos = 0;
         for (int p = 0; p < nprobe; ++p) {
@@ -1108,13 +1191,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
             const int nb = (int)(ix.blk_off[c + 1] - ix.blk_off[c]);
             st.tile_off[(size_t)slot * (nprobe + 1) + p] = tiles;
             st.blk_base[(size_t)slot * nprobe + p] = (int)pos;
-            const int rest = p == 0 ? max(0, nb - kFirstBlocks) : nb;
+            const int rest = p < sp_p ? 0 : p == sp_p ? nb - sp_b : nb;
             tiles += (rest + kTileBlocks - 1) / kTileBlocks;
             pos += nb;
         }
         st.tile_off[(size_t)slot * (nprobe + 1) + nprobe] = tiles;
-        st.npos[slot] = (int)min(pos, st.max_pos);
-        if (pos > st.max_pos) *err = 2;
+        if (pos != st.npos[slot]) *err = 2;
     }
 }
 
@@ -1168,7 +1250,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
         }
         const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
         const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
-        const int first = p == 0 ? kFirstBlocks : 0;
+        const int first = p == st.split_p[slot] ? st.split_b[slot] : 0;
         const int bstart = first + tile * kTileBlocks, bend = min(nb, bstart + kTileBlocks);
         if (tid == 0) {
             tl.blocks += bend - bstart;
@@ -1184,16 +1266,28 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
                 if (b < bend) {
                     const uint32_t cm = sm.cmask[w];
                     const int64_t pos = base + b;
-                    if (cm && pos < st.max_pos) {
-                        float *r = st.rec + ((size_t)slot * st.max_pos + pos) * st.rec_words;
+                    if (cm && pos < st.npos[slot]) {
+                        float *r = st.rec + (size_t)(st.pos_off[slot] + pos) * st.rec_words;
                         uint32_t *ri = reinterpret_cast<uint32_t *>(r);
+                        // summary: a later distk below the minimum estimate, or below a stage minimum,
+                        // leaves the block without effect
+                        float mn = ((cm >> lane) & 1u) ? sm.cur[w * 32 + lane] : __int_as_float(0x7fffffff);
+                        float mx = (S > 1 && lane < sm.nstage[w]) ? sm.stage[w * (S + 1) + lane] : __int_as_float(0x7fffffff);
+#pragma unroll
+                        for (int o = 16; o; o >>= 1) {
+                            mn = fminf(mn, __shfl_xor_sync(kFull, mn, o));
+                            mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+                        }
                         if (lane == 0) {
                             ri[0] = (uint32_t)pos;
                             ri[1] = cm;
                             ri[2] = (uint32_t)(S == 1 ? 0 : sm.nstage[w]);
                             ri[3] = (uint32_t)c;
                             ri[4] = (uint32_t)b;
-                            st.flag[(size_t)slot * st.max_pos + pos] = 1;
+                            ri[5] = (uint32_t)(uint64_t)v0;
+                            ri[6] = (uint32_t)((uint64_t)v0 >> 32);
+                            ri[7] = __float_as_uint(mx);
+                            st.summ[st.pos_off[slot] + pos] = make_float2(mn, mx);
                             if (counters) atomicAdd(counters + 3, (unsigned long long)__popc(cm));
                         }
                         if (S > 1 && lane <= S) r[8 + lane] = sm.stage[w * (S + 1) + lane];
@@ -1212,9 +1306,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
     }
 }
 
-// Per query on the list: walk its scan positions in order; flagged positions
-// are compacted CTA-wide, their records staged into shared memory by all warps
-// (kReplayChunk at a time), and warp 0 replays them.
+// Per query on the list: walk its scan positions in order, kScanThreads at a
+// time.  A record can matter only if a candidate estimate lies below distk and
+// no stage minimum above it; distk only shrinks, so positions whose summary
+// fails the distk at the chunk's start are dropped at once (they would fail at
+// their own turn too).  The rest are compacted, staged into shared memory
+// (kReplayChunk at a time) and replayed in order by warp 0.
 __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, int topk, SplitState st,
                                                               uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
                                                               unsigned long long *__restrict__ counters, int xstride) {
@@ -1238,8 +1335,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, i
         distk = st.tau[slot];
     }
     const int np = st.npos[slot];
-    const uint8_t *fl = st.flag + (size_t)slot * st.max_pos;
-    const float *rq = st.rec + (size_t)slot * st.max_pos * st.rec_words;
+    const float2 *su = st.summ + st.pos_off[slot];
+    const float *rq = st.rec + (size_t)st.pos_off[slot] * st.rec_words;
     const int RW = st.rec_words;
     unsigned long long rr = 0;
     float dk = FLT_MAX;
@@ -1251,7 +1348,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, i
     }
     for (int base = 0; base < np; base += kScanThreads) {
         const int pos = base + tid;
-        const bool f = pos < np && fl[pos];
+        const float dk0 = distk;
+        bool f = false;
+        if (pos < np) {
+            const float2 v = su[pos];
+            f = v.x < dk0 && !(v.y > dk0);
+        }
         const uint32_t bal = __ballot_sync(kFull, f);
         if (lane == 0) warp_cnt[w] = __popc(bal);
         __syncthreads();
@@ -1262,23 +1364,37 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, i
         }
         if (f) list[off + __popc(bal & ((1u << lane) - 1))] = pos;
         __syncthreads();
-        for (int c0 = 0; c0 < total; c0 += kReplayChunk) {
-            const int cn = min(kReplayChunk, total - c0);
-            for (int i = tid; i < cn * RW; i += blockDim.x) {
-                const int r = i / RW, k = i - r * RW;
-                stage_buf[i] = rq[(size_t)list[c0 + r] * RW + k];
+        // chunk k is replayed by warp 0 from one buffer while the other warps stage chunk k + 1
+        const int nch = (total + kReplayChunk - 1) / kReplayChunk;
+        auto stage = [&](int k, int t0, int nt) {
+            const int c0 = k * kReplayChunk, cn = min(kReplayChunk, total - c0);
+            float *buf = stage_buf + (size_t)(k & 1) * kReplayChunk * RW;
+            for (int i = t0; i < cn * RW; i += nt) {
+                const int r = i / RW, e = i - r * RW;
+                buf[i] = rq[(size_t)list[c0 + r] * RW + e];
+            }
+        };
+        if (nch) stage(0, tid, kScanThreads);
+        __syncthreads();
+        for (int k = 0; k < nch; ++k) {
+            if (w == 0) {
+                const float *buf = stage_buf + (size_t)(k & 1) * kReplayChunk * RW;
+                const int cn = min(kReplayChunk, total - k * kReplayChunk);
+                for (int r = 0; r < cn; ++r) {
+                    const float *rec = buf + r * RW;
+                    const uint32_t *ri = reinterpret_cast<const uint32_t *>(rec);
+                    const int64_t v0 = (int64_t)(((uint64_t)ri[6] << 32) | ri[5]);
+                    replay_block_warp(S, (int)ri[4], rec + 8 + (S + 1), __uint_as_float(ri[7]),
+                                      rec + 8 + (S + 1) + 32, ri[1], ix.ids + v0, sm.pool_id, sm.pool_d, sz, topk, dk,
+                                      rr);
+                }
+            } else if (k + 1 < nch) {
+                stage(k + 1, tid - 32, kScanThreads - 32);
             }
             __syncthreads();
-            if (w == 0)
-                for (int r = 0; r < cn; ++r) {
-                    const float *rec = stage_buf + r * RW;
-                    const uint32_t *ri = reinterpret_cast<const uint32_t *>(rec);
-                    const int c = (int)ri[3], bb = (int)ri[4];
-                    replay_block_warp(S, bb, rec + 8 + (S + 1), rec + 8, (int)ri[2], rec + 8 + (S + 1) + 32, ri[1],
-                                      ix.ids + ix.vec_off[c], sm.pool_id, sm.pool_d, sz, topk, dk, rr);
-                }
-            __syncthreads();
         }
+        if (tid == 0) distk = dk;
+        __syncthreads();
     }
     if (tid == 0) pool_size = sz;
     if (tid == 0 && counters) atomicAdd(counters + 2, rr);
@@ -1309,7 +1425,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
 }
 
 // Puts every query whose probes hold more than `defer_blocks` blocks (a giant
-// Zipf cluster) on the split list, while it has room.
+// Zipf cluster; every query when defer_blocks < 0) on the split list, each
+// with record positions for all its blocks, while the record space lasts.
 __global__ void k_defer(DevIndexView ix, const uint32_t *__restrict__ probe, int nprobe, int nq, int defer_blocks,
                         SplitState st, uint8_t *__restrict__ deferred) {
     const int qi = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1320,19 +1437,24 @@ __global__ void k_defer(DevIndexView ix, const uint32_t *__restrict__ probe, int
         total += ix.blk_off[c + 1] - ix.blk_off[c];
     }
     uint8_t d = 0;
-    if (defer_blocks > 0 && total > defer_blocks) {
-        const int t = atomicAdd(st.nlist, 1);
-        if (t < st.cap) {
-            st.qlist[t] = qi;
-            d = 1;
+    if (defer_blocks < 0 || (defer_blocks > 0 && total > defer_blocks)) {
+        // reserve [cur, cur + total) of the record space (lock-free; bounded retries)
+        unsigned long long cur = atomicAdd(st.pos_used, 0ull);
+        for (int tries = 0; tries < (1 << 16); ++tries) {
+            if (cur + (unsigned long long)total > (unsigned long long)st.pos_cap) break;
+            const unsigned long long prev = atomicCAS(st.pos_used, cur, cur + (unsigned long long)total);
+            if (prev == cur) {
+                const int t = atomicAdd(st.nlist, 1);  // < cap: cap is the batch size
+                st.qlist[t] = qi;
+                st.pos_off[t] = (int64_t)cur;
+                st.npos[t] = (int)total;
+                d = 1;
+                break;
+            }
+            cur = prev;
         }
     }
     deferred[qi] = d;
-}
-
-__global__ void k_iota(int *list, int *nlist, int n) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) list[i] = i;
-    if (threadIdx.x == 0) *nlist = n;
 }
 
 // ------------------------------------------------------------------ estimate
@@ -1417,10 +1539,10 @@ size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t np
     return b + 256;
 }
 
-size_t split_scratch_bytes(const Index &I, int64_t cap, int64_t topk, int64_t nprobe, int64_t max_pos, int64_t nq) {
+size_t split_scratch_bytes(const Index &I, int64_t cap, int64_t topk, int64_t nprobe, int64_t pos_cap) {
     size_t b = 0;
     auto add = [&](size_t x) { b += align16(x); };
-    add(4 * 16);                                 // nlist
+    add(4 * 16);                                 // nlist, pos_used
     add(4 * (size_t)cap);                        // qlist
     add(4 * (size_t)cap * topk);
     add(4 * (size_t)cap * topk);
@@ -1428,18 +1550,21 @@ size_t split_scratch_bytes(const Index &I, int64_t cap, int64_t topk, int64_t np
     add(4 * (size_t)cap);
     add(4 * (size_t)cap * (nprobe + 1));
     add(4 * (size_t)cap * nprobe);
+    add(8 * (size_t)cap);                        // split_p, split_b
     add(4 * (size_t)(cap + 1));
-    add(4 * (size_t)cap);
-    add((size_t)cap * max_pos);
-    add(4 * (size_t)cap * max_pos * rec_words_of(I.view.S));
-    add((size_t)nq);  // deferred flags, one per query
+    add(4 * (size_t)cap);                        // npos
+    add(8 * (size_t)cap);                        // pos_off
+    add(8 * (size_t)pos_cap);                    // record summaries
+    add(4 * (size_t)pos_cap * rec_words_of(I.view.S));
+    add((size_t)cap);                            // deferred flags, one per query
     return b + 256;
 }
 
-// Slots of the split pass for a batch: bounded by scratch memory.
-int64_t split_slots(const Index &I, int64_t max_pos, int64_t want) {
-    const size_t per = (size_t)max_pos * (4 * rec_words_of(I.view.S) + 1);
-    const int64_t by_mem = (int64_t)((size_t)4 << 30) / (int64_t)std::max<size_t>(per, 1);
+// Record positions of the split pass for a batch: every block of every query
+// (`want`), bounded by scratch memory.
+int64_t split_positions(const Index &I, int64_t want) {
+    const size_t per = 4 * (size_t)rec_words_of(I.view.S) + 8;
+    const int64_t by_mem = (int64_t)(((size_t)4 << 30) / per);
     return std::max<int64_t>(1, std::min(want, by_mem));
 }
 
@@ -1483,13 +1608,13 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
     float *od = bp.take<float>((size_t)nq * topk);
     int *flags = bp.take<int>(16);
     unsigned long long *counters = bp.take<unsigned long long>(8);
-    cudaEvent_t ev[5] = {};
+    cudaEvent_t ev[7] = {};
     if (stats)
         for (auto &e : ev) SAQG_CUDA_TRY(cudaEventCreate(&e));
     struct EvGuard {
         cudaEvent_t *e;
         ~EvGuard() {
-            for (int i = 0; i < 5; ++i)
+            for (int i = 0; i < 7; ++i)
                 if (e[i]) cudaEventDestroy(e[i]);
         }
     } evg{ev};
@@ -1541,10 +1666,13 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         } else {
             // split-pass state: every query (mode 1), or the deferred giant-cluster queries (mode 0)
             const int64_t max_pos = I.max_blocks_of_probes(nprobe);
-            const int64_t cap = mode == 1 ? nq : split_slots(I, max_pos, nq);
-            Bump sb{(char *)I.split_scratch_get(split_scratch_bytes(I, cap, topk, nprobe, max_pos, nq))};
+            const int64_t cap = nq;
+            const int64_t want = nq * max_pos;
+            const int64_t pos_cap = split_positions(I, want);
+            Bump sb{(char *)I.split_scratch_get(split_scratch_bytes(I, cap, topk, nprobe, pos_cap))};
             SplitState ss;
             ss.nlist = sb.take<int>(16);
+            ss.pos_used = reinterpret_cast<unsigned long long *>(ss.nlist + 2);
             ss.qlist = sb.take<int>(cap);
             ss.cap = (int)cap;
             ss.pool_id = sb.take<uint32_t>((size_t)cap * topk);
@@ -1553,36 +1681,42 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             ss.tau = sb.take<float>(cap);
             ss.tile_off = sb.take<int>((size_t)cap * (nprobe + 1));
             ss.blk_base = sb.take<int>((size_t)cap * nprobe);
+            ss.split_p = sb.take<int>(cap);
+            ss.split_b = sb.take<int>(cap);
             ss.q_tile_off = sb.take<int>(cap + 1);
             ss.npos = sb.take<int>(cap);
-            ss.flag = sb.take<uint8_t>((size_t)cap * max_pos);
-            ss.max_pos = max_pos;
+            ss.pos_off = sb.take<int64_t>(cap);
+            ss.pos_cap = pos_cap;
+            ss.summ = sb.take<float2>((size_t)pos_cap);
             ss.rec_words = rec_words_of(ix.S);
-            ss.rec = sb.take<float>((size_t)cap * max_pos * ss.rec_words);
+            ss.rec = sb.take<float>((size_t)pos_cap * ss.rec_words);
             uint8_t *deferred = sb.take<uint8_t>(nq);
-            SAQG_CUDA_TRY(cudaMemsetAsync(ss.flag, 0, (size_t)cap * max_pos, st));
-            cudaStream_t sp = st;  // stream of the split pass
+            SAQG_CUDA_TRY(cudaMemsetAsync(ss.summ, 0xff, 8 * (size_t)pos_cap, st));  // NaN: no record
+            SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 16, st));
+            int defer = -1;  // mode 1: every query
             if (mode == 0) {
-                SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 4, st));
-                int defer = kDeferBlocks;
-                if (const char *e = std::getenv("SAQG_DEFER_BLOCKS")) defer = std::atoi(e);
-                k_defer<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(ix, probe, (int)nprobe, (int)nq, defer, ss,
-                                                                       deferred);
-                check_launch("k_defer");
-                // the split pass runs beside the CTA scan on the index's auxiliary stream
-                sp = I.aux_stream();
-                SAQG_CUDA_TRY(cudaEventRecord(I.fork_event(), st));
-                SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, I.fork_event(), 0));
+                defer = kDeferBlocks;
+                if (const char *e = std::getenv("SAQG_DEFER_BLOCKS")) defer = std::max(0, std::atoi(e));
+            }
+            k_defer<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(ix, probe, (int)nprobe, (int)nq, defer, ss,
+                                                                   deferred);
+            check_launch("k_defer");
+            cudaStream_t sp = st;  // stream of the split pass
+            // the CTA scan serves what the split list does not hold: always in mode 0,
+            // in mode 1 only when the record space cannot hold every query
+            if (mode == 0 || pos_cap < want) {
+                if (mode == 0) {  // the split pass runs beside the CTA scan on the index's auxiliary stream
+                    sp = I.aux_stream();
+                    SAQG_CUDA_TRY(cudaEventRecord(I.fork_event(), st));
+                    SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, I.fork_event(), 0));
+                }
                 SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
                 k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk,
                                                                   ids_out, d_out, flags + 1, cnt, xs, deferred);
                 check_launch("k_scan");
-            } else {
-                k_iota<<<1, 256, 0, st>>>(ss.qlist, ss.nlist, (int)nq);
-                check_launch("k_iota");
             }
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
-            const size_t smem_r = smem + 4 * (size_t)kReplayChunk * ss.rec_words;
+            const size_t smem_r = smem + 2 * 4 * (size_t)kReplayChunk * ss.rec_words;
             SAQG_REQUIRE(smem_r <= 220 * 1024, "dimension / topk too large for the replay kernel's shared memory");
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_first, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_spec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
@@ -1592,6 +1726,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             check_launch("k_scan_first");
             k_tile_prefix<<<1, 32, 0, sp>>>(ss, (int)nprobe);
             check_launch("k_tile_prefix");
+            if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[5], sp));
             int dev = 0, sms = 0, per_sm = 0;
             SAQG_CUDA_TRY(cudaGetDevice(&dev));
             SAQG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1599,10 +1734,11 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             const unsigned grid = (unsigned)std::max(1, sms * std::max(1, per_sm));
             k_scan_spec<<<grid, kScanThreads, smem1, sp>>>(ix, probe, (int)nprobe, qrot, prune, ss, cnt, xs);
             check_launch("k_scan_spec");
+            if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[6], sp));
             k_scan_replay<<<(unsigned)cap, kScanThreads, smem_r, sp>>>(ix, (int)topk, ss, ids_out, d_out, cnt, xs);
             check_launch("k_scan_replay");
+            if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[4], sp));
             if (sp != st) {  // join
-                if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[4], sp));
                 SAQG_CUDA_TRY(cudaEventRecord(I.join_event(), sp));
                 SAQG_CUDA_TRY(cudaStreamWaitEvent(st, I.join_event(), 0));
             }
@@ -1634,11 +1770,16 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         stats->ms_qprep = t12;
         stats->ms_scan = t23;
         stats->ms_total = t03;
-        stats->ms_split = 0.0f;
-        if (cudaEventQuery(ev[4]) == cudaSuccess) {
-            float t24 = 0;
-            if (cudaEventElapsedTime(&t24, ev[2], ev[4]) == cudaSuccess) stats->ms_split = t24;
-        }
+        // split pass phases (0 when the call had no split pass)
+        auto span = [&](int a, int b) {
+            float t = 0.0f;
+            if (cudaEventQuery(ev[a]) != cudaSuccess || cudaEventQuery(ev[b]) != cudaSuccess) return 0.0f;
+            return cudaEventElapsedTime(&t, ev[a], ev[b]) == cudaSuccess ? t : 0.0f;
+        };
+        stats->ms_split = span(2, 4);
+        stats->ms_split_first = span(2, 5);
+        stats->ms_split_spec = span(5, 6);
+        stats->ms_split_replay = span(6, 4);
         cudaGetLastError();
         stats->probes = nq * nprobe;
         stats->blocks = (int64_t)hc[0];
