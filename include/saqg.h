@@ -122,6 +122,7 @@ typedef struct saqg_search_stats {
     float ms_split_first;  /* ... its exact prefix scans (the speculation bounds) */
     float ms_split_spec;   /* ... its speculative tile estimates */
     float ms_split_replay; /* ... its sequential replays */
+    int64_t probe_exact;   /* exact query-centroid distances evaluated for the probe ranking */
 } saqg_search_stats;
 
 /* saqg_search plus measurements: `stats` (may be NULL) and `probes` (may be

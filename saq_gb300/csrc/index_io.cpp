@@ -16,6 +16,8 @@
 #include <functional>
 #include <memory>
 
+#include <cublas_v2.h>
+
 #include "saqg_internal.h"
 
 namespace saqg {
@@ -79,6 +81,8 @@ Index::~Index() {
     if (scratch) cudaFree(scratch);
     if (split_scratch) cudaFree(split_scratch);
     if (aux) cudaStreamDestroy(aux);
+    if (cnorm2) cudaFree(cnorm2);
+    if (blas) cublasDestroy(static_cast<cublasHandle_t>(blas));
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
     cudaSetDevice(cur);

@@ -100,6 +100,9 @@ struct Index {
     mutable size_t scratch_bytes = 0;
     mutable void *split_scratch = nullptr;
     mutable size_t split_scratch_bytes = 0;
+    // probe shortlist: squared centroid norms and the BLAS handle (created on first use)
+    mutable float *cnorm2 = nullptr;
+    mutable void *blas = nullptr;
     // auxiliary stream and fork/join events (created on first use)
     mutable cudaStream_t aux = nullptr;
     mutable cudaEvent_t ev_fork = nullptr, ev_join = nullptr;

@@ -23,6 +23,8 @@
 #include <cstdlib>
 #include <string>
 
+#include <cublas_v2.h>
+
 #include "device_common.cuh"
 #include "saqg_internal.h"
 
@@ -43,6 +45,10 @@ struct SegScal {
 __device__ __forceinline__ uint32_t fkey(float f) {
     uint32_t u = __float_as_uint(f);
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ float key_to_float(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
 // ------------------------------------------------------------------ probe
@@ -155,11 +161,13 @@ constexpr int kSelMax = 1024;  // fast path handles nprobe <= 1024
 
 __global__ void __launch_bounds__(kSelThreads) k_probe_select(const float *__restrict__ dist, int K, int nprobe,
                                                               uint32_t *__restrict__ probe, Cand *__restrict__ work,
-                                                              int *__restrict__ fallback_count) {
+                                                              int *__restrict__ fallback_count,
+                                                              const uint8_t *__restrict__ only = nullptr) {
     __shared__ uint32_t hist[256];
     __shared__ uint32_t s_prefix, s_mask, s_rem, s_eq, s_n;
     __shared__ unsigned long long sel[kSelMax];
     const int qi = blockIdx.x, tid = threadIdx.x;
+    if (only && !only[qi]) return;  // ranked by the shortlist
     const float *dq = dist + (size_t)qi * K;
     if (tid == 0) {
         s_prefix = 0;
@@ -247,6 +255,202 @@ __global__ void __launch_bounds__(kSelThreads) k_probe_select(const float *__res
     }
 }
 
+// ------------------------------------------------------ probe: GEMM shortlist
+// Batches rank centroids from inner products q.c computed by a TF32
+// tensor-core GEMM.  Each approximate distance a = |q|^2 + |c|^2 - 2 q.c gets
+// a rigorous bound b on its distance from the reference's float distance
+// (TF32 operands are within 2^-10 of their FP32 values, so |q.c error| <=
+// (2^-9 + accumulation) |q||c|; the norms and the reference's own sum add
+// (2D + 32) * 2^-24 (|q| + |c|)^2).  Every centroid of the exact top-nprobe has
+// a - b <= T, T the nprobe-th smallest a + b, so only those centroids get the
+// exact Eigen-order distance and the ranking is the exact one.  A query with
+// equal distances among its first nprobe + 1 (where the standard library's
+// heap order decides), a non-finite value or more than kShortCap centroids on
+// its shortlist is ranked by the full exact path instead.
+constexpr int kShortThreads = 1024;
+constexpr int kShortCap = 4096;
+constexpr int kGemmMinQueries = 64;  // smaller calls rank with the exact kernels directly
+
+__global__ void k_cnorm2(DevIndexView ix, float *__restrict__ cn2) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= ix.K) return;
+    const float *cr = ix.centroids + (size_t)warp * ix.D;
+    float a = 0.0f;
+    for (int i = lane; i < ix.D; i += 32) a += cr[i] * cr[i];
+    for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
+    if (lane == 0) cn2[warp] = a;
+}
+
+struct ShortBound {
+    float e1, e2;  // b = e1 |q||c| + e2 (|q| + |c|)^2
+};
+
+__device__ __forceinline__ void approx_bounds(float qn2, float qn, float ip, float cn2, const ShortBound &sb, float &lo,
+                                              float &hi) {
+    const float cn = sqrtf(cn2);
+    const float a = (qn2 + cn2) - 2.0f * ip;
+    const float s = qn + cn;
+    const float b = (sb.e1 * qn * cn + sb.e2 * s * s) * 1.01f + 1e-30f;
+    lo = a - b;
+    hi = a + b;
+}
+
+__global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView ix, const float *__restrict__ q,
+                                                                   const float *__restrict__ ip,
+                                                                   const float *__restrict__ cn2, ShortBound sb,
+                                                                   int nprobe, uint32_t *__restrict__ probe,
+                                                                   uint8_t *__restrict__ full, int *__restrict__ fb_list,
+                                                                   int *__restrict__ fb_count,
+                                                                   unsigned long long *__restrict__ counters) {
+    extern __shared__ __align__(16) char smem_raw[];
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(smem_raw);  // [kShortCap]
+    uint32_t *cand = reinterpret_cast<uint32_t *>(keys + kShortCap);             // [kShortCap]
+    float *qs = reinterpret_cast<float *>(cand + kShortCap);                      // [D]
+    __shared__ uint32_t hist[256];
+    __shared__ uint32_t s_prefix, s_mask, s_rem, s_n;
+    __shared__ int s_bad;
+    __shared__ float s_red[kShortThreads / 32];
+    const int qi = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int K = ix.K, D = ix.D;
+    const float *ipq = ip + (size_t)qi * K;
+    float a = 0.0f;
+    for (int i = tid; i < D; i += kShortThreads) {
+        const float v = q[(size_t)qi * D + i];
+        qs[i] = v;
+        a += v * v;
+    }
+    for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
+    if (lane == 0) s_red[warp] = a;
+    if (tid == 0) {
+        s_prefix = 0;
+        s_mask = 0;
+        s_rem = (uint32_t)(nprobe - 1);
+        s_n = 0;
+        s_bad = 0;
+    }
+    __syncthreads();
+    float qn2 = 0.0f;
+    for (int i = 0; i < kShortThreads / 32; ++i) qn2 += s_red[i];
+    const float qn = sqrtf(qn2);
+    // T: the nprobe-th smallest upper end (radix select on the order-preserving keys)
+    for (int pass = 0; pass < 4; ++pass) {
+        const int shift = 24 - 8 * pass;
+        for (int i = tid; i < 256; i += kShortThreads) hist[i] = 0;
+        __syncthreads();
+        const uint32_t prefix = s_prefix, mask = s_mask;
+        for (int c = tid; c < K; c += kShortThreads) {
+            float lo, hi;
+            approx_bounds(qn2, qn, ipq[c], cn2[c], sb, lo, hi);
+            if (pass == 0 && !(isfinite(lo) && isfinite(hi))) s_bad = 1;
+            const uint32_t k = fkey(hi);
+            if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t cum = 0, rem = s_rem;
+            int b = 0;
+            for (; b < 256; ++b) {
+                if (cum + hist[b] > rem) break;
+                cum += hist[b];
+            }
+            s_rem = rem - cum;
+            s_prefix = prefix | ((uint32_t)b << shift);
+            s_mask = mask | (255u << shift);
+        }
+        __syncthreads();
+    }
+    const float T = key_to_float(s_prefix);
+    // the shortlist: lower end not above T
+    if (!s_bad)
+        for (int c = tid; c < K; c += kShortThreads) {
+            float lo, hi;
+            approx_bounds(qn2, qn, ipq[c], cn2[c], sb, lo, hi);
+            if (lo <= T) {
+                const uint32_t pos = atomicAdd(&s_n, 1u);
+                if (pos < kShortCap) cand[pos] = (uint32_t)c;
+            }
+        }
+    __syncthreads();
+    const int n = (int)s_n;
+    if (s_bad || n > kShortCap) {
+        if (tid == 0) {
+            full[qi] = 1;
+            fb_list[atomicAdd(fb_count, 1)] = qi;
+            if (counters) atomicAdd(counters + 4, (unsigned long long)K);
+        }
+        return;
+    }
+    // exact distances of the shortlist, in the reference's order (as k_probe_dist)
+    for (int i = warp; i < n; i += kShortThreads / 32) {
+        const uint32_t c = cand[i];
+        const float *cr = ix.centroids + (size_t)c * D;
+        const float d = warp_eigen_sum(D, [&](int e) {
+            const float t = __fsub_rn(cr[e], qs[e]);
+            return __fmul_rn(t, t);
+        });
+        if (lane == 0) {
+            if (d != d) s_bad = 1;
+            keys[i] = ((unsigned long long)fkey(d) << 32) | c;
+        }
+    }
+    int P = 1;
+    while (P < n) P <<= 1;
+    for (int i = n + tid; i < P; i += kShortThreads) keys[i] = ~0ull;
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < P; i += kShortThreads) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long x = keys[i], y = keys[ixj];
+                    if ((x > y) == ((i & k) == 0)) {
+                        keys[i] = y;
+                        keys[ixj] = x;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    // equal distances among the first nprobe + 1 leave the order to the heap
+    const int m = min(n, nprobe + 1);
+    for (int i = tid; i + 1 < m; i += kShortThreads)
+        if ((keys[i] >> 32) == (keys[i + 1] >> 32)) s_bad = 1;
+    __syncthreads();
+    if (s_bad || n < nprobe) {
+        if (tid == 0) {
+            full[qi] = 1;
+            fb_list[atomicAdd(fb_count, 1)] = qi;
+            if (counters) atomicAdd(counters + 4, (unsigned long long)K);
+        }
+        return;
+    }
+    for (int i = tid; i < nprobe; i += kShortThreads) probe[(size_t)qi * nprobe + i] = (uint32_t)(keys[i] & 0xffffffffu);
+    if (tid == 0) {
+        full[qi] = 0;
+        if (counters) atomicAdd(counters + 4, (unsigned long long)n);
+    }
+}
+
+// Exact distances to every centroid for the queries the shortlist handed back
+// (a grid-stride loop over (query, group of 8 centroids)).
+__global__ void k_probe_dist_list(DevIndexView ix, const float *__restrict__ q, float *__restrict__ dist,
+                                  const int *__restrict__ fb_list, const int *__restrict__ fb_count) {
+    const int nfb = *fb_count;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    const int groups = (ix.K + wpb - 1) / wpb;
+    for (long w = blockIdx.x; w < (long)nfb * groups; w += gridDim.x) {
+        const int qi = fb_list[w / groups], c = (int)(w % groups) * wpb + warp;
+        if (c >= ix.K) continue;
+        const float *cr = ix.centroids + (size_t)c * ix.D;
+        const float *qq = q + (size_t)qi * ix.D;
+        const float d = warp_eigen_sum(ix.D, [&](int i) {
+            const float t = __fsub_rn(cr[i], qq[i]);
+            return __fmul_rn(t, t);
+        });
+        if (lane == 0) dist[(size_t)qi * ix.K + c] = d;
+    }
+}
+
 // ------------------------------------------------------------------ query prep
 __global__ void k_qprep(DevIndexView ix, const float *__restrict__ q, float m, float *__restrict__ qrot,
                         float *__restrict__ prune) {
@@ -285,9 +489,6 @@ __global__ void k_qprep(DevIndexView ix, const float *__restrict__ q, float m, f
 }
 
 // ------------------------------------------------------------------ LUT
-__device__ __forceinline__ float key_to_float(uint32_t k) {
-    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
-}
 
 // 16 float LUT entries of one 4-dim codebook: fastscan::pack_lut (fastscan.hpp:236-248),
 // entry j = entry[j - lowbit(j)] + q[kPos[j]].
@@ -1532,6 +1733,8 @@ size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t np
     add(4 * (size_t)nq * nprobe);              // probe ids
     add(4 * (size_t)nq * I.view.Dtot);         // rotated queries
     add(4 * (size_t)nq * I.view.S);            // prune bounds
+    add((size_t)nq);                           // shortlist: queries on the full exact path
+    add(4 * (size_t)nq);                       // ... and their list
     add(4 * (size_t)nq * topk * 2);            // outputs (host io)
     add(64);                                   // flags
     add(64);                                   // counters
@@ -1587,6 +1790,49 @@ void check_launch(const char *what) {
     if (e != cudaSuccess) throw Error{SAQG_ERR_CUDA, std::string(what) + " launch failed: " + cudaGetErrorString(e)};
 }
 
+void blas_try(cublasStatus_t e, const char *what) {
+    if (e != CUBLAS_STATUS_SUCCESS) throw Error{SAQG_ERR_CUDA, std::string(what) + " failed (cuBLAS status " +
+                                                                   std::to_string((int)e) + ")"};
+}
+
+// Centroid ranking of a batch: TF32 GEMM of inner products, the shortlist
+// kernel, and the full exact path for the queries it hands back.
+void probe_shortlist(const Index &I, const float *q, int64_t nq, int64_t nprobe, float *dist, uint32_t *probe,
+                     uint8_t *full, int *fb_list, int *flags, Cand *work, unsigned long long *cnt, cudaStream_t st) {
+    const DevIndexView &ix = I.view;
+    if (!I.cnorm2) {
+        SAQG_CUDA_TRY(cudaMalloc(&I.cnorm2, 4 * (size_t)I.K));
+        k_cnorm2<<<(unsigned)((I.K * 32 + 255) / 256), 256, 0, st>>>(ix, I.cnorm2);
+        check_launch("k_cnorm2");
+    }
+    if (!I.blas) {
+        cublasHandle_t h = nullptr;
+        blas_try(cublasCreate(&h), "cublasCreate");
+        I.blas = h;
+    }
+    cublasHandle_t h = static_cast<cublasHandle_t>(I.blas);
+    blas_try(cublasSetStream(h, st), "cublasSetStream");
+    const float one = 1.0f, zero = 0.0f;
+    // dist (row-major nq x K) = Q C^T, i.e. column-major K x nq = C^T(op T) * Q^T
+    blas_try(cublasGemmEx(h, CUBLAS_OP_T, CUBLAS_OP_N, (int)I.K, (int)nq, (int)I.D, &one, ix.centroids, CUDA_R_32F,
+                          (int)I.D, q, CUDA_R_32F, (int)I.D, &zero, dist, CUDA_R_32F, (int)I.K,
+                          CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT),
+             "cublasGemmEx");
+    const double u = 1.0 / 16777216.0;
+    ShortBound sb;
+    sb.e1 = (float)(2.0 * (1.0 / 512 + 1.0 / 1048576 + (double)(I.D + 2) * u));
+    sb.e2 = (float)((2.0 * (double)I.D + 32.0) * u);
+    const size_t smem = 12 * (size_t)kShortCap + 4 * (size_t)I.D;
+    SAQG_CUDA_TRY(cudaFuncSetAttribute(k_probe_shortlist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_probe_shortlist<<<(unsigned)nq, kShortThreads, smem, st>>>(ix, q, dist, I.cnorm2, sb, (int)nprobe, probe, full,
+                                                                 fb_list, flags + 2, cnt);
+    check_launch("k_probe_shortlist");
+    k_probe_dist_list<<<608, 256, 0, st>>>(ix, q, dist, fb_list, flags + 2);
+    check_launch("k_probe_dist_list");
+    k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, work, flags, full);
+    check_launch("k_probe_select");
+}
+
 }  // namespace
 
 void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,
@@ -1604,11 +1850,14 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
     uint32_t *probe = bp.take<uint32_t>((size_t)nq * nprobe);
     float *qrot = bp.take<float>((size_t)nq * ix.Dtot);
     float *prune = bp.take<float>((size_t)nq * ix.S);
+    uint8_t *full = bp.take<uint8_t>((size_t)nq);
+    int *fb_list = bp.take<int>((size_t)nq);
     uint32_t *oid = bp.take<uint32_t>((size_t)nq * topk);
     float *od = bp.take<float>((size_t)nq * topk);
     int *flags = bp.take<int>(16);
     unsigned long long *counters = bp.take<unsigned long long>(8);
     cudaEvent_t ev[7] = {};
+    bool shortlist = false;  // centroid ranking by the GEMM shortlist
     if (stats)
         for (auto &e : ev) SAQG_CUDA_TRY(cudaEventCreate(&e));
     struct EvGuard {
@@ -1629,7 +1878,11 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         const int wpb = 8;
         dim3 grid((unsigned)((I.K + wpb - 1) / wpb), (unsigned)nq);
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[0], st));
-        if (nq >= 8 && I.D % 32 == 0 && I.D <= 32 * kProbeRegs) {
+        const char *pm = std::getenv("SAQG_PROBE");
+        shortlist = nq >= kGemmMinQueries && nprobe <= kShortCap && !(pm && std::string(pm) == "exact");
+        if (shortlist) {
+            probe_shortlist(I, qin, nq, nprobe, dist, probe, full, fb_list, flags, work, stats ? counters : nullptr, st);
+        } else if (nq >= 8 && I.D % 32 == 0 && I.D <= 32 * kProbeRegs) {
             const size_t qsm = 4 * (size_t)kProbeQT * I.D;
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_probe_dist_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm));
             const unsigned gx = (unsigned)std::min<int64_t>((I.K + kProbeWarps - 1) / kProbeWarps, 304);
@@ -1640,8 +1893,10 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             k_probe_dist<<<grid, wpb * 32, 0, st>>>(ix, qin, dist);
             check_launch("k_probe_dist");
         }
-        k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, work, flags);
-        check_launch("k_probe_select");
+        if (!shortlist) {
+            k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, work, flags);
+            check_launch("k_probe_select");
+        }
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[1], st));
         size_t qsm = 0;
         for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
@@ -1758,8 +2013,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         if (hflags[1]) throw Error{SAQG_ERR_INTERNAL, "scan replay met a lane without a precomputed distance"};
     }
     if (stats) {
-        unsigned long long hc[4] = {0, 0, 0, 0};
-        SAQG_CUDA_TRY(cudaMemcpyAsync(hc, counters, 32, cudaMemcpyDeviceToHost, st));
+        unsigned long long hc[5] = {0, 0, 0, 0, 0};
+        SAQG_CUDA_TRY(cudaMemcpyAsync(hc, counters, 40, cudaMemcpyDeviceToHost, st));
         SAQG_CUDA_TRY(cudaStreamSynchronize(st));
         float t01 = 0, t12 = 0, t23 = 0, t03 = 0;
         SAQG_CUDA_TRY(cudaEventElapsedTime(&t01, ev[0], ev[1]));
@@ -1786,6 +2041,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         stats->vectors = (int64_t)hc[1];
         stats->reranked = (int64_t)hc[2];
         stats->speculative = (int64_t)hc[3];
+        stats->probe_exact = shortlist ? (int64_t)hc[4] : nq * I.K;
         // Algorithmic bytes: per scanned block 32 lanes of 1-bit codes of
         // every coded segment and |o| of every segment; per probe the rotated centroid;
         // per re-ranked vector its ex-codes, ex factors and id.
