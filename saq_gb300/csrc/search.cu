@@ -1314,7 +1314,6 @@ struct SplitState {
 };
 
 __host__ __device__ inline int rec_words_of(int S) { return (8 + (S + 1) + 32 + 32 * S + 3) & ~3; }
-constexpr int kReplayChunk = 16;  // records staged in shared memory per replay step
 
 __device__ __forceinline__ int list_len(const SplitState &st) { return min(*st.nlist, st.cap); }
 
@@ -1507,12 +1506,54 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
     }
 }
 
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Whether a staged record changes the pool under the current distk / pool
+// size (some lane's insert would be accepted), and how many of its lanes the
+// reference evaluates accurately when nothing earlier in the record changes
+// distk.  Warp-uniform.
+__device__ __forceinline__ bool record_effect(int S, const float *rec, float dk, int sz, int topk, int &count) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t *ri = reinterpret_cast<const uint32_t *>(rec);
+    const uint32_t cm = ri[1];
+    count = 0;
+    if (!cm || (S > 1 && __uint_as_float(ri[7]) > dk)) return false;
+    const float *cur = rec + 8 + (S + 1), *part = cur + 32;
+    const bool in = (cm >> lane) & 1u;
+    const float c = in ? cur[lane] : FLT_MAX;
+    const bool pass = in && c < dk;
+    count = __popc(__ballot_sync(kFull, pass));
+    float acc = c;
+    if (S == 1) {
+        acc = pass ? part[lane] : FLT_MAX;
+    } else if (pass) {
+        for (int s = 0; s < S; ++s) {
+            acc = __fadd_rn(acc, part[s * 32 + lane]);
+            if (acc >= dk) break;
+        }
+    }
+    return __any_sync(kFull, pass && !(sz == topk && acc > dk));
+}
+
+constexpr int kReplayRecs = 32;  // records per staged chunk (double-buffered)
+
 // Per query on the list: walk its scan positions in order, kScanThreads at a
 // time.  A record can matter only if a candidate estimate lies below distk and
 // no stage minimum above it; distk only shrinks, so positions whose summary
-// fails the distk at the chunk's start are dropped at once (they would fail at
-// their own turn too).  The rest are compacted, staged into shared memory
-// (kReplayChunk at a time) and replayed in order by warp 0.
+// fails the distk at the window's start are dropped at once.  The rest are
+// staged into shared memory by asynchronous copies, kReplayRecs at a time
+// (the next chunk in flight while the current one is evaluated).  In a chunk,
+// every warp evaluates records under the current distk; the first record with
+// an accepted insert is replayed exactly by warp 0 (the records before it
+// change nothing and only add their counts), and evaluation resumes after it.
 __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, int topk, SplitState st,
                                                               uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
                                                               unsigned long long *__restrict__ counters, int xstride) {
@@ -1526,6 +1567,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, i
     __shared__ float distk;
     __shared__ int list[kScanThreads];
     __shared__ int warp_cnt[kScanWarps];
+    __shared__ int eff[kReplayRecs], cnt[kReplayRecs];
+    __shared__ int s_next;
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     for (int i = tid; i < topk; i += blockDim.x) {
         sm.pool_id[i] = st.pool_id[(size_t)slot * topk + i];
@@ -1538,15 +1581,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, i
     const int np = st.npos[slot];
     const float2 *su = st.summ + st.pos_off[slot];
     const float *rq = st.rec + (size_t)st.pos_off[slot] * st.rec_words;
-    const int RW = st.rec_words;
+    const int RW = st.rec_words, R16 = RW / 4;
     unsigned long long rr = 0;
-    float dk = FLT_MAX;
-    int sz = 0;
     __syncthreads();
-    if (w == 0) {
-        dk = distk;
-        sz = pool_size;
-    }
     for (int base = 0; base < np; base += kScanThreads) {
         const int pos = base + tid;
         const float dk0 = distk;
@@ -1565,41 +1602,70 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, i
         }
         if (f) list[off + __popc(bal & ((1u << lane) - 1))] = pos;
         __syncthreads();
-        // chunk k is replayed by warp 0 from one buffer while the other warps stage chunk k + 1
-        const int nch = (total + kReplayChunk - 1) / kReplayChunk;
-        auto stage = [&](int k, int t0, int nt) {
-            const int c0 = k * kReplayChunk, cn = min(kReplayChunk, total - c0);
-            float *buf = stage_buf + (size_t)(k & 1) * kReplayChunk * RW;
-            for (int i = t0; i < cn * RW; i += nt) {
-                const int r = i / RW, e = i - r * RW;
-                buf[i] = rq[(size_t)list[c0 + r] * RW + e];
+        const int nch = (total + kReplayRecs - 1) / kReplayRecs;
+        auto issue = [&](int k) {
+            const int c0 = k * kReplayRecs, cn = min(kReplayRecs, total - c0);
+            float *buf = stage_buf + (size_t)(k & 1) * kReplayRecs * RW;
+            for (int i = tid; i < cn * R16; i += kScanThreads) {
+                const int r = i / R16, e = i - r * R16;
+                cp_async16(buf + (size_t)r * RW + 4 * e, rq + (size_t)list[c0 + r] * RW + 4 * e);
             }
+            cp_async_commit();
         };
-        if (nch) stage(0, tid, kScanThreads);
-        __syncthreads();
+        if (nch) issue(0);
         for (int k = 0; k < nch; ++k) {
-            if (w == 0) {
-                const float *buf = stage_buf + (size_t)(k & 1) * kReplayChunk * RW;
-                const int cn = min(kReplayChunk, total - k * kReplayChunk);
-                for (int r = 0; r < cn; ++r) {
-                    const float *rec = buf + r * RW;
-                    const uint32_t *ri = reinterpret_cast<const uint32_t *>(rec);
-                    const int64_t v0 = (int64_t)(((uint64_t)ri[6] << 32) | ri[5]);
-                    replay_block_warp(S, (int)ri[4], rec + 8 + (S + 1), __uint_as_float(ri[7]),
-                                      rec + 8 + (S + 1) + 32, ri[1], ix.ids + v0, sm.pool_id, sm.pool_d, sz, topk, dk,
-                                      rr);
-                }
-            } else if (k + 1 < nch) {
-                stage(k + 1, tid - 32, kScanThreads - 32);
+            if (k + 1 < nch) {
+                issue(k + 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
             }
             __syncthreads();
+            const float *buf = stage_buf + (size_t)(k & 1) * kReplayRecs * RW;
+            const int cn = min(kReplayRecs, total - k * kReplayRecs);
+            int r0 = 0;
+            while (r0 < cn) {
+                const float dk = distk;
+                const int sz = pool_size;
+                for (int r = r0 + w; r < cn; r += kScanWarps) {
+                    int c;
+                    const bool e = record_effect(S, buf + (size_t)r * RW, dk, sz, topk, c);
+                    if (lane == 0) {
+                        eff[r] = e;
+                        cnt[r] = c;
+                    }
+                }
+                __syncthreads();
+                if (w == 0) {
+                    const bool mine = lane >= r0 && lane < cn;
+                    const uint32_t hit = __ballot_sync(kFull, mine && eff[lane]);
+                    const int rs = hit ? __ffs(hit) - 1 : cn;  // first record that changes the pool
+                    int c = (lane >= r0 && lane < rs) ? cnt[lane] : 0;
+                    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+                    rr += (unsigned long long)c;
+                    if (rs < cn) {
+                        const float *rec = buf + (size_t)rs * RW;
+                        const uint32_t *ri = reinterpret_cast<const uint32_t *>(rec);
+                        const int64_t v0 = (int64_t)(((uint64_t)ri[6] << 32) | ri[5]);
+                        float dkw = dk;
+                        int szw = sz;
+                        replay_block_warp(S, (int)ri[4], rec + 8 + (S + 1), __uint_as_float(ri[7]),
+                                          rec + 8 + (S + 1) + 32, ri[1], ix.ids + v0, sm.pool_id, sm.pool_d, szw, topk,
+                                          dkw, rr);
+                        if (lane == 0) {
+                            distk = dkw;
+                            pool_size = szw;
+                        }
+                    }
+                    if (lane == 0) s_next = rs + 1;
+                }
+                __syncthreads();
+                r0 = s_next;
+            }
         }
-        if (tid == 0) distk = dk;
-        __syncthreads();
     }
-    if (tid == 0) pool_size = sz;
-    if (tid == 0 && counters) atomicAdd(counters + 2, rr);
     __syncthreads();
+    if (tid == 0 && counters) atomicAdd(counters + 2, rr);
     write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
 }
 
@@ -1971,7 +2037,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                 check_launch("k_scan");
             }
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
-            const size_t smem_r = smem + 2 * 4 * (size_t)kReplayChunk * ss.rec_words;
+            const size_t smem_r = smem + 2 * 4 * (size_t)kReplayRecs * ss.rec_words;
             SAQG_REQUIRE(smem_r <= 220 * 1024, "dimension / topk too large for the replay kernel's shared memory");
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_first, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_spec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
