@@ -40,7 +40,19 @@ constexpr int kMaxTopK = 4096;
 
 struct SegScal {
     float delta, vl, sum_vl, sum_q, q_l2sqr, q_l2norm, c1, c2, vfac;
+    float rdelta;  // RN(1 / delta): the LUT quantizer's fast path
 };
+
+// A u16 LUT entry (uint16_t)(int)(x / d), x >= 0, with the division rounded to
+// nearest, mostly without dividing: y = RN(x * r), r = RN(1 / d), lies within
+// 3.02 * 2^-24 * y of RN(x / d), so when no integer lies within 2^-21 * y of y
+// both truncate to the same integer.  Otherwise (and for NaN / inf) divide.
+__device__ __forceinline__ uint32_t lut_quant(float x, float r, float d) {
+    const float y = __fmul_rn(x, r);
+    const float e = __fmul_rn(y, 4.76837158203125e-07f);  // 2^-21
+    if (floorf(__fsub_rn(y, e)) == floorf(__fadd_rn(y, e))) return (uint16_t)(int)y;
+    return (uint16_t)(int)__fdiv_rn(x, d);
+}
 
 __device__ __forceinline__ uint32_t fkey(float f) {
     uint32_t u = __float_as_uint(f);
@@ -271,23 +283,26 @@ constexpr int kShortThreads = 1024;
 constexpr int kShortCap = 4096;
 constexpr int kGemmMinQueries = 64;  // smaller calls rank with the exact kernels directly
 
-__global__ void k_cnorm2(DevIndexView ix, float *__restrict__ cn2) {
+constexpr int kShortKeys = 16384;    // clusters whose upper-bound keys the shortlist keeps in shared memory
+
+// |c|^2 and |c| of every centroid (any summation order: only the bounds use them)
+__global__ void k_cnorm2(DevIndexView ix, float2 *__restrict__ cn) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= ix.K) return;
     const float *cr = ix.centroids + (size_t)warp * ix.D;
     float a = 0.0f;
     for (int i = lane; i < ix.D; i += 32) a += cr[i] * cr[i];
     for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(kFull, a, o);
-    if (lane == 0) cn2[warp] = a;
+    if (lane == 0) cn[warp] = make_float2(a, sqrtf(a));
 }
 
 struct ShortBound {
     float e1, e2;  // b = e1 |q||c| + e2 (|q| + |c|)^2
 };
 
-__device__ __forceinline__ void approx_bounds(float qn2, float qn, float ip, float cn2, const ShortBound &sb, float &lo,
+__device__ __forceinline__ void approx_bounds(float qn2, float qn, float ip, float2 cnn, const ShortBound &sb, float &lo,
                                               float &hi) {
-    const float cn = sqrtf(cn2);
+    const float cn2 = cnn.x, cn = cnn.y;
     const float a = (qn2 + cn2) - 2.0f * ip;
     const float s = qn + cn;
     const float b = (sb.e1 * qn * cn + sb.e2 * s * s) * 1.01f + 1e-30f;
@@ -297,7 +312,7 @@ __device__ __forceinline__ void approx_bounds(float qn2, float qn, float ip, flo
 
 __global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView ix, const float *__restrict__ q,
                                                                    const float *__restrict__ ip,
-                                                                   const float *__restrict__ cn2, ShortBound sb,
+                                                                   const float2 *__restrict__ cn2, ShortBound sb,
                                                                    int nprobe, uint32_t *__restrict__ probe,
                                                                    uint8_t *__restrict__ full, int *__restrict__ fb_list,
                                                                    int *__restrict__ fb_count,
@@ -306,6 +321,8 @@ __global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView 
     unsigned long long *keys = reinterpret_cast<unsigned long long *>(smem_raw);  // [kShortCap]
     uint32_t *cand = reinterpret_cast<uint32_t *>(keys + kShortCap);             // [kShortCap]
     float *qs = reinterpret_cast<float *>(cand + kShortCap);                      // [D]
+    uint32_t *hk = reinterpret_cast<uint32_t *>(qs + ix.D);                       // [K] when K <= kShortKeys
+    const bool keep = ix.K <= kShortKeys;
     __shared__ uint32_t hist[256];
     __shared__ uint32_t s_prefix, s_mask, s_rem, s_n;
     __shared__ int s_bad;
@@ -339,10 +356,16 @@ __global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView 
         __syncthreads();
         const uint32_t prefix = s_prefix, mask = s_mask;
         for (int c = tid; c < K; c += kShortThreads) {
-            float lo, hi;
-            approx_bounds(qn2, qn, ipq[c], cn2[c], sb, lo, hi);
-            if (pass == 0 && !(isfinite(lo) && isfinite(hi))) s_bad = 1;
-            const uint32_t k = fkey(hi);
+            uint32_t k;
+            if (pass == 0 || !keep) {
+                float lo, hi;
+                approx_bounds(qn2, qn, ipq[c], cn2[c], sb, lo, hi);
+                if (pass == 0 && !(isfinite(lo) && isfinite(hi))) s_bad = 1;
+                k = fkey(hi);
+                if (keep) hk[c] = k;
+            } else {
+                k = hk[c];
+            }
             if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255u], 1u);
         }
         __syncthreads();
@@ -556,6 +579,58 @@ __device__ __forceinline__ void pool_insert(uint32_t *ids, float *d, int &size, 
     size += (size < cap);
 }
 
+// k_qprep for a tile of kQprepQT queries per CTA: each P element is read once
+// for the whole tile and drives kQprepQT independent chains, each in exactly
+// k_qprep's order (so the outputs are bit-identical); L2 traffic for the
+// rotations drops by the tile size.
+constexpr int kQprepQT = 16;
+__global__ void __launch_bounds__(256) k_qprep_tiled(DevIndexView ix, const float *__restrict__ q, int nq, float m,
+                                                     float *__restrict__ qrot, float *__restrict__ prune) {
+    extern __shared__ float cqs[];  // [kQprepQT][dim]
+    const int s = blockIdx.x, q0 = blockIdx.y * kQprepQT, nqt = min(kQprepQT, nq - q0);
+    const SegDev &g = ix.seg[s];
+    const int dim = g.dim, qoff = g.qoff;
+    for (int e = threadIdx.x; e < kQprepQT * dim; e += blockDim.x) {
+        const int t = e / dim, i = e - t * dim, gi = qoff + i;
+        cqs[e] = (t < nqt && gi < ix.D) ? q[(size_t)(q0 + t) * ix.D + gi] : 0.0f;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5;
+    for (int t = warp; t < nqt; t += blockDim.x >> 5) {
+        const float *cq = cqs + t * dim, *var = ix.var + qoff;
+        const float v2 = warp_eigen_sum(dim, [&](int i) { return __fmul_rn(var[i], __fmul_rn(cq[i], cq[i])); });
+        if ((threadIdx.x & 31) == 0) prune[(size_t)(q0 + t) * ix.S + s] = __fmul_rn(sqrtf(v2), m);
+    }
+    if (!g.P) {
+        for (int e = threadIdx.x; e < nqt * dim; e += blockDim.x) {
+            const int t = e / dim, i = e - t * dim;
+            qrot[(size_t)(q0 + t) * ix.Dtot + qoff + i] = cqs[e];
+        }
+        return;
+    }
+    const int bc = dim < 128 ? dim : 16;
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) {
+        float res[kQprepQT], c[kQprepQT];
+#pragma unroll
+        for (int t = 0; t < kQprepQT; ++t) res[t] = 0.0f;
+        for (int j2 = 0; j2 < dim; j2 += bc) {
+#pragma unroll
+            for (int t = 0; t < kQprepQT; ++t) c[t] = 0.0f;
+            const int je = min(j2 + bc, dim);
+            for (int j = j2; j < je; ++j) {
+                const float pv = g.P[(size_t)j * dim + i];
+#pragma unroll
+                for (int t = 0; t < kQprepQT; ++t) c[t] = fmaf(pv, cqs[t * dim + j], c[t]);
+            }
+#pragma unroll
+            for (int t = 0; t < kQprepQT; ++t) res[t] = fmaf(c[t], 1.0f, res[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < kQprepQT; ++t)
+            if (t < nqt) qrot[(size_t)(q0 + t) * ix.Dtot + qoff + i] = res[t];
+    }
+}
+
 // ------------------------------------------------------------------ scan
 struct ScanSmem {
     // laid out in dynamic shared memory by scan_smem_layout()
@@ -655,19 +730,32 @@ __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict_
         }
     }
     const int ncb_all = ix.Dtot / 4;
-    for (int cb = tid; cb < ncb_all; cb += nt) {
-        int s = 0;
-        while (s + 1 < S && cb * 4 >= ix.seg[s + 1].qoff) ++s;
-        float t[16];
-        lut_entries(sm.qres + cb * 4, t);
-        float lo = t[0], hi = t[0];
+    for (int cb0 = 0; cb0 < ncb_all; cb0 += nt) {  // warp-uniform trip count
+        const int cb = cb0 + tid;
+        int s = -1;
+        uint32_t kmin = 0xffffffffu, kmax = 0u;
+        if (cb < ncb_all) {
+            s = 0;
+            while (s + 1 < S && cb * 4 >= ix.seg[s + 1].qoff) ++s;
+            float t[16];
+            lut_entries(sm.qres + cb * 4, t);
+            float lo = t[0], hi = t[0];
 #pragma unroll
-        for (int j = 1; j < 16; ++j) {
-            lo = fminf(lo, t[j]);
-            hi = fmaxf(hi, t[j]);
+            for (int j = 1; j < 16; ++j) {
+                lo = fminf(lo, t[j]);
+                hi = fmaxf(hi, t[j]);
+            }
+            kmin = fkey(lo);
+            kmax = fkey(hi);
         }
-        atomicMin(&sm.mm[2 * s], fkey(lo));
-        atomicMax(&sm.mm[2 * s + 1], fkey(hi));
+        // one shared atomic per segment present in the warp
+        const unsigned grp = __match_any_sync(kFull, s);
+        kmin = __reduce_min_sync(grp, kmin);
+        kmax = __reduce_max_sync(grp, kmax);
+        if (s >= 0 && lane == __ffs(grp) - 1) {
+            atomicMin(&sm.mm[2 * s], kmin);
+            atomicMax(&sm.mm[2 * s + 1], kmax);
+        }
     }
     __syncthreads();
     if (tid < S) {
@@ -676,6 +764,7 @@ __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict_
         const float vl = key_to_float(sm.mm[2 * tid]), vr = key_to_float(sm.mm[2 * tid + 1]);
         const float delta = (float)__ddiv_rn((double)__fsub_rn(vr, vl), 65536.0 - 0.01);
         sc.delta = delta;
+        sc.rdelta = __frcp_rn(delta);
         sc.vl = vl;
         sc.sum_vl = (float)__dmul_rn(__dadd_rn((double)vl, __dmul_rn(0.5, (double)delta)), (double)(float)ncb);
         sc.q_l2norm = sqrtf(sc.q_l2sqr);
@@ -688,14 +777,14 @@ __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict_
     for (int cb = tid; cb < ncb_all; cb += nt) {
         int s = 0;
         while (s + 1 < S && cb * 4 >= ix.seg[s + 1].qoff) ++s;
-        const float vl = sm.scal[s].vl, delta = sm.scal[s].delta;
+        const float vl = sm.scal[s].vl, delta = sm.scal[s].delta, rd = sm.scal[s].rdelta;
         float t[16];
         lut_entries(sm.qres + cb * 4, t);
         uint32_t packed[8];
 #pragma unroll
         for (int j = 0; j < 16; j += 2) {
-            const uint32_t a = (uint16_t)(int)__fdiv_rn(__fsub_rn(t[j], vl), delta);
-            const uint32_t b = (uint16_t)(int)__fdiv_rn(__fsub_rn(t[j + 1], vl), delta);
+            const uint32_t a = lut_quant(__fsub_rn(t[j], vl), rd, delta);
+            const uint32_t b = lut_quant(__fsub_rn(t[j + 1], vl), rd, delta);
             packed[j / 2] = a | (b << 16);
         }
         uint4 *dst = reinterpret_cast<uint4 *>(sm.lut + cb * 16);
@@ -1867,8 +1956,8 @@ void probe_shortlist(const Index &I, const float *q, int64_t nq, int64_t nprobe,
                      uint8_t *full, int *fb_list, int *flags, Cand *work, unsigned long long *cnt, cudaStream_t st) {
     const DevIndexView &ix = I.view;
     if (!I.cnorm2) {
-        SAQG_CUDA_TRY(cudaMalloc(&I.cnorm2, 4 * (size_t)I.K));
-        k_cnorm2<<<(unsigned)((I.K * 32 + 255) / 256), 256, 0, st>>>(ix, I.cnorm2);
+        SAQG_CUDA_TRY(cudaMalloc(&I.cnorm2, 8 * (size_t)I.K));
+        k_cnorm2<<<(unsigned)((I.K * 32 + 255) / 256), 256, 0, st>>>(ix, reinterpret_cast<float2 *>(I.cnorm2));
         check_launch("k_cnorm2");
     }
     if (!I.blas) {
@@ -1888,9 +1977,11 @@ void probe_shortlist(const Index &I, const float *q, int64_t nq, int64_t nprobe,
     ShortBound sb;
     sb.e1 = (float)(2.0 * (1.0 / 512 + 1.0 / 1048576 + (double)(I.D + 2) * u));
     sb.e2 = (float)((2.0 * (double)I.D + 32.0) * u);
-    const size_t smem = 12 * (size_t)kShortCap + 4 * (size_t)I.D;
+    const size_t smem = 12 * (size_t)kShortCap + 4 * (size_t)I.D + (I.K <= kShortKeys ? 4 * (size_t)I.K : 0);
+    SAQG_REQUIRE(smem <= 220 * 1024, "dimension too large for the probe shortlist's shared memory");
     SAQG_CUDA_TRY(cudaFuncSetAttribute(k_probe_shortlist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_probe_shortlist<<<(unsigned)nq, kShortThreads, smem, st>>>(ix, q, dist, I.cnorm2, sb, (int)nprobe, probe, full,
+    k_probe_shortlist<<<(unsigned)nq, kShortThreads, smem, st>>>(ix, q, dist, reinterpret_cast<const float2 *>(I.cnorm2),
+                                                                 sb, (int)nprobe, probe, full,
                                                                  fb_list, flags + 2, cnt);
     check_launch("k_probe_shortlist");
     k_probe_dist_list<<<608, 256, 0, st>>>(ix, q, dist, fb_list, flags + 2);
@@ -1966,8 +2057,16 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[1], st));
         size_t qsm = 0;
         for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
-        k_qprep<<<dim3((unsigned)ix.S, (unsigned)nq), 256, qsm, st>>>(ix, qin, m, qrot, prune);
-        check_launch("k_qprep");
+        if (nq >= kQprepQT && kQprepQT * qsm <= 200 * 1024) {
+            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_qprep_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)(kQprepQT * qsm)));
+            k_qprep_tiled<<<dim3((unsigned)ix.S, (unsigned)((nq + kQprepQT - 1) / kQprepQT)), 256, kQprepQT * qsm,
+                            st>>>(ix, qin, (int)nq, m, qrot, prune);
+            check_launch("k_qprep_tiled");
+        } else {
+            k_qprep<<<dim3((unsigned)ix.S, (unsigned)nq), 256, qsm, st>>>(ix, qin, m, qrot, prune);
+            check_launch("k_qprep");
+        }
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[2], st));
         const int xs = xstride_of(ix);
         const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs);
