@@ -123,6 +123,8 @@ typedef struct saqg_search_stats {
     float ms_split_spec;   /* ... its speculative tile estimates */
     float ms_split_replay; /* ... its sequential replays */
     int64_t probe_exact;   /* exact query-centroid distances evaluated for the probe ranking */
+    int64_t probe_full;    /* queries ranked against every centroid exactly (no shortlist) */
+    int64_t probe_full_ties; /* ... of which because of equal distances on the shortlist */
 } saqg_search_stats;
 
 /* saqg_search plus measurements: `stats` (may be NULL) and `probes` (may be

@@ -39,7 +39,7 @@ class SearchStats(C.Structure):
                 ("probes", I64), ("blocks", I64), ("vectors", I64), ("reranked", I64), ("speculative", I64),
                 ("fast_bytes", I64), ("rerank_bytes", I64), ("ms_split", C.c_float),
                 ("ms_split_first", C.c_float), ("ms_split_spec", C.c_float), ("ms_split_replay", C.c_float),
-                ("probe_exact", I64)]
+                ("probe_exact", I64), ("probe_full", I64), ("probe_full_ties", I64)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

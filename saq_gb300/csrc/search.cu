@@ -168,6 +168,45 @@ __device__ void exact_partial_sort(Cand *a, long mid, long len) {
     }
 }
 
+// One radix-select step, by a whole warp: the first bin b with
+// hist[0] + ... + hist[b] > rem and the count of the bins before it (what a
+// sequential scan of the 256 bins finds).
+__device__ __forceinline__ void select_bin(const uint32_t *hist, uint32_t rem, int &b, uint32_t &below) {
+    const int lane = threadIdx.x & 31;
+    uint32_t h[8], sum = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        h[i] = hist[lane * 8 + i];
+        sum += h[i];
+    }
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t excl = incl - sum;
+    const uint32_t m = __ballot_sync(kFull, excl <= rem && rem < incl);
+    if (!m) {  // rem beyond every count: the scan runs off the end
+        b = 256;
+        below = __shfl_sync(kFull, incl, 31);
+        return;
+    }
+    const int L = __ffs(m) - 1;
+    int bb = 0;
+    uint32_t cum = excl;
+    if (lane == L) {
+        int i = 0;
+        for (; i < 8; ++i) {
+            if (cum + h[i] > rem) break;
+            cum += h[i];
+        }
+        bb = L * 8 + i;
+    }
+    b = __shfl_sync(kFull, bb, L);
+    below = __shfl_sync(kFull, cum, L);
+}
+
 constexpr int kSelThreads = 1024;
 constexpr int kSelMax = 1024;  // fast path handles nprobe <= 1024
 
@@ -197,18 +236,17 @@ __global__ void __launch_bounds__(kSelThreads) k_probe_select(const float *__res
             if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255u], 1u);
         }
         __syncthreads();
-        if (tid == 0) {
-            uint32_t cum = 0, rem = s_rem;
-            int b = 0;
-            for (; b < 256; ++b) {
-                if (cum + hist[b] > rem) break;
-                cum += hist[b];
+        if (tid < 32) {
+            int b;
+            uint32_t cum;
+            select_bin(hist, s_rem, b, cum);
+            if (tid == 0) {
+                s_rem = s_rem - cum;
+                s_prefix = prefix | ((uint32_t)b << shift);
+                s_mask = mask | (255u << shift);
+                s_eq = b < 256 ? hist[b] : 0u;
+                s_n = 0;
             }
-            s_rem = rem - cum;
-            s_prefix = prefix | ((uint32_t)b << shift);
-            s_mask = mask | (255u << shift);
-            s_eq = hist[b];
-            s_n = 0;
         }
         __syncthreads();
     }
@@ -258,12 +296,50 @@ __global__ void __launch_bounds__(kSelThreads) k_probe_select(const float *__res
         need_exact = true;
     }
     // exact fallback: the standard library's algorithm, sequentially
+    if (nprobe > kSelMax) {
+        if (tid == 0) {
+            atomicAdd(fallback_count, 1);
+            Cand *a = work + (size_t)qi * K;
+            for (int i = 0; i < K; ++i) a[i] = Cand{(uint32_t)i, dq[i]};
+            exact_partial_sort(a, nprobe, K);
+            for (int i = 0; i < nprobe; ++i) probe[(size_t)qi * nprobe + i] = a[i].id;
+        }
+        return;
+    }
+    // the same steps with the heap (the first nprobe slots of the array) in
+    // shared memory; the rest of the row is only ever compared against the
+    // heap's top at its turn, so it streams through in coalesced chunks
+    __shared__ float chunk[kSelThreads];
+    Cand *heap = reinterpret_cast<Cand *>(sel);
+    const int mid = nprobe;
+    for (int i = tid; i < mid; i += kSelThreads) heap[i] = Cand{(uint32_t)i, dq[i]};
+    __syncthreads();
     if (tid == 0) {
         atomicAdd(fallback_count, 1);
-        Cand *a = work + (size_t)qi * K;
-        for (int i = 0; i < K; ++i) a[i] = Cand{(uint32_t)i, dq[i]};
-        exact_partial_sort(a, nprobe, K);
-        for (int i = 0; i < nprobe; ++i) probe[(size_t)qi * nprobe + i] = a[i].id;
+        if (mid >= 2)
+            for (long parent = (mid - 2) / 2;; --parent) {
+                heap_adjust(heap, parent, mid, heap[parent]);
+                if (parent == 0) break;
+            }
+    }
+    for (int base = mid; base < K; base += kSelThreads) {
+        __syncthreads();
+        if (base + tid < K) chunk[tid] = dq[base + tid];
+        __syncthreads();
+        if (tid == 0) {
+            const int n = min(kSelThreads, K - base);
+            for (int j = 0; j < n; ++j)
+                if (chunk[j] < heap[0].d) heap_adjust(heap, 0, mid, Cand{(uint32_t)(base + j), chunk[j]});
+        }
+    }
+    if (tid == 0) {
+        for (long last = mid; last > 1;) {
+            --last;
+            const Cand v = heap[last];
+            heap[last] = heap[0];
+            heap_adjust(heap, 0, last, v);
+        }
+        for (int i = 0; i < mid; ++i) probe[(size_t)qi * nprobe + i] = heap[i].id;
     }
 }
 
@@ -369,16 +445,15 @@ __global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView 
             if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255u], 1u);
         }
         __syncthreads();
-        if (tid == 0) {
-            uint32_t cum = 0, rem = s_rem;
-            int b = 0;
-            for (; b < 256; ++b) {
-                if (cum + hist[b] > rem) break;
-                cum += hist[b];
+        if (tid < 32) {
+            int b;
+            uint32_t cum;
+            select_bin(hist, s_rem, b, cum);
+            if (tid == 0) {
+                s_rem = s_rem - cum;
+                s_prefix = prefix | ((uint32_t)b << shift);
+                s_mask = mask | (255u << shift);
             }
-            s_rem = rem - cum;
-            s_prefix = prefix | ((uint32_t)b << shift);
-            s_mask = mask | (255u << shift);
         }
         __syncthreads();
     }
@@ -399,6 +474,7 @@ __global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView 
         if (tid == 0) {
             full[qi] = 1;
             fb_list[atomicAdd(fb_count, 1)] = qi;
+            if (counters) atomicAdd(counters + 5, 1ull);
             if (counters) atomicAdd(counters + 4, (unsigned long long)K);
         }
         return;
@@ -443,6 +519,7 @@ __global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView 
         if (tid == 0) {
             full[qi] = 1;
             fb_list[atomicAdd(fb_count, 1)] = qi;
+            if (counters) atomicAdd(counters + 6, 1ull);
             if (counters) atomicAdd(counters + 4, (unsigned long long)K);
         }
         return;
@@ -2178,8 +2255,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         if (hflags[1]) throw Error{SAQG_ERR_INTERNAL, "scan replay met a lane without a precomputed distance"};
     }
     if (stats) {
-        unsigned long long hc[5] = {0, 0, 0, 0, 0};
-        SAQG_CUDA_TRY(cudaMemcpyAsync(hc, counters, 40, cudaMemcpyDeviceToHost, st));
+        unsigned long long hc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        SAQG_CUDA_TRY(cudaMemcpyAsync(hc, counters, 64, cudaMemcpyDeviceToHost, st));
         SAQG_CUDA_TRY(cudaStreamSynchronize(st));
         float t01 = 0, t12 = 0, t23 = 0, t03 = 0;
         SAQG_CUDA_TRY(cudaEventElapsedTime(&t01, ev[0], ev[1]));
@@ -2207,6 +2284,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         stats->reranked = (int64_t)hc[2];
         stats->speculative = (int64_t)hc[3];
         stats->probe_exact = shortlist ? (int64_t)hc[4] : nq * I.K;
+        stats->probe_full = shortlist ? (int64_t)(hc[5] + hc[6]) : nq;
+        stats->probe_full_ties = (int64_t)hc[6];
         // Algorithmic bytes: per scanned block 32 lanes of 1-bit codes of
         // every coded segment and |o| of every segment; per probe the rotated centroid;
         // per re-ranked vector its ex-codes, ex factors and id.
