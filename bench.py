@@ -45,7 +45,7 @@ CACHE_VERSION = 3
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=10_000_000)
@@ -74,7 +74,7 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
@@ -86,7 +86,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -279,6 +279,7 @@ def main():
     step_ms, scan_ms, fast_b, rr_b, spec, rr, probe_ms, qprep_ms, split_ms = [], [], [], [], [], [], [], [], []
     launches0 = lib.saqg_kernel_launches()
     with ClockSampler(local) as clk:
+        time.sleep(0.3)  # first sample before the timed region
         torch.cuda.synchronize()
         for _ in range(a.steps):
             flush.zero_()
@@ -388,7 +389,8 @@ def main():
         "batched_over_plain": value / world / plain_qps,
         "p99_ms": float(np.percentile(lat, 99)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "kernel": "k_scan", "peak_kind": peak_kind,
+                     "traffic": traffic, "kernel": "scan phase (k_scan beside the split pass)",
+                     "peak_kind": peak_kind,
                      "bytes_per_launch": compulsory, "effective_bytes_per_launch": effective,
                      "effective_gbs": effective / (mean_scan / 1e3) / 1e9, "scan_ms": mean_scan,
                      "reranked_per_query": float(np.mean(rr)) / B, "speculative_per_query": float(np.mean(spec)) / B,
