@@ -11,6 +11,7 @@
 // IVF::load reads every cluster K times in a nested loop (ivf.hpp:256-260,
 // harmless only because reads past EOF are no-ops); here each is read once.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <functional>
@@ -173,6 +174,12 @@ void finalize_view(Index &idx) {
     for (int s = 0; s < v.S; ++s) {
         v.seg[s].qoff = off;
         off += v.seg[s].dim;
+        // Lut::compFastIP's constant (lut.hpp:89-119): float (4 / 0.8) times the
+        // float of the double reciprocal of the float square root, each rounded
+        // to nearest as IEEE hosts and the device do
+        const float four_over = 4.0f / 0.8f;
+        const float inv_sqrt = (float)(1.0 / (double)std::sqrt((float)v.seg[s].dim));
+        v.seg[s].c2 = four_over * inv_sqrt;
     }
     v.Dtot = off;
 }

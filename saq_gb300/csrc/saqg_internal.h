@@ -59,6 +59,7 @@ struct SegDev {
     uint8_t *lcode = nullptr;
     float2 *exfac = nullptr;
     float *cent = nullptr;
+    float c2 = 0.0f;  // compFastIP's (4 / 0.8) * (1 / sqrt(dim)), fixed per segment
 };
 
 struct DevIndexView {  // passed to kernels by value

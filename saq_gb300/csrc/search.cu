@@ -722,12 +722,33 @@ struct ScanSmem {
     uint32_t *mm;     // per segment LUT min / max keys
     uint8_t *xbuf;    // per half-warp ex-code staging
     int xstride;
+    // second cluster state (LUT, residual query, scalars) for building the next
+    // cluster's while the current one finishes; null unless laid out with dbuf
+    uint16_t *lut2;
+    float *qres2;
+    SegScal *scal2;
 };
+
+// The cluster state `buf` (0 or 1) of a double-buffered layout.
+__device__ __forceinline__ ScanSmem cluster_view(const ScanSmem &sm, int buf) {
+    ScanSmem v = sm;
+    if (buf) {
+        v.lut = sm.lut2;
+        v.qres = sm.qres2;
+        v.scal = sm.scal2;
+    }
+    return v;
+}
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
-__host__ __device__ inline size_t scan_smem_bytes(int Dtot, int S, int topk, int xstride) {
+__host__ __device__ inline size_t scan_smem_bytes(int Dtot, int S, int topk, int xstride, bool dbuf = false) {
     size_t b = 0;
+    if (dbuf) {
+        b += align16(sizeof(uint16_t) * 4 * (size_t)Dtot);
+        b += align16(sizeof(float) * Dtot);
+        b += align16(sizeof(SegScal) * S);
+    }
     b += align16(sizeof(uint32_t) * 2 * S);
     b += align16((size_t)2 * kScanWarps * xstride);
     b += align16(sizeof(uint16_t) * 4 * (size_t)Dtot);
@@ -743,9 +764,20 @@ __host__ __device__ inline size_t scan_smem_bytes(int Dtot, int S, int topk, int
     return b;
 }
 
-__device__ ScanSmem scan_smem_layout(char *base, int Dtot, int S, int topk, int xstride) {
+__device__ ScanSmem scan_smem_layout(char *base, int Dtot, int S, int topk, int xstride, bool dbuf = false) {
     ScanSmem s;
     size_t o = 0;
+    s.lut2 = nullptr;
+    s.qres2 = nullptr;
+    s.scal2 = nullptr;
+    if (dbuf) {
+        s.lut2 = (uint16_t *)(base + o);
+        o += align16(sizeof(uint16_t) * 4 * (size_t)Dtot);
+        s.qres2 = (float *)(base + o);
+        o += align16(sizeof(float) * Dtot);
+        s.scal2 = (SegScal *)(base + o);
+        o += align16(sizeof(SegScal) * S);
+    }
     s.mm = (uint32_t *)(base + o);
     o += align16(sizeof(uint32_t) * 2 * S);
     s.xbuf = (uint8_t *)(base + o);
@@ -781,10 +813,16 @@ __device__ ScanSmem scan_smem_layout(char *base, int Dtot, int S, int topk, int 
 // whole CTA: residual query, its Eigen-order sum and squared norm, the float
 // LUT's min / max, delta = (max-min)/(65536-0.01) in double, the u16 LUT
 // trunc((entry-min)/delta), and the epilogue constants of compFastIP.
+// t_first > 0: only threads [t_first, blockDim.x) take part (whole warps),
+// synchronising on named barrier `bar` instead of __syncthreads.
 __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict__ qrot, const float *__restrict__ prune,
-                                int c, ScanSmem &sm) {
-    const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
+                                int c, ScanSmem &sm, int t_first = 0, int bar = 0) {
+    const int tid = (int)threadIdx.x - t_first, nt = (int)blockDim.x - t_first, warp = tid >> 5, lane = tid & 31;
     const int S = ix.S;
+    auto sync = [&]() {
+        if (bar) asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nt) : "memory");
+        else __syncthreads();
+    };
     for (int i = tid; i < ix.Dtot; i += nt) {
         int s = 0;
         while (s + 1 < S && i >= ix.seg[s + 1].qoff) ++s;
@@ -795,7 +833,7 @@ __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict_
         sm.mm[2 * tid] = 0xffffffffu;  // min key
         sm.mm[2 * tid + 1] = 0u;       // max key
     }
-    __syncthreads();
+    sync();
     for (int t = warp; t < 2 * S; t += nt / 32) {
         const int s = t >> 1;
         const float *qr = sm.qres + ix.seg[s].qoff;
@@ -834,7 +872,7 @@ __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict_
             atomicMax(&sm.mm[2 * s + 1], kmax);
         }
     }
-    __syncthreads();
+    sync();
     if (tid < S) {
         SegScal &sc = sm.scal[tid];
         const int dim = ix.seg[tid].dim, ncb = dim / 4;
@@ -846,11 +884,10 @@ __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict_
         sc.sum_vl = (float)__dmul_rn(__dadd_rn((double)vl, __dmul_rn(0.5, (double)delta)), (double)(float)ncb);
         sc.q_l2norm = sqrtf(sc.q_l2sqr);
         sc.c1 = (float)__dsub_rn(__dmul_rn(0.5, (double)sc.sum_q), (double)__fmul_rn(0.58f, sc.q_l2norm));
-        const float one_over_sqrtD = (float)__ddiv_rn(1.0, (double)sqrtf((float)dim));
-        sc.c2 = __fmul_rn(__fdiv_rn(4.0f, 0.8f), one_over_sqrtD);
+        sc.c2 = ix.seg[tid].c2;
         sc.vfac = __fsub_rn(sc.q_l2sqr, __fmul_rn(2.0f, prune[tid]));
     }
-    __syncthreads();
+    sync();
     for (int cb = tid; cb < ncb_all; cb += nt) {
         int s = 0;
         while (s + 1 < S && cb * 4 >= ix.seg[s + 1].qoff) ++s;
@@ -868,7 +905,7 @@ __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict_
         dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
         dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
     }
-    __syncthreads();
+    sync();
 }
 
 // Estimates of one block (this warp, lane = vector).  Fills cd/ipx for every
@@ -962,21 +999,30 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
         }
     }
     __syncthreads();
-    // accurate distances: one thread per (candidate vector, segment)
-    int total = 0;
-    for (int i = 0; i < kTileB; ++i) total += __popc(sm.cmask[i]);
-    total *= S;
-    // first pull every task's ex-code row into L1, so the chains below do not
-    // wait on memory group by group
-    for (int t = tid; t < total; t += blockDim.x) {
-        int r = t / S, s = t - r * S, ww = 0;
+    // accurate distances: one thread per (candidate vector, segment); the
+    // tasks of a segment start on a warp boundary, so a warp's lanes run the
+    // same code (one ex-code width and length) instead of diverging over all
+    int ncand = 0;
+    for (int i = 0; i < kTileB; ++i) ncand += __popc(sm.cmask[i]);
+    const int P = (ncand + 31) & ~31;
+    const int total = S * P;
+    auto decode = [&](int r, int &ww, int &j) {
+        ww = 0;
         while (r >= __popc(sm.cmask[ww])) {
             r -= __popc(sm.cmask[ww]);
             ++ww;
         }
         uint32_t mk = sm.cmask[ww];
         for (int i = 0; i < r; ++i) mk &= mk - 1;
-        const int j = __ffs(mk) - 1;
+        j = __ffs(mk) - 1;
+    };
+    // first pull every task's ex-code row into L1, so the chains below do not
+    // wait on memory group by group
+    for (int t = tid; t < total; t += blockDim.x) {
+        const int s = t / P, r = t - s * P;
+        if (r >= ncand) continue;
+        int ww, j;
+        decode(r, ww, j);
         const SegDev &g = ix.seg[s];
         if (g.bits > 1) {
             const uint8_t *row = g.lcode + (size_t)(v0 + (int64_t)(t0 + ww) * 32 + j) * g.lstride;
@@ -984,14 +1030,10 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
         }
     }
     for (int t = tid; t < total; t += blockDim.x) {
-        int r = t / S, s = t - r * S, ww = 0;
-        while (r >= __popc(sm.cmask[ww])) {
-            r -= __popc(sm.cmask[ww]);
-            ++ww;
-        }
-        uint32_t mk = sm.cmask[ww];
-        for (int i = 0; i < r; ++i) mk &= mk - 1;
-        const int j = __ffs(mk) - 1;
+        const int s = t / P, r = t - s * P;
+        if (r >= ncand) continue;
+        int ww, j;
+        decode(r, ww, j);
         const int64_t gb = b0 + t0 + ww, gv = v0 + (int64_t)(t0 + ww) * 32 + j;
         const SegDev &g = ix.seg[s];
         const float ex =
@@ -1152,20 +1194,32 @@ struct ScanTally {
 };
 
 // Exact sequential scan of probes [p_begin, p_end) of one query, continuing
-// the pool held in shared memory (pool_size / distk in shared memory).
+// the pool held in shared memory (pool_size / distk in shared memory).  With
+// a double-buffered layout (sm.lut2 set) the next cluster's state is built by
+// warps 1.. while warp 0 replays the current cluster's last tile.
 __device__ void scan_probes(const DevIndexView &ix, const uint32_t *__restrict__ probe, int p_begin, int p_end,
                             const float *__restrict__ qrot, const float *__restrict__ prune, int topk, ScanSmem &sm,
                             int &pool_size, float &distk, int *err, ScanTally &tl) {
     const int S = ix.S, tid = threadIdx.x;
+    const bool dbuf = sm.lut2 != nullptr;
+    if (p_begin >= p_end) return;
+    {
+        ScanSmem v0 = cluster_view(sm, 0);
+        prepare_cluster(ix, qrot, prune, (int)probe[p_begin], v0);
+    }
     for (int p = p_begin; p < p_end; ++p) {
+        const int buf = dbuf ? (p - p_begin) & 1 : 0;
+        ScanSmem v = cluster_view(sm, buf);
+        if (!dbuf && p > p_begin) prepare_cluster(ix, qrot, prune, (int)probe[p], v);
         const int c = (int)probe[p];
-        prepare_cluster(ix, qrot, prune, c, sm);
         const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
         const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
+        const bool ahead = dbuf && p + 1 < p_end;  // build the next cluster's state during the last replay
         tl.blocks += nb;
         tl.vecs += n;
         for (int t0 = 0; t0 < nb; t0 += kTileB) {
-            tile_candidates(ix, sm, b0, v0, nb, n, t0, nb, distk);
+            tile_candidates(ix, v, b0, v0, nb, n, t0, nb, distk);
+            const bool last = t0 + kTileB >= nb;
             if (tid < 32) {
                 if (tid == 0)
                     for (int i = 0; i < kTileB; ++i) tl.spec += __popc(sm.cmask[i]);
@@ -1180,8 +1234,15 @@ __device__ void scan_probes(const DevIndexView &ix, const uint32_t *__restrict__
                     distk = dk;
                     pool_size = sz;
                 }
+            } else if (last && ahead) {
+                ScanSmem vn = cluster_view(sm, buf ^ 1);
+                prepare_cluster(ix, qrot, prune, (int)probe[p + 1], vn, 32, 1);
             }
             __syncthreads();
+        }
+        if (ahead && nb == 0) {  // an empty cluster: nothing to overlap with
+            ScanSmem vn = cluster_view(sm, buf ^ 1);
+            prepare_cluster(ix, qrot, prune, (int)probe[p + 1], vn);
         }
     }
 }
@@ -1846,7 +1907,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
     extern __shared__ __align__(16) char smem_raw[];
     const int qi = blockIdx.x;
     if (deferred && deferred[qi]) return;  // answered by the split pass
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, topk, xstride);
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, topk, xstride, true);
     __shared__ int pool_size;
     __shared__ float distk;
     ScanTally tl;
@@ -2207,8 +2268,10 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                     SAQG_CUDA_TRY(cudaEventRecord(I.fork_event(), st));
                     SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, I.fork_event(), 0));
                 }
-                SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk,
+                const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs, true);
+                SAQG_REQUIRE(smem_k <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
+                SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_k));
+                k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk,
                                                                   ids_out, d_out, flags + 1, cnt, xs, deferred);
                 check_launch("k_scan");
             }
@@ -2454,8 +2517,10 @@ void run_search_static(const Index &I, const float *q, int64_t nq, int64_t topk,
     for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
     k_qprep<<<dim3((unsigned)ix.S, (unsigned)nq), 256, qsm, st>>>(ix, q, m, qrot, prune);
     check_launch("k_qprep");
-    SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ids, dists,
+    const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xstride_of(ix), true);
+    SAQG_REQUIRE(smem_k <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
+    SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_k));
+    k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ids, dists,
                                                       flags + 1, nullptr, xstride_of(ix), nullptr);
     check_launch("k_scan");
     count_launch(4);
