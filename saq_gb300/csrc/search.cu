@@ -974,6 +974,22 @@ __device__ __forceinline__ bool stages_pass(const float *st, int n, float tau) {
 __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0, int64_t v0, int nb, int n, int t0,
                                 int t_end, float tau) {
     const int S = ix.S, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    // pull the code lines and |o| of the blocks this warp takes in the next tile
+    // of the cluster into L2 while this tile computes
+#pragma unroll
+    for (int k = 0; k < kBlocksPerWarp; ++k) {
+        const int b = t0 + kTileB + w + k * kScanWarps;
+        if (b < nb)
+            for (int s = 0; s < S; ++s) {
+                const SegDev &g = ix.seg[s];
+                const int nc = g.dim / 64;
+                if (g.bits && lane < 2 * nc)
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const char *>(
+                                                                     g.codes + (size_t)(b0 + b) * nc * 32) +
+                                                                 lane * 128));
+                if (lane == 31) asm volatile("prefetch.global.L2 [%0];" ::"l"(g.onorm + (b0 + b) * 32));
+            }
+    }
 #pragma unroll
     for (int k = 0; k < kBlocksPerWarp; ++k) {
         const int slot = w + k * kScanWarps, b = t0 + slot;
@@ -1515,7 +1531,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_scan_warp(DevIndexView ix
 // anything (none of their lanes is below tau1 >= distk), so the replay is exact.
 constexpr int kTileBlocks = 16;
 constexpr int kFirstBlocks = 16;
-constexpr int kDeferBlocks = 2048;  // a query scanning more blocks than this takes the split pass
+constexpr int kDeferBlocks = 1024;  // a query scanning more blocks than this takes the split pass
                                      // (SAQG_DEFER_BLOCKS overrides it; 0 disables deferral)
 
 struct SplitState {
