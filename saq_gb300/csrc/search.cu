@@ -613,17 +613,19 @@ __device__ __forceinline__ float fast_est(const SegDev &g, const uint16_t *__res
 #pragma unroll 4
     for (int c8 = 0; c8 < nc; ++c8) {
         const uint2 w = cp[(size_t)c8 * 32];
-        const uint16_t *L = lut + c8 * 256;
+        const char *L = reinterpret_cast<const char *>(lut + c8 * 256);
+        // byte k of these holds 2 x (high / low nibble of code byte k): the byte
+        // offset of the entry within its 16-entry u16 table
+        const uint32_t hx = (w.x >> 3) & 0x1E1E1E1Eu, lx = (w.x << 1) & 0x1E1E1E1Eu;
+        const uint32_t hy = (w.y >> 3) & 0x1E1E1E1Eu, ly = (w.y << 1) & 0x1E1E1E1Eu;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t b = (w.x >> (8 * j)) & 255u;
-            sum += L[(2 * j) * 16 + (b >> 4)] + L[(2 * j + 1) * 16 + (b & 15u)];
-        }
+        for (int j = 0; j < 4; ++j)
+            sum += *reinterpret_cast<const uint16_t *>(L + (2 * j) * 32 + __byte_perm(hx, 0u, 0x4440u | j)) +
+                   *reinterpret_cast<const uint16_t *>(L + (2 * j + 1) * 32 + __byte_perm(lx, 0u, 0x4440u | j));
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t b = (w.y >> (8 * j)) & 255u;
-            sum += L[(8 + 2 * j) * 16 + (b >> 4)] + L[(8 + 2 * j + 1) * 16 + (b & 15u)];
-        }
+        for (int j = 0; j < 4; ++j)
+            sum += *reinterpret_cast<const uint16_t *>(L + (8 + 2 * j) * 32 + __byte_perm(hy, 0u, 0x4440u | j)) +
+                   *reinterpret_cast<const uint16_t *>(L + (8 + 2 * j + 1) * 32 + __byte_perm(ly, 0u, 0x4440u | j));
     }
     float t = __fmul_rn((float)sum, sc.delta);
     t = __fadd_rn(t, sc.sum_vl);
