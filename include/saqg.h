@@ -37,6 +37,9 @@ extern "C" {
 #define SAQG_MEM_HOST 0
 #define SAQG_MEM_DEVICE 1
 
+#define SAQG_FORMAT_REFERENCE 0 /* the reference's .index format (IVF::save) */
+#define SAQG_FORMAT_V2 1        /* versioned, checksummed, tile-aligned device layout */
+
 #define SAQG_DIST_L2 1 /* DistType::L2Sqr (defines.hpp); the only type the search supports */
 
 /* QuantizeConfig + QuantSingleConfig (quantization/config.h:12-74), field for field. */
@@ -78,6 +81,19 @@ int64_t saqg_kernel_launches(void);
 int saqg_index_load(const char *path, saqg_index **out);
 /* IVF::save (index/ivf.hpp:197-228): writes the reference's binary format. */
 int saqg_index_save(const saqg_index *index, const char *path);
+
+/* No counterpart in the reference: writes the index in format v2 (a
+ * versioned header, the device layout as-is with every array at a 4096-byte
+ * aligned offset, a 64-bit checksum per array and for the header).
+ * saqg_index_load reads either format (detected by the magic "SAQGIDX2"). */
+int saqg_index_save_v2(const saqg_index *index, const char *path);
+
+/* Converts an index file between the reference format and v2 on the host,
+ * without a GPU (the source format is detected; `format` is
+ * SAQG_FORMAT_REFERENCE or SAQG_FORMAT_V2).  A reference -> v2 -> reference
+ * round trip reproduces the file byte for byte.  Corrupt v2 files fail with
+ * SAQG_ERR_IO (checksum mismatch). */
+int saqg_index_convert(const char *src_path, const char *dst_path, int format);
 int saqg_index_free(saqg_index *index);
 int saqg_index_get_info(const saqg_index *index, saqg_index_info *out);
 

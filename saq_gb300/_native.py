@@ -14,6 +14,8 @@ from .build import LIB
 SAQG_MEM_HOST = 0
 SAQG_MEM_DEVICE = 1
 SAQG_STATIC_SCRATCH_BYTES = 16 << 20
+SAQG_FORMAT_REFERENCE = 0
+SAQG_FORMAT_V2 = 1
 SAQG_DIST_L2 = 1
 
 I64 = C.c_int64
@@ -57,6 +59,8 @@ EXPORTS = {
     "saqg_kernel_launches": (I64, []),
     "saqg_index_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
     "saqg_index_save": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "saqg_index_save_v2": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "saqg_index_convert": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int]),
     "saqg_index_free": (C.c_int, [C.c_void_p]),
     "saqg_index_get_info": (C.c_int, [C.c_void_p, C.POINTER(IndexInfo)]),
     "saqg_index_construct": (C.c_int, [C.c_void_p, I64, I64, C.c_void_p, I64, C.c_void_p, C.POINTER(QuantizeConfig),

@@ -65,6 +65,21 @@ int saqg_index_save(const saqg_index *index, const char *path) {
     });
 }
 
+int saqg_index_save_v2(const saqg_index *index, const char *path) {
+    return guarded([&] {
+        SAQG_REQUIRE(index && path, "null argument");
+        save_index_v2(*index->impl, path);
+    });
+}
+
+int saqg_index_convert(const char *src_path, const char *dst_path, int format) {
+    return guarded([&] {
+        SAQG_REQUIRE(src_path && dst_path, "null argument");
+        SAQG_REQUIRE(format == SAQG_FORMAT_REFERENCE || format == SAQG_FORMAT_V2, "unknown index format");
+        convert_index_file(src_path, dst_path, format);
+    });
+}
+
 int saqg_index_free(saqg_index *index) {
     return guarded([&] {
         if (!index) return;

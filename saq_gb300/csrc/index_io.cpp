@@ -46,16 +46,16 @@ struct SegSizes {
     int64_t block_bytes = 0, long_stride = 0;
 };
 
-SegSizes seg_sizes(const Index &idx) {
+SegSizes seg_sizes(const std::vector<Index::SegHost> &segs, bool compact) {
     SegSizes z;
-    const size_t S = idx.segs.size();
+    const size_t S = segs.size();
     z.sc.resize(S);
     z.pv.resize(S);
     z.loff.resize(S);
     z.scoff.resize(S);
     for (size_t s = 0; s < S; ++s) {
-        z.sc[s] = idx.segs[s].bits ? idx.segs[s].dim * kBlock / 8 : 0;
-        z.pv[s] = idx.segs[s].bits ? idx.segs[s].dim * (idx.segs[s].bits - 1) / 8 : 0;
+        z.sc[s] = segs[s].bits ? segs[s].dim * kBlock / 8 : 0;
+        z.pv[s] = segs[s].bits ? segs[s].dim * (segs[s].bits - 1) / 8 : 0;
     }
     if (S == 1) {
         z.block_bytes = 64 * 4 + z.sc[0];
@@ -65,13 +65,28 @@ SegSizes seg_sizes(const Index &idx) {
             z.scoff[s] = z.block_bytes;
             z.block_bytes += z.sc[s];
             z.loff[s] = z.long_stride;
-            z.long_stride += idx.compact ? z.pv[s] : (z.pv[s] + 15) / 16 * 16;
+            z.long_stride += compact ? z.pv[s] : (z.pv[s] + 15) / 16 * 16;
         }
     }
     return z;
 }
 
 int64_t lstride_of(int64_t pv) { return (pv + 15) / 16 * 16; }
+
+// An index in host memory, arrays already in the device layout of
+// saqg_internal.h (what load uploads and save downloads).
+struct HostIndex {
+    int64_t N = 0, D = 0, K = 0;
+    uint8_t qcfg_raw[32] = {0};
+    std::vector<float> var;
+    std::vector<Index::SegHost> segs;
+    bool compact = false;
+    std::vector<int64_t> sizes;
+    std::vector<float> cent;
+    std::vector<uint32_t> ids;
+    std::vector<std::vector<uint8_t>> codes, lcode;
+    std::vector<std::vector<float>> onorm, ipc, rcent, exfac;
+};
 }  // namespace
 
 Index::~Index() {
@@ -184,19 +199,19 @@ void finalize_view(Index &idx) {
     v.Dtot = off;
 }
 
-Index *load_index_file(const std::string &path) {
+HostIndex parse_reference(const std::string &path) {
     FILE *f = std::fopen(path.c_str(), "rb");
     if (!f) throw Error{SAQG_ERR_IO, "cannot open index file " + path};
     std::unique_ptr<FILE, int (*)(FILE *)> guard(f, std::fclose);
     Reader r{f, path};
-    auto idx = std::make_unique<Index>();
-    cudaGetDevice(&idx->device);
+    auto idx = std::make_unique<HostIndex>();
     idx->N = (int64_t)r.u64();
     idx->D = (int64_t)r.u64();
     idx->K = (int64_t)r.u64();
     if (idx->D <= 0 || idx->K <= 0 || idx->N < 0 || idx->D > (1 << 20) || idx->K > (1 << 28))
         throw Error{SAQG_ERR_IO, "implausible header in " + path};
-    std::vector<float> cent(idx->K * idx->D);
+    std::vector<float> &cent = idx->cent;
+    cent.resize(idx->K * idx->D);
     r.read(cent.data(), 4 * cent.size());
     r.read(idx->qcfg_raw, 32);
     int64_t num_dim = (int64_t)r.u64();
@@ -230,22 +245,26 @@ Index *load_index_file(const std::string &path) {
     idx->compact = nseg == 1 || idx->qcfg_raw[9] != 0;
     idx->sizes.resize(idx->K);
     r.read(idx->sizes.data(), 8 * idx->K);
-    idx->blk_off.assign(idx->K + 1, 0);
-    idx->vec_off.assign(idx->K + 1, 0);
+    std::vector<int64_t> blk_off(idx->K + 1, 0), vec_off(idx->K + 1, 0);
     for (int64_t c = 0; c < idx->K; ++c) {
-        idx->blk_off[c + 1] = idx->blk_off[c] + (idx->sizes[c] + kBlock - 1) / kBlock;
-        idx->vec_off[c + 1] = idx->vec_off[c] + idx->sizes[c];
+        if (idx->sizes[c] < 0) throw Error{SAQG_ERR_IO, "negative cluster size in " + path};
+        blk_off[c + 1] = blk_off[c] + (idx->sizes[c] + kBlock - 1) / kBlock;
+        vec_off[c + 1] = vec_off[c] + idx->sizes[c];
     }
-    if (idx->vec_off[idx->K] != idx->N) throw Error{SAQG_ERR_IO, "cluster sizes do not sum to N in " + path};
-    const int64_t NB = idx->blk_off[idx->K], N = idx->N;
-    idx->total_blocks = NB;
-    const SegSizes z = seg_sizes(*idx);
+    if (vec_off[idx->K] != idx->N) throw Error{SAQG_ERR_IO, "cluster sizes do not sum to N in " + path};
+    const int64_t NB = blk_off[idx->K], N = idx->N;
+    const SegSizes z = seg_sizes(idx->segs, idx->compact);
     const size_t S = idx->segs.size();
 
     // host staging of the device layout
-    std::vector<std::vector<uint8_t>> codes(S), lcode(S);
-    std::vector<std::vector<float>> onorm(S), ipc(S), rcent(S);
-    std::vector<std::vector<float>> exfac(S);
+    auto &codes = idx->codes, &lcode = idx->lcode;
+    auto &onorm = idx->onorm, &ipc = idx->ipc, &rcent = idx->rcent, &exfac = idx->exfac;
+    codes.resize(S);
+    lcode.resize(S);
+    onorm.resize(S);
+    ipc.resize(S);
+    rcent.resize(S);
+    exfac.resize(S);
     for (size_t s = 0; s < S; ++s) {
         const int64_t dim = idx->segs[s].dim;
         codes[s].assign(idx->segs[s].bits ? NB * kBlock * dim / 8 : 0, 0);
@@ -255,11 +274,12 @@ Index *load_index_file(const std::string &path) {
         exfac[s].assign(2 * N, 0.0f);
         rcent[s].assign(idx->K * dim, 0.0f);
     }
-    std::vector<uint32_t> ids(N);
+    std::vector<uint32_t> &ids = idx->ids;
+    ids.resize(N);
     std::vector<float> sfac, blk, lfac;
     std::vector<uint8_t> scode, lc;
     for (int64_t c = 0; c < idx->K; ++c) {
-        const int64_t n = idx->sizes[c], nb = (n + kBlock - 1) / kBlock, b0 = idx->blk_off[c], v0 = idx->vec_off[c];
+        const int64_t n = idx->sizes[c], nb = (n + kBlock - 1) / kBlock, b0 = blk_off[c], v0 = vec_off[c];
         if (S > 1) {
             sfac.resize(64 * S * nb);
             r.read(sfac.data(), 4 * sfac.size());
@@ -317,8 +337,37 @@ Index *load_index_file(const std::string &path) {
     }
     uint8_t extra;
     if (std::fread(&extra, 1, 1, f) == 1) throw Error{SAQG_ERR_IO, "trailing bytes in index file " + path};
+    return std::move(*idx);
+}
 
-    // upload
+// Device arrays from a host index (consumed).
+Index *upload_index(HostIndex &&h) {
+    auto idx = std::make_unique<Index>();
+    cudaGetDevice(&idx->device);
+    idx->N = h.N;
+    idx->D = h.D;
+    idx->K = h.K;
+    std::memcpy(idx->qcfg_raw, h.qcfg_raw, 32);
+    idx->var = std::move(h.var);
+    idx->segs = std::move(h.segs);
+    idx->compact = h.compact;
+    idx->sizes = std::move(h.sizes);
+    idx->blk_off.assign(idx->K + 1, 0);
+    idx->vec_off.assign(idx->K + 1, 0);
+    for (int64_t c = 0; c < idx->K; ++c) {
+        idx->blk_off[c + 1] = idx->blk_off[c] + (idx->sizes[c] + kBlock - 1) / kBlock;
+        idx->vec_off[c + 1] = idx->vec_off[c] + idx->sizes[c];
+    }
+    idx->total_blocks = idx->blk_off[idx->K];
+    const int64_t N = idx->N;
+    const SegSizes z = seg_sizes(idx->segs, idx->compact);
+    const size_t S = idx->segs.size();
+    int64_t dsum = 0;
+    for (auto &sg : idx->segs) dsum += sg.dim;
+    auto &cent = h.cent;
+    auto &ids = h.ids;
+    auto &codes = h.codes, &lcode = h.lcode;
+    auto &onorm = h.onorm, &ipc = h.ipc, &rcent = h.rcent, &exfac = h.exfac;
     Index &I = *idx;
     DevIndexView &v = I.view;
     float *dcent = (float *)I.dalloc(4 * cent.size());
@@ -365,20 +414,36 @@ Index *load_index_file(const std::string &path) {
     return idx.release();
 }
 
-// Device layout -> reference file (IVF::save, ivf.hpp:197-228).
-void save_index_file(const Index &I, const std::string &path) {
+// Host copy of a device index.
+HostIndex download_index(const Index &I) {
+    HostIndex h;
+    h.N = I.N;
+    h.D = I.D;
+    h.K = I.K;
+    std::memcpy(h.qcfg_raw, I.qcfg_raw, 32);
+    h.var = I.var;
+    h.segs = I.segs;
+    h.compact = I.compact;
+    h.sizes = I.sizes;
     const size_t S = I.segs.size();
     const int64_t N = I.N, NB = I.total_blocks;
-    const SegSizes z = seg_sizes(I);
     auto down = [](void *dst, const void *src, size_t bytes) {
         if (bytes) SAQG_CUDA_TRY(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
     };
-    std::vector<float> cent(I.K * I.D);
+    auto &cent = h.cent;
+    cent.resize(I.K * I.D);
     down(cent.data(), I.view.centroids, 4 * cent.size());
-    std::vector<uint32_t> ids(N);
+    auto &ids = h.ids;
+    ids.resize(N);
     down(ids.data(), I.view.ids, 4 * N);
-    std::vector<std::vector<uint8_t>> codes(S), lcode(S);
-    std::vector<std::vector<float>> onorm(S), ipc(S), rcent(S), exfac(S);
+    auto &codes = h.codes, &lcode = h.lcode;
+    auto &onorm = h.onorm, &ipc = h.ipc, &rcent = h.rcent, &exfac = h.exfac;
+    codes.resize(S);
+    lcode.resize(S);
+    onorm.resize(S);
+    ipc.resize(S);
+    rcent.resize(S);
+    exfac.resize(S);
     for (size_t s = 0; s < S; ++s) {
         const SegDev &g = I.view.seg[s];
         codes[s].resize(g.bits ? NB * kBlock * g.dim / 8 : 0);
@@ -394,6 +459,23 @@ void save_index_file(const Index &I, const std::string &path) {
         rcent[s].resize(I.K * g.dim);
         down(rcent[s].data(), g.cent, 4 * rcent[s].size());
     }
+    return h;
+}
+
+// Reference file (IVF::save, ivf.hpp:197-228) from a host index.
+void write_reference(const HostIndex &h, const std::string &path) {
+    const size_t S = h.segs.size();
+    const SegSizes z = seg_sizes(h.segs, h.compact);
+    const int64_t N = h.N;
+    std::vector<int64_t> blk_off(h.K + 1, 0), vec_off(h.K + 1, 0);
+    for (int64_t c = 0; c < h.K; ++c) {
+        blk_off[c + 1] = blk_off[c] + (h.sizes[c] + kBlock - 1) / kBlock;
+        vec_off[c + 1] = vec_off[c] + h.sizes[c];
+    }
+    const auto &cent = h.cent;
+    const auto &ids = h.ids;
+    const auto &codes = h.codes, &lcode = h.lcode;
+    const auto &onorm = h.onorm, &ipc = h.ipc, &rcent = h.rcent, &exfac = h.exfac;
     FILE *f = std::fopen(path.c_str(), "wb");
     if (!f) throw Error{SAQG_ERR_IO, "cannot write " + path};
     std::unique_ptr<FILE, int (*)(FILE *)> guard(f, std::fclose);
@@ -402,15 +484,15 @@ void save_index_file(const Index &I, const std::string &path) {
     };
     auto w64 = [&](uint64_t v) { w(&v, 8); };
     w64(N);
-    w64(I.D);
-    w64(I.K);
+    w64(h.D);
+    w64(h.K);
     w(cent.data(), 4 * cent.size());
-    w(I.qcfg_raw, 32);
-    w64(I.D);
-    w64(I.var.size());
-    w(I.var.data(), 4 * I.var.size());
+    w(h.qcfg_raw, 32);
+    w64(h.D);
+    w64(h.var.size());
+    w(h.var.data(), 4 * h.var.size());
     w64(S);
-    for (auto &sg : I.segs) {
+    for (auto &sg : h.segs) {
         w64(sg.dim);
         w64(sg.bits);
         w(sg.cfg_raw, 20);
@@ -418,22 +500,22 @@ void save_index_file(const Index &I, const std::string &path) {
         w(&flag, 1);
         if (sg.rotated) w(sg.P.data(), 4 * sg.P.size());
     }
-    w(I.sizes.data(), 8 * I.K);
+    w(h.sizes.data(), 8 * h.K);
     std::vector<float> sfac;
     std::vector<uint8_t> scode, lc;
     std::vector<float> lfac;
-    for (int64_t c = 0; c < I.K; ++c) {
-        const int64_t n = I.sizes[c], nb = (n + kBlock - 1) / kBlock, b0 = I.blk_off[c], v0 = I.vec_off[c];
+    for (int64_t c = 0; c < h.K; ++c) {
+        const int64_t n = h.sizes[c], nb = (n + kBlock - 1) / kBlock, b0 = blk_off[c], v0 = vec_off[c];
         sfac.assign(S > 1 ? 64 * S * nb : 0, 0.0f);
         scode.assign(z.block_bytes * nb, 0);
         for (size_t s = 0; s < S; ++s) {
-            const int64_t dim = I.segs[s].dim, cols = dim / 8;
+            const int64_t dim = h.segs[s].dim, cols = dim / 8;
             for (int64_t b = 0; b < nb; ++b) {
                 float *fac = S == 1 ? reinterpret_cast<float *>(scode.data() + b * z.block_bytes)
                                     : sfac.data() + (b * S + s) * 64;
                 std::memcpy(fac, &onorm[s][(b0 + b) * kBlock], 4 * kBlock);
                 std::memcpy(fac + kBlock, &ipc[s][(b0 + b) * kBlock], 4 * kBlock);
-                if (!I.segs[s].bits) continue;
+                if (!h.segs[s].bits) continue;
                 uint8_t *blkp = scode.data() + b * z.block_bytes + (S == 1 ? 256 : z.scoff[s]);
                 const uint8_t *src = codes[s].data() + (b0 + b) * kBlock * cols;
                 for (int64_t i = 0; i < cols; ++i)
@@ -449,11 +531,11 @@ void save_index_file(const Index &I, const std::string &path) {
         lfac.assign(2 * S * n, 0.0f);
         for (size_t s = 0; s < S; ++s) {
             int64_t seg_base = 0;
-            if (S > 1 && I.compact)
+            if (S > 1 && h.compact)
                 for (size_t t = 0; t < s; ++t) seg_base += (z.pv[t] * n + 15) / 16 * 16;
             const int64_t ls = lstride_of(z.pv[s]);
             for (int64_t v = 0; v < n; ++v) {
-                int64_t off = S == 1 ? v * z.pv[0] : I.compact ? seg_base + v * z.pv[s] : v * z.long_stride + z.loff[s];
+                int64_t off = S == 1 ? v * z.pv[0] : h.compact ? seg_base + v * z.pv[s] : v * z.long_stride + z.loff[s];
                 if (z.pv[s] && off + z.pv[s] <= (int64_t)lc.size())
                     std::memcpy(lc.data() + off, &lcode[s][(v0 + v) * ls], z.pv[s]);
                 lfac[(v * S + s) * 2] = exfac[s][2 * (v0 + v)];
@@ -465,8 +547,304 @@ void save_index_file(const Index &I, const std::string &path) {
         w(lc.data(), lc.size());
         w(lfac.data(), 4 * lfac.size());
         w(ids.data() + v0, 4 * n);
-        for (size_t s = 0; s < S; ++s) w(rcent[s].data() + c * I.segs[s].dim, 4 * I.segs[s].dim);
+        for (size_t s = 0; s < S; ++s) w(rcent[s].data() + c * h.segs[s].dim, 4 * h.segs[s].dim);
     }
+}
+
+
+// ------------------------------------------------------------ format v2
+// A versioned, checksummed file holding the device layout as-is, each array
+// at a 4096-byte aligned offset, so loading is a read and a copy per array:
+//   header: magic "SAQGIDX2", u32 version (2), u32 header bytes, u64 N, D, K,
+//     #segments, compact flag, #variance values, QuantizeConfig (32 raw
+//     bytes); per segment: u64 dim, bits; QuantSingleConfig (20 raw bytes),
+//     u8 rotated, 3 zero bytes; u64 #sections; per section: u32 kind, u32
+//     segment, u64 offset, u64 bytes, u64 checksum; u64 checksum of the header
+//     up to here.
+//   sections: 1 centroids [K][D] f32, 2 variance f32, 3 cluster sizes [K] i64,
+//     4 ids [N] u32; per segment 10 P [dim][dim] f32 (rotated segments),
+//     11 1-bit codes [block][dim/64][32] x 8 bytes, 12 |o| [block][32] f32,
+//     13 ip_cent_oa [block][32] f32, 14 ex-codes [N][row padded to 16 bytes],
+//     15 ex factors [N] (rescale, error) f32, 16 rotated centroids [K][dim] f32.
+// Checksum: 64-bit FNV-1a over 8-byte little-endian words, the tail padded
+// with zero bytes.
+namespace {
+const char kMagicV2[8] = {'S', 'A', 'Q', 'G', 'I', 'D', 'X', '2'};
+constexpr uint32_t kVersionV2 = 2;
+constexpr uint64_t kAlignV2 = 4096;
+
+uint64_t checksum64(const void *data, size_t n) {
+    const uint8_t *p = static_cast<const uint8_t *>(data);
+    uint64_t h = 1469598103934665603ull;
+    size_t i = 0;
+    for (; i + 8 <= n; i += 8) {
+        uint64_t w;
+        std::memcpy(&w, p + i, 8);
+        h = (h ^ w) * 1099511628211ull;
+    }
+    if (i < n) {
+        uint64_t w = 0;
+        std::memcpy(&w, p + i, n - i);
+        h = (h ^ w) * 1099511628211ull;
+    }
+    return h;
+}
+
+struct SectionV2 {
+    uint32_t kind, seg;
+    uint64_t offset, bytes, sum;
+};
+
+struct ByteWriter {
+    std::vector<uint8_t> b;
+    void put(const void *p, size_t n) {
+        const uint8_t *c = static_cast<const uint8_t *>(p);
+        b.insert(b.end(), c, c + n);
+    }
+    void u32(uint32_t v) { put(&v, 4); }
+    void u64(uint64_t v) { put(&v, 8); }
+};
+
+struct ByteReader {
+    const uint8_t *p;
+    size_t n, at = 0;
+    std::string path;
+    void get(void *dst, size_t k) {
+        if (at + k > n) throw Error{SAQG_ERR_IO, "truncated header in " + path};
+        std::memcpy(dst, p + at, k);
+        at += k;
+    }
+    uint32_t u32() {
+        uint32_t v;
+        get(&v, 4);
+        return v;
+    }
+    uint64_t u64() {
+        uint64_t v;
+        get(&v, 8);
+        return v;
+    }
+};
+}  // namespace
+
+bool is_v2_file(const std::string &path) {
+    FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f) throw Error{SAQG_ERR_IO, "cannot open index file " + path};
+    char m[8] = {0};
+    const size_t got = std::fread(m, 1, 8, f);
+    std::fclose(f);
+    return got == 8 && std::memcmp(m, kMagicV2, 8) == 0;
+}
+
+void write_v2(const HostIndex &h, const std::string &path) {
+    struct Piece {
+        uint32_t kind, seg;
+        const void *data;
+        uint64_t bytes;
+    };
+    std::vector<Piece> pieces;
+    pieces.push_back({1, 0, h.cent.data(), 4 * (uint64_t)h.cent.size()});
+    pieces.push_back({2, 0, h.var.data(), 4 * (uint64_t)h.var.size()});
+    pieces.push_back({3, 0, h.sizes.data(), 8 * (uint64_t)h.sizes.size()});
+    pieces.push_back({4, 0, h.ids.data(), 4 * (uint64_t)h.ids.size()});
+    for (uint32_t s = 0; s < h.segs.size(); ++s) {
+        if (h.segs[s].rotated) pieces.push_back({10, s, h.segs[s].P.data(), 4 * (uint64_t)h.segs[s].P.size()});
+        pieces.push_back({11, s, h.codes[s].data(), (uint64_t)h.codes[s].size()});
+        pieces.push_back({12, s, h.onorm[s].data(), 4 * (uint64_t)h.onorm[s].size()});
+        pieces.push_back({13, s, h.ipc[s].data(), 4 * (uint64_t)h.ipc[s].size()});
+        pieces.push_back({14, s, h.lcode[s].data(), (uint64_t)h.lcode[s].size()});
+        pieces.push_back({15, s, h.exfac[s].data(), 4 * (uint64_t)h.exfac[s].size()});
+        pieces.push_back({16, s, h.rcent[s].data(), 4 * (uint64_t)h.rcent[s].size()});
+    }
+    // header size is known before the offsets: fixed part + segments + section table + checksum
+    const uint64_t hdr_bytes = 8 + 4 + 4 + 6 * 8 + 32 + h.segs.size() * (16 + 20 + 4) + 8 + pieces.size() * 32 + 8;
+    uint64_t off = (hdr_bytes + kAlignV2 - 1) / kAlignV2 * kAlignV2;
+    std::vector<SectionV2> secs;
+    for (auto &pc : pieces) {
+        secs.push_back({pc.kind, pc.seg, off, pc.bytes, checksum64(pc.data, pc.bytes)});
+        off += (pc.bytes + kAlignV2 - 1) / kAlignV2 * kAlignV2;
+    }
+    ByteWriter w;
+    w.put(kMagicV2, 8);
+    w.u32(kVersionV2);
+    w.u32((uint32_t)hdr_bytes);
+    w.u64(h.N);
+    w.u64(h.D);
+    w.u64(h.K);
+    w.u64(h.segs.size());
+    w.u64(h.compact ? 1 : 0);
+    w.u64(h.var.size());
+    w.put(h.qcfg_raw, 32);
+    for (auto &sg : h.segs) {
+        w.u64(sg.dim);
+        w.u64(sg.bits);
+        w.put(sg.cfg_raw, 20);
+        const uint8_t tail[4] = {(uint8_t)(sg.rotated ? 1 : 0), 0, 0, 0};
+        w.put(tail, 4);
+    }
+    w.u64(secs.size());
+    for (auto &sc : secs) {
+        w.u32(sc.kind);
+        w.u32(sc.seg);
+        w.u64(sc.offset);
+        w.u64(sc.bytes);
+        w.u64(sc.sum);
+    }
+    w.u64(checksum64(w.b.data(), w.b.size()));
+    if (w.b.size() != hdr_bytes) throw Error{SAQG_ERR_INTERNAL, "v2 header size mismatch"};
+    FILE *f = std::fopen(path.c_str(), "wb");
+    if (!f) throw Error{SAQG_ERR_IO, "cannot write " + path};
+    std::unique_ptr<FILE, int (*)(FILE *)> guard(f, std::fclose);
+    auto put = [&](const void *p, size_t n) {
+        if (n && std::fwrite(p, 1, n, f) != n) throw Error{SAQG_ERR_IO, "write failed: " + path};
+    };
+    put(w.b.data(), w.b.size());
+    uint64_t at = w.b.size();
+    static const std::vector<uint8_t> zeros(kAlignV2, 0);
+    for (size_t i = 0; i < pieces.size(); ++i) {
+        if (secs[i].offset > at) put(zeros.data(), secs[i].offset - at);
+        put(pieces[i].data, pieces[i].bytes);
+        at = secs[i].offset + pieces[i].bytes;
+    }
+    const uint64_t end = (at + kAlignV2 - 1) / kAlignV2 * kAlignV2;
+    if (end > at) put(zeros.data(), end - at);
+}
+
+HostIndex parse_v2(const std::string &path) {
+    FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f) throw Error{SAQG_ERR_IO, "cannot open index file " + path};
+    std::unique_ptr<FILE, int (*)(FILE *)> guard(f, std::fclose);
+    uint8_t fixed[16];
+    if (std::fread(fixed, 1, 16, f) != 16 || std::memcmp(fixed, kMagicV2, 8) != 0)
+        throw Error{SAQG_ERR_IO, "not a v2 index file: " + path};
+    uint32_t version, hdr_bytes;
+    std::memcpy(&version, fixed + 8, 4);
+    std::memcpy(&hdr_bytes, fixed + 12, 4);
+    if (version != kVersionV2) throw Error{SAQG_ERR_IO, "unsupported v2 index version in " + path};
+    if (hdr_bytes < 16 + 8 || hdr_bytes > (1u << 24)) throw Error{SAQG_ERR_IO, "implausible v2 header in " + path};
+    std::vector<uint8_t> hdr(hdr_bytes);
+    std::memcpy(hdr.data(), fixed, 16);
+    if (std::fread(hdr.data() + 16, 1, hdr_bytes - 16, f) != hdr_bytes - 16)
+        throw Error{SAQG_ERR_IO, "truncated v2 header in " + path};
+    uint64_t want;
+    std::memcpy(&want, hdr.data() + hdr_bytes - 8, 8);
+    if (checksum64(hdr.data(), hdr_bytes - 8) != want) throw Error{SAQG_ERR_IO, "v2 header checksum mismatch in " + path};
+    ByteReader r{hdr.data(), hdr_bytes - 8, 16, path};
+    HostIndex h;
+    h.N = (int64_t)r.u64();
+    h.D = (int64_t)r.u64();
+    h.K = (int64_t)r.u64();
+    const uint64_t S = r.u64();
+    h.compact = r.u64() != 0;
+    const uint64_t nvar = r.u64();
+    r.get(h.qcfg_raw, 32);
+    if (h.D <= 0 || h.K <= 0 || h.N < 0 || h.D > (1 << 20) || h.K > (1 << 28) || S < 1 || S > (uint64_t)kMaxSeg ||
+        nvar != (uint64_t)h.D)
+        throw Error{SAQG_ERR_IO, "implausible v2 header in " + path};
+    for (uint64_t s = 0; s < S; ++s) {
+        Index::SegHost sg;
+        sg.dim = (int64_t)r.u64();
+        sg.bits = (int64_t)r.u64();
+        r.get(sg.cfg_raw, 20);
+        uint8_t tail[4];
+        r.get(tail, 4);
+        sg.rotated = tail[0] != 0;
+        if (sg.dim <= 0 || sg.dim % 64 || sg.bits > kMaxBits || sg.dim > 16384)
+            throw Error{SAQG_ERR_IO, "unsupported segment in " + path};
+        h.segs.push_back(std::move(sg));
+    }
+    const uint64_t nsec = r.u64();
+    if (nsec > 4 + 7 * S) throw Error{SAQG_ERR_IO, "implausible v2 section table in " + path};
+    std::vector<SectionV2> secs(nsec);
+    for (auto &sc : secs) {
+        sc.kind = r.u32();
+        sc.seg = r.u32();
+        sc.offset = r.u64();
+        sc.bytes = r.u64();
+        sc.sum = r.u64();
+        if (sc.seg >= S) throw Error{SAQG_ERR_IO, "bad v2 section in " + path};
+    }
+    // sizes first: they fix every other array's length
+    std::vector<int64_t> blk_off(h.K + 1, 0);
+    h.codes.resize(S);
+    h.lcode.resize(S);
+    h.onorm.resize(S);
+    h.ipc.resize(S);
+    h.rcent.resize(S);
+    h.exfac.resize(S);
+    auto load = [&](const SectionV2 &sc, void *dst, uint64_t expect) {
+        if (sc.bytes != expect) throw Error{SAQG_ERR_IO, "v2 section size mismatch in " + path};
+        if (!expect) return;
+        if (std::fseek(f, (long)sc.offset, SEEK_SET) != 0 || std::fread(dst, 1, expect, f) != expect)
+            throw Error{SAQG_ERR_IO, "truncated v2 section in " + path};
+        if (checksum64(dst, expect) != sc.sum) throw Error{SAQG_ERR_IO, "v2 section checksum mismatch in " + path};
+    };
+    auto find = [&](uint32_t kind, uint32_t seg) -> const SectionV2 * {
+        for (auto &sc : secs)
+            if (sc.kind == kind && sc.seg == seg) return &sc;
+        return nullptr;
+    };
+    auto need = [&](uint32_t kind, uint32_t seg) -> const SectionV2 & {
+        const SectionV2 *sc = find(kind, seg);
+        if (!sc) throw Error{SAQG_ERR_IO, "missing v2 section in " + path};
+        return *sc;
+    };
+    h.sizes.resize(h.K);
+    load(need(3, 0), h.sizes.data(), 8 * (uint64_t)h.K);
+    int64_t total = 0;
+    for (int64_t c = 0; c < h.K; ++c) {
+        if (h.sizes[c] < 0) throw Error{SAQG_ERR_IO, "negative cluster size in " + path};
+        blk_off[c + 1] = blk_off[c] + (h.sizes[c] + kBlock - 1) / kBlock;
+        total += h.sizes[c];
+    }
+    if (total != h.N) throw Error{SAQG_ERR_IO, "cluster sizes do not sum to N in " + path};
+    const int64_t NB = blk_off[h.K];
+    const SegSizes z = seg_sizes(h.segs, h.compact);
+    h.cent.resize(h.K * h.D);
+    load(need(1, 0), h.cent.data(), 4 * (uint64_t)h.cent.size());
+    h.var.resize(nvar);
+    load(need(2, 0), h.var.data(), 4 * nvar);
+    h.ids.resize(h.N);
+    load(need(4, 0), h.ids.data(), 4 * (uint64_t)h.N);
+    for (uint32_t s = 0; s < S; ++s) {
+        auto &sg = h.segs[s];
+        if (sg.rotated) {
+            sg.P.resize(sg.dim * sg.dim);
+            load(need(10, s), sg.P.data(), 4 * (uint64_t)sg.P.size());
+        } else if (find(10, s)) {
+            throw Error{SAQG_ERR_IO, "unexpected rotation in " + path};
+        }
+        h.codes[s].resize(sg.bits ? NB * kBlock * sg.dim / 8 : 0);
+        load(need(11, s), h.codes[s].data(), h.codes[s].size());
+        h.onorm[s].resize(NB * kBlock);
+        load(need(12, s), h.onorm[s].data(), 4 * (uint64_t)h.onorm[s].size());
+        h.ipc[s].resize(NB * kBlock);
+        load(need(13, s), h.ipc[s].data(), 4 * (uint64_t)h.ipc[s].size());
+        h.lcode[s].resize((size_t)h.N * lstride_of(z.pv[s]));
+        load(need(14, s), h.lcode[s].data(), h.lcode[s].size());
+        h.exfac[s].resize(2 * h.N);
+        load(need(15, s), h.exfac[s].data(), 4 * (uint64_t)h.exfac[s].size());
+        h.rcent[s].resize(h.K * sg.dim);
+        load(need(16, s), h.rcent[s].data(), 4 * (uint64_t)h.rcent[s].size());
+    }
+    int64_t dsum = 0;
+    for (auto &sg : h.segs) dsum += sg.dim;
+    if (dsum < h.D || h.D % 64 != 0) throw Error{SAQG_ERR_IO, "dimension must be a multiple of 64 in " + path};
+    return h;
+}
+
+Index *load_index_file(const std::string &path) {
+    return upload_index(is_v2_file(path) ? parse_v2(path) : parse_reference(path));
+}
+
+void save_index_file(const Index &I, const std::string &path) { write_reference(download_index(I), path); }
+
+void save_index_v2(const Index &I, const std::string &path) { write_v2(download_index(I), path); }
+
+void convert_index_file(const std::string &src, const std::string &dst, int format) {
+    HostIndex h = is_v2_file(src) ? parse_v2(src) : parse_reference(src);
+    if (format == SAQG_FORMAT_V2) write_v2(h, dst);
+    else write_reference(h, dst);
 }
 
 }  // namespace saqg

@@ -125,6 +125,10 @@ struct Index {
 Index *load_index_file(const std::string &path);
 void save_index_file(const Index &idx, const std::string &path);
 void finalize_view(Index &idx);
+void save_index_v2(const Index &idx, const std::string &path);
+// Host-only conversion between the reference format and v2 (either direction;
+// the source format is detected).
+void convert_index_file(const std::string &src, const std::string &dst, int format);
 
 // search.cu
 void run_search(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,

@@ -81,8 +81,14 @@ class IVF:
         ivf.num_data, ivf.num_dim, ivf.num_cen = info["num_data"], info["num_dim"], info["num_clusters"]
         return ivf
 
-    def save(self, path: str) -> None:
-        N.check(self.lib.saqg_index_save(self._h, path.encode()))
+    def save(self, path: str, format: str = "reference") -> None:
+        """IVF::save in the reference's format, or format="v2" (checksummed device layout)."""
+        if format == "v2":
+            N.check(self.lib.saqg_index_save_v2(self._h, path.encode()))
+        elif format == "reference":
+            N.check(self.lib.saqg_index_save(self._h, path.encode()))
+        else:
+            raise ValueError(f"unknown index format {format!r}")
 
     def set_variance(self, vars_) -> None:
         self._variance = np.ascontiguousarray(vars_, np.float32).reshape(-1)
@@ -158,6 +164,13 @@ class IVF:
                                        acc.ctypes.data, fast.ctypes.data, var.ctypes.data, cap, C.byref(cnt)))
         n = cnt.value
         return ids[:n], acc[:n], fast[:n], var[:n]
+
+
+def convert(src: str, dst: str, format: str = "v2") -> None:
+    """Host-only conversion of an index file to `format` ("v2" or "reference")."""
+    lib = N.load()
+    fmt = {"v2": N.SAQG_FORMAT_V2, "reference": N.SAQG_FORMAT_REFERENCE}[format]
+    N.check(lib.saqg_index_convert(src.encode(), dst.encode(), fmt))
 
 
 def plan(variance, avg_bits: float, enable_segmentation: bool = True, seg_eqseg: int = 0):

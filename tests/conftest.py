@@ -49,3 +49,16 @@ def golden_dir(tmp_path_factory):
 @pytest.fixture(params=INDEX_CASES)
 def golden_case(request, golden_dir):
     return GoldenCase(request.param, golden_dir)
+
+
+@pytest.fixture
+def golden_case_by_name(golden_dir):
+    """Path of a golden case's reference-format index file, by case name."""
+    def get(name):
+        path = os.path.join(golden_dir, name + ".index")
+        if not os.path.exists(path):
+            z = np.load(os.path.join(GOLDEN, name + ".npz"))
+            with open(path, "wb") as f:
+                f.write(z["index_bytes"].tobytes())
+        return path
+    return get
