@@ -169,6 +169,16 @@ int saqg_search_ex(const saqg_index *index, const float *queries, int64_t nq, in
 int saqg_search_static(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
                        const saqg_searcher_config *cfg, uint32_t *ids, float *dists, void *stream);
 
+/* IVF::search for a batch whose queries carry their own nprobe and topk
+ * (each query an independent call of the reference with its own arguments):
+ * `nprobe_per_query` / `topk_per_query` are host arrays of nq values (either
+ * may be NULL: then `nprobe` / `topk` for every query).  ids / dists rows are
+ * max(topk) long; query i's first topk_i entries are its result and the rest
+ * id 0 / FLT_MAX.  `stats` may be NULL; other arguments as saqg_search. */
+int saqg_search_batch(const saqg_index *index, const float *queries, int64_t nq, const int32_t *nprobe_per_query,
+                      const int32_t *topk_per_query, int64_t nprobe, int64_t topk, const saqg_searcher_config *cfg,
+                      uint32_t *ids, float *dists, int mem, void *stream, saqg_search_stats *stats);
+
 /* IVF::estimate<L2Sqr> (index/ivf.hpp:313-362) for one query: every vector of
  * the `nprobe` probed clusters, in probe order, with its accurate, fast and
  * variance-bound estimates.  Host outputs of capacity `cap`; *count receives

@@ -69,6 +69,9 @@ EXPORTS = {
                               C.c_void_p, C.c_int, C.c_void_p]),
     "saqg_search_ex": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig), C.c_void_p,
                                  C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "saqg_search_batch": (C.c_int, [C.c_void_p, C.c_void_p, I64, C.c_void_p, C.c_void_p, I64, I64,
+                                    C.POINTER(SearcherConfig), C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                    C.c_void_p]),
     "saqg_search_static": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig), C.c_void_p,
                                      C.c_void_p, C.c_void_p]),
     "saqg_estimate": (C.c_int, [C.c_void_p, C.c_void_p, I64, C.POINTER(SearcherConfig), C.c_void_p, C.c_void_p,

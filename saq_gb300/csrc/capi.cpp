@@ -142,6 +142,19 @@ int saqg_search_ex(const saqg_index *index, const float *queries, int64_t nq, in
     });
 }
 
+int saqg_search_batch(const saqg_index *index, const float *queries, int64_t nq, const int32_t *nprobe_per_query,
+                      const int32_t *topk_per_query, int64_t nprobe, int64_t topk, const saqg_searcher_config *cfg,
+                      uint32_t *ids, float *dists, int mem, void *stream, saqg_search_stats *stats) {
+    return guarded([&] {
+        SAQG_REQUIRE(index && queries && ids, "null argument");
+        SAQG_REQUIRE(mem == SAQG_MEM_HOST || mem == SAQG_MEM_DEVICE, "mem must be SAQG_MEM_HOST or SAQG_MEM_DEVICE");
+        SAQG_REQUIRE(!cfg || cfg->dist_type == SAQG_DIST_L2, "only L2 search is supported");
+        const float m = cfg ? cfg->searcher_vars_bound_m : 4.0f;
+        run_search(*index->impl, queries, nq, topk, nprobe, m, ids, dists, mem, (cudaStream_t)stream, stats, nullptr,
+                   nprobe_per_query, topk_per_query);
+    });
+}
+
 int saqg_search_static(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
                        const saqg_searcher_config *cfg, uint32_t *ids, float *dists, void *stream) {
     return guarded([&] {

@@ -133,7 +133,7 @@ void convert_index_file(const std::string &src, const std::string &dst, int form
 // search.cu
 void run_search(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,
                 float *dists, int mem, cudaStream_t st, saqg_search_stats *stats = nullptr,
-                uint32_t *probes_out = nullptr);
+                uint32_t *probes_out = nullptr, const int *np_host = nullptr, const int *k_host = nullptr);
 // saqg_search for device pointers with its scratch in a static device array.
 void run_search_static(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m,
                        uint32_t *ids, float *dists, cudaStream_t stream);

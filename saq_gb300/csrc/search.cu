@@ -63,6 +63,15 @@ __device__ __forceinline__ float key_to_float(uint32_t k) {
     return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
+// Per-query nprobe and k of a batch (null arrays: every query uses the
+// maxima).  Probe rows are np_max long and result rows k_max long.
+struct QueryShape {
+    const int *np = nullptr, *k = nullptr;
+    int np_max = 0, k_max = 0;
+    __device__ __forceinline__ int np_of(int qi) const { return np ? np[qi] : np_max; }
+    __device__ __forceinline__ int k_of(int qi) const { return k ? k[qi] : k_max; }
+};
+
 // ------------------------------------------------------------------ probe
 __global__ void k_probe_dist(DevIndexView ix, const float *__restrict__ q, float *__restrict__ dist) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -210,15 +219,17 @@ __device__ __forceinline__ void select_bin(const uint32_t *hist, uint32_t rem, i
 constexpr int kSelThreads = 1024;
 constexpr int kSelMax = 1024;  // fast path handles nprobe <= 1024
 
-__global__ void __launch_bounds__(kSelThreads) k_probe_select(const float *__restrict__ dist, int K, int nprobe,
+__global__ void __launch_bounds__(kSelThreads) k_probe_select(const float *__restrict__ dist, int K, int nprobe_max,
                                                               uint32_t *__restrict__ probe, Cand *__restrict__ work,
                                                               int *__restrict__ fallback_count,
-                                                              const uint8_t *__restrict__ only = nullptr) {
+                                                              const uint8_t *__restrict__ only = nullptr,
+                                                              const int *__restrict__ qnp = nullptr) {
     __shared__ uint32_t hist[256];
     __shared__ uint32_t s_prefix, s_mask, s_rem, s_eq, s_n;
     __shared__ unsigned long long sel[kSelMax];
     const int qi = blockIdx.x, tid = threadIdx.x;
     if (only && !only[qi]) return;  // ranked by the shortlist
+    const int nprobe = qnp ? qnp[qi] : nprobe_max;  // this query's nprobe; rows are nprobe_max long
     const float *dq = dist + (size_t)qi * K;
     if (tid == 0) {
         s_prefix = 0;
@@ -290,7 +301,7 @@ __global__ void __launch_bounds__(kSelThreads) k_probe_select(const float *__res
             if ((sel[i] >> 32) == (sel[i + 1] >> 32)) s_dup = 1;
         __syncthreads();
         if (!s_dup) {
-            for (int i = tid; i < nprobe; i += kSelThreads) probe[(size_t)qi * nprobe + i] = (uint32_t)(sel[i] & 0xffffffffu);
+            for (int i = tid; i < nprobe; i += kSelThreads) probe[(size_t)qi * nprobe_max + i] = (uint32_t)(sel[i] & 0xffffffffu);
             return;
         }
         need_exact = true;
@@ -302,7 +313,7 @@ __global__ void __launch_bounds__(kSelThreads) k_probe_select(const float *__res
             Cand *a = work + (size_t)qi * K;
             for (int i = 0; i < K; ++i) a[i] = Cand{(uint32_t)i, dq[i]};
             exact_partial_sort(a, nprobe, K);
-            for (int i = 0; i < nprobe; ++i) probe[(size_t)qi * nprobe + i] = a[i].id;
+            for (int i = 0; i < nprobe; ++i) probe[(size_t)qi * nprobe_max + i] = a[i].id;
         }
         return;
     }
@@ -339,7 +350,7 @@ __global__ void __launch_bounds__(kSelThreads) k_probe_select(const float *__res
             heap[last] = heap[0];
             heap_adjust(heap, 0, last, v);
         }
-        for (int i = 0; i < mid; ++i) probe[(size_t)qi * nprobe + i] = heap[i].id;
+        for (int i = 0; i < mid; ++i) probe[(size_t)qi * nprobe_max + i] = heap[i].id;
     }
 }
 
@@ -389,7 +400,8 @@ __device__ __forceinline__ void approx_bounds(float qn2, float qn, float ip, flo
 __global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView ix, const float *__restrict__ q,
                                                                    const float *__restrict__ ip,
                                                                    const float2 *__restrict__ cn2, ShortBound sb,
-                                                                   int nprobe, uint32_t *__restrict__ probe,
+                                                                   int nprobe_max, const int *__restrict__ qnp,
+                                                                   uint32_t *__restrict__ probe,
                                                                    uint8_t *__restrict__ full, int *__restrict__ fb_list,
                                                                    int *__restrict__ fb_count,
                                                                    unsigned long long *__restrict__ counters) {
@@ -405,6 +417,7 @@ __global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView 
     __shared__ float s_red[kShortThreads / 32];
     const int qi = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int K = ix.K, D = ix.D;
+    const int nprobe = qnp ? qnp[qi] : nprobe_max;
     const float *ipq = ip + (size_t)qi * K;
     float a = 0.0f;
     for (int i = tid; i < D; i += kShortThreads) {
@@ -524,7 +537,7 @@ __global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView 
         }
         return;
     }
-    for (int i = tid; i < nprobe; i += kShortThreads) probe[(size_t)qi * nprobe + i] = (uint32_t)(keys[i] & 0xffffffffu);
+    for (int i = tid; i < nprobe; i += kShortThreads) probe[(size_t)qi * nprobe_max + i] = (uint32_t)(keys[i] & 0xffffffffu);
     if (tid == 0) {
         full[qi] = 0;
         if (counters) atomicAdd(counters + 4, (unsigned long long)n);
@@ -1286,10 +1299,12 @@ __device__ void flush_tally(const ScanTally &tl, unsigned long long *counters) {
     }
 }
 
-__device__ void write_results(const ScanSmem &sm, int pool_size, int topk, uint32_t *out_ids, float *out_d) {
-    for (int i = threadIdx.x; i < topk; i += blockDim.x) {
-        out_ids[i] = sm.pool_id[i];
-        if (out_d) out_d[i] = i < pool_size ? sm.pool_d[i] : FLT_MAX;
+// The pool as the reference returns it (unfilled slots id 0), then, for a
+// row longer than this query's k, id 0 / FLT_MAX up to k_max.
+__device__ void write_results(const ScanSmem &sm, int pool_size, int topk, int k_max, uint32_t *out_ids, float *out_d) {
+    for (int i = threadIdx.x; i < k_max; i += blockDim.x) {
+        out_ids[i] = i < topk ? sm.pool_id[i] : 0u;
+        if (out_d) out_d[i] = i < pool_size && i < topk ? sm.pool_d[i] : FLT_MAX;
     }
 }
 
@@ -1556,6 +1571,7 @@ struct SplitState {
     float *rec;          // [pos_cap][rec_words]
     int64_t pos_cap;
     int rec_words;
+    QueryShape qsh;      // per-query nprobe and k (strides np_max, k_max)
 };
 
 __host__ __device__ inline int rec_words_of(int S) { return (8 + (S + 1) + 32 + 32 * S + 3) & ~3; }
@@ -1563,20 +1579,21 @@ __host__ __device__ inline int rec_words_of(int S) { return (8 + (S + 1) + 32 + 
 __device__ __forceinline__ int list_len(const SplitState &st) { return min(*st.nlist, st.cap); }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, const uint32_t *__restrict__ probe,
-                                                             int nprobe, const float *__restrict__ qrot_all,
-                                                             const float *__restrict__ prune_all, int topk,
-                                                             SplitState st, int *__restrict__ err,
+                                                             const float *__restrict__ qrot_all,
+                                                             const float *__restrict__ prune_all, SplitState st, int *__restrict__ err,
                                                              unsigned long long *__restrict__ counters, int xstride) {
     extern __shared__ __align__(16) char smem_raw[];
     const int S = ix.S, tid = threadIdx.x, slot = blockIdx.x;
     if (slot >= list_len(st)) return;
     const int qi = st.qlist[slot];
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, topk, xstride);
+    const int np_max = st.qsh.np_max, k_max = st.qsh.k_max;
+    const int nprobe = st.qsh.np_of(qi), topk = st.qsh.k_of(qi);
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, k_max, xstride);
     __shared__ int pool_size;
     __shared__ float distk;
     ScanTally tl;
     init_pool(sm, topk, pool_size, distk);
-    const uint32_t *pr = probe + (size_t)qi * nprobe;
+    const uint32_t *pr = probe + (size_t)qi * np_max;
     const float *qrot = qrot_all + (size_t)qi * ix.Dtot, *prune = prune_all + (size_t)qi * S;
     // the exact prefix, as scan_probes does: whole tiles in scan order until at
     // least kFirstBlocks blocks are done and the pool is full (its distk then
@@ -1621,8 +1638,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
     }
     flush_tally(tl, counters);
     for (int i = tid; i < topk; i += blockDim.x) {
-        st.pool_id[(size_t)slot * topk + i] = sm.pool_id[i];
-        st.pool_d[(size_t)slot * topk + i] = sm.pool_d[i];
+        st.pool_id[(size_t)slot * k_max + i] = sm.pool_id[i];
+        st.pool_d[(size_t)slot * k_max + i] = sm.pool_d[i];
     }
     if (tid == 0) {
         st.pool_size[slot] = pool_size;
@@ -1634,18 +1651,19 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
         for (int p = 0; p < nprobe; ++p) {
             const int c = (int)pr[p];
             const int nb = (int)(ix.blk_off[c + 1] - ix.blk_off[c]);
-            st.tile_off[(size_t)slot * (nprobe + 1) + p] = tiles;
-            st.blk_base[(size_t)slot * nprobe + p] = (int)pos;
+            st.tile_off[(size_t)slot * (np_max + 1) + p] = tiles;
+            st.blk_base[(size_t)slot * np_max + p] = (int)pos;
             const int rest = p < sp_p ? 0 : p == sp_p ? nb - sp_b : nb;
             tiles += (rest + kTileBlocks - 1) / kTileBlocks;
             pos += nb;
         }
-        st.tile_off[(size_t)slot * (nprobe + 1) + nprobe] = tiles;
+        for (int p = nprobe; p <= np_max; ++p) st.tile_off[(size_t)slot * (np_max + 1) + p] = tiles;
         if (pos != st.npos[slot]) *err = 2;
     }
 }
 
-__global__ void k_tile_prefix(SplitState st, int nprobe) {
+__global__ void k_tile_prefix(SplitState st) {
+    const int nprobe = st.qsh.np_max;
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int n = list_len(st);
     int acc = 0;
@@ -1799,15 +1817,16 @@ constexpr int kReplayRecs = 32;  // records per staged chunk (double-buffered)
 // every warp evaluates records under the current distk; the first record with
 // an accepted insert is replayed exactly by warp 0 (the records before it
 // change nothing and only add their counts), and evaluation resumes after it.
-__global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, int topk, SplitState st,
+__global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, SplitState st,
                                                               uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
                                                               unsigned long long *__restrict__ counters, int xstride) {
     extern __shared__ __align__(16) char smem_raw[];
     const int S = ix.S, slot = blockIdx.x;
     if (slot >= list_len(st)) return;
     const int qi = st.qlist[slot];
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, topk, xstride);
-    float *stage_buf = reinterpret_cast<float *>(smem_raw + scan_smem_bytes(ix.Dtot, S, topk, xstride));
+    const int k_max = st.qsh.k_max, topk = st.qsh.k_of(qi);
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, k_max, xstride);
+    float *stage_buf = reinterpret_cast<float *>(smem_raw + scan_smem_bytes(ix.Dtot, S, k_max, xstride));
     __shared__ int pool_size;
     __shared__ float distk;
     __shared__ int list[kScanThreads];
@@ -1816,8 +1835,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, i
     __shared__ int s_next;
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     for (int i = tid; i < topk; i += blockDim.x) {
-        sm.pool_id[i] = st.pool_id[(size_t)slot * topk + i];
-        sm.pool_d[i] = st.pool_d[(size_t)slot * topk + i];
+        sm.pool_id[i] = st.pool_id[(size_t)slot * k_max + i];
+        sm.pool_d[i] = st.pool_d[(size_t)slot * k_max + i];
     }
     if (tid == 0) {
         pool_size = st.pool_size[slot];
@@ -1911,41 +1930,44 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, i
     }
     __syncthreads();
     if (tid == 0 && counters) atomicAdd(counters + 2, rr);
-    write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
+    write_results(sm, pool_size, topk, k_max, out_ids + (size_t)qi * k_max, out_d ? out_d + (size_t)qi * k_max : nullptr);
 }
 
 // One CTA per query: the whole probe list sequentially (queries deferred to
 // the split pass are skipped).
-__global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const uint32_t *__restrict__ probe, int nprobe,
-                                                       const float *__restrict__ qrot_all,
-                                                       const float *__restrict__ prune_all, int topk,
+__global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const uint32_t *__restrict__ probe,
+                                                       QueryShape qsh, const float *__restrict__ qrot_all,
+                                                       const float *__restrict__ prune_all,
                                                        uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
                                                        int *__restrict__ err, unsigned long long *__restrict__ counters,
                                                        int xstride, const uint8_t *__restrict__ deferred) {
     extern __shared__ __align__(16) char smem_raw[];
     const int qi = blockIdx.x;
     if (deferred && deferred[qi]) return;  // answered by the split pass
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, topk, xstride, true);
+    const int np = qsh.np_of(qi), topk = qsh.k_of(qi);
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, qsh.k_max, xstride, true);
     __shared__ int pool_size;
     __shared__ float distk;
     ScanTally tl;
     init_pool(sm, topk, pool_size, distk);
-    scan_probes(ix, probe + (size_t)qi * nprobe, 0, nprobe, qrot_all + (size_t)qi * ix.Dtot, prune_all + (size_t)qi * ix.S,
-                topk, sm, pool_size, distk, err, tl);
+    scan_probes(ix, probe + (size_t)qi * qsh.np_max, 0, np, qrot_all + (size_t)qi * ix.Dtot,
+                prune_all + (size_t)qi * ix.S, topk, sm, pool_size, distk, err, tl);
     flush_tally(tl, counters);
-    write_results(sm, pool_size, topk, out_ids + (size_t)qi * topk, out_d ? out_d + (size_t)qi * topk : nullptr);
+    write_results(sm, pool_size, topk, qsh.k_max, out_ids + (size_t)qi * qsh.k_max,
+                  out_d ? out_d + (size_t)qi * qsh.k_max : nullptr);
 }
 
 // Puts every query whose probes hold more than `defer_blocks` blocks (a giant
 // Zipf cluster; every query when defer_blocks < 0) on the split list, each
 // with record positions for all its blocks, while the record space lasts.
-__global__ void k_defer(DevIndexView ix, const uint32_t *__restrict__ probe, int nprobe, int nq, int defer_blocks,
-                        SplitState st, uint8_t *__restrict__ deferred) {
+__global__ void k_defer(DevIndexView ix, const uint32_t *__restrict__ probe, int nq, int defer_blocks, SplitState st,
+                        uint8_t *__restrict__ deferred) {
     const int qi = blockIdx.x * blockDim.x + threadIdx.x;
     if (qi >= nq) return;
     int64_t total = 0;
+    const int nprobe = st.qsh.np_of(qi);
     for (int p = 0; p < nprobe; ++p) {
-        const int c = (int)probe[(size_t)qi * nprobe + p];
+        const int c = (int)probe[(size_t)qi * st.qsh.np_max + p];
         total += ix.blk_off[c + 1] - ix.blk_off[c];
     }
     uint8_t d = 0;
@@ -2047,6 +2069,7 @@ size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t np
     add((size_t)nq);                           // shortlist: queries on the full exact path
     add(4 * (size_t)nq);                       // ... and their list
     add(4 * (size_t)nq * topk * 2);            // outputs (host io)
+    add(4 * (size_t)nq * 2);                   // per-query nprobe / k
     add(64);                                   // flags
     add(64);                                   // counters
     (void)host_io;
@@ -2108,8 +2131,9 @@ void blas_try(cublasStatus_t e, const char *what) {
 
 // Centroid ranking of a batch: TF32 GEMM of inner products, the shortlist
 // kernel, and the full exact path for the queries it hands back.
-void probe_shortlist(const Index &I, const float *q, int64_t nq, int64_t nprobe, float *dist, uint32_t *probe,
-                     uint8_t *full, int *fb_list, int *flags, Cand *work, unsigned long long *cnt, cudaStream_t st) {
+void probe_shortlist(const Index &I, const float *q, int64_t nq, int64_t nprobe, const int *qnp, float *dist,
+                     uint32_t *probe, uint8_t *full, int *fb_list, int *flags, Cand *work, unsigned long long *cnt,
+                     cudaStream_t st) {
     const DevIndexView &ix = I.view;
     if (!I.cnorm2) {
         SAQG_CUDA_TRY(cudaMalloc(&I.cnorm2, 8 * (size_t)I.K));
@@ -2137,19 +2161,36 @@ void probe_shortlist(const Index &I, const float *q, int64_t nq, int64_t nprobe,
     SAQG_REQUIRE(smem <= 220 * 1024, "dimension too large for the probe shortlist's shared memory");
     SAQG_CUDA_TRY(cudaFuncSetAttribute(k_probe_shortlist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_probe_shortlist<<<(unsigned)nq, kShortThreads, smem, st>>>(ix, q, dist, reinterpret_cast<const float2 *>(I.cnorm2),
-                                                                 sb, (int)nprobe, probe, full,
+                                                                 sb, (int)nprobe, qnp, probe, full,
                                                                  fb_list, flags + 2, cnt);
     check_launch("k_probe_shortlist");
     k_probe_dist_list<<<608, 256, 0, st>>>(ix, q, dist, fb_list, flags + 2);
     check_launch("k_probe_dist_list");
-    k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, work, flags, full);
+    k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, work, flags, full, qnp);
     check_launch("k_probe_select");
 }
 
 }  // namespace
 
 void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,
-                float *dists, int mem, cudaStream_t st, saqg_search_stats *stats, uint32_t *probes_out) {
+                float *dists, int mem, cudaStream_t st, saqg_search_stats *stats, uint32_t *probes_out,
+                const int *np_host, const int *k_host) {
+    // per-query nprobe / k (host arrays): the scalars become their maxima
+    int64_t sum_np = nq * nprobe;
+    if (np_host || k_host) {
+        int64_t npm = 0, km = 0;
+        sum_np = 0;
+        for (int64_t i = 0; i < nq; ++i) {
+            const int a = np_host ? np_host[i] : (int)nprobe, b = k_host ? k_host[i] : (int)topk;
+            SAQG_REQUIRE(a >= 1 && a <= I.K, "every nprobe must be in [1, number of clusters]");
+            SAQG_REQUIRE(b >= 1 && b <= kMaxTopK, "every topk must be in [1, 4096]");
+            npm = std::max<int64_t>(npm, a);
+            km = std::max<int64_t>(km, b);
+            sum_np += a;
+        }
+        if (np_host) nprobe = npm;
+        if (k_host) topk = km;
+    }
     SAQG_REQUIRE(nq >= 0 && topk >= 1 && topk <= kMaxTopK, "topk must be in [1, 4096]");
     SAQG_REQUIRE(nprobe >= 1 && nprobe <= I.K, "nprobe must be in [1, number of clusters]");
     if (nq == 0) return;
@@ -2157,6 +2198,19 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
     std::lock_guard<std::mutex> lock(I.mu);
     const bool host = mem == SAQG_MEM_HOST;
     Bump bp{(char *)I.scratch_get(search_scratch_bytes(I, nq, topk, nprobe, host))};
+    QueryShape qsh;
+    qsh.np_max = (int)nprobe;
+    qsh.k_max = (int)topk;
+    if (np_host) {
+        int *d = bp.take<int>(nq);
+        SAQG_CUDA_TRY(cudaMemcpyAsync(d, np_host, 4 * (size_t)nq, cudaMemcpyHostToDevice, st));
+        qsh.np = d;
+    }
+    if (k_host) {
+        int *d = bp.take<int>(nq);
+        SAQG_CUDA_TRY(cudaMemcpyAsync(d, k_host, 4 * (size_t)nq, cudaMemcpyHostToDevice, st));
+        qsh.k = d;
+    }
     float *dq = bp.take<float>((size_t)nq * I.D);
     float *dist = bp.take<float>((size_t)nq * I.K);
     Cand *work = bp.take<Cand>((size_t)nq * I.K);
@@ -2194,7 +2248,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         const char *pm = std::getenv("SAQG_PROBE");
         shortlist = nq >= kGemmMinQueries && nprobe <= kShortCap && !(pm && std::string(pm) == "exact");
         if (shortlist) {
-            probe_shortlist(I, qin, nq, nprobe, dist, probe, full, fb_list, flags, work, stats ? counters : nullptr, st);
+            probe_shortlist(I, qin, nq, nprobe, qsh.np, dist, probe, full, fb_list, flags, work,
+                            stats ? counters : nullptr, st);
         } else if (nq >= 8 && I.D % 32 == 0 && I.D <= 32 * kProbeRegs) {
             const size_t qsm = 4 * (size_t)kProbeQT * I.D;
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_probe_dist_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm));
@@ -2207,7 +2262,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             check_launch("k_probe_dist");
         }
         if (!shortlist) {
-            k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, work, flags);
+            k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, work, flags,
+                                                                  nullptr, qsh.np);
             check_launch("k_probe_select");
         }
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[1], st));
@@ -2230,7 +2286,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         uint32_t *ids_out = host ? oid : ids;
         float *d_out = host ? od : dists;
         unsigned long long *cnt = stats ? counters : nullptr;
-        const int mode = scan_mode(nq, topk);
+        const int mode = (qsh.np || qsh.k) && scan_mode(nq, topk) == 2 ? 0 : scan_mode(nq, topk);
         if (mode == 2) {
             const size_t per_warp = align16(warp_smem_bytes(ix.Dtot, ix.S, (int)topk));
             const size_t wsm = per_warp * kWarpsPerCta;
@@ -2266,6 +2322,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             ss.summ = sb.take<float2>((size_t)pos_cap);
             ss.rec_words = rec_words_of(ix.S);
             ss.rec = sb.take<float>((size_t)pos_cap * ss.rec_words);
+            ss.qsh = qsh;
             uint8_t *deferred = sb.take<uint8_t>(nq);
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.summ, 0xff, 8 * (size_t)pos_cap, st));  // NaN: no record
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 16, st));
@@ -2274,8 +2331,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                 defer = kDeferBlocks;
                 if (const char *e = std::getenv("SAQG_DEFER_BLOCKS")) defer = std::max(0, std::atoi(e));
             }
-            k_defer<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(ix, probe, (int)nprobe, (int)nq, defer, ss,
-                                                                   deferred);
+            k_defer<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(ix, probe, (int)nq, defer, ss, deferred);
             check_launch("k_defer");
             cudaStream_t sp = st;  // stream of the split pass
             // the CTA scan serves what the split list does not hold: always in mode 0,
@@ -2289,8 +2345,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                 const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs, true);
                 SAQG_REQUIRE(smem_k <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
                 SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_k));
-                k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk,
-                                                                  ids_out, d_out, flags + 1, cnt, xs, deferred);
+                k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, qsh, qrot, prune, ids_out, d_out,
+                                                                    flags + 1, cnt, xs, deferred);
                 check_launch("k_scan");
             }
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
@@ -2299,10 +2355,9 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_first, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_spec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
-            k_scan_first<<<(unsigned)cap, kScanThreads, smem, sp>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ss,
-                                                                     flags + 1, cnt, xs);
+            k_scan_first<<<(unsigned)cap, kScanThreads, smem, sp>>>(ix, probe, qrot, prune, ss, flags + 1, cnt, xs);
             check_launch("k_scan_first");
-            k_tile_prefix<<<1, 32, 0, sp>>>(ss, (int)nprobe);
+            k_tile_prefix<<<1, 32, 0, sp>>>(ss);
             check_launch("k_tile_prefix");
             if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[5], sp));
             int dev = 0, sms = 0, per_sm = 0;
@@ -2313,7 +2368,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             k_scan_spec<<<grid, kScanThreads, smem1, sp>>>(ix, probe, (int)nprobe, qrot, prune, ss, cnt, xs);
             check_launch("k_scan_spec");
             if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[6], sp));
-            k_scan_replay<<<(unsigned)cap, kScanThreads, smem_r, sp>>>(ix, (int)topk, ss, ids_out, d_out, cnt, xs);
+            k_scan_replay<<<(unsigned)cap, kScanThreads, smem_r, sp>>>(ix, ss, ids_out, d_out, cnt, xs);
             check_launch("k_scan_replay");
             if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[4], sp));
             if (sp != st) {  // join
@@ -2359,7 +2414,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         stats->ms_split_spec = span(5, 6);
         stats->ms_split_replay = span(6, 4);
         cudaGetLastError();
-        stats->probes = nq * nprobe;
+        stats->probes = sum_np;
         stats->blocks = (int64_t)hc[0];
         stats->vectors = (int64_t)hc[1];
         stats->reranked = (int64_t)hc[2];
@@ -2538,7 +2593,10 @@ void run_search_static(const Index &I, const float *q, int64_t nq, int64_t topk,
     const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xstride_of(ix), true);
     SAQG_REQUIRE(smem_k <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
     SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_k));
-    k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, (int)nprobe, qrot, prune, (int)topk, ids, dists,
+    QueryShape qsh;
+    qsh.np_max = (int)nprobe;
+    qsh.k_max = (int)topk;
+    k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, qsh, qrot, prune, ids, dists,
                                                       flags + 1, nullptr, xstride_of(ix), nullptr);
     check_launch("k_scan");
     count_launch(4);

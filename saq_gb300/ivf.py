@@ -124,9 +124,13 @@ class IVF:
                     plan=[(inf.seg_dim[i], inf.seg_bits[i]) for i in range(S)], device_bytes=inf.device_bytes)
 
     # -- search -----------------------------------------------------------
-    def search(self, query, topk: int, nprobe: int, searcher_cfg: SearcherConfig | None = None,
+    def search(self, query, topk, nprobe, searcher_cfg: SearcherConfig | None = None,
                return_dists: bool = False, out=None, stream=None):
+        """IVF::search for one query or a batch.  `topk` / `nprobe` may be per-query
+        sequences (rows are then max(topk) long, padded with id 0 / inf)."""
         cfg = (searcher_cfg or SearcherConfig()).to_c()
+        if not (np.isscalar(topk) and np.isscalar(nprobe)):
+            return self._search_mixed(query, topk, nprobe, cfg, return_dists, stream)
         if _is_cuda_tensor(query):
             import torch
             q = query.contiguous().view(-1, self.num_dim)
@@ -148,6 +152,31 @@ class IVF:
                                      dists.ctypes.data, N.SAQG_MEM_HOST, _stream_ptr(stream)))
         if single:
             ids, dists = ids[0], dists[0]
+        return (ids, dists) if return_dists else ids
+
+    def _search_mixed(self, query, topk, nprobe, cfg, return_dists, stream):
+        if _is_cuda_tensor(query):
+            import torch
+            q = query.contiguous().view(-1, self.num_dim)
+            nq = q.shape[0]
+        else:
+            q = np.ascontiguousarray(query, np.float32).reshape(-1, self.num_dim)
+            nq = q.shape[0]
+        ks = np.broadcast_to(np.asarray(topk, np.int32), (nq,)).copy()
+        nps = np.broadcast_to(np.asarray(nprobe, np.int32), (nq,)).copy()
+        kmax = int(ks.max())
+        if _is_cuda_tensor(query):
+            ids = torch.empty((nq, kmax), dtype=torch.int32, device=q.device)
+            dists = torch.empty((nq, kmax), dtype=torch.float32, device=q.device)
+            N.check(self.lib.saqg_search_batch(self._h, q.data_ptr(), nq, nps.ctypes.data, ks.ctypes.data,
+                                               int(nps.max()), kmax, C.byref(cfg), ids.data_ptr(), dists.data_ptr(),
+                                               N.SAQG_MEM_DEVICE, _stream_ptr(stream), None))
+        else:
+            ids = np.zeros((nq, kmax), np.uint32)
+            dists = np.zeros((nq, kmax), np.float32)
+            N.check(self.lib.saqg_search_batch(self._h, q.ctypes.data, nq, nps.ctypes.data, ks.ctypes.data,
+                                               int(nps.max()), kmax, C.byref(cfg), ids.ctypes.data, dists.ctypes.data,
+                                               N.SAQG_MEM_HOST, _stream_ptr(stream), None))
         return (ids, dists) if return_dists else ids
 
     def estimate(self, query, nprobe: int, searcher_cfg: SearcherConfig | None = None):

@@ -1,0 +1,48 @@
+"""Batches whose queries carry their own nprobe and k (the uneven batches of
+the batching and serving forms).  Each query's answer must equal the oracle's
+for that query alone, bit for bit, in every scan form; rows are padded to the
+largest k with id 0 / inf."""
+import numpy as np
+import pytest
+
+import oracle as O
+from saq_gb300 import data
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def built(tmp_path_factory):
+    from saq_gb300 import ivf
+    tmp = tmp_path_factory.mktemp("mixed")
+    x, q = data.gaussian_mixture(12000, 128, 300, sigma=0.6, seed=6, n_query=120)
+    cent, cids = data.kmeans(x, 160, iters=6, seed=2)
+    rng = np.random.default_rng(3)
+    plan = O.plan(O.colwise_var(x), 4.0, True, 0)
+    rots = np.concatenate([data.random_orthogonal(d, rng).astype(np.float32).reshape(-1) for d, _ in plan])
+    index = ivf.IVF(x.shape[0], 128, 160, ivf.QuantizeConfig(avg_bits=4.0))
+    index.construct(x, cent, cids, rotations=rots)
+    opath = str(tmp / "o.index")
+    O.build_index(opath, x, cent, cids, 4.0, True, 0, rots)
+    return index, O.OracleIndex(opath), q
+
+
+@pytest.mark.parametrize("mode,defer", [(None, None), ("seq", "1"), ("seq", "0"), ("split", None)])
+@pytest.mark.parametrize("nq", [40, 120])
+def test_mixed_nprobe_and_k(built, mode, defer, nq, monkeypatch):
+    index, oi, q = built
+    if mode:
+        monkeypatch.setenv("SAQG_SCAN_MODE", mode)
+    if defer:
+        monkeypatch.setenv("SAQG_DEFER_BLOCKS", defer)
+    rng = np.random.default_rng(nq)
+    qq = q[:nq]
+    nps = rng.integers(4, 41, size=nq).astype(np.int32)
+    ks = rng.choice([10, 100], size=nq).astype(np.int32)
+    ids, d = index.search(qq, ks, nps, return_dists=True)
+    assert ids.shape == (nq, 100)
+    for i in range(nq):
+        oids, od = oi.search(qq[i:i + 1], int(ks[i]), int(nps[i]), with_dists=True)
+        assert np.array_equal(ids[i, :ks[i]], oids[0]), i
+        assert np.array_equal(d[i, :ks[i]].view(np.uint32), od[0].view(np.uint32)), i
+        assert np.all(ids[i, ks[i]:] == 0) and np.all(np.isinf(d[i, ks[i]:]) | (d[i, ks[i]:] == np.float32(3.4028235e38)))
