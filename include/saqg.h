@@ -33,6 +33,7 @@ extern "C" {
 #define SAQG_ERR_CUDA 3     /* a CUDA runtime call failed */
 #define SAQG_ERR_NOMEM 4    /* device or host allocation failed */
 #define SAQG_ERR_INTERNAL 5 /* a device-side consistency check failed */
+#define SAQG_ERR_TIMEOUT 6  /* a server result was not ready within the timeout */
 
 #define SAQG_MEM_HOST 0
 #define SAQG_MEM_DEVICE 1
@@ -178,6 +179,49 @@ int saqg_search_static(const saqg_index *index, const float *queries, int64_t nq
 int saqg_search_batch(const saqg_index *index, const float *queries, int64_t nq, const int32_t *nprobe_per_query,
                       const int32_t *topk_per_query, int64_t nprobe, int64_t topk, const saqg_searcher_config *cfg,
                       uint32_t *ids, float *dists, int mem, void *stream, saqg_search_stats *stats);
+
+/* ---- serving ----------------------------------------------------------- */
+/* No counterpart in the reference (its drivers call IVF::search from a thread
+ * pool): a serving loop with continuous batching on one index.  Submitted
+ * queries (each with its own nprobe and topk) are batched on the device as
+ * slots free up: up to `max_inflight` batches run at once on their own streams
+ * and search contexts, so a batch is admitted while earlier ones still run.
+ * A batch is also cut down until its scratch fits `mem_budget_bytes` minus what
+ * the other in-flight batches hold.  Every answer equals the reference's for
+ * that query alone (saqg_search_batch's path). */
+typedef struct saqg_server saqg_server;
+typedef struct saqg_server_config {
+    int32_t max_batch;        /* queries per batch at most (0: 4096) */
+    int32_t max_inflight;     /* batches on the device at once (0: 2; at most 16) */
+    int32_t max_topk;         /* largest topk a request may ask (0: 100) */
+    int32_t max_nprobe;       /* largest nprobe a request may ask (0: min(256, clusters)) */
+    int32_t max_wait_us;      /* how long a partial batch waits for arrivals while others run */
+    float searcher_vars_bound_m; /* SearcherConfig::searcher_vars_bound_m (0: 4) */
+    int64_t mem_budget_bytes; /* device scratch for in-flight batches (0: half the free memory) */
+} saqg_server_config;
+
+typedef struct saqg_server_stats {
+    int64_t submitted, completed, batches, admission_shrinks;
+    int32_t max_batch_seen, max_inflight_seen;
+    double mean_batch, p50_ms, p99_ms; /* latency from submit to result ready */
+} saqg_server_stats;
+
+int saqg_server_create(const saqg_index *index, const saqg_server_config *cfg, saqg_server **out);
+/* Queues one query (host memory, dim floats); returns its ticket. */
+int saqg_server_submit(saqg_server *server, const float *query, int32_t nprobe, int32_t topk, uint64_t *ticket);
+/* Waits for a ticket's result (timeout_ms < 0: no limit) and copies its topk
+ * ids / dists (either may be NULL) and latency; the ticket is then spent. */
+int saqg_server_wait(saqg_server *server, uint64_t ticket, uint32_t *ids, float *dists, double *latency_ms,
+                     int32_t timeout_ms);
+int saqg_server_get_stats(saqg_server *server, saqg_server_stats *out);
+/* Open-loop load: submits n queries (n x dim host floats) at `arrival_s`
+ * seconds from the call, with their nprobe / topk, and collects every result
+ * into rows of `row` entries (ids / dists may be NULL) and latencies. */
+int saqg_server_run_trace(saqg_server *server, const float *queries, int64_t n, const double *arrival_s,
+                          const int32_t *nprobe, const int32_t *topk, int32_t row, uint32_t *ids, float *dists,
+                          double *latency_ms);
+/* Drains the queue (every submitted query is answered) and releases the server. */
+int saqg_server_free(saqg_server *server);
 
 /* IVF::estimate<L2Sqr> (index/ivf.hpp:313-362) for one query: every vector of
  * the `nprobe` probed clusters, in probe order, with its accurate, fast and

@@ -53,6 +53,21 @@ class SaqgError(RuntimeError):
 
 _lib = None
 
+class ServerConfig(C.Structure):
+    _fields_ = [("max_batch", C.c_int32), ("max_inflight", C.c_int32), ("max_topk", C.c_int32),
+                ("max_nprobe", C.c_int32), ("max_wait_us", C.c_int32), ("searcher_vars_bound_m", C.c_float),
+                ("mem_budget_bytes", I64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", I64), ("completed", I64), ("batches", I64), ("admission_shrinks", I64),
+                ("max_batch_seen", C.c_int32), ("max_inflight_seen", C.c_int32), ("mean_batch", C.c_double),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 EXPORTS = {
     "saqg_version": (C.c_int, []),
     "saqg_last_error": (C.c_char_p, []),
@@ -74,6 +89,14 @@ EXPORTS = {
                                     C.c_void_p]),
     "saqg_search_static": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig), C.c_void_p,
                                      C.c_void_p, C.c_void_p]),
+    "saqg_server_create": (C.c_int, [C.c_void_p, C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    "saqg_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_uint64)]),
+    "saqg_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.POINTER(C.c_double),
+                                   C.c_int32]),
+    "saqg_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    "saqg_server_run_trace": (C.c_int, [C.c_void_p, C.c_void_p, I64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                        C.c_void_p, C.c_void_p, C.c_void_p]),
+    "saqg_server_free": (C.c_int, [C.c_void_p]),
     "saqg_estimate": (C.c_int, [C.c_void_p, C.c_void_p, I64, C.POINTER(SearcherConfig), C.c_void_p, C.c_void_p,
                                 C.c_void_p, C.c_void_p, I64, C.POINTER(I64)]),
     "saqg_plan": (C.c_int, [C.c_void_p, I64, C.c_float, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,

@@ -41,6 +41,10 @@ struct saqg_index {
     Index *impl;
 };
 
+struct saqg_server {
+    Server *impl;
+};
+
 extern "C" {
 
 int saqg_version(void) { return 1; }
@@ -162,6 +166,55 @@ int saqg_search_static(const saqg_index *index, const float *queries, int64_t nq
         SAQG_REQUIRE(!cfg || cfg->dist_type == SAQG_DIST_L2, "only L2 search is supported");
         const float m = cfg ? cfg->searcher_vars_bound_m : 4.0f;
         run_search_static(*index->impl, queries, nq, topk, nprobe, m, ids, dists, (cudaStream_t)stream);
+    });
+}
+
+int saqg_server_create(const saqg_index *index, const saqg_server_config *cfg, saqg_server **out) {
+    return guarded([&] {
+        SAQG_REQUIRE(index && out, "null argument");
+        *out = nullptr;
+        Server *s = server_create(*index->impl, cfg);
+        *out = new saqg_server{s};
+    });
+}
+
+int saqg_server_submit(saqg_server *server, const float *query, int32_t nprobe, int32_t topk, uint64_t *ticket) {
+    return guarded([&] {
+        SAQG_REQUIRE(server && query && ticket, "null argument");
+        *ticket = server_submit(server->impl, query, nprobe, topk);
+    });
+}
+
+int saqg_server_wait(saqg_server *server, uint64_t ticket, uint32_t *ids, float *dists, double *latency_ms,
+                     int32_t timeout_ms) {
+    return guarded([&] {
+        SAQG_REQUIRE(server, "null argument");
+        server_wait(server->impl, ticket, ids, dists, latency_ms, timeout_ms);
+    });
+}
+
+int saqg_server_get_stats(saqg_server *server, saqg_server_stats *out) {
+    return guarded([&] {
+        SAQG_REQUIRE(server && out, "null argument");
+        server_stats(server->impl, out);
+    });
+}
+
+int saqg_server_run_trace(saqg_server *server, const float *queries, int64_t n, const double *arrival_s,
+                          const int32_t *nprobe, const int32_t *topk, int32_t row, uint32_t *ids, float *dists,
+                          double *latency_ms) {
+    return guarded([&] {
+        SAQG_REQUIRE(server && queries && arrival_s && nprobe && topk, "null argument");
+        SAQG_REQUIRE(n >= 0 && row >= 1, "bad trace shape");
+        server_run_trace(server->impl, queries, n, arrival_s, nprobe, topk, row, ids, dists, latency_ms);
+    });
+}
+
+int saqg_server_free(saqg_server *server) {
+    return guarded([&] {
+        if (!server) return;
+        server_free(server->impl);
+        delete server;
     });
 }
 

@@ -94,14 +94,17 @@ Index::~Index() {
     cudaGetDevice(&cur);
     cudaSetDevice(device);
     for (void *p : allocations) cudaFree(p);
+    if (cnorm2) cudaFree(cnorm2);
+    cudaSetDevice(cur);
+}
+
+SearchCtx::~SearchCtx() {
     if (scratch) cudaFree(scratch);
     if (split_scratch) cudaFree(split_scratch);
     if (aux) cudaStreamDestroy(aux);
-    if (cnorm2) cudaFree(cnorm2);
-    if (blas) cublasDestroy(static_cast<cublasHandle_t>(blas));
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
-    cudaSetDevice(cur);
+    if (blas) cublasDestroy(static_cast<cublasHandle_t>(blas));
 }
 
 void *Index::dalloc(size_t bytes) {
@@ -133,11 +136,12 @@ static void *grow(void *&buf, size_t &have, size_t bytes) {
     return buf;
 }
 
-void *Index::split_scratch_get(size_t bytes) const { return grow(split_scratch, split_scratch_bytes, bytes); }
+void *SearchCtx::scratch_get(size_t bytes) { return grow(scratch, scratch_bytes, bytes); }
+void *SearchCtx::split_scratch_get(size_t bytes) { return grow(split_scratch, split_scratch_bytes, bytes); }
 
 // The split pass is a batch's critical path: its stream gets the device's
 // highest priority, so its CTAs go first while the CTA scan beside it fills in.
-cudaStream_t Index::aux_stream() const {
+cudaStream_t SearchCtx::aux_stream() {
     if (!aux) {
         int least = 0, greatest = 0;
         SAQG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
@@ -145,27 +149,13 @@ cudaStream_t Index::aux_stream() const {
     }
     return aux;
 }
-cudaEvent_t Index::fork_event() const {
+cudaEvent_t SearchCtx::fork_event() {
     if (!ev_fork) SAQG_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     return ev_fork;
 }
-cudaEvent_t Index::join_event() const {
+cudaEvent_t SearchCtx::join_event() {
     if (!ev_join) SAQG_CUDA_TRY(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     return ev_join;
-}
-
-void *Index::scratch_get(size_t bytes) const {
-    if (bytes > scratch_bytes) {
-        SAQG_CUDA_TRY(cudaDeviceSynchronize());
-        if (scratch) SAQG_CUDA_TRY(cudaFree(scratch));
-        scratch = nullptr;
-        scratch_bytes = 0;
-        size_t want = bytes + bytes / 4 + (1 << 20);
-        cudaError_t e = cudaMalloc(&scratch, want);
-        if (e != cudaSuccess) throw Error{SAQG_ERR_NOMEM, std::string("scratch cudaMalloc failed: ") + cudaGetErrorString(e)};
-        scratch_bytes = want;
-    }
-    return scratch;
 }
 
 int64_t Index::max_blocks_of_probes(int64_t nprobe) const {

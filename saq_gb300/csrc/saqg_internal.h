@@ -75,6 +75,30 @@ struct DevIndexView {  // passed to kernels by value
     SegDev seg[kMaxSeg];
 };
 
+// What one in-flight search owns: scratch arenas, the auxiliary stream of the
+// split pass with its fork / join events, and a BLAS handle.  Searches on
+// different contexts may run concurrently on different streams.
+struct SearchCtx {
+    std::mutex mu;
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    void *split_scratch = nullptr;
+    size_t split_scratch_bytes = 0;
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    void *blas = nullptr;
+    SearchCtx() = default;
+    SearchCtx(const SearchCtx &) = delete;
+    SearchCtx &operator=(const SearchCtx &) = delete;
+    ~SearchCtx();
+    void *scratch_get(size_t bytes);
+    void *split_scratch_get(size_t bytes);
+    cudaStream_t aux_stream();
+    cudaEvent_t fork_event();
+    cudaEvent_t join_event();
+    size_t held_bytes() const { return scratch_bytes + split_scratch_bytes; }
+};
+
 struct Index {
     // metadata
     int64_t N = 0, D = 0, K = 0;
@@ -95,27 +119,14 @@ struct Index {
     std::vector<void *> allocations;
     int64_t device_bytes = 0;
     int device = 0;
-    // scratch arena for searches (guarded)
-    mutable std::mutex mu;
-    mutable void *scratch = nullptr;
-    mutable size_t scratch_bytes = 0;
-    mutable void *split_scratch = nullptr;
-    mutable size_t split_scratch_bytes = 0;
-    // probe shortlist: squared centroid norms and the BLAS handle (created on first use)
+    // the search context of ordinary calls (serialised by its mutex)
+    mutable SearchCtx ctx;
+    // probe shortlist: squared centroid norms (built on first use, under init_mu)
+    mutable std::mutex init_mu;
     mutable float *cnorm2 = nullptr;
-    mutable void *blas = nullptr;
-    // auxiliary stream and fork/join events (created on first use)
-    mutable cudaStream_t aux = nullptr;
-    mutable cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    cudaStream_t aux_stream() const;
-    cudaEvent_t fork_event() const;
-    cudaEvent_t join_event() const;
-
     ~Index();
     void *dalloc(size_t bytes);
     void upload(void *dst, const void *src, size_t bytes);
-    void *scratch_get(size_t bytes) const;
-    void *split_scratch_get(size_t bytes) const;
     // most blocks any nprobe clusters can hold (sizes of the largest clusters)
     std::vector<int64_t> top_blocks_prefix;
     int64_t max_blocks_of_probes(int64_t nprobe) const;
@@ -133,12 +144,28 @@ void convert_index_file(const std::string &src, const std::string &dst, int form
 // search.cu
 void run_search(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,
                 float *dists, int mem, cudaStream_t st, saqg_search_stats *stats = nullptr,
-                uint32_t *probes_out = nullptr, const int *np_host = nullptr, const int *k_host = nullptr);
+                uint32_t *probes_out = nullptr, const int *np_host = nullptr, const int *k_host = nullptr,
+                SearchCtx *ctx = nullptr);
+// Scratch bytes a batch of this shape needs (both arenas), for admission by memory.
+size_t search_bytes_estimate(const Index &idx, int64_t nq, int64_t topk, int64_t nprobe);
+// Grows a context's arenas (and creates its stream, events and BLAS handle)
+// for batches up to this shape, so later searches allocate nothing.
+void presize_ctx(const Index &idx, SearchCtx &ctx, int64_t nq, int64_t topk, int64_t nprobe);
 // saqg_search for device pointers with its scratch in a static device array.
 void run_search_static(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m,
                        uint32_t *ids, float *dists, cudaStream_t stream);
 int64_t run_estimate(const Index &idx, const float *q_host, int64_t nprobe, float m, uint32_t *ids, float *acc,
                      float *fast, float *vars, int64_t cap);
+
+// serve.cpp
+struct Server;
+Server *server_create(const Index &idx, const saqg_server_config *cfg);
+void server_free(Server *s);
+uint64_t server_submit(Server *s, const float *q, int nprobe, int topk);
+void server_wait(Server *s, uint64_t ticket, uint32_t *ids, float *dists, double *latency_ms, int timeout_ms);
+void server_stats(Server *s, saqg_server_stats *out);
+void server_run_trace(Server *s, const float *queries, int64_t n, const double *arrival_s, const int *nprobe,
+                      const int *topk, int row, uint32_t *ids, float *dists, double *latency_ms);
 
 // encode.cu
 void run_caq_encode(const float *resid, int64_t n, int64_t dim, int bits, const float *cent, int rdlmt, float eps,

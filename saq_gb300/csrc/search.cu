@@ -2131,21 +2131,27 @@ void blas_try(cublasStatus_t e, const char *what) {
 
 // Centroid ranking of a batch: TF32 GEMM of inner products, the shortlist
 // kernel, and the full exact path for the queries it hands back.
-void probe_shortlist(const Index &I, const float *q, int64_t nq, int64_t nprobe, const int *qnp, float *dist,
-                     uint32_t *probe, uint8_t *full, int *fb_list, int *flags, Cand *work, unsigned long long *cnt,
-                     cudaStream_t st) {
+void probe_shortlist(const Index &I, SearchCtx &C, const float *q, int64_t nq, int64_t nprobe, const int *qnp,
+                     float *dist, uint32_t *probe, uint8_t *full, int *fb_list, int *flags, Cand *work,
+                     unsigned long long *cnt, cudaStream_t st) {
     const DevIndexView &ix = I.view;
-    if (!I.cnorm2) {
-        SAQG_CUDA_TRY(cudaMalloc(&I.cnorm2, 8 * (size_t)I.K));
-        k_cnorm2<<<(unsigned)((I.K * 32 + 255) / 256), 256, 0, st>>>(ix, reinterpret_cast<float2 *>(I.cnorm2));
-        check_launch("k_cnorm2");
+    {
+        std::lock_guard<std::mutex> lk(I.init_mu);
+        if (!I.cnorm2) {
+            float *p = nullptr;
+            SAQG_CUDA_TRY(cudaMalloc(&p, 8 * (size_t)I.K));
+            k_cnorm2<<<(unsigned)((I.K * 32 + 255) / 256), 256, 0, st>>>(ix, reinterpret_cast<float2 *>(p));
+            check_launch("k_cnorm2");
+            SAQG_CUDA_TRY(cudaStreamSynchronize(st));  // other contexts read it on their own streams
+            I.cnorm2 = p;
+        }
     }
-    if (!I.blas) {
+    if (!C.blas) {
         cublasHandle_t h = nullptr;
         blas_try(cublasCreate(&h), "cublasCreate");
-        I.blas = h;
+        C.blas = h;
     }
-    cublasHandle_t h = static_cast<cublasHandle_t>(I.blas);
+    cublasHandle_t h = static_cast<cublasHandle_t>(C.blas);
     blas_try(cublasSetStream(h, st), "cublasSetStream");
     const float one = 1.0f, zero = 0.0f;
     // dist (row-major nq x K) = Q C^T, i.e. column-major K x nq = C^T(op T) * Q^T
@@ -2172,9 +2178,31 @@ void probe_shortlist(const Index &I, const float *q, int64_t nq, int64_t nprobe,
 
 }  // namespace
 
+void presize_ctx(const Index &I, SearchCtx &C, int64_t nq, int64_t topk, int64_t nprobe) {
+    std::lock_guard<std::mutex> lock(C.mu);
+    C.scratch_get(search_scratch_bytes(I, nq, topk, nprobe, false));
+    const int64_t pos_cap = split_positions(I, nq * I.max_blocks_of_probes(nprobe));
+    C.split_scratch_get(split_scratch_bytes(I, nq, topk, nprobe, pos_cap));
+    C.aux_stream();
+    C.fork_event();
+    C.join_event();
+    if (!C.blas) {
+        cublasHandle_t h = nullptr;
+        blas_try(cublasCreate(&h), "cublasCreate");
+        C.blas = h;
+    }
+}
+
+size_t search_bytes_estimate(const Index &I, int64_t nq, int64_t topk, int64_t nprobe) {
+    const int64_t max_pos = I.max_blocks_of_probes(nprobe);
+    const int64_t pos_cap = split_positions(I, nq * max_pos);
+    return search_scratch_bytes(I, nq, topk, nprobe, false) + split_scratch_bytes(I, nq, topk, nprobe, pos_cap);
+}
+
 void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,
                 float *dists, int mem, cudaStream_t st, saqg_search_stats *stats, uint32_t *probes_out,
-                const int *np_host, const int *k_host) {
+                const int *np_host, const int *k_host, SearchCtx *ctx) {
+    SearchCtx &C = ctx ? *ctx : I.ctx;
     // per-query nprobe / k (host arrays): the scalars become their maxima
     int64_t sum_np = nq * nprobe;
     if (np_host || k_host) {
@@ -2195,9 +2223,9 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
     SAQG_REQUIRE(nprobe >= 1 && nprobe <= I.K, "nprobe must be in [1, number of clusters]");
     if (nq == 0) return;
     const DevIndexView &ix = I.view;
-    std::lock_guard<std::mutex> lock(I.mu);
+    std::lock_guard<std::mutex> lock(C.mu);
     const bool host = mem == SAQG_MEM_HOST;
-    Bump bp{(char *)I.scratch_get(search_scratch_bytes(I, nq, topk, nprobe, host))};
+    Bump bp{(char *)C.scratch_get(search_scratch_bytes(I, nq, topk, nprobe, host))};
     QueryShape qsh;
     qsh.np_max = (int)nprobe;
     qsh.k_max = (int)topk;
@@ -2248,7 +2276,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         const char *pm = std::getenv("SAQG_PROBE");
         shortlist = nq >= kGemmMinQueries && nprobe <= kShortCap && !(pm && std::string(pm) == "exact");
         if (shortlist) {
-            probe_shortlist(I, qin, nq, nprobe, qsh.np, dist, probe, full, fb_list, flags, work,
+            probe_shortlist(I, C, qin, nq, nprobe, qsh.np, dist, probe, full, fb_list, flags, work,
                             stats ? counters : nullptr, st);
         } else if (nq >= 8 && I.D % 32 == 0 && I.D <= 32 * kProbeRegs) {
             const size_t qsm = 4 * (size_t)kProbeQT * I.D;
@@ -2301,7 +2329,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             const int64_t cap = nq;
             const int64_t want = nq * max_pos;
             const int64_t pos_cap = split_positions(I, want);
-            Bump sb{(char *)I.split_scratch_get(split_scratch_bytes(I, cap, topk, nprobe, pos_cap))};
+            Bump sb{(char *)C.split_scratch_get(split_scratch_bytes(I, cap, topk, nprobe, pos_cap))};
             SplitState ss;
             ss.nlist = sb.take<int>(16);
             ss.pos_used = reinterpret_cast<unsigned long long *>(ss.nlist + 2);
@@ -2338,9 +2366,9 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             // in mode 1 only when the record space cannot hold every query
             if (mode == 0 || pos_cap < want) {
                 if (mode == 0) {  // the split pass runs beside the CTA scan on the index's auxiliary stream
-                    sp = I.aux_stream();
-                    SAQG_CUDA_TRY(cudaEventRecord(I.fork_event(), st));
-                    SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, I.fork_event(), 0));
+                    sp = C.aux_stream();
+                    SAQG_CUDA_TRY(cudaEventRecord(C.fork_event(), st));
+                    SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, C.fork_event(), 0));
                 }
                 const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs, true);
                 SAQG_REQUIRE(smem_k <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
@@ -2372,8 +2400,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             check_launch("k_scan_replay");
             if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[4], sp));
             if (sp != st) {  // join
-                SAQG_CUDA_TRY(cudaEventRecord(I.join_event(), sp));
-                SAQG_CUDA_TRY(cudaStreamWaitEvent(st, I.join_event(), 0));
+                SAQG_CUDA_TRY(cudaEventRecord(C.join_event(), sp));
+                SAQG_CUDA_TRY(cudaStreamWaitEvent(st, C.join_event(), 0));
             }
             count_launch(mode == 0 ? 8 : 8);
         }
@@ -2439,9 +2467,9 @@ int64_t run_estimate(const Index &I, const float *q_host, int64_t nprobe, float 
                      float *fast, float *vars, int64_t cap) {
     SAQG_REQUIRE(nprobe >= 1 && nprobe <= I.K, "nprobe must be in [1, number of clusters]");
     const DevIndexView &ix = I.view;
-    std::lock_guard<std::mutex> lock(I.mu);
+    std::lock_guard<std::mutex> lock(I.ctx.mu);
     cudaStream_t st = 0;
-    Bump bp{(char *)I.scratch_get(search_scratch_bytes(I, 1, 1, nprobe, true))};
+    Bump bp{(char *)I.ctx.scratch_get(search_scratch_bytes(I, 1, 1, nprobe, true))};
     float *dq = bp.take<float>(I.D);
     float *dist = bp.take<float>(I.K);
     Cand *work = bp.take<Cand>(I.K);

@@ -195,6 +195,65 @@ class IVF:
         return ids[:n], acc[:n], fast[:n], var[:n]
 
 
+class Server:
+    """Serving loop with continuous batching over an IVF (saqg_server_*): queries
+    submitted one by one, batched on the device as slots and memory free up."""
+
+    def __init__(self, index: IVF, max_batch: int = 4096, max_inflight: int = 2, max_topk: int = 100,
+                 max_nprobe: int = 0, max_wait_us: int = 200, mem_budget_bytes: int = 0,
+                 searcher_cfg: SearcherConfig | None = None):
+        self.index = index
+        self.lib = index.lib
+        cfg = N.ServerConfig(max_batch, max_inflight, max_topk, max_nprobe, max_wait_us,
+                             (searcher_cfg or SearcherConfig()).searcher_vars_bound_m, mem_budget_bytes)
+        self._h = C.c_void_p()
+        N.check(self.lib.saqg_server_create(index._h, C.byref(cfg), C.byref(self._h)))
+
+    def submit(self, query, nprobe: int, topk: int) -> int:
+        q = np.ascontiguousarray(query, np.float32).reshape(-1)
+        t = C.c_uint64()
+        N.check(self.lib.saqg_server_submit(self._h, q.ctypes.data, int(nprobe), int(topk), C.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, topk: int, timeout_ms: int = -1):
+        ids = np.zeros(topk, np.uint32)
+        d = np.zeros(topk, np.float32)
+        lat = C.c_double()
+        N.check(self.lib.saqg_server_wait(self._h, ticket, ids.ctypes.data, d.ctypes.data, C.byref(lat), timeout_ms))
+        return ids, d, lat.value
+
+    def run_trace(self, queries, arrival_s, nprobe, topk):
+        """Open-loop load from native code: query i submitted at arrival_s[i] seconds."""
+        q = np.ascontiguousarray(queries, np.float32)
+        n = q.shape[0]
+        arr = np.ascontiguousarray(arrival_s, np.float64)
+        nps = np.ascontiguousarray(np.broadcast_to(nprobe, (n,)), np.int32)
+        ks = np.ascontiguousarray(np.broadcast_to(topk, (n,)), np.int32)
+        row = int(ks.max())
+        ids = np.zeros((n, row), np.uint32)
+        d = np.full((n, row), np.inf, np.float32)
+        lat = np.zeros(n, np.float64)
+        N.check(self.lib.saqg_server_run_trace(self._h, q.ctypes.data, n, arr.ctypes.data, nps.ctypes.data,
+                                               ks.ctypes.data, row, ids.ctypes.data, d.ctypes.data, lat.ctypes.data))
+        return ids, d, lat
+
+    def stats(self) -> dict:
+        st = N.ServerStats()
+        N.check(self.lib.saqg_server_get_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            N.check(self.lib.saqg_server_free(self._h))
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def convert(src: str, dst: str, format: str = "v2") -> None:
     """Host-only conversion of an index file to `format` ("v2" or "reference")."""
     lib = N.load()
