@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--sigma", type=float, default=0.2)
     ap.add_argument("--noise-alpha", type=float, default=1.6)
     ap.add_argument("--query-clusters", default="uniform", choices=["uniform", "zipf"])
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[20000, 50000, 100000, 200000])
+    ap.add_argument("--serve-seconds", type=float, default=0.3)
     return ap.parse_args()
 
 
@@ -366,6 +368,53 @@ def main():
     lat = np.array(lat)
     plain_qps = P / (lat.sum() / 1e3)
 
+    # ---- uneven batch: per-query nprobe ~ U[16, 256], k in {10, 100} (saqg_search_batch) ----
+    rng = np.random.default_rng(7)
+    np_mix = rng.integers(16, 257, size=B).astype(np.int32)
+    k_mix = rng.choice([10, 100], size=B).astype(np.int32)
+    ids_m = torch.empty((B, 100), dtype=torch.int32, device="cuda")
+    d_m = torch.empty((B, 100), dtype=torch.float32, device="cuda")
+
+    def mixed():
+        N.check(lib.saqg_search_batch(index._h, qdev.data_ptr(), B, np_mix.ctypes.data, k_mix.ctypes.data, 256, 100,
+                                      C.byref(scfg), ids_m.data_ptr(), d_m.data_ptr(), N.SAQG_MEM_DEVICE, sptr, None))
+    mixed()
+    mixed_ms = []
+    for _ in range(max(3, min(10, a.steps // 10))):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        mixed()
+        e1.record(stream)
+        e1.synchronize()
+        mixed_ms.append(e0.elapsed_time(e1))
+    mixed_line = {"qps": B / (float(np.mean(mixed_ms)) / 1e3), "batch": B, "ms_per_batch": float(np.mean(mixed_ms)),
+                  "nprobe": "U[16,256] per query (mean %.0f)" % float(np_mix.mean()), "k": "10 or 100 per query"}
+
+    # ---- serving: Poisson arrivals through the continuous-batching server ----
+    serving = []
+    if a.serve_seconds > 0:
+        srv = ivf.Server(index, max_batch=B, max_inflight=2, max_topk=100, max_nprobe=256, max_wait_us=200)
+        qpool = wl.q.cpu().numpy()
+        for rate in a.serve_rates:
+            n = max(1000, int(rate * a.serve_seconds))
+            arr = np.cumsum(rng.exponential(1.0 / rate, size=n))
+            qs = qpool[np.arange(n) % qpool.shape[0]]
+            nps = rng.integers(16, 257, size=n).astype(np.int32)
+            ks = rng.choice([10, 100], size=n).astype(np.int32)
+            before = srv.stats()
+            t0 = time.perf_counter()
+            _, _, lat_s = srv.run_trace(qs, arr, nps, ks)
+            wall = time.perf_counter() - t0
+            after = srv.stats()
+            nb = after["batches"] - before["batches"]
+            serving.append({"offered_qps": rate, "achieved_qps": n / wall, "queries": n,
+                            "p50_ms": float(np.percentile(lat_s, 50)), "p99_ms": float(np.percentile(lat_s, 99)),
+                            "mean_batch": n / max(1, nb)})
+            log(f"serving {rate}/s: p50 {serving[-1]['p50_ms']:.2f} ms p99 {serving[-1]['p99_ms']:.2f} ms "
+                f"achieved {serving[-1]['achieved_qps']:.0f}/s")
+        srv.close()
+
     # ---- CPU baseline (oracle port) on a bounded sample ----
     cpu = None
     if rank == 0:
@@ -396,6 +445,10 @@ def main():
                      "reranked_per_query": float(np.mean(rr)) / B, "speculative_per_query": float(np.mean(spec)) / B,
                      "probe_ms": float(np.mean(probe_ms)), "qprep_ms": float(np.mean(qprep_ms)),
                      "split_pass_ms": float(np.mean(split_ms))},
+        "uneven_batch": mixed_line,
+        "serving": {"server": "continuous batching, 2 batches in flight, max batch %d" % B,
+                    "nprobe": "U[16,256] per query", "k": "10 or 100 per query", "arrivals": "Poisson",
+                    "rates": serving},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_v, "unit": "queries/s", "h2d_bytes_per_step": B * a.dim * 4,
                 "d2h_bytes_per_step": B * a.topk * 8},
