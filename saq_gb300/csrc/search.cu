@@ -989,22 +989,6 @@ __device__ __forceinline__ bool stages_pass(const float *st, int n, float tau) {
 __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0, int64_t v0, int nb, int n, int t0,
                                 int t_end, float tau) {
     const int S = ix.S, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    // pull the code lines and |o| of the blocks this warp takes in the next tile
-    // of the cluster into L2 while this tile computes
-#pragma unroll
-    for (int k = 0; k < kBlocksPerWarp; ++k) {
-        const int b = t0 + kTileB + w + k * kScanWarps;
-        if (b < nb)
-            for (int s = 0; s < S; ++s) {
-                const SegDev &g = ix.seg[s];
-                const int nc = g.dim / 64;
-                if (g.bits && lane < 2 * nc)
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const char *>(
-                                                                     g.codes + (size_t)(b0 + b) * nc * 32) +
-                                                                 lane * 128));
-                if (lane == 31) asm volatile("prefetch.global.L2 [%0];" ::"l"(g.onorm + (b0 + b) * 32));
-            }
-    }
 #pragma unroll
     for (int k = 0; k < kBlocksPerWarp; ++k) {
         const int slot = w + k * kScanWarps, b = t0 + slot;
@@ -1220,6 +1204,11 @@ __device__ __forceinline__ void replay_block_warp(int S, int bb, const float *cu
     }
 }
 
+// Whether k_scan builds the next cluster's LUT during the last replay of the
+// current one (double-buffered cluster state).  Off: the overlap's extra
+// registers cost more occupancy than the overlap gains.
+constexpr bool kScanOverlap = false;
+
 struct ScanTally {
     unsigned long long blocks = 0, vecs = 0, rr = 0, spec = 0;
 };
@@ -1228,11 +1217,12 @@ struct ScanTally {
 // the pool held in shared memory (pool_size / distk in shared memory).  With
 // a double-buffered layout (sm.lut2 set) the next cluster's state is built by
 // warps 1.. while warp 0 replays the current cluster's last tile.
+template <bool kOverlap>
 __device__ void scan_probes(const DevIndexView &ix, const uint32_t *__restrict__ probe, int p_begin, int p_end,
                             const float *__restrict__ qrot, const float *__restrict__ prune, int topk, ScanSmem &sm,
                             int &pool_size, float &distk, int *err, ScanTally &tl) {
     const int S = ix.S, tid = threadIdx.x;
-    const bool dbuf = sm.lut2 != nullptr;
+    const bool dbuf = kOverlap && sm.lut2 != nullptr;
     if (p_begin >= p_end) return;
     {
         ScanSmem v0 = cluster_view(sm, 0);
@@ -1265,13 +1255,13 @@ __device__ void scan_probes(const DevIndexView &ix, const uint32_t *__restrict__
                     distk = dk;
                     pool_size = sz;
                 }
-            } else if (last && ahead) {
+            } else if (kOverlap && last && ahead) {
                 ScanSmem vn = cluster_view(sm, buf ^ 1);
                 prepare_cluster(ix, qrot, prune, (int)probe[p + 1], vn, 32, 1);
             }
             __syncthreads();
         }
-        if (ahead && nb == 0) {  // an empty cluster: nothing to overlap with
+        if (kOverlap && ahead && nb == 0) {  // an empty cluster: nothing to overlap with
             ScanSmem vn = cluster_view(sm, buf ^ 1);
             prepare_cluster(ix, qrot, prune, (int)probe[p + 1], vn);
         }
@@ -1945,12 +1935,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
     const int qi = blockIdx.x;
     if (deferred && deferred[qi]) return;  // answered by the split pass
     const int np = qsh.np_of(qi), topk = qsh.k_of(qi);
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, qsh.k_max, xstride, true);
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, qsh.k_max, xstride, kScanOverlap);
     __shared__ int pool_size;
     __shared__ float distk;
     ScanTally tl;
     init_pool(sm, topk, pool_size, distk);
-    scan_probes(ix, probe + (size_t)qi * qsh.np_max, 0, np, qrot_all + (size_t)qi * ix.Dtot,
+    scan_probes<kScanOverlap>(ix, probe + (size_t)qi * qsh.np_max, 0, np, qrot_all + (size_t)qi * ix.Dtot,
                 prune_all + (size_t)qi * ix.S, topk, sm, pool_size, distk, err, tl);
     flush_tally(tl, counters);
     write_results(sm, pool_size, topk, qsh.k_max, out_ids + (size_t)qi * qsh.k_max,
@@ -2370,7 +2360,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                     SAQG_CUDA_TRY(cudaEventRecord(C.fork_event(), st));
                     SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, C.fork_event(), 0));
                 }
-                const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs, true);
+                const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs, kScanOverlap);
                 SAQG_REQUIRE(smem_k <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
                 SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_k));
                 k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, qsh, qrot, prune, ids_out, d_out,
@@ -2618,7 +2608,7 @@ void run_search_static(const Index &I, const float *q, int64_t nq, int64_t topk,
     for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
     k_qprep<<<dim3((unsigned)ix.S, (unsigned)nq), 256, qsm, st>>>(ix, q, m, qrot, prune);
     check_launch("k_qprep");
-    const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xstride_of(ix), true);
+    const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xstride_of(ix), kScanOverlap);
     SAQG_REQUIRE(smem_k <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
     SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_k));
     QueryShape qsh;
