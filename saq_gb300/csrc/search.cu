@@ -366,8 +366,8 @@ __global__ void __launch_bounds__(kSelThreads) k_probe_select(const float *__res
 // equal distances among its first nprobe + 1 (where the standard library's
 // heap order decides), a non-finite value or more than kShortCap centroids on
 // its shortlist is ranked by the full exact path instead.
-constexpr int kShortThreads = 1024;
-constexpr int kShortCap = 4096;
+constexpr int kShortThreads = 512;
+constexpr int kShortCap = 1024;  // shortlist capacity (more: the full exact path); keeps 2 CTAs per SM
 constexpr int kGemmMinQueries = 64;  // smaller calls rank with the exact kernels directly
 
 constexpr int kShortKeys = 16384;    // clusters whose upper-bound keys the shortlist keeps in shared memory
