@@ -678,7 +678,7 @@ __device__ __forceinline__ void pool_insert(uint32_t *ids, float *d, int &size, 
 constexpr int kQprepQT = 16;
 __global__ void __launch_bounds__(256) k_qprep_tiled(DevIndexView ix, const float *__restrict__ q, int nq, float m,
                                                      float *__restrict__ qrot, float *__restrict__ prune) {
-    extern __shared__ float cqs[];  // [kQprepQT][dim]
+    extern __shared__ __align__(16) float cqs[];  // [kQprepQT][dim]
     const int s = blockIdx.x, q0 = blockIdx.y * kQprepQT, nqt = min(kQprepQT, nq - q0);
     const SegDev &g = ix.seg[s];
     const int dim = g.dim, qoff = g.qoff;
@@ -708,11 +708,18 @@ __global__ void __launch_bounds__(256) k_qprep_tiled(DevIndexView ix, const floa
         for (int j2 = 0; j2 < dim; j2 += bc) {
 #pragma unroll
             for (int t = 0; t < kQprepQT; ++t) c[t] = 0.0f;
-            const int je = min(j2 + bc, dim);
-            for (int j = j2; j < je; ++j) {
-                const float pv = g.P[(size_t)j * dim + i];
+            const int je = min(j2 + bc, dim);  // dims are multiples of 64: blocks split into groups of 4
+            for (int j = j2; j < je; j += 4) {
+                const float p0 = g.P[(size_t)j * dim + i], p1 = g.P[(size_t)(j + 1) * dim + i];
+                const float p2 = g.P[(size_t)(j + 2) * dim + i], p3 = g.P[(size_t)(j + 3) * dim + i];
 #pragma unroll
-                for (int t = 0; t < kQprepQT; ++t) c[t] = fmaf(pv, cqs[t * dim + j], c[t]);
+                for (int t = 0; t < kQprepQT; ++t) {
+                    const float4 v = *reinterpret_cast<const float4 *>(cqs + t * dim + j);
+                    c[t] = fmaf(p0, v.x, c[t]);
+                    c[t] = fmaf(p1, v.y, c[t]);
+                    c[t] = fmaf(p2, v.z, c[t]);
+                    c[t] = fmaf(p3, v.w, c[t]);
+                }
             }
 #pragma unroll
             for (int t = 0; t < kQprepQT; ++t) res[t] = fmaf(c[t], 1.0f, res[t]);
@@ -1797,6 +1804,7 @@ __device__ __forceinline__ bool record_effect(int S, const float *rec, float dk,
 }
 
 constexpr int kReplayRecs = 32;  // records per staged chunk (double-buffered)
+constexpr int kReplayPer = 4;    // scan positions per thread in a window
 
 // Per query on the list: walk its scan positions in order, kScanThreads at a
 // time.  A record can matter only if a candidate estimate lies below distk and
@@ -1819,7 +1827,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, S
     float *stage_buf = reinterpret_cast<float *>(smem_raw + scan_smem_bytes(ix.Dtot, S, k_max, xstride));
     __shared__ int pool_size;
     __shared__ float distk;
-    __shared__ int list[kScanThreads];
+    __shared__ int list[kScanThreads * kReplayPer];
     __shared__ int warp_cnt[kScanWarps];
     __shared__ int eff[kReplayRecs], cnt[kReplayRecs];
     __shared__ int s_next;
@@ -1838,23 +1846,38 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, S
     const int RW = st.rec_words, R16 = RW / 4;
     unsigned long long rr = 0;
     __syncthreads();
-    for (int base = 0; base < np; base += kScanThreads) {
-        const int pos = base + tid;
+    for (int base = 0; base < np; base += kScanThreads * kReplayPer) {
+        // thread t tests positions base + kReplayPer t .. + kReplayPer - 1; a
+        // block-wide prefix of the counts keeps the list in position order
+        const int p0 = base + kReplayPer * tid;
         const float dk0 = distk;
-        bool f = false;
-        if (pos < np) {
-            const float2 v = su[pos];
-            f = v.x < dk0 && !(v.y > dk0);
+        bool f[kReplayPer];
+        int mine = 0;
+#pragma unroll
+        for (int r = 0; r < kReplayPer; ++r) {
+            f[r] = false;
+            if (p0 + r < np) {
+                const float2 v = su[p0 + r];
+                f[r] = v.x < dk0 && !(v.y > dk0);
+            }
+            mine += f[r];
         }
-        const uint32_t bal = __ballot_sync(kFull, f);
-        if (lane == 0) warp_cnt[w] = __popc(bal);
+        int incl = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) warp_cnt[w] = incl;
         __syncthreads();
-        int off = 0, total = 0;
+        int off = incl - mine, total = 0;
         for (int i = 0; i < kScanWarps; ++i) {
             if (i < w) off += warp_cnt[i];
             total += warp_cnt[i];
         }
-        if (f) list[off + __popc(bal & ((1u << lane) - 1))] = pos;
+#pragma unroll
+        for (int r = 0; r < kReplayPer; ++r)
+            if (f[r]) list[off++] = p0 + r;
         __syncthreads();
         const int nch = (total + kReplayRecs - 1) / kReplayRecs;
         auto issue = [&](int k) {
