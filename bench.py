@@ -368,6 +368,26 @@ def main():
     lat = np.array(lat)
     plain_qps = P / (lat.sum() / 1e3)
 
+    # ---- plain single query through a captured graph (query copied into the bound buffer) ----
+    gq = torch.empty((1, a.dim), dtype=torch.float32, device="cuda")
+    gq.copy_(qp[0:1])
+    gids = torch.empty((1, a.topk), dtype=torch.int32, device="cuda")
+    gd = torch.empty((1, a.topk), dtype=torch.float32, device="cuda")
+    graph = C.c_void_p()
+    N.check(lib.saqg_search_graph_create(index._h, gq.data_ptr(), 1, a.topk, nprobe, C.byref(scfg), gids.data_ptr(),
+                                         gd.data_ptr(), sptr, C.byref(graph)))
+    glat = []
+    for i in range(P):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        gq.copy_(qp[i:i + 1])
+        N.check(lib.saqg_search_graph_launch(graph, sptr))
+        e1.record(stream)
+        e1.synchronize()
+        glat.append(e0.elapsed_time(e1))
+    N.check(lib.saqg_search_graph_free(graph))
+    glat = np.array(glat)
+
     # ---- uneven batch: per-query nprobe ~ U[16, 256], k in {10, 100} (saqg_search_batch) ----
     rng = np.random.default_rng(7)
     np_mix = rng.integers(16, 257, size=B).astype(np.int32)
@@ -434,7 +454,10 @@ def main():
         "batched": {"qps": value, "batch": B, "p50_ms": float(np.median(step_ms)),
                     "p99_ms": float(np.percentile(step_ms, 99)), f"recall@{a.topk}": round(batch_recall, 4)},
         "plain": {"qps": plain_qps, "queries": P, "p50_ms": float(np.median(lat)),
-                  "p99_ms": float(np.percentile(lat, 99))},
+                  "p99_ms": float(np.percentile(lat, 99)),
+                  "graph": {"qps": P / (glat.sum() / 1e3), "p50_ms": float(np.median(glat)),
+                            "p99_ms": float(np.percentile(glat, 99)),
+                            "note": "saqg_search_graph_launch of a captured single-query search"}},
         "batched_over_plain": value / world / plain_qps,
         "p99_ms": float(np.percentile(lat, 99)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,

@@ -180,6 +180,21 @@ int saqg_search_batch(const saqg_index *index, const float *queries, int64_t nq,
                       const int32_t *topk_per_query, int64_t nprobe, int64_t topk, const saqg_searcher_config *cfg,
                       uint32_t *ids, float *dists, int mem, void *stream, saqg_search_stats *stats);
 
+/* ---- graph-captured search ---------------------------------------------- */
+/* No counterpart in the reference: saqg_search for a fixed shape (nq, topk,
+ * nprobe) on device buffers, captured into a CUDA graph.  Creation runs the
+ * search twice on `stream` (a warm-up, then the capture), so `queries` must
+ * hold valid data; each saqg_search_graph_launch then replays every kernel and
+ * copy with one call, reading `queries` and writing `ids` / `dists` (bound at
+ * creation; update the queries in place between launches).  Results equal
+ * saqg_search's.  Launches of one graph must not overlap. */
+typedef struct saqg_search_graph saqg_search_graph;
+int saqg_search_graph_create(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
+                             const saqg_searcher_config *cfg, uint32_t *ids, float *dists, void *stream,
+                             saqg_search_graph **out);
+int saqg_search_graph_launch(saqg_search_graph *graph, void *stream);
+int saqg_search_graph_free(saqg_search_graph *graph);
+
 /* ---- serving ----------------------------------------------------------- */
 /* No counterpart in the reference (its drivers call IVF::search from a thread
  * pool): a serving loop with continuous batching on one index.  Submitted

@@ -89,6 +89,10 @@ EXPORTS = {
                                     C.c_void_p]),
     "saqg_search_static": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig), C.c_void_p,
                                      C.c_void_p, C.c_void_p]),
+    "saqg_search_graph_create": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig),
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "saqg_search_graph_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "saqg_search_graph_free": (C.c_int, [C.c_void_p]),
     "saqg_server_create": (C.c_int, [C.c_void_p, C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
     "saqg_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_uint64)]),
     "saqg_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.POINTER(C.c_double),

@@ -45,6 +45,10 @@ struct saqg_server {
     Server *impl;
 };
 
+struct saqg_search_graph {
+    SearchGraph *impl;
+};
+
 extern "C" {
 
 int saqg_version(void) { return 1; }
@@ -166,6 +170,34 @@ int saqg_search_static(const saqg_index *index, const float *queries, int64_t nq
         SAQG_REQUIRE(!cfg || cfg->dist_type == SAQG_DIST_L2, "only L2 search is supported");
         const float m = cfg ? cfg->searcher_vars_bound_m : 4.0f;
         run_search_static(*index->impl, queries, nq, topk, nprobe, m, ids, dists, (cudaStream_t)stream);
+    });
+}
+
+int saqg_search_graph_create(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
+                             const saqg_searcher_config *cfg, uint32_t *ids, float *dists, void *stream,
+                             saqg_search_graph **out) {
+    return guarded([&] {
+        SAQG_REQUIRE(index && queries && ids && out, "null argument");
+        SAQG_REQUIRE(!cfg || cfg->dist_type == SAQG_DIST_L2, "only L2 search is supported");
+        *out = nullptr;
+        const float m = cfg ? cfg->searcher_vars_bound_m : 4.0f;
+        SearchGraph *g = graph_create(*index->impl, nq, topk, nprobe, m, queries, ids, dists, (cudaStream_t)stream);
+        *out = new saqg_search_graph{g};
+    });
+}
+
+int saqg_search_graph_launch(saqg_search_graph *graph, void *stream) {
+    return guarded([&] {
+        SAQG_REQUIRE(graph, "null argument");
+        graph_launch(graph->impl, (cudaStream_t)stream);
+    });
+}
+
+int saqg_search_graph_free(saqg_search_graph *graph) {
+    return guarded([&] {
+        if (!graph) return;
+        graph_free(graph->impl);
+        delete graph;
     });
 }
 

@@ -105,6 +105,7 @@ SearchCtx::~SearchCtx() {
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
     if (blas) cublasDestroy(static_cast<cublasHandle_t>(blas));
+    if (blas_ws) cudaFree(blas_ws);
 }
 
 void *Index::dalloc(size_t bytes) {

@@ -87,6 +87,8 @@ struct SearchCtx {
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     void *blas = nullptr;
+    void *blas_ws = nullptr;  // cuBLAS workspace owned by the context (graph capture needs one)
+    size_t blas_ws_bytes = 0;
     SearchCtx() = default;
     SearchCtx(const SearchCtx &) = delete;
     SearchCtx &operator=(const SearchCtx &) = delete;
@@ -156,6 +158,13 @@ void run_search_static(const Index &idx, const float *q, int64_t nq, int64_t top
                        uint32_t *ids, float *dists, cudaStream_t stream);
 int64_t run_estimate(const Index &idx, const float *q_host, int64_t nprobe, float m, uint32_t *ids, float *acc,
                      float *fast, float *vars, int64_t cap);
+
+// graph.cpp
+struct SearchGraph;
+SearchGraph *graph_create(const Index &idx, int64_t nq, int64_t topk, int64_t nprobe, float m, const float *q_dev,
+                          uint32_t *ids_dev, float *dists_dev, cudaStream_t st);
+void graph_launch(SearchGraph *g, cudaStream_t st);
+void graph_free(SearchGraph *g);
 
 // serve.cpp
 struct Server;

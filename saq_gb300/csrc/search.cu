@@ -2204,6 +2204,12 @@ void presize_ctx(const Index &I, SearchCtx &C, int64_t nq, int64_t topk, int64_t
         blas_try(cublasCreate(&h), "cublasCreate");
         C.blas = h;
     }
+    if (!C.blas_ws) {  // a workspace of its own: cuBLAS then allocates nothing inside a call
+        C.blas_ws_bytes = 32u << 20;
+        SAQG_CUDA_TRY(cudaMalloc(&C.blas_ws, C.blas_ws_bytes));
+        blas_try(cublasSetWorkspace(static_cast<cublasHandle_t>(C.blas), C.blas_ws, C.blas_ws_bytes),
+                 "cublasSetWorkspace");
+    }
 }
 
 size_t search_bytes_estimate(const Index &I, int64_t nq, int64_t topk, int64_t nprobe) {
