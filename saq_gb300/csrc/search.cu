@@ -671,6 +671,53 @@ __device__ __forceinline__ void pool_insert(uint32_t *ids, float *d, int &size, 
     size += (size < cap);
 }
 
+// k_qprep for a few queries, spread for latency: in Eigen's GEMV order the
+// 16-input block sums c_b of an output are independent (only their fold
+// res = fma(c_b, 1, res) runs in block order), so a CTA takes 32 outputs of
+// one (segment, query), its warps compute the block sums (lane = output, a
+// 16-step chain each), and warp 0 folds them in order.  Bit-identical to
+// k_qprep; the prune bound comes from the CTA holding the first 32 outputs.
+constexpr int kQprepOut = 32;
+__global__ void __launch_bounds__(256) k_qprep_small(DevIndexView ix, const float *__restrict__ q, float m,
+                                                     float *__restrict__ qrot, float *__restrict__ prune) {
+    extern __shared__ __align__(16) float qsm[];  // [dim] query slice, then [dim / 16][32] block sums
+    const int s = blockIdx.x, qi = blockIdx.y, o0 = blockIdx.z * kQprepOut;
+    const SegDev &g = ix.seg[s];
+    const int dim = g.dim, qoff = g.qoff;
+    if (o0 >= dim) return;
+    float *cq = qsm, *part = qsm + dim;
+    for (int i = threadIdx.x; i < dim; i += blockDim.x) {
+        const int gi = qoff + i;
+        cq[i] = gi < ix.D ? q[(size_t)qi * ix.D + gi] : 0.0f;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, i = o0 + lane;
+    if (blockIdx.z == 0 && warp == 1) {
+        const float *var = ix.var + qoff;
+        const float v2 = warp_eigen_sum(dim, [&](int e) { return __fmul_rn(var[e], __fmul_rn(cq[e], cq[e])); });
+        if (lane == 0) prune[(size_t)qi * ix.S + s] = __fmul_rn(sqrtf(v2), m);
+    }
+    float *out = qrot + (size_t)qi * ix.Dtot + qoff;
+    if (!g.P) {
+        if (warp == 0 && i < dim) out[i] = cq[i];
+        return;
+    }
+    const int bc = dim < 128 ? dim : 16, nbk = (dim + bc - 1) / bc;
+    for (int b = warp; b < nbk; b += blockDim.x >> 5) {
+        float c = 0.0f;
+        const int j2 = b * bc, je = min(j2 + bc, dim);
+        if (i < dim)
+            for (int j = j2; j < je; ++j) c = fmaf(g.P[(size_t)j * dim + i], cq[j], c);
+        part[b * kQprepOut + lane] = c;
+    }
+    __syncthreads();
+    if (warp == 0 && i < dim) {
+        float res = 0.0f;
+        for (int b = 0; b < nbk; ++b) res = fmaf(part[b * kQprepOut + lane], 1.0f, res);
+        out[i] = res;
+    }
+}
+
 // k_qprep for a tile of kQprepQT queries per CTA: each P element is read once
 // for the whole tile and drives kQprepQT independent chains, each in exactly
 // k_qprep's order (so the outputs are bit-identical); L2 traffic for the
@@ -1569,6 +1616,7 @@ struct SplitState {
     int64_t pos_cap;
     int rec_words;
     QueryShape qsh;      // per-query nprobe and k (strides np_max, k_max)
+    int first_blocks;    // exact prefix: at least this many blocks, and a full pool
 };
 
 __host__ __device__ inline int rec_words_of(int S) { return (8 + (S + 1) + 32 + 32 * S + 3) & ~3; }
@@ -1602,7 +1650,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
         const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
         bool prepared = false;
         for (int t0 = 0; t0 < nb; t0 += kTileB) {
-            if (tl.blocks >= kFirstBlocks && pool_size == topk) {
+            if (tl.blocks >= st.first_blocks && pool_size == topk) {
                 sp_p = p;
                 sp_b = t0;
                 break;
@@ -2323,8 +2371,12 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                             st>>>(ix, qin, (int)nq, m, qrot, prune);
             check_launch("k_qprep_tiled");
         } else {
-            k_qprep<<<dim3((unsigned)ix.S, (unsigned)nq), 256, qsm, st>>>(ix, qin, m, qrot, prune);
-            check_launch("k_qprep");
+            int dmax = 0;
+            for (int s = 0; s < ix.S; ++s) dmax = std::max(dmax, ix.seg[s].dim);
+            const size_t sm_small = 4 * ((size_t)dmax + (size_t)(dmax / 16 + 1) * kQprepOut);
+            k_qprep_small<<<dim3((unsigned)ix.S, (unsigned)nq, (unsigned)((dmax + kQprepOut - 1) / kQprepOut)), 256,
+                            sm_small, st>>>(ix, qin, m, qrot, prune);
+            check_launch("k_qprep_small");
         }
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[2], st));
         const int xs = xstride_of(ix);
@@ -2370,6 +2422,9 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             ss.rec_words = rec_words_of(ix.S);
             ss.rec = sb.take<float>((size_t)pos_cap * ss.rec_words);
             ss.qsh = qsh;
+            // heavy queries beside a batch: a longer prefix for a tighter bound; a
+            // few queries alone: the speculative part has the GPU, so only the pool must fill
+            ss.first_blocks = mode == 0 ? kFirstBlocks : 1;
             uint8_t *deferred = sb.take<uint8_t>(nq);
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.summ, 0xff, 8 * (size_t)pos_cap, st));  // NaN: no record
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 16, st));
