@@ -333,15 +333,33 @@ __global__ void __launch_bounds__(kSelThreads) k_probe_select(const float *__res
                 if (parent == 0) break;
             }
     }
+    // the heap's top only shrinks, so an element not below the top at its
+    // chunk's start is skipped at its own turn too: each chunk is filtered in
+    // parallel against that top and thread 0 runs the steps on the rest, in order
+    __shared__ int s_wcnt[kSelThreads / 32];
+    __shared__ int s_list[kSelThreads];
+    const int lane = tid & 31, wp = tid >> 5;
     for (int base = mid; base < K; base += kSelThreads) {
         __syncthreads();
-        if (base + tid < K) chunk[tid] = dq[base + tid];
+        const float top = heap[0].d;
+        const float v = base + tid < K ? dq[base + tid] : 0.0f;
+        const bool in = base + tid < K && v < top;
+        const uint32_t bal = __ballot_sync(kFull, in);
+        if (lane == 0) s_wcnt[wp] = __popc(bal);
+        chunk[tid] = v;
         __syncthreads();
-        if (tid == 0) {
-            const int n = min(kSelThreads, K - base);
-            for (int j = 0; j < n; ++j)
-                if (chunk[j] < heap[0].d) heap_adjust(heap, 0, mid, Cand{(uint32_t)(base + j), chunk[j]});
+        int off = 0, total = 0;
+        for (int i = 0; i < kSelThreads / 32; ++i) {
+            if (i < wp) off += s_wcnt[i];
+            total += s_wcnt[i];
         }
+        if (in) s_list[off + __popc(bal & ((1u << lane) - 1))] = tid;
+        __syncthreads();
+        if (tid == 0)
+            for (int r = 0; r < total; ++r) {
+                const int j = s_list[r];
+                if (chunk[j] < heap[0].d) heap_adjust(heap, 0, mid, Cand{(uint32_t)(base + j), chunk[j]});
+            }
     }
     if (tid == 0) {
         for (long last = mid; last > 1;) {
