@@ -998,7 +998,10 @@ __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict_
 // Estimates of one block (this warp, lane = vector).  Fills cd/ipx for every
 // segment and, for several segments, the running sum and the pruning-stage
 // minima of SAQSearcher::searchCluster steps 1-2 (saq_searcher.hpp:87-132).
-__device__ void block_estimates(const DevIndexView &ix, int64_t gb, ScanSmem &sm, int w, int lane) {
+// Like the reference, it stops at the first stage whose minimum exceeds the
+// bound `tau` (>= every distk the block will meet): such a block has no
+// candidate lanes, so the later segments' estimates would never be read.
+__device__ void block_estimates(const DevIndexView &ix, int64_t gb, ScanSmem &sm, int w, int lane, float tau) {
     const int S = ix.S;
     if (S == 1) {
         const SegDev &g = ix.seg[0];
@@ -1022,7 +1025,7 @@ __device__ void block_estimates(const DevIndexView &ix, int64_t gb, ScanSmem &sm
     float mi = warp_min_tree(cur);
     if (lane == 0) sm.stage[w * (S + 1) + k] = mi;
     ++k;
-    for (int s = 0; s < S; ++s) {
+    for (int s = 0; s < S && !(mi > tau); ++s) {  // mi is warp-uniform
         const SegDev &g = ix.seg[s];
         if (!g.bits) continue;
         const float on = g.onorm[gb * 32 + lane];
@@ -1064,7 +1067,7 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
 #pragma unroll
     for (int k = 0; k < kBlocksPerWarp; ++k) {
         const int slot = w + k * kScanWarps, b = t0 + slot;
-        if (b < t_end) block_estimates(ix, b0 + b, sm, slot, lane);
+        if (b < t_end) block_estimates(ix, b0 + b, sm, slot, lane, tau);
     }
     __syncthreads();
 #pragma unroll
