@@ -1612,7 +1612,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_scan_warp(DevIndexView ix
 // reference's decisions on the records.  Blocks without a record cannot insert
 // anything (none of their lanes is below tau1 >= distk), so the replay is exact.
 constexpr int kTileBlocks = 16;
-constexpr int kFirstBlocks = 16;
+constexpr int kFirstBlocks = 384;  // exact prefix of a deferred query (its distk bounds the speculation)
 constexpr int kDeferBlocks = 1024;  // a query scanning more blocks than this takes the split pass
                                      // (SAQG_DEFER_BLOCKS overrides it; 0 disables deferral)
 
@@ -2446,6 +2446,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             // heavy queries beside a batch: a longer prefix for a tighter bound; a
             // few queries alone: the speculative part has the GPU, so only the pool must fill
             ss.first_blocks = mode == 0 ? kFirstBlocks : 1;
+            if (const char *e = std::getenv("SAQG_FIRST_BLOCKS")) ss.first_blocks = std::max(1, std::atoi(e));
             uint8_t *deferred = sb.take<uint8_t>(nq);
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.summ, 0xff, 8 * (size_t)pos_cap, st));  // NaN: no record
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 16, st));
