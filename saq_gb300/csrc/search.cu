@@ -19,6 +19,7 @@
 //                  (saq_searcher.hpp:68-214) and the ResultPool inserts
 //                  (utils/pool.hpp:17-30) exactly in the reference's order.
 #include <cfloat>
+#include <climits>
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -1612,7 +1613,10 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_scan_warp(DevIndexView ix
 // reference's decisions on the records.  Blocks without a record cannot insert
 // anything (none of their lanes is below tau1 >= distk), so the replay is exact.
 constexpr int kTileBlocks = 16;
-constexpr int kFirstBlocks = 384;  // exact prefix of a deferred query (its distk bounds the speculation)
+constexpr int kFirstBlocks = 16;  // exact prefix of a deferred query (its distk bounds the first level)
+// Levels of the speculation for deferred queries, in tiles after the split
+// point: [0, 8), [8, 64), [64, end).
+constexpr int kSpecLevels[] = {0, 8, 64};
 constexpr int kDeferBlocks = 1024;  // a query scanning more blocks than this takes the split pass
                                      // (SAQG_DEFER_BLOCKS overrides it; 0 disables deferral)
 
@@ -1638,7 +1642,27 @@ struct SplitState {
     int rec_words;
     QueryShape qsh;      // per-query nprobe and k (strides np_max, k_max)
     int first_blocks;    // exact prefix: at least this many blocks, and a full pool
+    // the level being speculated and replayed: tiles [t_lo, t_hi) after the split
+    // point of each query (distk at the level's start bounds its speculation)
+    int t_lo, t_hi;
+    int final_level;     // the last level writes the results, the others the pool
 };
+
+// Scan-order position of the first block of tile t after a query's split
+// point (npos when t is past its last tile).
+__device__ __forceinline__ int tile_pos(const SplitState &st, int slot, int t) {
+    const int npm = st.qsh.np_max;
+    const int *to = st.tile_off + (size_t)slot * (npm + 1);
+    if (t >= to[npm]) return st.npos[slot];
+    int lo = 0, hi = npm;  // probe: last p with to[p] <= t
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (to[mid] <= t) lo = mid;
+        else hi = mid;
+    }
+    const int first = lo == st.split_p[slot] ? st.split_b[slot] : 0;
+    return st.blk_base[(size_t)slot * npm + lo] + first + (t - to[lo]) * kTileBlocks;
+}
 
 __host__ __device__ inline int rec_words_of(int S) { return (8 + (S + 1) + 32 + 32 * S + 3) & ~3; }
 
@@ -1728,6 +1752,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
     }
 }
 
+// Work offsets of the level's tiles: slot q holds tiles [t_lo, t_hi) of its own.
 __global__ void k_tile_prefix(SplitState st) {
     const int nprobe = st.qsh.np_max;
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -1735,7 +1760,8 @@ __global__ void k_tile_prefix(SplitState st) {
     int acc = 0;
     for (int q = 0; q < n; ++q) {
         st.q_tile_off[q] = acc;
-        acc += st.tile_off[(size_t)q * (nprobe + 1) + nprobe];
+        const int nt = st.tile_off[(size_t)q * (nprobe + 1) + nprobe];
+        acc += max(0, min(nt, st.t_hi) - min(nt, st.t_lo));
     }
     st.q_tile_off[n] = acc;
 }
@@ -1762,7 +1788,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
             else hi = mid;
         }
         const int slot = lo, q = st.qlist[slot];
-        const int local = wi - st.q_tile_off[slot];
+        const int local = st.t_lo + (wi - st.q_tile_off[slot]);
         const int *to = st.tile_off + (size_t)slot * (nprobe + 1);
         int plo = 0, phi = nprobe;  // probe: last p with to[p] <= local
         while (phi - plo > 1) {
@@ -1899,7 +1925,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, S
     __shared__ int list[kScanThreads * kReplayPer];
     __shared__ int warp_cnt[kScanWarps];
     __shared__ int eff[kReplayRecs], cnt[kReplayRecs];
-    __shared__ int s_next;
+    __shared__ int s_next, s_plo, s_phi;
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     for (int i = tid; i < topk; i += blockDim.x) {
         sm.pool_id[i] = st.pool_id[(size_t)slot * k_max + i];
@@ -1908,6 +1934,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, S
     if (tid == 0) {
         pool_size = st.pool_size[slot];
         distk = st.tau[slot];
+        s_plo = tile_pos(st, slot, st.t_lo);  // this level's scan positions
+        s_phi = tile_pos(st, slot, st.t_hi);
     }
     const int np = st.npos[slot];
     const float2 *su = st.summ + st.pos_off[slot];
@@ -1915,7 +1943,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, S
     const int RW = st.rec_words, R16 = RW / 4;
     unsigned long long rr = 0;
     __syncthreads();
-    for (int base = 0; base < np; base += kScanThreads * kReplayPer) {
+    const int pos_end = min(np, s_phi);
+    for (int base = s_plo; base < pos_end; base += kScanThreads * kReplayPer) {
         // thread t tests positions base + kReplayPer t .. + kReplayPer - 1; a
         // block-wide prefix of the counts keeps the list in position order
         const int p0 = base + kReplayPer * tid;
@@ -1925,7 +1954,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, S
 #pragma unroll
         for (int r = 0; r < kReplayPer; ++r) {
             f[r] = false;
-            if (p0 + r < np) {
+            if (p0 + r < pos_end) {
                 const float2 v = su[p0 + r];
                 f[r] = v.x < dk0 && !(v.y > dk0);
             }
@@ -2012,7 +2041,19 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, S
     }
     __syncthreads();
     if (tid == 0 && counters) atomicAdd(counters + 2, rr);
-    write_results(sm, pool_size, topk, k_max, out_ids + (size_t)qi * k_max, out_d ? out_d + (size_t)qi * k_max : nullptr);
+    if (st.final_level) {
+        write_results(sm, pool_size, topk, k_max, out_ids + (size_t)qi * k_max,
+                      out_d ? out_d + (size_t)qi * k_max : nullptr);
+    } else {  // the pool and its distk carry over to the next level
+        for (int i = tid; i < topk; i += blockDim.x) {
+            st.pool_id[(size_t)slot * k_max + i] = sm.pool_id[i];
+            st.pool_d[(size_t)slot * k_max + i] = sm.pool_d[i];
+        }
+        if (tid == 0) {
+            st.pool_size[slot] = pool_size;
+            st.tau[slot] = distk;
+        }
+    }
 }
 
 // One CTA per query: the whole probe list sequentially (queries deferred to
@@ -2446,6 +2487,9 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             // heavy queries beside a batch: a longer prefix for a tighter bound; a
             // few queries alone: the speculative part has the GPU, so only the pool must fill
             ss.first_blocks = mode == 0 ? kFirstBlocks : 1;
+            ss.t_lo = 0;
+            ss.t_hi = INT_MAX;
+            ss.final_level = 1;
             if (const char *e = std::getenv("SAQG_FIRST_BLOCKS")) ss.first_blocks = std::max(1, std::atoi(e));
             uint8_t *deferred = sb.take<uint8_t>(nq);
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.summ, 0xff, 8 * (size_t)pos_cap, st));  // NaN: no record
@@ -2481,19 +2525,28 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
             k_scan_first<<<(unsigned)cap, kScanThreads, smem, sp>>>(ix, probe, qrot, prune, ss, flags + 1, cnt, xs);
             check_launch("k_scan_first");
-            k_tile_prefix<<<1, 32, 0, sp>>>(ss);
-            check_launch("k_tile_prefix");
             if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[5], sp));
             int dev = 0, sms = 0, per_sm = 0;
             SAQG_CUDA_TRY(cudaGetDevice(&dev));
             SAQG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
             SAQG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scan_spec, kScanThreads, smem1));
             const unsigned grid = (unsigned)std::max(1, sms * std::max(1, per_sm));
-            k_scan_spec<<<grid, kScanThreads, smem1, sp>>>(ix, probe, (int)nprobe, qrot, prune, ss, cnt, xs);
-            check_launch("k_scan_spec");
-            if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[6], sp));
-            k_scan_replay<<<(unsigned)cap, kScanThreads, smem_r, sp>>>(ix, ss, ids_out, d_out, cnt, xs);
-            check_launch("k_scan_replay");
+            // levels of speculation (tiles after the split point): each level's
+            // replay leaves the exact pool, whose distk bounds the next level
+            const int nlev = mode == 0 ? (int)(sizeof(kSpecLevels) / sizeof(kSpecLevels[0])) : 1;
+            for (int L = 0; L < nlev; ++L) {
+                SplitState sl = ss;
+                sl.t_lo = mode == 0 ? kSpecLevels[L] : 0;
+                sl.t_hi = L + 1 < nlev ? kSpecLevels[L + 1] : INT_MAX;
+                sl.final_level = L + 1 == nlev;
+                k_tile_prefix<<<1, 32, 0, sp>>>(sl);
+                check_launch("k_tile_prefix");
+                k_scan_spec<<<grid, kScanThreads, smem1, sp>>>(ix, probe, (int)nprobe, qrot, prune, sl, cnt, xs);
+                check_launch("k_scan_spec");
+                if (stats && sl.final_level) SAQG_CUDA_TRY(cudaEventRecord(ev[6], sp));
+                k_scan_replay<<<(unsigned)cap, kScanThreads, smem_r, sp>>>(ix, sl, ids_out, d_out, cnt, xs);
+                check_launch("k_scan_replay");
+            }
             if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[4], sp));
             if (sp != st) {  // join
                 SAQG_CUDA_TRY(cudaEventRecord(C.join_event(), sp));
