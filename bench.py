@@ -279,6 +279,7 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     step_ms, scan_ms, fast_b, rr_b, spec, rr, probe_ms, qprep_ms, split_ms = [], [], [], [], [], [], [], [], []
+    vec_counts = []
     launches0 = lib.saqg_kernel_launches()
     with ClockSampler(local) as clk:
         time.sleep(0.3)  # first sample before the timed region
@@ -299,6 +300,7 @@ def main():
             rr_b.append(stats.rerank_bytes)
             spec.append(stats.speculative)
             rr.append(stats.reranked)
+            vec_counts.append(stats.vectors)
         torch.cuda.synchronize()
     launches = lib.saqg_kernel_launches() - launches0
     tot_ms = float(sum(step_ms))
@@ -322,6 +324,10 @@ def main():
     compulsory = int((nblk[distinct] * 32 * per_lane).sum() + len(distinct) * 4 * a.dim + rr_b[-1])
     effective = fast_b[-1] + rr_b[-1]
     mean_scan = float(np.mean(scan_ms))
+    coded_dims = sum(d for d, b in info["plan"] if b)
+    lookups = float(np.mean(vec_counts)) * coded_dims / 4
+    props = torch.cuda.get_device_properties(local)
+    lookup_peak = props.multi_processor_count * 32 * 2070e6  # 32 lanes x SMs x max SM clock
     hbm, peak_kind = peaks()
     achieved = compulsory / (mean_scan / 1e3) / 1e9
     traffic = None
@@ -467,7 +473,12 @@ def main():
                      "effective_gbs": effective / (mean_scan / 1e3) / 1e9, "scan_ms": mean_scan,
                      "reranked_per_query": float(np.mean(rr)) / B, "speculative_per_query": float(np.mean(spec)) / B,
                      "probe_ms": float(np.mean(probe_ms)), "qprep_ms": float(np.mean(qprep_ms)),
-                     "split_pass_ms": float(np.mean(split_ms))},
+                     "split_pass_ms": float(np.mean(split_ms)),
+                     # what bounds the scan: one shared-memory LUT lookup per 4 coded dims per
+                     # (query, vector); peak one 32-lane lookup per SM per cycle
+                     "lut_lookups_per_s": lookups / (mean_scan / 1e3),
+                     "lut_lookup_peak_per_s": lookup_peak,
+                     "lut_lookup_frac": lookups / (mean_scan / 1e3) / lookup_peak},
         "uneven_batch": mixed_line,
         "serving": {"server": "continuous batching, 2 batches in flight, max batch %d" % B,
                     "nprobe": "U[16,256] per query", "k": "10 or 100 per query", "arrivals": "Poisson",
