@@ -64,7 +64,148 @@ def parse():
     ap.add_argument("--query-clusters", default="uniform", choices=["uniform", "zipf"])
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[20000, 50000, 100000, 200000])
     ap.add_argument("--serve-seconds", type=float, default=0.3)
+    ap.add_argument("--tc-shortlist", type=int, default=40)
+    ap.add_argument("--precision-bits", type=int, nargs="*", default=[6, 8])
+    ap.add_argument("--precision-n", type=int, default=1_000_000)
+    ap.add_argument("--precision-dim", type=int, default=1536)
+    ap.add_argument("--precision-clusters", type=int, default=4096)
+    ap.add_argument("--precision-nprobe", type=int, default=32)
+    ap.add_argument("--precision-batches", type=int, nargs="*", default=[256, 2048])
     return ap.parse_args()
+
+
+def bf16_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
+def time_calls(torch, fn, flush, steps, warmup=2):
+    """Mean ms of `fn` on the current stream (CUDA events, L2 flushed before each call)."""
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        fn()
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return float(np.mean(ms)), ms
+
+
+def overlap(a_ids, b_ids, k):
+    hit = 0
+    for x, y in zip(a_ids, b_ids):
+        hit += len(set(x[:k].tolist()) & set(y[:k].tolist()))
+    return hit / (k * len(a_ids))
+
+
+def exact_dists(torch, x, q, ids):
+    """FP64 squared L2 from each query to each of its returned ids."""
+    with torch.no_grad():
+        idx = torch.as_tensor(ids.astype(np.int64), device=x.device)
+        v = x[idx.reshape(-1)].double().reshape(ids.shape[0], ids.shape[1], -1)
+        return ((v - q.double()[:, None, :]) ** 2).sum(-1).cpu().numpy()
+
+
+def precision_leg(a, torch, flush, log):
+    """Precision form: B=6 / 8 CAQ codes at 1M x 1536 (spectrum i^-1), the
+    ex-code contraction on the tensor cores (saqg_search_tc) beside the FP32
+    CUDA-core search (saqg_search) on the same batches."""
+    import ctypes as C
+    from saq_gb300 import _native as N, ivf, workloads
+    t0 = time.time()
+    nmax = max(a.precision_batches)
+    wl = workloads.zipf_aniso(a.precision_n, a.precision_dim, a.precision_clusters, nq=nmax, s=0.0, alpha=1.0,
+                              sigma=a.sigma, noise_alpha=1.0, seed=1, query_clusters="uniform")
+    gt = workloads.ground_truth(wl.x, wl.q, 10)
+    log(f"precision workload generated in {time.time() - t0:.1f}s")
+    peak_tf, peak_tf_kind = bf16_peak()
+    hbm, hbm_kind = peaks()
+    out = {"workload": f"{a.precision_n // 1_000_000}M x {a.precision_dim}, unit-norm, spectrum i^-1, "
+                       f"{a.precision_clusters} clusters (equal sizes), CAQ (no segmentation), k=10, "
+                       f"nprobe {a.precision_nprobe}, shortlist {a.tc_shortlist}",
+           "operands": "codes BF16 (exact integers), queries BF16, FP32 accumulation in TMEM (tcgen05.mma kind::f16)",
+           "configs": []}
+    for bits in a.precision_bits:
+        t0 = time.time()
+        index = ivf.IVF(a.precision_n, a.precision_dim, a.precision_clusters,
+                        ivf.QuantizeConfig(avg_bits=float(bits), enable_segmentation=False))
+        index.set_variance(wl.variance)
+        index.construct(wl.x, wl.centroids.cpu().numpy(), wl.cids.cpu().numpy().astype(np.uint32), seed=1)
+        torch.cuda.synchronize()
+        build_s = time.time() - t0
+        lib = index.lib
+        cfg = {"bits": bits, "encode_vectors_per_s": a.precision_n / build_s, "plan": index.info()["plan"],
+               "batches": []}
+        log(f"precision B={bits}: index built in {build_s:.1f}s")
+        for B in a.precision_batches:
+            q = wl.q[:B].contiguous()
+            ids_tc = torch.empty((B, 10), dtype=torch.int32, device="cuda")
+            d_tc = torch.empty((B, 10), dtype=torch.float32, device="cuda")
+            ap_tc = torch.empty((B, 10), dtype=torch.float32, device="cuda")
+            st = N.TcStats()
+            scfg = ivf.SearcherConfig().to_c()
+            sptr = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+            def tc(with_stats=False):
+                N.check(lib.saqg_search_tc(index._h, q.data_ptr(), B, 10, a.precision_nprobe, a.tc_shortlist,
+                                           C.byref(scfg), ids_tc.data_ptr(), d_tc.data_ptr(), ap_tc.data_ptr(),
+                                           N.SAQG_MEM_DEVICE, sptr, C.byref(st) if with_stats else None))
+            ids_c = torch.empty((B, 10), dtype=torch.int32, device="cuda")
+            d_c = torch.empty((B, 10), dtype=torch.float32, device="cuda")
+
+            def core():
+                N.check(lib.saqg_search(index._h, q.data_ptr(), B, 10, a.precision_nprobe, C.byref(scfg),
+                                        ids_c.data_ptr(), d_c.data_ptr(), N.SAQG_MEM_DEVICE, sptr))
+            ms_tc, _ = time_calls(torch, tc, flush, 5)
+            ms_core, _ = time_calls(torch, core, flush, 5)
+            flush.zero_()
+            tc(True)
+            torch.cuda.synchronize()
+            it = ids_tc.cpu().numpy().view(np.uint32)
+            ic = ids_c.cpu().numpy().view(np.uint32)
+            dt = d_tc.cpu().numpy()
+            apx = ap_tc.cpu().numpy()
+            ex = exact_dists(torch, wl.x, q, it)
+            rel_est = np.abs(dt.astype(np.float64) - ex) / np.maximum(ex, 1e-12)
+            rel_apx = np.abs(apx.astype(np.float64) - ex) / np.maximum(ex, 1e-12)
+            rel_apx_est = np.abs(apx.astype(np.float64) - dt) / np.maximum(np.abs(dt.astype(np.float64)), 1e-12)
+            s = st.as_dict()
+            tflops = s["flops"] / (s["ms_contract"] / 1e3) / 1e12
+            row = {"batch": B, "tc_qps": B / (ms_tc / 1e3), "tc_ms": ms_tc, "core_qps": B / (ms_core / 1e3),
+                   "core_ms": ms_core, "tc_over_core": ms_core / ms_tc,
+                   "recall@10_tc_vs_core": overlap(it, ic, 10),
+                   "recall@10_tc_vs_fp64": workloads.recall_at(it, gt[:B], 10),
+                   "recall@10_core_vs_fp64": workloads.recall_at(ic, gt[:B], 10),
+                   "dist_rel_err_vs_fp64": {"median": float(np.median(rel_est)), "p99": float(np.percentile(rel_est, 99)),
+                                            "note": "returned distances (the exact search's estimator) vs FP64 |x-q|^2"},
+                   "tc_approx_rel_err_vs_fp64": {"median": float(np.median(rel_apx)),
+                                                 "p99": float(np.percentile(rel_apx, 99))},
+                   "tc_approx_rel_err_vs_fp32_estimator": {"median": float(np.median(rel_apx_est)),
+                                                           "p99": float(np.percentile(rel_apx_est, 99))},
+                   "stages_ms": {k: s[k] for k in ("ms_probe", "ms_pairs", "ms_contract", "ms_select", "ms_rerank")},
+                   "contract_roofline": {"tensor_tflops": tflops, "tensor_peak": peak_tf, "tensor_frac": tflops / peak_tf,
+                                         "tensor_peak_kind": peak_tf_kind,
+                                         "issued_tflops": s["mma_flops"] / (s["ms_contract"] / 1e3) / 1e12,
+                                         "code_gbs": s["code_bytes"] / (s["ms_contract"] / 1e3) / 1e9,
+                                         "hbm_peak": hbm, "hbm_frac": s["code_bytes"] / (s["ms_contract"] / 1e3) / 1e9 / hbm,
+                                         "flops": s["flops"], "code_bytes": s["code_bytes"], "tiles": s["tiles"]}}
+            cfg["batches"].append(row)
+            log(f"precision B={bits} batch {B}: tc {row['tc_qps']:.0f} q/s, core {row['core_qps']:.0f} q/s, "
+                f"recall tc/core {row['recall@10_tc_vs_core']:.4f}, contract {s['ms_contract']:.3f} ms "
+                f"({tflops:.1f} TF/s, {row['contract_roofline']['code_gbs']:.0f} GB/s)")
+        out["configs"].append(cfg)
+        del index
+        torch.cuda.empty_cache()
+    del wl
+    torch.cuda.empty_cache()
+    return out
 
 
 def peaks():
@@ -441,6 +582,33 @@ def main():
                 f"achieved {serving[-1]['achieved_qps']:.0f}/s")
         srv.close()
 
+    # ---- tensor-core form on the same batch (saqg_search_tc) ----
+    tc_line = None
+    if rank == 0 and a.tc_shortlist > 0:
+        ids_t = torch.empty((B, a.topk), dtype=torch.int32, device="cuda")
+        d_t = torch.empty((B, a.topk), dtype=torch.float32, device="cuda")
+        tst = N.TcStats()
+
+        def tcb(with_stats=False):
+            N.check(lib.saqg_search_tc(index._h, qdev.data_ptr(), B, a.topk, nprobe, a.tc_shortlist, C.byref(scfg),
+                                       ids_t.data_ptr(), d_t.data_ptr(), None, N.SAQG_MEM_DEVICE, sptr,
+                                       C.byref(tst) if with_stats else None))
+        tc_ms, _ = time_calls(torch, tcb, flush, max(3, min(10, a.steps // 10)))
+        flush.zero_()
+        tcb(True)
+        torch.cuda.synchronize()
+        it = ids_t.cpu().numpy().view(np.uint32)
+        ts = tst.as_dict()
+        tc_line = {"qps": B / (tc_ms / 1e3), "ms_per_batch": tc_ms, "shortlist": a.tc_shortlist,
+                   f"recall@{a.topk}": round(workloads.recall_at(it[:ng], gt[:ng], a.topk), 4),
+                   f"recall@{a.topk}_vs_exact_search": round(overlap(it, got, a.topk), 4),
+                   "over_plain": B / (tc_ms / 1e3) / plain_qps,
+                   "stages_ms": {k: ts[k] for k in ("ms_probe", "ms_pairs", "ms_contract", "ms_select", "ms_rerank")},
+                   "contract_code_gbs": ts["code_bytes"] / (ts["ms_contract"] / 1e3) / 1e9,
+                   "contract_tflops": ts["flops"] / (ts["ms_contract"] / 1e3) / 1e12}
+        log(f"tensor-core form: {tc_line['qps']:.0f} q/s, recall {tc_line[f'recall@{a.topk}']}, "
+            f"stages {tc_line['stages_ms']}")
+
     # ---- CPU baseline (oracle port) on a bounded sample ----
     cpu = None
     if rank == 0:
@@ -450,6 +618,10 @@ def main():
         cpu = {"value": r, "unit": "queries/s", "cores": threads, "kind": "port",
                "sample": f"{ns} queries of the batch on the same index ({dt:.1f}s, {threads} threads)",
                "ids_equal_gpu": same}
+
+    precision = None
+    if rank == 0 and a.precision_bits:
+        precision = precision_leg(a, torch, flush, log)
 
     clocks = clk.summary()
     line = {
@@ -480,6 +652,8 @@ def main():
                      "lut_lookup_peak_per_s": lookup_peak,
                      "lut_lookup_frac": lookups / (mean_scan / 1e3) / lookup_peak},
         "uneven_batch": mixed_line,
+        "tensor_core_form": tc_line,
+        "precision": precision,
         "serving": {"server": "continuous batching, 2 batches in flight, max batch %d" % B,
                     "nprobe": "U[16,256] per query", "k": "10 or 100 per query", "arrivals": "Poisson",
                     "rates": serving},

@@ -180,6 +180,39 @@ int saqg_search_batch(const saqg_index *index, const float *queries, int64_t nq,
                       const int32_t *topk_per_query, int64_t nprobe, int64_t topk, const saqg_searcher_config *cfg,
                       uint32_t *ids, float *dists, int mem, void *stream, saqg_search_stats *stats);
 
+/* ---- tensor-core form ---------------------------------------------------- */
+/* No counterpart in the reference (its search is one query at a time on
+ * AVX-512): a batch of queries answered through a dense product on the tensor
+ * cores.  Every probed cluster's full CAQ codes (BF16, exact below 2^8) are
+ * multiplied with the BF16-rounded residual queries of the queries probing it
+ * (FP32 accumulation); the `shortlist` smallest of these approximate distances
+ * per query are re-ranked with the exact distance saqg_search computes for a
+ * vector, and the topk smallest of those are returned (equal distances: the
+ * later-scanned vector first, as ResultPool orders them).  `dists` (may be
+ * NULL) are therefore bit-identical to saqg_search's distance for the same id;
+ * `approx` (may be NULL) is each returned vector's tensor-core distance.  Ids a
+ * query would see through saqg_search but whose approximate distance ranks
+ * beyond the shortlist are missed.  Needs every segment coded (bits >= 1),
+ * nq <= 8192, topk <= shortlist <= 1024.  The first call on an index builds
+ * the code matrix (2 bytes per vector and dimension of device memory). */
+typedef struct saqg_tc_stats {
+    float ms_probe;      /* centroid ranking + query rotation */
+    float ms_pairs;      /* (query, cluster) pairs bucketed by cluster */
+    float ms_contract;   /* the tensor-core contraction (k_tc_contract) */
+    float ms_select;     /* shortlist selection */
+    float ms_rerank;     /* exact re-rank of the shortlist + top-k */
+    int64_t pairs;       /* (query, probed cluster) pairs */
+    int64_t candidates;  /* approximate distances produced */
+    int64_t tiles;       /* 128-vector tiles contracted */
+    int64_t flops;       /* 2 * dim * sum over clusters of (queries x vectors) */
+    int64_t mma_flops;   /* ... as issued (tiles of 128 vectors, pairs padded to 16) */
+    int64_t code_bytes;  /* code bytes of the probed clusters (each read once) */
+} saqg_tc_stats;
+
+int saqg_search_tc(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
+                   int64_t shortlist, const saqg_searcher_config *cfg, uint32_t *ids, float *dists, float *approx,
+                   int mem, void *stream, saqg_tc_stats *stats);
+
 /* ---- graph-captured search ---------------------------------------------- */
 /* No counterpart in the reference: saqg_search for a fixed shape (nq, topk,
  * nprobe) on device buffers, captured into a CUDA graph.  Creation runs the

@@ -47,6 +47,15 @@ class SearchStats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class TcStats(C.Structure):
+    _fields_ = [("ms_probe", C.c_float), ("ms_pairs", C.c_float), ("ms_contract", C.c_float),
+                ("ms_select", C.c_float), ("ms_rerank", C.c_float), ("pairs", I64), ("candidates", I64),
+                ("tiles", I64), ("flops", I64), ("mma_flops", I64), ("code_bytes", I64)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class SaqgError(RuntimeError):
     pass
 
@@ -89,6 +98,8 @@ EXPORTS = {
                                     C.c_void_p]),
     "saqg_search_static": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig), C.c_void_p,
                                      C.c_void_p, C.c_void_p]),
+    "saqg_search_tc": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, I64, C.POINTER(SearcherConfig), C.c_void_p,
+                                 C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(TcStats)]),
     "saqg_search_graph_create": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig),
                                            C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "saqg_search_graph_launch": (C.c_int, [C.c_void_p, C.c_void_p]),

@@ -95,6 +95,8 @@ Index::~Index() {
     cudaSetDevice(device);
     for (void *p : allocations) cudaFree(p);
     if (cnorm2) cudaFree(cnorm2);
+    if (tc_codes) cudaFree(tc_codes);
+    if (tc_tiles) cudaFree(tc_tiles);
     cudaSetDevice(cur);
 }
 

@@ -126,6 +126,10 @@ struct Index {
     // probe shortlist: squared centroid norms (built on first use, under init_mu)
     mutable std::mutex init_mu;
     mutable float *cnorm2 = nullptr;
+    // tensor-core form: BF16 code matrix [N][Dtot] and the (cluster, tile) list (built on first use, under init_mu)
+    mutable void *tc_codes = nullptr;
+    mutable void *tc_tiles = nullptr;
+    mutable int64_t tc_ntiles = 0;
     ~Index();
     void *dalloc(size_t bytes);
     void upload(void *dst, const void *src, size_t bytes);
@@ -158,6 +162,20 @@ void run_search_static(const Index &idx, const float *q, int64_t nq, int64_t top
                        uint32_t *ids, float *dists, cudaStream_t stream);
 int64_t run_estimate(const Index &idx, const float *q_host, int64_t nprobe, float m, uint32_t *ids, float *acc,
                      float *fast, float *vars, int64_t cap);
+
+// Tensor-core form (search.cu): centroid ranking + query rotation of a batch,
+// and the exact re-rank of its shortlist.
+void tc_rank_rotate(const Index &idx, SearchCtx &ctx, const float *q, int64_t nq, int64_t nprobe, float m, float *dist,
+                    void *work, uint32_t *probe, float *qrot, float *prune, uint8_t *full, int *fb_list, int *flags,
+                    cudaStream_t st);
+size_t tc_probe_work_bytes(const Index &idx, int64_t nq);
+void tc_rerank(const Index &idx, const uint32_t *probe, int64_t nq, int64_t nprobe, const float *qrot,
+               const float *prune, const int *lp, const int *sl_pos, const float *sl_apx, const int *sl_cnt, int L,
+               int64_t topk, uint32_t *ids, float *dists, float *apx, cudaStream_t st);
+// tc_search.cu
+void run_search_tc(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, int64_t shortlist,
+                   float m, uint32_t *ids, float *dists, float *approx, int mem, cudaStream_t st,
+                   saqg_tc_stats *stats);
 
 // graph.cpp
 struct SearchGraph;

@@ -2779,4 +2779,192 @@ void run_search_static(const Index &I, const float *q, int64_t nq, int64_t topk,
     count_launch(4);
 }
 
+// ------------------------------------------ tensor-core form: probes and re-rank
+namespace {
+
+// Distance the search inserts for a vector that passes every pruning stage
+// (block_estimates + the accurate pass + replay_block): one segment, the
+// accurate distance; several, the running sum of variance bounds, each coded
+// segment's bound replaced by its fast estimate, then every segment's
+// estimate replaced by its accurate distance, in segment order.
+__device__ float searched_dist(const DevIndexView &ix, const ScanSmem &sm, int64_t gb, int64_t gv, int ln, int lane) {
+    const int S = ix.S;
+    float v[kMaxSeg], f[kMaxSeg], ipx[kMaxSeg];
+    for (int s = 0; s < S; ++s) {
+        const SegDev &g = ix.seg[s];
+        const float on = g.onorm[gb * 32 + lane];
+        v[s] = vars_est(sm.scal[s], on);
+        float ip = 0.0f;
+        f[s] = g.bits ? fast_est(g, sm.lut + 4 * g.qoff, sm.scal[s], gb, lane, on, ip) : v[s];
+        ipx[s] = __shfl_sync(kFull, ip, ln);
+        v[s] = __shfl_sync(kFull, v[s], ln);
+        f[s] = __shfl_sync(kFull, f[s], ln);
+    }
+    float d = 0.0f;
+    if (lane == 0) {
+        float acc[kMaxSeg];
+        for (int s = 0; s < S; ++s) {
+            const SegDev &g = ix.seg[s];
+            const float ex = g.bits > 1 ? excode_ip_thread(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim,
+                                                           g.bits - 1)
+                                        : 0.0f;
+            acc[s] = accurate_dist(g.onorm[gb * 32 + ln], ipx[s], ex, g.exfac[gv].x, g.bits, sm.scal[s].sum_q,
+                                   sm.scal[s].q_l2sqr);
+        }
+        if (S == 1) {
+            d = acc[0];
+        } else {
+            float cur = 0.0f;
+            for (int s = 0; s < S; ++s) cur = __fadd_rn(cur, v[s]);
+            for (int s = 0; s < S; ++s)
+                if (ix.seg[s].bits) cur = __fadd_rn(__fsub_rn(cur, v[s]), f[s]);
+            d = cur;
+            for (int s = 0; s < S; ++s) d = __fadd_rn(d, __fsub_rn(acc[s], ix.seg[s].bits ? f[s] : v[s]));
+        }
+    }
+    return __shfl_sync(kFull, d, 0);
+}
+
+// Re-rank of the tensor-core shortlist, one CTA per query.  The shortlist
+// (positions in the query's candidate order, ascending, so grouped by probe)
+// is evaluated cluster by cluster: Lut::prepare for the cluster, then every
+// shortlisted vector's distance as the search computes it (searched_dist).
+// The top-k is ordered by distance, equal distances the later-scanned first,
+// which is where ResultPool::insert puts an equal distance (pool.hpp:17-30).
+__global__ void __launch_bounds__(kScanThreads) k_tc_rerank(DevIndexView ix, const uint32_t *__restrict__ probe,
+                                                            int nprobe, const float *__restrict__ qrot,
+                                                            const float *__restrict__ prune,
+                                                            const int *__restrict__ lp, const int *__restrict__ sl_pos,
+                                                            const float *__restrict__ sl_apx,
+                                                            const int *__restrict__ sl_cnt, int L, int L2, int topk,
+                                                            uint32_t *__restrict__ ids, float *__restrict__ dists,
+                                                            float *__restrict__ apx_out) {
+    extern __shared__ __align__(16) char smem_raw[];
+    const size_t base = align16(scan_smem_bytes(ix.Dtot, ix.S, 1, 0));
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, 1, 0);
+    float *dist = reinterpret_cast<float *>(smem_raw + base);
+    unsigned long long *key = reinterpret_cast<unsigned long long *>(smem_raw + base + align16(4 * (size_t)L));
+    const int qi = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int n = sl_cnt[qi];
+    const int *pos = sl_pos + (size_t)qi * L;
+    const int *lq = lp + (size_t)qi * (nprobe + 1);
+    int g0 = 0;
+    while (g0 < n) {  // uniform: one probed cluster per round
+        int lo = 0, hi = nprobe - 1;  // last j with lq[j] <= pos[g0]
+        const int p0 = pos[g0];
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (lq[mid] <= p0) lo = mid;
+            else hi = mid - 1;
+        }
+        const int j = lo, end = lq[j + 1];
+        int g1 = g0 + 1;
+        while (g1 < n && pos[g1] < end) ++g1;
+        const int c = (int)probe[(size_t)qi * nprobe + j];
+        prepare_cluster(ix, qrot + (size_t)qi * ix.Dtot, prune + (size_t)qi * ix.S, c, sm);
+        const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
+        for (int e = g0 + w; e < g1; e += kScanWarps) {
+            const int r = pos[e] - lq[j];
+            const float d = searched_dist(ix, sm, b0 + r / 32, v0 + r, r & 31, lane);
+            if (lane == 0) dist[e] = d;
+        }
+        __syncthreads();
+        g0 = g1;
+    }
+    // (distance key, later position first) sorted ascending
+    for (int e = tid; e < L2; e += blockDim.x)
+        key[e] = e < n ? ((unsigned long long)fkey(dist[e]) << 32) | (unsigned)(0x7fffffff - pos[e]) : ~0ull;
+    __syncthreads();
+    for (int k = 2; k <= L2; k <<= 1)
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            for (int e = tid; e < L2; e += blockDim.x) {
+                const int o = e ^ jj;
+                if (o > e) {
+                    const unsigned long long a = key[e], b = key[o];
+                    if ((a > b) == ((e & k) == 0)) {
+                        key[e] = b;
+                        key[o] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int t = tid; t < topk; t += blockDim.x) {
+        uint32_t id = 0;
+        float d = FLT_MAX, a = FLT_MAX;
+        if (t < n) {
+            const int p = 0x7fffffff - (int)(unsigned)(key[t] & 0xffffffffull);
+            int lo = 0, hi = n - 1;  // the shortlist entry of position p
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (pos[mid] < p) lo = mid + 1;
+                else hi = mid;
+            }
+            int jlo = 0, jhi = nprobe - 1;
+            while (jlo < jhi) {
+                const int mid = (jlo + jhi + 1) >> 1;
+                if (lq[mid] <= p) jlo = mid;
+                else jhi = mid - 1;
+            }
+            const int c = (int)probe[(size_t)qi * nprobe + jlo];
+            id = ix.ids[ix.vec_off[c] + (p - lq[jlo])];
+            d = dist[lo];
+            a = sl_apx[(size_t)qi * L + lo];
+        }
+        ids[(size_t)qi * topk + t] = id;
+        if (dists) dists[(size_t)qi * topk + t] = d;
+        if (apx_out) apx_out[(size_t)qi * topk + t] = a;
+    }
+}
+
+}  // namespace
+
+void tc_rank_rotate(const Index &I, SearchCtx &C, const float *q, int64_t nq, int64_t nprobe, float m, float *dist,
+                    void *work, uint32_t *probe, float *qrot, float *prune, uint8_t *full, int *fb_list, int *flags,
+                    cudaStream_t st) {
+    const DevIndexView &ix = I.view;
+    SAQG_CUDA_TRY(cudaMemsetAsync(flags, 0, 64, st));
+    Cand *wk = static_cast<Cand *>(work);
+    const char *pm = std::getenv("SAQG_PROBE");
+    const bool shortlist = nq >= kGemmMinQueries && nprobe <= kShortCap && !(pm && std::string(pm) == "exact");
+    if (shortlist) {
+        probe_shortlist(I, C, q, nq, nprobe, nullptr, dist, probe, full, fb_list, flags, wk, nullptr, st);
+    } else {
+        k_probe_dist<<<dim3((unsigned)((I.K + 7) / 8), (unsigned)nq), 256, 0, st>>>(ix, q, dist);
+        check_launch("k_probe_dist");
+        k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, wk, flags);
+        check_launch("k_probe_select");
+    }
+    size_t qsm = 0;
+    for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
+    if (nq >= kQprepQT && kQprepQT * qsm <= 200 * 1024) {
+        SAQG_CUDA_TRY(cudaFuncSetAttribute(k_qprep_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(kQprepQT * qsm)));
+        k_qprep_tiled<<<dim3((unsigned)ix.S, (unsigned)((nq + kQprepQT - 1) / kQprepQT)), 256, kQprepQT * qsm, st>>>(
+            ix, q, (int)nq, m, qrot, prune);
+        check_launch("k_qprep_tiled");
+    } else {
+        k_qprep<<<dim3((unsigned)ix.S, (unsigned)nq), 256, qsm, st>>>(ix, q, m, qrot, prune);
+        check_launch("k_qprep");
+    }
+    count_launch(4);
+}
+
+size_t tc_probe_work_bytes(const Index &I, int64_t nq) { return sizeof(Cand) * (size_t)nq * I.K; }
+
+void tc_rerank(const Index &I, const uint32_t *probe, int64_t nq, int64_t nprobe, const float *qrot,
+               const float *prune, const int *lp, const int *sl_pos, const float *sl_apx, const int *sl_cnt, int L,
+               int64_t topk, uint32_t *ids, float *dists, float *apx, cudaStream_t st) {
+    const DevIndexView &ix = I.view;
+    int L2 = 1;
+    while (L2 < L) L2 <<= 1;
+    const size_t smem = align16(scan_smem_bytes(ix.Dtot, ix.S, 1, 0)) + align16(4 * (size_t)L) + 8 * (size_t)L2;
+    SAQG_REQUIRE(smem <= 200 * 1024, "dimension / shortlist too large for the re-rank kernel's shared memory");
+    SAQG_CUDA_TRY(cudaFuncSetAttribute(k_tc_rerank, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_tc_rerank<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, lp, sl_pos, sl_apx,
+                                                          sl_cnt, L, L2, (int)topk, ids, dists, apx);
+    check_launch("k_tc_rerank");
+    count_launch(1);
+}
+
 }  // namespace saqg

@@ -1,0 +1,956 @@
+// Tensor-core form of the batched search (no counterpart in the reference,
+// whose search is one query at a time on AVX-512).
+//
+// For a batch of queries the quantized codes of every probed cluster are
+// contracted with the queries that probe it as one dense product on the
+// 5th-generation tensor cores:
+//
+//   approx(q, o) = sum_s |o_s|^2 + |r_s|^2 - 2 rescale_s (delta_s <r_s, u_s> + (delta_s/2 - 1) sum(r_s))
+//
+// where r_s = q_s P_s - c_s P_s is the query's rotated residual on segment s,
+// u_s the vector's full B-bit CAQ code (1-bit part << (B-1) | ex-code) and
+// delta_s = 2 / 2^B: CaqCluEstimator::compAccurateDist (caq_estimator.hpp:190-217)
+// with the FastScan LUT of the 1-bit part replaced by the exact code.  Codes are
+// held as BF16 (integers below 2^8 are exact), queries are rounded to BF16,
+// products accumulate in FP32 in tensor memory.  The `shortlist` smallest
+// approximate distances of each query are then re-ranked with the distance the
+// exact search computes (k_tc_rerank), and the top-k of those is the answer.
+//
+// Kernels, in launch order:
+//   k_tc_codes     (once per index) BF16 code matrix [vector][dim], clusters concatenated
+//   k_tc_pairs     per-query candidate offsets (probe order) and per-cluster pair counts
+//   k_excl_scan    exclusive prefix sums (query offsets, cluster bucket offsets)
+//   k_tc_fill / k_tc_sort   pairs bucketed by cluster, each bucket in pair order
+//   k_tc_contract  one CTA per 128-vector tile of a cluster: TMA streams the code
+//                  tile through a 3-stage shared-memory ring (128-byte swizzle),
+//                  four warps build the BF16 residual queries of the tile's pairs in
+//                  the same layout, one thread issues tcgen05.mma (M=128, N=pairs,
+//                  K=16 per instruction) into per-segment TMEM accumulators, and the
+//                  four warps read them back with tcgen05.ld for the epilogue
+//   k_tc_select    per query: the shortlist by radix select, in candidate order
+//   k_tc_rerank    (search.cu) exact distances of the shortlist, top-k
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "saqg_internal.h"
+
+namespace saqg {
+
+namespace {
+
+constexpr int kTcBM = 128;           // vectors per tile: the MMA's M
+constexpr int kTcBK = 64;            // dims per pipeline stage: one 128-byte BF16 row
+constexpr int kTcStages = 3;         // ring depth (two CTAs per SM)
+constexpr int kTcThreads = 192;      // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-5 queries + epilogue
+constexpr int kTcStageBytes = 16384; // 128 rows x 128 bytes (A), at most 128 x 128 bytes (B)
+constexpr int kTcCols = 256;         // TMEM columns a CTA may hold: segments x pairs per chunk
+constexpr int kTcMaxN = 128;         // pairs per chunk at most (the MMA's N)
+constexpr int kTcMaxShort = 1024;    // shortlist length at most
+constexpr int kTcMaxBatch = 8192;    // queries per call at most (bucket sort in shared memory)
+constexpr unsigned kFullMask = 0xffffffffu;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t gtimer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase of parity `parity` of `bar`.  Gives up after one second,
+// or at once when another role of the CTA gave up (`abort`), so that no wait
+// outlives a lost arrival; the caller then records the failure.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort) {
+    if (mbar_try(bar, parity)) return true;
+    const uint64_t t0 = gtimer();
+    for (;;) {
+        if (mbar_try(bar, parity)) return true;
+        if (*abort) return false;
+        if (gtimer() - t0 > 1000000000ull) {
+            *abort = 1;
+            return false;
+        }
+    }
+}
+
+// Bounded wait that ignores `abort` (draining copies in flight before exit).
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+    const uint64_t t0 = gtimer();
+    while (!mbar_try(bar, parity))
+        if (gtimer() - t0 > 1000000000ull) return;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            dst),
+        "l"((uint64_t)map), "r"(bar), "r"(x), "r"(y)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor (tcgen05): K-major operand in the 128-byte
+// swizzle layout, rows of 128 bytes, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, M = 128, N = n.
+__device__ __forceinline__ uint32_t idesc_bf16(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void named_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+// ------------------------------------------------------------ code matrix
+// Value of dimension d of an ex-code of `b` bits in the reference's compacted
+// layouts (CodeHelper<B>::compacted_code8/16, code_helper.hpp).
+__device__ __forceinline__ uint32_t ex_bits8(const uint8_t *__restrict__ y, int D, int b, int d) {
+    switch (b) {
+    case 1:
+        return (y[d >> 3] >> (d & 7)) & 1u;
+    case 2:
+    case 3: {
+        const uint8_t *g = y + (d >> 6) * (b == 2 ? 16 : 24);
+        const int k = d & 63;
+        uint32_t v = (g[k & 15] >> (2 * (k >> 4))) & 3u;
+        if (b == 3) v |= ((g[16 + (k & 7)] >> (k >> 3)) & 1u) << 2;
+        return v;
+    }
+    case 4: {
+        const uint8_t *g = y + (d >> 5) * 16;
+        const int k = d & 31;
+        return k < 16 ? (g[k] & 15u) : (uint32_t)(g[k - 16] >> 4);
+    }
+    case 5:
+        return (ex_bits8(y, D, 4, d) << 1) | ex_bits8(y + D / 2, D, 1, d);
+    case 6:
+    case 7: {
+        const uint8_t *g = y + (d >> 6) * (b == 6 ? 48 : 56);
+        const int k = d & 63, r = k & 15;
+        uint32_t v;
+        if (k < 16) v = g[r] & 63u;
+        else if (k < 32) v = g[16 + r] & 63u;
+        else if (k < 48) v = ((uint32_t)(g[r] >> 6) << 4) | (g[32 + r] & 15u);
+        else v = ((uint32_t)(g[16 + r] >> 6) << 4) | (uint32_t)(g[32 + r] >> 4);
+        if (b == 7) v |= ((g[48 + (k & 7)] >> (k >> 3)) & 1u) << 6;
+        return v;
+    }
+    case 8:
+        return y[d];
+    default:
+        return 0;
+    }
+}
+
+__device__ __forceinline__ uint32_t ex_value(const uint8_t *__restrict__ y, int D, int exb, int d) {
+    if (exb > 8) return y[d] | (ex_bits8(y + D, D, exb - 8, d) << 8);
+    return ex_bits8(y, D, exb, d);
+}
+
+// Full CAQ code u = (1-bit code << (B-1)) | ex-code of every vector, as BF16,
+// row-major [vector][Dtot] (segments at their query offsets).  One thread per
+// (vector, 8 dims).
+__global__ void k_tc_codes(DevIndexView ix, const int32_t *__restrict__ cl_of, int64_t n, __nv_bfloat16 *__restrict__ A) {
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int per = ix.Dtot / 8;
+    if (gid >= n * per) return;
+    const int64_t v = gid / per;
+    const int k8 = (int)(gid - v * per) * 8;
+    int s = 0;
+    while (s + 1 < ix.S && k8 >= ix.seg[s + 1].qoff) ++s;
+    const SegDev &g = ix.seg[s];
+    const int d0 = k8 - g.qoff;
+    const int c = cl_of[v];
+    const int64_t pos = v - ix.vec_off[c];
+    const int64_t gb = ix.blk_off[c] + pos / 32;
+    const int lane = (int)(pos % 32);
+    const uint8_t *cb = reinterpret_cast<const uint8_t *>(g.codes) + (size_t)gb * (g.dim / 8) * 32;
+    const int i = d0 / 8;
+    const uint32_t msb = cb[((size_t)(i / 8) * 32 + lane) * 8 + (i % 8)];
+    const uint8_t *y = g.lcode + (size_t)v * g.lstride;
+    uint32_t w[4];
+#pragma unroll
+    for (int e = 0; e < 8; e += 2) {
+        float f[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int d = d0 + e + h;
+            uint32_t u = (msb >> (7 - ((e + h) & 7))) & 1u;
+            if (g.bits > 1) u = (u << (g.bits - 1)) | ex_value(y, g.dim, g.bits - 1, d);
+            f[h] = (float)u;
+        }
+        w[e / 2] = pack_bf16x2(f[0], f[1]);
+    }
+    *reinterpret_cast<uint4 *>(A + (size_t)v * ix.Dtot + k8) = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+__global__ void k_tc_cluster_of(const int64_t *__restrict__ vec_off, int K, int32_t *__restrict__ cl_of) {
+    const int c = blockIdx.x;
+    for (int64_t v = vec_off[c] + threadIdx.x; v < vec_off[c + 1]; v += blockDim.x) cl_of[v] = c;
+}
+
+// ------------------------------------------------------------ pairs
+// One warp per query: candidate offsets of its probes in probe order
+// (lp[i][j] = sizes of probes 0..j-1; lp[i][nprobe] = its candidates) and the
+// per-cluster pair counts.
+__global__ void k_tc_pairs(DevIndexView ix, const uint32_t *__restrict__ probe, int nq, int nprobe, int *__restrict__ lp,
+                           int *__restrict__ qtot, int *__restrict__ bcnt) {
+    const int qi = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (qi >= nq) return;
+    int run = 0;
+    for (int j0 = 0; j0 < nprobe; j0 += 32) {
+        const int j = j0 + lane;
+        int sz = 0;
+        if (j < nprobe) {
+            const uint32_t c = probe[(size_t)qi * nprobe + j];
+            sz = (int)(ix.vec_off[c + 1] - ix.vec_off[c]);
+            atomicAdd(&bcnt[c], 1);
+        }
+        int x = sz;  // inclusive warp scan
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(kFullMask, x, o);
+            if (lane >= o) x += y;
+        }
+        if (j < nprobe) lp[(size_t)qi * (nprobe + 1) + j] = run + x - sz;
+        run += __shfl_sync(kFullMask, x, 31);
+    }
+    if (lane == 0) {
+        lp[(size_t)qi * (nprobe + 1) + nprobe] = run;
+        qtot[qi] = run;
+    }
+}
+
+// Exclusive prefix sum of n ints into n + 1 int64s (the last is the total);
+// one CTA of 1024 threads, each over a contiguous run.
+__global__ void __launch_bounds__(1024) k_excl_scan(const int *__restrict__ in, int n, long long *__restrict__ out) {
+    __shared__ long long wsum[32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int per = (n + 1023) / 1024, b = min(n, tid * per), e = min(n, b + per);
+    long long s = 0;
+    for (int i = b; i < e; ++i) s += in[i];
+    long long x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(kFullMask, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        long long t = wsum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(kFullMask, t, o);
+            if (lane >= o) t += y;
+        }
+        wsum[lane] = t;
+    }
+    __syncthreads();
+    long long run = x - s + (w ? wsum[w - 1] : 0);
+    for (int i = b; i < e; ++i) {
+        out[i] = run;
+        run += in[i];
+    }
+    if (tid == 1023) out[n] = run;
+}
+
+__global__ void k_tc_fill(const uint32_t *__restrict__ probe, int npairs, const long long *__restrict__ boff,
+                          int *__restrict__ bfill, int *__restrict__ bucket) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npairs) return;
+    const uint32_t c = probe[p];
+    const int slot = atomicAdd(&bfill[c], 1);
+    bucket[boff[c] + slot] = p;
+}
+
+// Each cluster's bucket in ascending pair order (pair = query * nprobe + j):
+// rank sort in shared memory, one CTA per cluster.
+__global__ void __launch_bounds__(256) k_tc_sort(const int *__restrict__ bcnt, const long long *__restrict__ boff,
+                                                 const int *__restrict__ bucket, int *__restrict__ sorted) {
+    __shared__ int v[kTcMaxBatch];
+    const int c = blockIdx.x, n = bcnt[c];
+    if (n == 0) return;
+    const int *in = bucket + boff[c];
+    int *out = sorted + boff[c];
+    for (int e = threadIdx.x; e < n; e += blockDim.x) v[e] = in[e];
+    __syncthreads();
+    for (int e = threadIdx.x; e < n; e += blockDim.x) {
+        const int x = v[e];
+        int r = 0;
+        for (int k = 0; k < n; ++k) r += v[k] < x;
+        out[r] = x;
+    }
+}
+
+// ------------------------------------------------------------ contraction
+struct TcWork {
+    const int2 *tiles;          // (cluster, tile) of every 128-vector tile
+    const int *bcnt;            // pairs per cluster
+    const long long *boff;      // bucket offsets
+    const int *bucket;          // pairs by cluster, ascending
+    const float *qrot;          // [nq][Dtot] rotated queries
+    const int *lp;              // [nq][nprobe + 1]
+    const long long *qbase;     // [nq] candidate offsets
+    float *cand;                // approximate distances
+    int nprobe;
+    int BN;                     // pairs per chunk (multiple of 16)
+    int *err;
+};
+
+__global__ void __launch_bounds__(kTcThreads, 2) k_tc_contract(const __grid_constant__ CUtensorMap tmA, DevIndexView ix,
+                                                               TcWork w) {
+    extern __shared__ uint8_t tc_smem[];
+    const int2 tile = w.tiles[blockIdx.x];
+    const int c = tile.x, t = tile.y;
+    const int cnt = w.bcnt[c];
+    if (cnt == 0) return;  // no query probes this cluster
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int S = ix.S, BN = w.BN, kch = ix.Dtot / kTcBK;
+    const int nchunk = (cnt + BN - 1) / BN;
+    const int64_t v0 = ix.vec_off[c];
+    const int nc = (int)(ix.vec_off[c + 1] - v0);
+    const int row0 = (int)(v0 + (int64_t)t * kTcBM);
+
+    const uint32_t raw = smem_u32(tc_smem);
+    const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
+    uint8_t *sm = tc_smem + pad;
+    const uint32_t sA = raw + pad, sB = sA + kTcStages * kTcStageBytes;
+    uint8_t *pB = sm + kTcStages * kTcStageBytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + 2 * kTcStages * kTcStageBytes);
+    // barriers: afull[st] (TMA bytes), bfull[st] (4 query warps), empty[st] (MMA done), accf, done
+    const uint32_t b0 = smem_u32(bars);
+    auto afull = [&](int st) { return b0 + 8u * st; };
+    auto bfull = [&](int st) { return b0 + 8u * (kTcStages + st); };
+    auto empty = [&](int st) { return b0 + 8u * (2 * kTcStages + st); };
+    const uint32_t accf = b0 + 8u * (3 * kTcStages), done = accf + 8u;
+    int *misc = reinterpret_cast<int *>(bars + 3 * kTcStages + 2);  // [0] TMEM address, [1] abort
+    int *pq = misc + 4;                                            // [kTcMaxN] query of each column
+    int *pj = pq + kTcMaxN;                                        // [kTcMaxN] probe index
+    float *ssum = reinterpret_cast<float *>(pj + kTcMaxN);         // [S * BN] residual sums
+    float *ssq = ssum + kTcCols;                                   // [S * BN] residual squared norms
+    volatile int *abort = misc + 1;
+
+    int ncols = 32;
+    while (ncols < S * BN) ncols <<= 1;
+    if (tid == 0) {
+        for (int st = 0; st < kTcStages; ++st) {
+            mbar_init(afull(st), 1);
+            mbar_init(bfull(st), 4);
+            mbar_init(empty(st), 1);
+        }
+        mbar_init(accf, 1);
+        mbar_init(done, 1);
+        misc[1] = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(misc)),
+                     "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = (uint32_t)misc[0];
+
+    if (warp == 0) {
+        // ---- TMA producer: the code tile, 64 dims per stage
+        if (lane == 0) {
+            int it = 0;
+            bool ok = true;
+            for (int ch = 0; ch < nchunk && ok; ++ch)
+                for (int kc = 0; kc < kch; ++kc, ++it) {
+                    const int st = it % kTcStages;
+                    const uint32_t ph = (uint32_t)(it / kTcStages) & 1u;
+                    if (!mbar_wait(empty(st), ph ^ 1u, abort)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_expect_tx(afull(st), kTcStageBytes);
+                    tma_load_2d(sA + st * kTcStageBytes, &tmA, afull(st), kc * kTcBK, row0);
+                }
+            if (!ok) {
+                atomicExch(w.err, 1);
+                for (int k = max(0, it - kTcStages); k < it; ++k)  // copies possibly in flight
+                    mbar_drain(afull(k % kTcStages), (uint32_t)(k / kTcStages) & 1u);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---- MMA issuer
+        if (lane == 0) {
+            int it = 0;
+            bool ok = true;
+            for (int ch = 0; ch < nchunk && ok; ++ch) {
+                const int nh = min(BN, cnt - ch * BN), npad = (nh + 15) & ~15;
+                const uint32_t idesc = idesc_bf16(npad);
+                for (int kc = 0; kc < kch; ++kc, ++it) {
+                    const int st = it % kTcStages;
+                    const uint32_t ph = (uint32_t)(it / kTcStages) & 1u;
+                    if (!mbar_wait(afull(st), ph, abort) || !mbar_wait(bfull(st), ph, abort)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const int k0 = kc * kTcBK;
+                    int s = 0;
+                    while (s + 1 < S && k0 >= ix.seg[s + 1].qoff) ++s;
+                    const bool first = k0 == ix.seg[s].qoff;
+                    const uint32_t d = tmem + (uint32_t)(s * BN);
+                    const uint64_t da = sw128_desc(sA + st * kTcStageBytes), db = sw128_desc(sB + st * kTcStageBytes);
+#pragma unroll
+                    for (int kk = 0; kk < kTcBK / 16; ++kk)  // 16 BF16 = 32 bytes per instruction
+                        mma_bf16(d, da + 2 * kk, db + 2 * kk, idesc, (first && kk == 0) ? 0u : 1u);
+                    mma_commit(empty(st));
+                }
+                if (ok) mma_commit(accf);
+            }
+            if (!ok) atomicExch(w.err, 1);
+            mma_commit(done);  // every MMA issued has finished once `done` completes
+            mbar_drain(done, 0);
+        }
+        __syncwarp();
+    } else {
+        // ---- query operand (residuals in BF16) and epilogue: warps 2-5
+        const int tb = tid - 64, qt = warp & 3;
+        const int r = qt * 32 + lane, rl = t * kTcBM + r;
+        const bool vrow = rl < nc;
+        const int64_t gv = v0 + rl, gb = ix.blk_off[c] + rl / 32;
+        const int ln = rl & 31;
+        int it = 0;
+        bool ok = true;
+        for (int ch = 0; ch < nchunk; ++ch) {
+            const int nh = min(BN, cnt - ch * BN), npad = (nh + 15) & ~15, nu = npad / 16;
+            for (int n = tb; n < nh; n += 128) {
+                const int p = w.bucket[w.boff[c] + (long long)ch * BN + n];
+                pq[n] = p / w.nprobe;
+                pj[n] = p - (p / w.nprobe) * w.nprobe;
+            }
+            named_sync(1, 128);
+            float as[kTcMaxN / 16], aq[kTcMaxN / 16];
+#pragma unroll
+            for (int u = 0; u < kTcMaxN / 16; ++u) as[u] = aq[u] = 0.0f;
+            for (int kc = 0; kc < kch; ++kc, ++it) {
+                const int st = it % kTcStages;
+                const uint32_t ph = (uint32_t)(it / kTcStages) & 1u;
+                if (ok && !mbar_wait(empty(st), ph ^ 1u, abort)) ok = false;
+                const int k0 = kc * kTcBK;
+                int s = 0;
+                while (s + 1 < S && k0 >= ix.seg[s + 1].qoff) ++s;
+                const SegDev &g = ix.seg[s];
+                const float *cen = g.cent + (size_t)c * g.dim + (k0 - g.qoff);
+                uint8_t *dstB = pB + st * kTcStageBytes;
+#pragma unroll
+                for (int u = 0; u < kTcMaxN / 16; ++u) {
+                    if (u >= nu) break;
+                    const int idx = tb + 128 * u, n = idx >> 3, j = idx & 7;
+                    uint4 out = make_uint4(0, 0, 0, 0);
+                    float ps = 0.0f, pq2 = 0.0f;
+                    if (ok && n < nh) {
+                        const float4 *qr = reinterpret_cast<const float4 *>(w.qrot + (size_t)pq[n] * ix.Dtot + k0 + 8 * j);
+                        const float4 *cr = reinterpret_cast<const float4 *>(cen + 8 * j);
+                        const float4 a0 = qr[0], a1 = qr[1], c0 = __ldg(cr), c1 = __ldg(cr + 1);
+                        const float e[8] = {__fsub_rn(a0.x, c0.x), __fsub_rn(a0.y, c0.y), __fsub_rn(a0.z, c0.z),
+                                            __fsub_rn(a0.w, c0.w), __fsub_rn(a1.x, c1.x), __fsub_rn(a1.y, c1.y),
+                                            __fsub_rn(a1.z, c1.z), __fsub_rn(a1.w, c1.w)};
+#pragma unroll
+                        for (int h = 0; h < 8; ++h) {
+                            ps = __fadd_rn(ps, e[h]);
+                            pq2 = __fmaf_rn(e[h], e[h], pq2);
+                        }
+                        out = make_uint4(pack_bf16x2(e[0], e[1]), pack_bf16x2(e[2], e[3]), pack_bf16x2(e[4], e[5]),
+                                         pack_bf16x2(e[6], e[7]));
+                    }
+                    *reinterpret_cast<uint4 *>(dstB + n * 128 + ((j ^ (n & 7)) << 4)) = out;
+                    // the row's 8 chunks sit in 8 consecutive lanes: butterfly sums (same value in all 8)
+#pragma unroll
+                    for (int o = 1; o < 8; o <<= 1) {
+                        ps = __fadd_rn(ps, __shfl_xor_sync(kFullMask, ps, o));
+                        pq2 = __fadd_rn(pq2, __shfl_xor_sync(kFullMask, pq2, o));
+                    }
+                    as[u] = __fadd_rn(as[u], ps);
+                    aq[u] = __fadd_rn(aq[u], pq2);
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(bfull(st));
+                if (k0 + kTcBK == g.qoff + g.dim) {  // segment complete: its per-pair scalars
+#pragma unroll
+                    for (int u = 0; u < kTcMaxN / 16; ++u) {
+                        if (u >= nu) break;
+                        const int idx = tb + 128 * u, n = idx >> 3;
+                        if ((idx & 7) == 0 && n < nh) {
+                            ssum[s * BN + n] = as[u];
+                            ssq[s * BN + n] = aq[u];
+                        }
+                        as[u] = aq[u] = 0.0f;
+                    }
+                }
+            }
+            named_sync(1, 128);  // scalars of every pair visible
+            if (ok && !mbar_wait(accf, (uint32_t)ch & 1u, abort)) ok = false;
+            tc_fence_after();
+            const bool good = __all_sync(kFullMask, ok);
+            if (good) {
+                for (int n0 = 0; n0 < npad; n0 += 16) {
+                    float d[16];
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) d[i] = 0.0f;
+                    for (int s = 0; s < S; ++s) {
+                        float v[16];
+                        tmem_ld16(tmem + ((uint32_t)(qt * 32) << 16) + (uint32_t)(s * BN + n0), v);
+                        const SegDev &g = ix.seg[s];
+                        const float on = vrow ? g.onorm[gb * 32 + ln] : 0.0f;
+                        const float o2 = __fmul_rn(on, on), rs = vrow ? g.exfac[gv].x : 0.0f;
+                        const float dl = 2.0f / (float)(1 << g.bits), cst = __fsub_rn(__fmul_rn(dl, 0.5f), 1.0f);
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) {
+                            const int n = n0 + i;
+                            const float sq = n < nh ? ssum[s * BN + n] : 0.0f, q2 = n < nh ? ssq[s * BN + n] : 0.0f;
+                            const float ip = __fmaf_rn(dl, v[i], __fmul_rn(cst, sq));
+                            d[i] = __fadd_rn(d[i], __fsub_rn(__fadd_rn(o2, q2), __fmul_rn(2.0f, __fmul_rn(rs, ip))));
+                        }
+                    }
+                    if (vrow) {
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) {
+                            const int n = n0 + i;
+                            if (n < nh) {
+                                const int qi = pq[n];
+                                w.cand[w.qbase[qi] + w.lp[(size_t)qi * (w.nprobe + 1) + pj[n]] + rl] = d[i];
+                            }
+                        }
+                    }
+                }
+            } else if (lane == 0) {
+                atomicExch(w.err, 1);
+            }
+            tc_fence_before();
+            named_sync(1, 128);  // pair lists and scalars are rewritten by the next chunk
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    }
+}
+
+constexpr size_t tc_contract_smem() {
+    return 1024 + 2 * (size_t)kTcStages * kTcStageBytes + 8 * (3 * kTcStages + 2) + 16 + 8 * kTcMaxN + 8 * kTcCols;
+}
+
+// ------------------------------------------------------------ shortlist
+__device__ __forceinline__ uint32_t dkey(float f) {
+    if (f != f) return 0xffffffffu;
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// Block-wide exclusive scan of a 0/1 flag (256 threads); returns the prefix
+// and the block total in *tot.
+__device__ __forceinline__ int block_prefix(int f, int *wtot, int *tot) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned b = __ballot_sync(kFullMask, f);
+    if (lane == 0) wtot[w] = __popc(b);
+    __syncthreads();
+    int base = 0, all = 0;
+    for (int i = 0; i < 8; ++i) {
+        base += i < w ? wtot[i] : 0;
+        all += wtot[i];
+    }
+    __syncthreads();
+    *tot = all;
+    return base + __popc(b & ((1u << lane) - 1u));
+}
+
+// The L smallest approximate distances of one query (ties: earlier position),
+// written in candidate order with their distances.
+__global__ void __launch_bounds__(256) k_tc_select(const float *__restrict__ cand, const long long *__restrict__ qbase,
+                                                   const int *__restrict__ qtot, int L, int *__restrict__ sl_pos,
+                                                   float *__restrict__ sl_apx, int *__restrict__ sl_cnt) {
+    __shared__ int hist[256];
+    __shared__ int wtot[8];
+    __shared__ uint32_t s_prefix;
+    __shared__ int s_need;
+    const int qi = blockIdx.x, tid = threadIdx.x;
+    const int M = qtot[qi];
+    const float *x = cand + qbase[qi];
+    int *po = sl_pos + (size_t)qi * L;
+    float *ao = sl_apx + (size_t)qi * L;
+    const int take = min(L, M);
+    if (tid == 0) sl_cnt[qi] = take;
+    if (M <= L) {
+        for (int e = tid; e < M; e += 256) {
+            po[e] = e;
+            ao[e] = x[e];
+        }
+        return;
+    }
+    // radix select of the L-th smallest key, 8 bits per pass
+    uint32_t prefix = 0, mask = 0;
+    int need = L;
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        hist[tid] = 0;
+        __syncthreads();
+        for (int e = tid; e < M; e += 256) {
+            const uint32_t k = dkey(x[e]);
+            if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255], 1);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int acc = 0, b = 0;
+            while (acc + hist[b] < need) acc += hist[b++];
+            s_prefix = prefix | ((uint32_t)b << shift);
+            s_need = need - acc;
+        }
+        __syncthreads();
+        prefix = s_prefix;
+        need = s_need;
+        mask |= 255u << shift;
+        __syncthreads();
+    }
+    // keys below the threshold, then the first `need` equal keys, in candidate order
+    int taken = 0, eq_seen = 0;
+    for (int e0 = 0; e0 < M; e0 += 256) {
+        const int e = e0 + tid;
+        const uint32_t k = e < M ? dkey(x[e]) : 0xffffffffu;
+        const int lt = e < M && k < prefix, eq = e < M && k == prefix;
+        int eq_tot;
+        const int eq_rank = eq_seen + block_prefix(eq, wtot, &eq_tot);
+        const int f = lt || (eq && eq_rank < need);
+        int f_tot;
+        const int slot = taken + block_prefix(f, wtot, &f_tot);
+        if (f) {
+            po[slot] = e;
+            ao[slot] = x[e];
+        }
+        taken += f_tot;
+        eq_seen += eq_tot;
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ host
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    if (!fn) throw Error{SAQG_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver"};
+    return fn;
+}
+
+// The BF16 code matrix and the tile list of an index, built on first use.
+void ensure_tc_state(const Index &I, cudaStream_t st) {
+    std::lock_guard<std::mutex> lk(I.init_mu);
+    if (I.tc_codes) return;
+    const DevIndexView &ix = I.view;
+    const size_t bytes = 2 * (size_t)I.N * ix.Dtot;
+    void *A = nullptr, *cl = nullptr, *tiles = nullptr;
+    std::vector<int2> ht;
+    for (int64_t c = 0; c < I.K; ++c)
+        for (int64_t t = 0; t * kTcBM < I.sizes[c]; ++t) ht.push_back(make_int2((int)c, (int)t));
+    SAQG_CUDA_TRY(cudaMalloc(&A, std::max<size_t>(bytes, 16)));
+    try {
+        SAQG_CUDA_TRY(cudaMalloc(&cl, 4 * std::max<size_t>(1, (size_t)I.N)));
+        SAQG_CUDA_TRY(cudaMalloc(&tiles, sizeof(int2) * std::max<size_t>(1, ht.size())));
+        if (!ht.empty())
+            SAQG_CUDA_TRY(cudaMemcpyAsync(tiles, ht.data(), sizeof(int2) * ht.size(), cudaMemcpyHostToDevice, st));
+        if (I.N > 0) {
+            k_tc_cluster_of<<<(unsigned)I.K, 256, 0, st>>>(ix.vec_off, (int)I.K, static_cast<int32_t *>(cl));
+            const int64_t work = I.N * (ix.Dtot / 8);
+            k_tc_codes<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(ix, static_cast<const int32_t *>(cl), I.N,
+                                                                      static_cast<__nv_bfloat16 *>(A));
+            const cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) throw Error{SAQG_ERR_CUDA, std::string("k_tc_codes launch failed: ") + cudaGetErrorString(e)};
+            count_launch(2);
+        }
+        SAQG_CUDA_TRY(cudaStreamSynchronize(st));
+    } catch (...) {
+        cudaFree(A);
+        if (cl) cudaFree(cl);
+        if (tiles) cudaFree(tiles);
+        throw;
+    }
+    cudaFree(cl);
+    I.tc_codes = A;
+    I.tc_tiles = tiles;
+    I.tc_ntiles = (int64_t)ht.size();
+}
+
+void launch_check(const char *what) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw Error{SAQG_ERR_CUDA, std::string(what) + " launch failed: " + cudaGetErrorString(e)};
+}
+
+size_t a16(size_t x) { return (x + 15) & ~size_t(15); }
+
+}  // namespace
+
+void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, int64_t L, float m,
+                   uint32_t *ids, float *dists, float *approx, int mem, cudaStream_t st, saqg_tc_stats *stats) {
+    const DevIndexView &ix = I.view;
+    SAQG_REQUIRE(nq >= 0 && nq <= kTcMaxBatch, "the tensor-core search takes at most 8192 queries per call");
+    SAQG_REQUIRE(topk >= 1 && topk <= kTcMaxShort, "topk must be in [1, 1024]");
+    SAQG_REQUIRE(L >= topk && L <= kTcMaxShort, "shortlist must be in [topk, 1024]");
+    SAQG_REQUIRE(nprobe >= 1 && nprobe <= I.K, "nprobe must be in [1, number of clusters]");
+    for (int s = 0; s < ix.S; ++s)
+        SAQG_REQUIRE(ix.seg[s].bits >= 1 && ix.seg[s].dim % kTcBK == 0,
+                     "the tensor-core search needs every segment coded (bits >= 1) and 64-dim aligned");
+    SAQG_REQUIRE(I.N < (int64_t)1 << 31 && nq * nprobe < (int64_t)1 << 31, "index or batch too large");
+    if (nq == 0) return;
+    int BN = std::min(kTcMaxN, (kTcCols / ix.S) / 16 * 16);
+    SAQG_REQUIRE(BN >= 16, "too many segments for the tensor-core search");
+    ensure_tc_state(I, st);
+
+    SearchCtx &C = I.ctx;
+    std::lock_guard<std::mutex> lock(C.mu);
+    const bool host = mem == SAQG_MEM_HOST;
+    const int64_t P = nq * nprobe;
+    size_t need = 0;
+    auto add = [&](size_t b) { need += a16(b); };
+    add(4 * (size_t)nq * I.D);                  // queries
+    add(4 * (size_t)nq * I.K);                  // centroid distances
+    add(tc_probe_work_bytes(I, nq));            // selection work
+    add(4 * (size_t)P);                         // probes
+    add(4 * (size_t)nq * ix.Dtot);              // rotated queries
+    add(4 * (size_t)nq * ix.S);                 // prune bounds
+    add((size_t)nq);                            // full-path flags
+    add(4 * (size_t)nq);                        // full-path list
+    add(64);                                    // flags
+    add(4 * (size_t)nq * (nprobe + 1));         // lp
+    add(4 * (size_t)nq);                        // qtot
+    add(8 * (size_t)(nq + 1));                  // qbase
+    add(4 * (size_t)I.K * 2);                   // bcnt, bfill
+    add(8 * (size_t)(I.K + 1));                 // boff
+    add(4 * (size_t)P * 2);                     // bucket, sorted
+    add(4 * (size_t)nq * L * 2);                // sl_pos, sl_apx
+    add(4 * (size_t)nq);                        // sl_cnt
+    add(4 * (size_t)nq * topk * 3);             // outputs (host io)
+    add(16);                                    // error word
+    char *base = static_cast<char *>(C.scratch_get(need + 256));
+    size_t off = 0;
+    auto take = [&](size_t b) {
+        char *p = base + off;
+        off += a16(b);
+        return p;
+    };
+    float *dq = reinterpret_cast<float *>(take(4 * (size_t)nq * I.D));
+    float *dist = reinterpret_cast<float *>(take(4 * (size_t)nq * I.K));
+    void *work = take(tc_probe_work_bytes(I, nq));
+    uint32_t *probe = reinterpret_cast<uint32_t *>(take(4 * (size_t)P));
+    float *qrot = reinterpret_cast<float *>(take(4 * (size_t)nq * ix.Dtot));
+    float *prune = reinterpret_cast<float *>(take(4 * (size_t)nq * ix.S));
+    uint8_t *full = reinterpret_cast<uint8_t *>(take((size_t)nq));
+    int *fb = reinterpret_cast<int *>(take(4 * (size_t)nq));
+    int *flags = reinterpret_cast<int *>(take(64));
+    int *lp = reinterpret_cast<int *>(take(4 * (size_t)nq * (nprobe + 1)));
+    int *qtot = reinterpret_cast<int *>(take(4 * (size_t)nq));
+    long long *qbase = reinterpret_cast<long long *>(take(8 * (size_t)(nq + 1)));
+    int *bcnt = reinterpret_cast<int *>(take(4 * (size_t)I.K * 2));
+    int *bfill = bcnt + I.K;
+    long long *boff = reinterpret_cast<long long *>(take(8 * (size_t)(I.K + 1)));
+    int *bucket = reinterpret_cast<int *>(take(4 * (size_t)P * 2));
+    int *sorted = bucket + P;
+    int *sl_pos = reinterpret_cast<int *>(take(4 * (size_t)nq * L * 2));
+    float *sl_apx = reinterpret_cast<float *>(sl_pos + nq * L);
+    int *sl_cnt = reinterpret_cast<int *>(take(4 * (size_t)nq));
+    uint32_t *oid = reinterpret_cast<uint32_t *>(take(4 * (size_t)nq * topk * 3));
+    float *od = reinterpret_cast<float *>(oid + nq * topk);
+    float *oa = od + nq * topk;
+    int *err = reinterpret_cast<int *>(take(16));
+
+    cudaEvent_t ev[6] = {};
+    struct EvGuard {
+        cudaEvent_t *e;
+        ~EvGuard() {
+            for (int i = 0; i < 6; ++i)
+                if (e[i]) cudaEventDestroy(e[i]);
+        }
+    } evg{ev};
+    if (stats)
+        for (auto &e : ev) SAQG_CUDA_TRY(cudaEventCreate(&e));
+    auto mark = [&](int i) {
+        if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[i], st));
+    };
+
+    const float *qin = q;
+    if (host) {
+        SAQG_CUDA_TRY(cudaMemcpyAsync(dq, q, 4 * (size_t)nq * I.D, cudaMemcpyHostToDevice, st));
+        qin = dq;
+    }
+    mark(0);
+    tc_rank_rotate(I, C, qin, nq, nprobe, m, dist, work, probe, qrot, prune, full, fb, flags, st);
+    mark(1);
+    // pairs: candidate offsets per query, buckets per cluster
+    SAQG_CUDA_TRY(cudaMemsetAsync(bcnt, 0, 8 * (size_t)I.K, st));
+    SAQG_CUDA_TRY(cudaMemsetAsync(err, 0, 16, st));
+    k_tc_pairs<<<(unsigned)((nq + 7) / 8), 256, 0, st>>>(ix, probe, (int)nq, (int)nprobe, lp, qtot, bcnt);
+    launch_check("k_tc_pairs");
+    k_excl_scan<<<1, 1024, 0, st>>>(qtot, (int)nq, qbase);
+    launch_check("k_excl_scan");
+    k_excl_scan<<<1, 1024, 0, st>>>(bcnt, (int)I.K, boff);
+    launch_check("k_excl_scan");
+    k_tc_fill<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(probe, (int)P, boff, bfill, bucket);
+    launch_check("k_tc_fill");
+    k_tc_sort<<<(unsigned)I.K, 256, 0, st>>>(bcnt, boff, bucket, sorted);
+    launch_check("k_tc_sort");
+    long long total = 0;
+    SAQG_CUDA_TRY(cudaMemcpyAsync(&total, qbase + nq, 8, cudaMemcpyDeviceToHost, st));
+    SAQG_CUDA_TRY(cudaStreamSynchronize(st));
+    float *cand = static_cast<float *>(C.split_scratch_get(4 * (size_t)std::max<long long>(total, 1)));
+    mark(2);
+    // contraction
+    CUtensorMap tmA;
+    {
+        const cuuint64_t gdim[2] = {(cuuint64_t)ix.Dtot, (cuuint64_t)std::max<int64_t>(I.N, 1)};
+        const cuuint64_t gstride[1] = {(cuuint64_t)ix.Dtot * 2};
+        const cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)kTcBM};
+        const cuuint32_t estr[2] = {1, 1};
+        const CUresult r = tensor_map_encoder()(&tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, I.tc_codes, gdim, gstride,
+                                                box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) throw Error{SAQG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r)};
+    }
+    TcWork wk;
+    wk.tiles = static_cast<const int2 *>(I.tc_tiles);
+    wk.bcnt = bcnt;
+    wk.boff = boff;
+    wk.bucket = sorted;
+    wk.qrot = qrot;
+    wk.lp = lp;
+    wk.qbase = qbase;
+    wk.cand = cand;
+    wk.nprobe = (int)nprobe;
+    wk.BN = BN;
+    wk.err = err;
+    const size_t smem = tc_contract_smem();
+    SAQG_CUDA_TRY(cudaFuncSetAttribute(k_tc_contract, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (I.tc_ntiles > 0) {
+        k_tc_contract<<<(unsigned)I.tc_ntiles, kTcThreads, smem, st>>>(tmA, ix, wk);
+        launch_check("k_tc_contract");
+    }
+    mark(3);
+    k_tc_select<<<(unsigned)nq, 256, 0, st>>>(cand, qbase, qtot, (int)L, sl_pos, sl_apx, sl_cnt);
+    launch_check("k_tc_select");
+    mark(4);
+    tc_rerank(I, probe, nq, nprobe, qrot, prune, lp, sl_pos, sl_apx, sl_cnt, (int)L, topk, host ? oid : ids,
+              host ? od : dists, host ? oa : approx, st);
+    mark(5);
+    count_launch(7);
+    int herr = 0;
+    SAQG_CUDA_TRY(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+    if (host) {
+        SAQG_CUDA_TRY(cudaMemcpyAsync(ids, oid, 4 * (size_t)nq * topk, cudaMemcpyDeviceToHost, st));
+        if (dists) SAQG_CUDA_TRY(cudaMemcpyAsync(dists, od, 4 * (size_t)nq * topk, cudaMemcpyDeviceToHost, st));
+        if (approx) SAQG_CUDA_TRY(cudaMemcpyAsync(approx, oa, 4 * (size_t)nq * topk, cudaMemcpyDeviceToHost, st));
+    }
+    SAQG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (herr) throw Error{SAQG_ERR_INTERNAL, "tensor-core contraction: a pipeline wait timed out"};
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        float t[5] = {0, 0, 0, 0, 0};
+        for (int i = 0; i < 5; ++i) SAQG_CUDA_TRY(cudaEventElapsedTime(&t[i], ev[i], ev[i + 1]));
+        stats->ms_probe = t[0];
+        stats->ms_pairs = t[1];
+        stats->ms_contract = t[2];
+        stats->ms_select = t[3];
+        stats->ms_rerank = t[4];
+        std::vector<int> hc((size_t)I.K);
+        SAQG_CUDA_TRY(cudaMemcpy(hc.data(), bcnt, 4 * (size_t)I.K, cudaMemcpyDeviceToHost));
+        int64_t flops = 0, bytes = 0, tiles = 0, padded = 0;
+        for (int64_t c = 0; c < I.K; ++c) {
+            if (!hc[c]) continue;
+            const int64_t nt = (I.sizes[c] + kTcBM - 1) / kTcBM;
+            flops += 2 * (int64_t)ix.Dtot * hc[c] * I.sizes[c];
+            bytes += 2 * (int64_t)ix.Dtot * I.sizes[c];
+            tiles += nt;
+            const int64_t nch = (hc[c] + BN - 1) / BN, npad = (nch - 1) * BN + (((hc[c] - (nch - 1) * BN) + 15) & ~15);
+            padded += 2 * (int64_t)ix.Dtot * kTcBM * nt * npad;
+        }
+        stats->pairs = P;
+        stats->candidates = total;
+        stats->tiles = tiles;
+        stats->flops = flops;
+        stats->mma_flops = padded;
+        stats->code_bytes = bytes;
+    }
+}
+
+}  // namespace saqg

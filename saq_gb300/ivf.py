@@ -179,6 +179,46 @@ class IVF:
                                                N.SAQG_MEM_HOST, _stream_ptr(stream), None))
         return (ids, dists) if return_dists else ids
 
+    def search_tc(self, query, topk: int, nprobe: int, shortlist: int | None = None,
+                  searcher_cfg: SearcherConfig | None = None, return_dists: bool = False,
+                  return_approx: bool = False, stats: bool = False, stream=None):
+        """Tensor-core form of a batched search (saqg_search_tc): the approximate
+        distances of every probed vector come from one dense BF16 product per
+        cluster on the tensor cores, the `shortlist` (default 4 * topk) smallest
+        per query are re-ranked with the exact search's distance.  Returns ids
+        [, dists] [, approx] [, stats dict]."""
+        cfg = (searcher_cfg or SearcherConfig()).to_c()
+        L = int(shortlist if shortlist is not None else max(4 * topk, topk))
+        st = N.TcStats()
+        sp = C.byref(st) if stats else None
+        if _is_cuda_tensor(query):
+            import torch
+            q = query.contiguous().view(-1, self.num_dim)
+            nq = q.shape[0]
+            ids = torch.empty((nq, topk), dtype=torch.int32, device=q.device)
+            dists = torch.empty((nq, topk), dtype=torch.float32, device=q.device)
+            apx = torch.empty((nq, topk), dtype=torch.float32, device=q.device)
+            N.check(self.lib.saqg_search_tc(self._h, q.data_ptr(), nq, topk, nprobe, L, C.byref(cfg), ids.data_ptr(),
+                                            dists.data_ptr(), apx.data_ptr(), N.SAQG_MEM_DEVICE, _stream_ptr(stream),
+                                            sp))
+        else:
+            q = np.ascontiguousarray(query, np.float32).reshape(-1, self.num_dim)
+            nq = q.shape[0]
+            ids = np.zeros((nq, topk), np.uint32)
+            dists = np.zeros((nq, topk), np.float32)
+            apx = np.zeros((nq, topk), np.float32)
+            N.check(self.lib.saqg_search_tc(self._h, q.ctypes.data, nq, topk, nprobe, L, C.byref(cfg), ids.ctypes.data,
+                                            dists.ctypes.data, apx.ctypes.data, N.SAQG_MEM_HOST, _stream_ptr(stream),
+                                            sp))
+        out = [ids]
+        if return_dists:
+            out.append(dists)
+        if return_approx:
+            out.append(apx)
+        if stats:
+            out.append(st.as_dict())
+        return out[0] if len(out) == 1 else tuple(out)
+
     def estimate(self, query, nprobe: int, searcher_cfg: SearcherConfig | None = None):
         """IVF::estimate: ([(id, accurate)], fast list, vars list) for every vector of the probed clusters."""
         cfg = (searcher_cfg or SearcherConfig()).to_c()

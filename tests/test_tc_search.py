@@ -1,0 +1,130 @@
+"""Tensor-core form of the batched search (saqg_search_tc).
+
+The approximate distances come from the tensor cores; what the form returns is
+checked against the oracle: every returned (id, distance) must be the oracle's
+exact search distance for that vector (IVF::estimate's accurate distance for
+one segment, bit for bit), and with a shortlist that holds every candidate the
+answer must equal the oracle's top-k of those distances over all probed
+vectors (ties: the later-scanned vector first).  With the default shortlist of
+4 k, recall@10 against that full top-10 is measured and bounded."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import GOLDEN
+from saq_gb300 import data
+
+pytestmark = pytest.mark.gpu
+
+
+def _build(tmp, bits, seg, d=256, n=8000, k=128, seed=11, eqseg=0):
+    from saq_gb300 import ivf
+    x, q = data.gaussian_mixture(n, d, 200, sigma=0.6, seed=seed, n_query=300)
+    cent, cids = data.kmeans(x, k, iters=6, seed=2)
+    rng = np.random.default_rng(5)
+    plan = O.plan(O.colwise_var(x), float(bits), seg, eqseg)
+    rots = np.concatenate([data.random_orthogonal(dd, rng).astype(np.float32).reshape(-1) for dd, _ in plan])
+    index = ivf.IVF(n, d, k, ivf.QuantizeConfig(avg_bits=float(bits), enable_segmentation=seg,
+                                                     seg_eqseg=eqseg))
+    index.construct(x, cent, cids, rotations=rots)
+    opath = str(tmp / f"tc_{bits}_{int(seg)}.index")
+    O.build_index(opath, x, cent, cids, float(bits), seg, eqseg, rots)
+    return index, O.OracleIndex(opath), q, plan
+
+
+@pytest.fixture(scope="module", params=[6, 8, 4])
+def built(request, tmp_path_factory):
+    return _build(tmp_path_factory.mktemp("tc"), request.param, False)
+
+
+def _full_topk(oi, q, nprobe, topk):
+    """Oracle: top-k over every probed vector by the accurate distance, equal
+    distances the later position first."""
+    ids, acc, _, _ = oi.estimate(q, nprobe)
+    order = sorted(range(len(acc)), key=lambda e: (np.float32(acc[e]), -e))[:topk]
+    return ids[order], acc[order], dict(zip(ids.tolist(), acc.tolist())), len(acc)
+
+
+@pytest.mark.parametrize("nq", [300, 20])
+def test_full_shortlist_equals_oracle_topk(built, nq):
+    index, oi, q, plan = built
+    assert len(plan) == 1
+    nprobe, topk = 3, 10
+    ids, d = index.search_tc(q[:nq], topk, nprobe, shortlist=1024, return_dists=True)
+    covered = 0
+    for i in range(nq):
+        oid, od, _, m = _full_topk(oi, q[i], nprobe, topk)
+        if m > 1024:  # the shortlist does not hold every candidate of this query
+            continue
+        covered += 1
+        assert np.array_equal(ids[i], oid), i
+        assert np.array_equal(d[i].view(np.uint32), od.astype(np.float32).view(np.uint32)), i
+    assert covered >= 0.8 * nq
+
+
+def test_default_shortlist(built):
+    index, oi, q, _ = built
+    nprobe, topk = 16, 10
+    ids, d, apx, st = index.search_tc(q, topk, nprobe, return_dists=True, return_approx=True, stats=True)
+    hits, rel = 0, []
+    for i in range(q.shape[0]):
+        oid, od, accmap, _ = _full_topk(oi, q[i], nprobe, topk)
+        for j in range(topk):  # every returned distance is the oracle's for that id
+            assert accmap[int(ids[i, j])] == d[i, j], (i, j)
+        assert np.all(np.diff(d[i]) >= 0)
+        hits += len(set(ids[i].tolist()) & set(oid.tolist()))
+        rel.extend(np.abs(apx[i] - d[i]) / np.maximum(np.abs(d[i]), 1e-6))
+    recall = hits / (q.shape[0] * topk)
+    assert recall >= 0.98, recall
+    assert np.median(rel) < 2e-2, np.median(rel)
+    assert st["pairs"] == q.shape[0] * nprobe and st["flops"] > 0 and st["ms_contract"] > 0
+
+
+def test_batch_equals_single_queries(built):
+    index, _, q, _ = built
+    nprobe, topk = 12, 10
+    ids, d = index.search_tc(q[:96], topk, nprobe, return_dists=True)
+    for i in (0, 17, 95):
+        si, sd = index.search_tc(q[i:i + 1], topk, nprobe, return_dists=True)
+        assert np.array_equal(si[0], ids[i]) and np.array_equal(sd[0], d[i]), i
+
+
+def test_device_buffers_match_host(built):
+    torch = pytest.importorskip("torch")
+    index, _, q, _ = built
+    ids, d = index.search_tc(q[:128], 10, 8, return_dists=True)
+    qt = torch.as_tensor(q[:128], device="cuda")
+    tids, td = index.search_tc(qt, 10, 8, return_dists=True)
+    torch.cuda.synchronize()
+    assert np.array_equal(tids.cpu().numpy().view(np.uint32), ids)
+    assert np.array_equal(td.cpu().numpy(), d)
+
+
+def test_multi_segment_distances_match_search(tmp_path):
+    """Several coded segments: a returned id that the exact search also
+    returns carries the exact search's distance bit for bit."""
+    index, oi, q, plan = _build(tmp_path, 6, True, d=384, n=6000, k=64, seed=4, eqseg=3)
+    assert len(plan) == 3 and all(b >= 1 for _, b in plan), plan
+    nprobe, topk = 8, 10
+    ids, d = index.search_tc(q[:120], topk, nprobe, shortlist=200, return_dists=True)
+    oids, od = oi.search(q[:120], topk, nprobe, with_dists=True)
+    common = 0
+    for i in range(120):
+        ref = dict(zip(oids[i].tolist(), od[i].tolist()))
+        for j in range(topk):
+            if int(ids[i, j]) in ref:
+                common += 1
+                assert np.float32(ref[int(ids[i, j])]) == d[i, j], (i, j)
+    assert common >= 0.9 * 120 * topk
+
+
+def test_rejects_uncoded_segments(golden_case_by_name):
+    """An index with a 0-bit segment has no codes there to contract."""
+    from saq_gb300 import _native as N, ivf
+    z = np.load(os.path.join(GOLDEN, "aniso_b15_seg_0bit.npz"))
+    assert any(int(b) == 0 for _, b in z["plan"])
+    index = ivf.IVF.load(golden_case_by_name("aniso_b15_seg_0bit"))
+    with pytest.raises(N.SaqgError, match="every segment coded"):
+        index.search_tc(z["q"][:4], 10, 4)
