@@ -171,7 +171,8 @@ void tc_rank_rotate(const Index &idx, SearchCtx &ctx, const float *q, int64_t nq
 size_t tc_probe_work_bytes(const Index &idx, int64_t nq);
 void tc_rerank(const Index &idx, const uint32_t *probe, int64_t nq, int64_t nprobe, const float *qrot,
                const float *prune, const int *lp, const int *sl_pos, const float *sl_apx, const int *sl_cnt, int L,
-               int64_t topk, uint32_t *ids, float *dists, float *apx, cudaStream_t st);
+               int64_t topk, int *grp, int *gj, int *ng, float *sl_dist, uint32_t *ids, float *dists, float *apx,
+               cudaStream_t st);
 // tc_search.cu
 void run_search_tc(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, int64_t shortlist,
                    float m, uint32_t *ids, float *dists, float *approx, int mem, cudaStream_t st,

@@ -2825,53 +2825,76 @@ __device__ float searched_dist(const DevIndexView &ix, const ScanSmem &sm, int64
     return __shfl_sync(kFull, d, 0);
 }
 
-// Re-rank of the tensor-core shortlist, one CTA per query.  The shortlist
-// (positions in the query's candidate order, ascending, so grouped by probe)
-// is evaluated cluster by cluster: Lut::prepare for the cluster, then every
-// shortlisted vector's distance as the search computes it (searched_dist).
-// The top-k is ordered by distance, equal distances the later-scanned first,
-// which is where ResultPool::insert puts an equal distance (pool.hpp:17-30).
+// Groups of a query's shortlist (positions ascending, so grouped by probe):
+// the first entry and the probe index of each probed cluster holding
+// shortlisted vectors.  One thread per query.
+__global__ void k_tc_groups(const int *__restrict__ sl_pos, const int *__restrict__ sl_cnt,
+                            const int *__restrict__ lp, int nq, int nprobe, int L, int *__restrict__ grp,
+                            int *__restrict__ gj, int *__restrict__ ng) {
+    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= nq) return;
+    const int n = sl_cnt[qi];
+    const int *pos = sl_pos + (size_t)qi * L;
+    const int *lq = lp + (size_t)qi * (nprobe + 1);
+    int cnt = 0, j = 0;
+    for (int e = 0; e < n; ++e) {
+        if (e > 0 && pos[e] < lq[j + 1]) continue;  // same probe as the previous entry
+        while (lq[j + 1] <= pos[e]) ++j;           // probes are visited in order
+        grp[(size_t)qi * L + cnt] = e;
+        gj[(size_t)qi * L + cnt] = j;
+        ++cnt;
+    }
+    ng[qi] = cnt;
+}
+
+// Re-rank of the tensor-core shortlist: CTA (g, query) takes the query's g-th
+// group, i.e. one probed cluster: Lut::prepare for it, then the distance the
+// search computes (searched_dist) of each of its shortlisted vectors.
 __global__ void __launch_bounds__(kScanThreads) k_tc_rerank(DevIndexView ix, const uint32_t *__restrict__ probe,
                                                             int nprobe, const float *__restrict__ qrot,
                                                             const float *__restrict__ prune,
                                                             const int *__restrict__ lp, const int *__restrict__ sl_pos,
-                                                            const float *__restrict__ sl_apx,
-                                                            const int *__restrict__ sl_cnt, int L, int L2, int topk,
-                                                            uint32_t *__restrict__ ids, float *__restrict__ dists,
-                                                            float *__restrict__ apx_out) {
+                                                            const int *__restrict__ sl_cnt, const int *__restrict__ grp,
+                                                            const int *__restrict__ gj, const int *__restrict__ ng,
+                                                            int L, float *__restrict__ sl_dist) {
     extern __shared__ __align__(16) char smem_raw[];
-    const size_t base = align16(scan_smem_bytes(ix.Dtot, ix.S, 1, 0));
+    const int qi = blockIdx.y, g = blockIdx.x;
+    const int ngq = ng[qi];
+    if (g >= ngq) return;
     ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, 1, 0);
-    float *dist = reinterpret_cast<float *>(smem_raw + base);
-    unsigned long long *key = reinterpret_cast<unsigned long long *>(smem_raw + base + align16(4 * (size_t)L));
-    const int qi = blockIdx.x, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g0 = grp[(size_t)qi * L + g], g1 = g + 1 < ngq ? grp[(size_t)qi * L + g + 1] : sl_cnt[qi];
+    const int j = gj[(size_t)qi * L + g];
+    const int base = lp[(size_t)qi * (nprobe + 1) + j];
+    const int c = (int)probe[(size_t)qi * nprobe + j];
+    prepare_cluster(ix, qrot + (size_t)qi * ix.Dtot, prune + (size_t)qi * ix.S, c, sm);
+    const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
+    const int *pos = sl_pos + (size_t)qi * L;
+    for (int e = g0 + w; e < g1; e += kScanWarps) {
+        const int r = pos[e] - base;
+        const float d = searched_dist(ix, sm, b0 + r / 32, v0 + r, r & 31, lane);
+        if (lane == 0) sl_dist[(size_t)qi * L + e] = d;
+    }
+}
+
+// Top-k of the re-ranked shortlist, one CTA per query: ordered by distance,
+// equal distances the later-scanned first, which is where ResultPool::insert
+// puts an equal distance (pool.hpp:17-30).
+__global__ void __launch_bounds__(kScanThreads) k_tc_topk(DevIndexView ix, const uint32_t *__restrict__ probe,
+                                                          int nprobe, const int *__restrict__ lp,
+                                                          const int *__restrict__ sl_pos,
+                                                          const float *__restrict__ sl_apx,
+                                                          const int *__restrict__ sl_cnt,
+                                                          const float *__restrict__ sl_dist, int L, int L2, int topk,
+                                                          uint32_t *__restrict__ ids, float *__restrict__ dists,
+                                                          float *__restrict__ apx_out) {
+    extern __shared__ __align__(16) char smem_raw[];
+    unsigned long long *key = reinterpret_cast<unsigned long long *>(smem_raw);
+    const int qi = blockIdx.x, tid = threadIdx.x;
     const int n = sl_cnt[qi];
     const int *pos = sl_pos + (size_t)qi * L;
+    const float *dist = sl_dist + (size_t)qi * L;
     const int *lq = lp + (size_t)qi * (nprobe + 1);
-    int g0 = 0;
-    while (g0 < n) {  // uniform: one probed cluster per round
-        int lo = 0, hi = nprobe - 1;  // last j with lq[j] <= pos[g0]
-        const int p0 = pos[g0];
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (lq[mid] <= p0) lo = mid;
-            else hi = mid - 1;
-        }
-        const int j = lo, end = lq[j + 1];
-        int g1 = g0 + 1;
-        while (g1 < n && pos[g1] < end) ++g1;
-        const int c = (int)probe[(size_t)qi * nprobe + j];
-        prepare_cluster(ix, qrot + (size_t)qi * ix.Dtot, prune + (size_t)qi * ix.S, c, sm);
-        const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
-        for (int e = g0 + w; e < g1; e += kScanWarps) {
-            const int r = pos[e] - lq[j];
-            const float d = searched_dist(ix, sm, b0 + r / 32, v0 + r, r & 31, lane);
-            if (lane == 0) dist[e] = d;
-        }
-        __syncthreads();
-        g0 = g1;
-    }
-    // (distance key, later position first) sorted ascending
     for (int e = tid; e < L2; e += blockDim.x)
         key[e] = e < n ? ((unsigned long long)fkey(dist[e]) << 32) | (unsigned)(0x7fffffff - pos[e]) : ~0ull;
     __syncthreads();
@@ -2900,7 +2923,7 @@ __global__ void __launch_bounds__(kScanThreads) k_tc_rerank(DevIndexView ix, con
                 if (pos[mid] < p) lo = mid + 1;
                 else hi = mid;
             }
-            int jlo = 0, jhi = nprobe - 1;
+            int jlo = 0, jhi = nprobe - 1;  // its probe: the last j with lq[j] <= p
             while (jlo < jhi) {
                 const int mid = (jlo + jhi + 1) >> 1;
                 if (lq[mid] <= p) jlo = mid;
@@ -2954,17 +2977,24 @@ size_t tc_probe_work_bytes(const Index &I, int64_t nq) { return sizeof(Cand) * (
 
 void tc_rerank(const Index &I, const uint32_t *probe, int64_t nq, int64_t nprobe, const float *qrot,
                const float *prune, const int *lp, const int *sl_pos, const float *sl_apx, const int *sl_cnt, int L,
-               int64_t topk, uint32_t *ids, float *dists, float *apx, cudaStream_t st) {
+               int64_t topk, int *grp, int *gj, int *ng, float *sl_dist, uint32_t *ids, float *dists, float *apx,
+               cudaStream_t st) {
     const DevIndexView &ix = I.view;
     int L2 = 1;
     while (L2 < L) L2 <<= 1;
-    const size_t smem = align16(scan_smem_bytes(ix.Dtot, ix.S, 1, 0)) + align16(4 * (size_t)L) + 8 * (size_t)L2;
-    SAQG_REQUIRE(smem <= 200 * 1024, "dimension / shortlist too large for the re-rank kernel's shared memory");
+    k_tc_groups<<<(unsigned)((nq + 127) / 128), 128, 0, st>>>(sl_pos, sl_cnt, lp, (int)nq, (int)nprobe, L, grp, gj,
+                                                               ng);
+    check_launch("k_tc_groups");
+    const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, 1, 0);
+    SAQG_REQUIRE(smem <= 200 * 1024, "dimension too large for the re-rank kernel's shared memory");
     SAQG_CUDA_TRY(cudaFuncSetAttribute(k_tc_rerank, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_tc_rerank<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, lp, sl_pos, sl_apx,
-                                                          sl_cnt, L, L2, (int)topk, ids, dists, apx);
+    k_tc_rerank<<<dim3((unsigned)L, (unsigned)nq), kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, lp,
+                                                                             sl_pos, sl_cnt, grp, gj, ng, L, sl_dist);
     check_launch("k_tc_rerank");
-    count_launch(1);
+    k_tc_topk<<<(unsigned)nq, kScanThreads, 8 * (size_t)L2, st>>>(ix, probe, (int)nprobe, lp, sl_pos, sl_apx, sl_cnt,
+                                                                  sl_dist, L, L2, (int)topk, ids, dists, apx);
+    check_launch("k_tc_topk");
+    count_launch(3);
 }
 
 }  // namespace saqg

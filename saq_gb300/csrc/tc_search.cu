@@ -21,20 +21,25 @@
 //   k_tc_pairs     per-query candidate offsets (probe order) and per-cluster pair counts
 //   k_excl_scan    exclusive prefix sums (query offsets, cluster bucket offsets)
 //   k_tc_fill / k_tc_sort   pairs bucketed by cluster, each bucket in pair order
-//   k_tc_contract  one CTA per 128-vector tile of a cluster: TMA streams the code
-//                  tile through a 3-stage shared-memory ring (128-byte swizzle),
-//                  four warps build the BF16 residual queries of the tile's pairs in
-//                  the same layout, one thread issues tcgen05.mma (M=128, N=pairs,
-//                  K=16 per instruction) into per-segment TMEM accumulators, and the
+//   k_tc_gather    BF16 residual query row of every pair (cluster order), with
+//                  its per-segment sum and squared norm
+//   k_tc_contract  persistent, one CTA per SM over the 128-vector tiles of the
+//                  clusters: TMA streams the code tile and the chunk's query rows
+//                  through a 6-stage shared-memory ring (128-byte swizzle), one
+//                  thread issues tcgen05.mma (M=128, N=pairs, K=16 per instruction)
+//                  into per-segment TMEM accumulators (two, alternating by chunk),
 //                  four warps read them back with tcgen05.ld for the epilogue
-//   k_tc_select    per query: the shortlist by radix select, in candidate order
-//   k_tc_rerank    (search.cu) exact distances of the shortlist, top-k
+//   k_tc_select1/2 per query: the shortlist by radix select over 4,096-candidate
+//                  chunks, then over the chunks' survivors, in candidate order
+//   k_tc_groups / k_tc_rerank / k_tc_topk  (search.cu) exact distances of the
+//                  shortlist, one CTA per (query, probed cluster), then top-k
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cfloat>
+#include <climits>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -48,10 +53,10 @@ namespace {
 
 constexpr int kTcBM = 128;           // vectors per tile: the MMA's M
 constexpr int kTcBK = 64;            // dims per pipeline stage: one 128-byte BF16 row
-constexpr int kTcStages = 3;         // ring depth (two CTAs per SM)
+constexpr int kTcStages = 6;         // ring depth (one persistent CTA per SM)
 constexpr int kTcThreads = 192;      // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-5 queries + epilogue
 constexpr int kTcStageBytes = 16384; // 128 rows x 128 bytes (A), at most 128 x 128 bytes (B)
-constexpr int kTcCols = 256;         // TMEM columns a CTA may hold: segments x pairs per chunk
+constexpr int kTcCols = 256;         // TMEM columns of one accumulator (segments x pairs per chunk); a CTA holds two
 constexpr int kTcMaxN = 128;         // pairs per chunk at most (the MMA's N)
 constexpr int kTcMaxShort = 1024;    // shortlist length at most
 constexpr int kTcMaxBatch = 8192;    // queries per call at most (bucket sort in shared memory)
@@ -154,8 +159,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
-
-__device__ __forceinline__ void named_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
     __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
@@ -344,64 +347,108 @@ __global__ void __launch_bounds__(256) k_tc_sort(const int *__restrict__ bcnt, c
     }
 }
 
+// ------------------------------------------------------------ query operand
+// One warp per bucket row b (a (query, probed cluster) pair in cluster order):
+// the BF16 residual r = q P - c P of every segment, row-major [b][Dtot], the
+// per-segment sum and squared norm of r in FP32 (fixed order: lane-strided
+// partials, then a butterfly), and the row's candidate offset.
+__global__ void k_tc_gather(DevIndexView ix, const uint32_t *__restrict__ probe, const int *__restrict__ sorted,
+                            int P, int nprobe, const float *__restrict__ qrot, const long long *__restrict__ qbase,
+                            const int *__restrict__ lp, __nv_bfloat16 *__restrict__ Bq, float2 *__restrict__ pscal,
+                            long long *__restrict__ cbase) {
+    const int b = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (b >= P) return;
+    const int p = sorted[b], qi = p / nprobe, j = p - qi * nprobe;
+    const int c = (int)probe[p];
+    if (lane == 0) cbase[b] = qbase[qi] + lp[(size_t)qi * (nprobe + 1) + j];
+    const float *qr = qrot + (size_t)qi * ix.Dtot;
+    __nv_bfloat16 *out = Bq + (size_t)b * ix.Dtot;
+    for (int s = 0; s < ix.S; ++s) {
+        const SegDev &g = ix.seg[s];
+        const float *cen = g.cent + (size_t)c * g.dim;
+        float sum = 0.0f, sq = 0.0f;
+        for (int d0 = lane * 8; d0 < g.dim; d0 += 256) {
+            const float4 a0 = *reinterpret_cast<const float4 *>(qr + g.qoff + d0);
+            const float4 a1 = *reinterpret_cast<const float4 *>(qr + g.qoff + d0 + 4);
+            const float4 c0 = *reinterpret_cast<const float4 *>(cen + d0);
+            const float4 c1 = *reinterpret_cast<const float4 *>(cen + d0 + 4);
+            const float e[8] = {__fsub_rn(a0.x, c0.x), __fsub_rn(a0.y, c0.y), __fsub_rn(a0.z, c0.z),
+                                __fsub_rn(a0.w, c0.w), __fsub_rn(a1.x, c1.x), __fsub_rn(a1.y, c1.y),
+                                __fsub_rn(a1.z, c1.z), __fsub_rn(a1.w, c1.w)};
+#pragma unroll
+            for (int h = 0; h < 8; ++h) {
+                sum = __fadd_rn(sum, e[h]);
+                sq = __fmaf_rn(e[h], e[h], sq);
+            }
+            *reinterpret_cast<uint4 *>(out + g.qoff + d0) =
+                make_uint4(pack_bf16x2(e[0], e[1]), pack_bf16x2(e[2], e[3]), pack_bf16x2(e[4], e[5]),
+                           pack_bf16x2(e[6], e[7]));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sum = __fadd_rn(sum, __shfl_xor_sync(kFullMask, sum, o));
+            sq = __fadd_rn(sq, __shfl_xor_sync(kFullMask, sq, o));
+        }
+        if (lane == 0) pscal[(size_t)b * ix.S + s] = make_float2(sum, sq);
+    }
+}
+
 // ------------------------------------------------------------ contraction
 struct TcWork {
     const int2 *tiles;          // (cluster, tile) of every 128-vector tile
+    int ntiles;
     const int *bcnt;            // pairs per cluster
-    const long long *boff;      // bucket offsets
-    const int *bucket;          // pairs by cluster, ascending
-    const float *qrot;          // [nq][Dtot] rotated queries
-    const int *lp;              // [nq][nprobe + 1]
-    const long long *qbase;     // [nq] candidate offsets
+    const long long *boff;      // bucket offsets (rows of the query operand)
+    const long long *cbase;     // [P] candidate offset of each bucket row
+    const float2 *pscal;        // [P][S] residual sum / squared norm per segment
     float *cand;                // approximate distances
-    int nprobe;
     int BN;                     // pairs per chunk (multiple of 16)
     int *err;
 };
 
-__global__ void __launch_bounds__(kTcThreads, 2) k_tc_contract(const __grid_constant__ CUtensorMap tmA, DevIndexView ix,
-                                                               TcWork w) {
+// Persistent contraction, one CTA per SM, tiles round-robin.  Roles:
+//   warp 0 (one thread)  TMA: per 64-dim stage the 128-row code tile and the
+//                        chunk's query rows (16-row boxes), into a 6-stage ring
+//   warp 1 (one thread)  tcgen05.mma into one of two TMEM accumulators
+//                        (segment s at columns s * BN), commits free the stage /
+//                        publish the accumulator; warp 1 also owns TMEM
+//   warps 2-5            epilogue: tcgen05.ld of their 32 lanes, the distance
+//                        formula, coalesced stores; then hand the accumulator back
+// Chunk g uses accumulator g & 1, so the MMAs of chunk g+1 overlap the epilogue
+// of chunk g.  Every wait is bounded (mbar_wait): on a timeout the CTA records
+// the error, drains its copies and MMAs in flight, frees TMEM and returns.
+__global__ void __launch_bounds__(kTcThreads, 1) k_tc_contract(const __grid_constant__ CUtensorMap tmA,
+                                                               const __grid_constant__ CUtensorMap tmB,
+                                                               DevIndexView ix, TcWork w) {
     extern __shared__ uint8_t tc_smem[];
-    const int2 tile = w.tiles[blockIdx.x];
-    const int c = tile.x, t = tile.y;
-    const int cnt = w.bcnt[c];
-    if (cnt == 0) return;  // no query probes this cluster
-
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int S = ix.S, BN = w.BN, kch = ix.Dtot / kTcBK;
-    const int nchunk = (cnt + BN - 1) / BN;
-    const int64_t v0 = ix.vec_off[c];
-    const int nc = (int)(ix.vec_off[c + 1] - v0);
-    const int row0 = (int)(v0 + (int64_t)t * kTcBM);
 
     const uint32_t raw = smem_u32(tc_smem);
     const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
     uint8_t *sm = tc_smem + pad;
     const uint32_t sA = raw + pad, sB = sA + kTcStages * kTcStageBytes;
-    uint8_t *pB = sm + kTcStages * kTcStageBytes;
     uint64_t *bars = reinterpret_cast<uint64_t *>(sm + 2 * kTcStages * kTcStageBytes);
-    // barriers: afull[st] (TMA bytes), bfull[st] (4 query warps), empty[st] (MMA done), accf, done
     const uint32_t b0 = smem_u32(bars);
-    auto afull = [&](int st) { return b0 + 8u * st; };
-    auto bfull = [&](int st) { return b0 + 8u * (kTcStages + st); };
-    auto empty = [&](int st) { return b0 + 8u * (2 * kTcStages + st); };
-    const uint32_t accf = b0 + 8u * (3 * kTcStages), done = accf + 8u;
-    int *misc = reinterpret_cast<int *>(bars + 3 * kTcStages + 2);  // [0] TMEM address, [1] abort
-    int *pq = misc + 4;                                            // [kTcMaxN] query of each column
-    int *pj = pq + kTcMaxN;                                        // [kTcMaxN] probe index
-    float *ssum = reinterpret_cast<float *>(pj + kTcMaxN);         // [S * BN] residual sums
-    float *ssq = ssum + kTcCols;                                   // [S * BN] residual squared norms
+    auto full = [&](int st) { return b0 + 8u * st; };
+    auto empty = [&](int st) { return b0 + 8u * (kTcStages + st); };
+    auto accf = [&](int i) { return b0 + 8u * (2 * kTcStages + i); };
+    auto acce = [&](int i) { return b0 + 8u * (2 * kTcStages + 2 + i); };
+    const uint32_t done = b0 + 8u * (2 * kTcStages + 4);
+    int *misc = reinterpret_cast<int *>(bars + 2 * kTcStages + 5);  // [0] TMEM address, [1] abort
     volatile int *abort = misc + 1;
 
     int ncols = 32;
-    while (ncols < S * BN) ncols <<= 1;
+    while (ncols < 2 * S * BN) ncols <<= 1;
     if (tid == 0) {
         for (int st = 0; st < kTcStages; ++st) {
-            mbar_init(afull(st), 1);
-            mbar_init(bfull(st), 4);
+            mbar_init(full(st), 1);
             mbar_init(empty(st), 1);
         }
-        mbar_init(accf, 1);
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(accf(i), 1);
+            mbar_init(acce(i), 4);
+        }
         mbar_init(done, 1);
         misc[1] = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -419,56 +466,76 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tc_contract(const __grid_cons
     const uint32_t tmem = (uint32_t)misc[0];
 
     if (warp == 0) {
-        // ---- TMA producer: the code tile, 64 dims per stage
+        // ---- TMA producer
         if (lane == 0) {
             int it = 0;
             bool ok = true;
-            for (int ch = 0; ch < nchunk && ok; ++ch)
-                for (int kc = 0; kc < kch; ++kc, ++it) {
-                    const int st = it % kTcStages;
-                    const uint32_t ph = (uint32_t)(it / kTcStages) & 1u;
-                    if (!mbar_wait(empty(st), ph ^ 1u, abort)) {
-                        ok = false;
-                        break;
+            for (int ti = blockIdx.x; ti < w.ntiles && ok; ti += gridDim.x) {
+                const int2 tile = w.tiles[ti];
+                const int cnt = w.bcnt[tile.x];
+                const int row0 = (int)(ix.vec_off[tile.x] + (int64_t)tile.y * kTcBM);
+                for (int ch = 0; ch * BN < cnt && ok; ++ch) {
+                    const int nh = min(BN, cnt - ch * BN), npad = (nh + 15) & ~15;
+                    const int brow = (int)(w.boff[tile.x] + (long long)ch * BN);
+                    for (int kc = 0; kc < kch; ++kc, ++it) {
+                        const int st = it % kTcStages;
+                        const uint32_t ph = (uint32_t)(it / kTcStages) & 1u;
+                        if (!mbar_wait(empty(st), ph ^ 1u, abort)) {
+                            ok = false;
+                            break;
+                        }
+                        mbar_expect_tx(full(st), kTcStageBytes + npad * 128);
+                        tma_load_2d(sA + st * kTcStageBytes, &tmA, full(st), kc * kTcBK, row0);
+                        for (int bx = 0; bx < npad / 16; ++bx)
+                            tma_load_2d(sB + st * kTcStageBytes + bx * 2048, &tmB, full(st), kc * kTcBK, brow + 16 * bx);
                     }
-                    mbar_expect_tx(afull(st), kTcStageBytes);
-                    tma_load_2d(sA + st * kTcStageBytes, &tmA, afull(st), kc * kTcBK, row0);
                 }
+            }
             if (!ok) {
                 atomicExch(w.err, 1);
                 for (int k = max(0, it - kTcStages); k < it; ++k)  // copies possibly in flight
-                    mbar_drain(afull(k % kTcStages), (uint32_t)(k / kTcStages) & 1u);
+                    mbar_drain(full(k % kTcStages), (uint32_t)(k / kTcStages) & 1u);
             }
         }
         __syncwarp();
     } else if (warp == 1) {
         // ---- MMA issuer
         if (lane == 0) {
-            int it = 0;
+            int it = 0, g = 0;
             bool ok = true;
-            for (int ch = 0; ch < nchunk && ok; ++ch) {
-                const int nh = min(BN, cnt - ch * BN), npad = (nh + 15) & ~15;
-                const uint32_t idesc = idesc_bf16(npad);
-                for (int kc = 0; kc < kch; ++kc, ++it) {
-                    const int st = it % kTcStages;
-                    const uint32_t ph = (uint32_t)(it / kTcStages) & 1u;
-                    if (!mbar_wait(afull(st), ph, abort) || !mbar_wait(bfull(st), ph, abort)) {
+            for (int ti = blockIdx.x; ti < w.ntiles && ok; ti += gridDim.x) {
+                const int cnt = w.bcnt[w.tiles[ti].x];
+                for (int ch = 0; ch * BN < cnt && ok; ++ch, ++g) {
+                    const int nh = min(BN, cnt - ch * BN), npad = (nh + 15) & ~15;
+                    const uint32_t idesc = idesc_bf16(npad);
+                    const int buf = g & 1;
+                    if (!mbar_wait(acce(buf), (((uint32_t)g >> 1) & 1u) ^ 1u, abort)) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
-                    const int k0 = kc * kTcBK;
-                    int s = 0;
-                    while (s + 1 < S && k0 >= ix.seg[s + 1].qoff) ++s;
-                    const bool first = k0 == ix.seg[s].qoff;
-                    const uint32_t d = tmem + (uint32_t)(s * BN);
-                    const uint64_t da = sw128_desc(sA + st * kTcStageBytes), db = sw128_desc(sB + st * kTcStageBytes);
+                    const uint32_t dacc = tmem + (uint32_t)(buf * S * BN);
+                    for (int kc = 0; kc < kch; ++kc, ++it) {
+                        const int st = it % kTcStages;
+                        const uint32_t ph = (uint32_t)(it / kTcStages) & 1u;
+                        if (!mbar_wait(full(st), ph, abort)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const int k0 = kc * kTcBK;
+                        int s = 0;
+                        while (s + 1 < S && k0 >= ix.seg[s + 1].qoff) ++s;
+                        const bool first = k0 == ix.seg[s].qoff;
+                        const uint64_t da = sw128_desc(sA + st * kTcStageBytes), db = sw128_desc(sB + st * kTcStageBytes);
 #pragma unroll
-                    for (int kk = 0; kk < kTcBK / 16; ++kk)  // 16 BF16 = 32 bytes per instruction
-                        mma_bf16(d, da + 2 * kk, db + 2 * kk, idesc, (first && kk == 0) ? 0u : 1u);
-                    mma_commit(empty(st));
+                        for (int kk = 0; kk < kTcBK / 16; ++kk)  // 16 BF16 = 32 bytes per instruction
+                            mma_bf16(dacc + (uint32_t)(s * BN), da + 2 * kk, db + 2 * kk, idesc,
+                                     (first && kk == 0) ? 0u : 1u);
+                        mma_commit(empty(st));
+                    }
+                    if (ok) mma_commit(accf(buf));
                 }
-                if (ok) mma_commit(accf);
             }
             if (!ok) atomicExch(w.err, 1);
             mma_commit(done);  // every MMA issued has finished once `done` completes
@@ -476,123 +543,61 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tc_contract(const __grid_cons
         }
         __syncwarp();
     } else {
-        // ---- query operand (residuals in BF16) and epilogue: warps 2-5
-        const int tb = tid - 64, qt = warp & 3;
-        const int r = qt * 32 + lane, rl = t * kTcBM + r;
-        const bool vrow = rl < nc;
-        const int64_t gv = v0 + rl, gb = ix.blk_off[c] + rl / 32;
-        const int ln = rl & 31;
-        int it = 0;
+        // ---- epilogue: warps 2-5, TMEM lanes (warp % 4) * 32 + lane
+        const int qt = warp & 3, r = qt * 32 + lane;
+        int g = 0;
         bool ok = true;
-        for (int ch = 0; ch < nchunk; ++ch) {
-            const int nh = min(BN, cnt - ch * BN), npad = (nh + 15) & ~15, nu = npad / 16;
-            for (int n = tb; n < nh; n += 128) {
-                const int p = w.bucket[w.boff[c] + (long long)ch * BN + n];
-                pq[n] = p / w.nprobe;
-                pj[n] = p - (p / w.nprobe) * w.nprobe;
-            }
-            named_sync(1, 128);
-            float as[kTcMaxN / 16], aq[kTcMaxN / 16];
-#pragma unroll
-            for (int u = 0; u < kTcMaxN / 16; ++u) as[u] = aq[u] = 0.0f;
-            for (int kc = 0; kc < kch; ++kc, ++it) {
-                const int st = it % kTcStages;
-                const uint32_t ph = (uint32_t)(it / kTcStages) & 1u;
-                if (ok && !mbar_wait(empty(st), ph ^ 1u, abort)) ok = false;
-                const int k0 = kc * kTcBK;
-                int s = 0;
-                while (s + 1 < S && k0 >= ix.seg[s + 1].qoff) ++s;
-                const SegDev &g = ix.seg[s];
-                const float *cen = g.cent + (size_t)c * g.dim + (k0 - g.qoff);
-                uint8_t *dstB = pB + st * kTcStageBytes;
-#pragma unroll
-                for (int u = 0; u < kTcMaxN / 16; ++u) {
-                    if (u >= nu) break;
-                    const int idx = tb + 128 * u, n = idx >> 3, j = idx & 7;
-                    uint4 out = make_uint4(0, 0, 0, 0);
-                    float ps = 0.0f, pq2 = 0.0f;
-                    if (ok && n < nh) {
-                        const float4 *qr = reinterpret_cast<const float4 *>(w.qrot + (size_t)pq[n] * ix.Dtot + k0 + 8 * j);
-                        const float4 *cr = reinterpret_cast<const float4 *>(cen + 8 * j);
-                        const float4 a0 = qr[0], a1 = qr[1], c0 = __ldg(cr), c1 = __ldg(cr + 1);
-                        const float e[8] = {__fsub_rn(a0.x, c0.x), __fsub_rn(a0.y, c0.y), __fsub_rn(a0.z, c0.z),
-                                            __fsub_rn(a0.w, c0.w), __fsub_rn(a1.x, c1.x), __fsub_rn(a1.y, c1.y),
-                                            __fsub_rn(a1.z, c1.z), __fsub_rn(a1.w, c1.w)};
-#pragma unroll
-                        for (int h = 0; h < 8; ++h) {
-                            ps = __fadd_rn(ps, e[h]);
-                            pq2 = __fmaf_rn(e[h], e[h], pq2);
-                        }
-                        out = make_uint4(pack_bf16x2(e[0], e[1]), pack_bf16x2(e[2], e[3]), pack_bf16x2(e[4], e[5]),
-                                         pack_bf16x2(e[6], e[7]));
-                    }
-                    *reinterpret_cast<uint4 *>(dstB + n * 128 + ((j ^ (n & 7)) << 4)) = out;
-                    // the row's 8 chunks sit in 8 consecutive lanes: butterfly sums (same value in all 8)
-#pragma unroll
-                    for (int o = 1; o < 8; o <<= 1) {
-                        ps = __fadd_rn(ps, __shfl_xor_sync(kFullMask, ps, o));
-                        pq2 = __fadd_rn(pq2, __shfl_xor_sync(kFullMask, pq2, o));
-                    }
-                    as[u] = __fadd_rn(as[u], ps);
-                    aq[u] = __fadd_rn(aq[u], pq2);
+        for (int ti = blockIdx.x; ti < w.ntiles && ok; ti += gridDim.x) {
+            const int2 tile = w.tiles[ti];
+            const int c = tile.x, cnt = w.bcnt[c];
+            if (cnt == 0) continue;
+            const int64_t v0 = ix.vec_off[c];
+            const int nc = (int)(ix.vec_off[c + 1] - v0);
+            const int rl = tile.y * kTcBM + r;
+            const bool vrow = rl < nc;
+            const int64_t gv = v0 + rl, gb = ix.blk_off[c] + rl / 32;
+            const int ln = rl & 31;
+            for (int ch = 0; ch * BN < cnt; ++ch, ++g) {
+                const int nh = min(BN, cnt - ch * BN), npad = (nh + 15) & ~15;
+                const int buf = g & 1;
+                if (ok && !mbar_wait(accf(buf), ((uint32_t)g >> 1) & 1u, abort)) ok = false;
+                tc_fence_after();
+                if (!__all_sync(kFullMask, ok)) {
+                    ok = false;
+                    break;
                 }
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                __syncwarp();
-                if (lane == 0) mbar_arrive(bfull(st));
-                if (k0 + kTcBK == g.qoff + g.dim) {  // segment complete: its per-pair scalars
-#pragma unroll
-                    for (int u = 0; u < kTcMaxN / 16; ++u) {
-                        if (u >= nu) break;
-                        const int idx = tb + 128 * u, n = idx >> 3;
-                        if ((idx & 7) == 0 && n < nh) {
-                            ssum[s * BN + n] = as[u];
-                            ssq[s * BN + n] = aq[u];
-                        }
-                        as[u] = aq[u] = 0.0f;
-                    }
-                }
-            }
-            named_sync(1, 128);  // scalars of every pair visible
-            if (ok && !mbar_wait(accf, (uint32_t)ch & 1u, abort)) ok = false;
-            tc_fence_after();
-            const bool good = __all_sync(kFullMask, ok);
-            if (good) {
+                const long long rb = w.boff[c] + (long long)ch * BN;
                 for (int n0 = 0; n0 < npad; n0 += 16) {
                     float d[16];
 #pragma unroll
                     for (int i = 0; i < 16; ++i) d[i] = 0.0f;
                     for (int s = 0; s < S; ++s) {
                         float v[16];
-                        tmem_ld16(tmem + ((uint32_t)(qt * 32) << 16) + (uint32_t)(s * BN + n0), v);
-                        const SegDev &g = ix.seg[s];
-                        const float on = vrow ? g.onorm[gb * 32 + ln] : 0.0f;
-                        const float o2 = __fmul_rn(on, on), rs = vrow ? g.exfac[gv].x : 0.0f;
-                        const float dl = 2.0f / (float)(1 << g.bits), cst = __fsub_rn(__fmul_rn(dl, 0.5f), 1.0f);
+                        tmem_ld16(tmem + ((uint32_t)(qt * 32) << 16) + (uint32_t)(buf * S * BN + s * BN + n0), v);
+                        const SegDev &sg = ix.seg[s];
+                        const float on = vrow ? sg.onorm[gb * 32 + ln] : 0.0f;
+                        const float o2 = __fmul_rn(on, on), rs = vrow ? sg.exfac[gv].x : 0.0f;
+                        const float dl = 2.0f / (float)(1 << sg.bits), cst = __fsub_rn(__fmul_rn(dl, 0.5f), 1.0f);
 #pragma unroll
                         for (int i = 0; i < 16; ++i) {
                             const int n = n0 + i;
-                            const float sq = n < nh ? ssum[s * BN + n] : 0.0f, q2 = n < nh ? ssq[s * BN + n] : 0.0f;
-                            const float ip = __fmaf_rn(dl, v[i], __fmul_rn(cst, sq));
-                            d[i] = __fadd_rn(d[i], __fsub_rn(__fadd_rn(o2, q2), __fmul_rn(2.0f, __fmul_rn(rs, ip))));
+                            const float2 ps = n < nh ? w.pscal[(rb + n) * S + s] : make_float2(0.0f, 0.0f);
+                            const float ip = __fmaf_rn(dl, v[i], __fmul_rn(cst, ps.x));
+                            d[i] = __fadd_rn(d[i], __fsub_rn(__fadd_rn(o2, ps.y), __fmul_rn(2.0f, __fmul_rn(rs, ip))));
                         }
                     }
                     if (vrow) {
 #pragma unroll
-                        for (int i = 0; i < 16; ++i) {
-                            const int n = n0 + i;
-                            if (n < nh) {
-                                const int qi = pq[n];
-                                w.cand[w.qbase[qi] + w.lp[(size_t)qi * (w.nprobe + 1) + pj[n]] + rl] = d[i];
-                            }
-                        }
+                        for (int i = 0; i < 16; ++i)
+                            if (n0 + i < nh) w.cand[w.cbase[rb + n0 + i] + rl] = d[i];
                     }
                 }
-            } else if (lane == 0) {
-                atomicExch(w.err, 1);
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(acce(buf));
             }
-            tc_fence_before();
-            named_sync(1, 128);  // pair lists and scalars are rewritten by the next chunk
         }
+        if (!ok && lane == 0) atomicExch(w.err, 1);
     }
     tc_fence_before();
     __syncthreads();
@@ -602,9 +607,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tc_contract(const __grid_cons
     }
 }
 
-constexpr size_t tc_contract_smem() {
-    return 1024 + 2 * (size_t)kTcStages * kTcStageBytes + 8 * (3 * kTcStages + 2) + 16 + 8 * kTcMaxN + 8 * kTcCols;
-}
+constexpr size_t tc_contract_smem() { return 1024 + 2 * (size_t)kTcStages * kTcStageBytes + 8 * (2 * kTcStages + 5) + 16; }
 
 // ------------------------------------------------------------ shortlist
 __device__ __forceinline__ uint32_t dkey(float f) {
@@ -630,37 +633,22 @@ __device__ __forceinline__ int block_prefix(int f, int *wtot, int *tot) {
     return base + __popc(b & ((1u << lane) - 1u));
 }
 
-// The L smallest approximate distances of one query (ties: earlier position),
-// written in candidate order with their distances.
-__global__ void __launch_bounds__(256) k_tc_select(const float *__restrict__ cand, const long long *__restrict__ qbase,
-                                                   const int *__restrict__ qtot, int L, int *__restrict__ sl_pos,
-                                                   float *__restrict__ sl_apx, int *__restrict__ sl_cnt) {
+// The L smallest keys of key(e), e in [0, M) (ties: smaller e first), written
+// in ascending e as (pos(e), value(e)).  256 threads; radix select, 8 bits per pass.
+template <class Key, class Emit>
+__device__ void select_smallest(int M, int L, Key key, Emit emit) {
     __shared__ int hist[256];
     __shared__ int wtot[8];
     __shared__ uint32_t s_prefix;
     __shared__ int s_need;
-    const int qi = blockIdx.x, tid = threadIdx.x;
-    const int M = qtot[qi];
-    const float *x = cand + qbase[qi];
-    int *po = sl_pos + (size_t)qi * L;
-    float *ao = sl_apx + (size_t)qi * L;
-    const int take = min(L, M);
-    if (tid == 0) sl_cnt[qi] = take;
-    if (M <= L) {
-        for (int e = tid; e < M; e += 256) {
-            po[e] = e;
-            ao[e] = x[e];
-        }
-        return;
-    }
-    // radix select of the L-th smallest key, 8 bits per pass
+    const int tid = threadIdx.x;
     uint32_t prefix = 0, mask = 0;
     int need = L;
     for (int shift = 24; shift >= 0; shift -= 8) {
         hist[tid] = 0;
         __syncthreads();
         for (int e = tid; e < M; e += 256) {
-            const uint32_t k = dkey(x[e]);
+            const uint32_t k = key(e);
             if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255], 1);
         }
         __syncthreads();
@@ -676,24 +664,94 @@ __global__ void __launch_bounds__(256) k_tc_select(const float *__restrict__ can
         mask |= 255u << shift;
         __syncthreads();
     }
-    // keys below the threshold, then the first `need` equal keys, in candidate order
     int taken = 0, eq_seen = 0;
     for (int e0 = 0; e0 < M; e0 += 256) {
         const int e = e0 + tid;
-        const uint32_t k = e < M ? dkey(x[e]) : 0xffffffffu;
+        const uint32_t k = e < M ? key(e) : 0xffffffffu;
         const int lt = e < M && k < prefix, eq = e < M && k == prefix;
         int eq_tot;
         const int eq_rank = eq_seen + block_prefix(eq, wtot, &eq_tot);
         const int f = lt || (eq && eq_rank < need);
         int f_tot;
         const int slot = taken + block_prefix(f, wtot, &f_tot);
-        if (f) {
-            po[slot] = e;
-            ao[slot] = x[e];
-        }
+        if (f) emit(slot, e);
         taken += f_tot;
         eq_seen += eq_tot;
     }
+}
+
+constexpr int kTcSelChunk = 4096;  // candidates per first-phase CTA
+
+// Phase 1: the L smallest of each 4,096-candidate chunk of a query (chunks of
+// all queries concatenated: qchunk = exclusive prefix of chunks per query),
+// padded to L entries with (INT_MAX, NaN) so each query's survivors are a
+// dense array in candidate order.
+__global__ void __launch_bounds__(256) k_tc_select1(const float *__restrict__ cand, const long long *__restrict__ qbase,
+                                                    const int *__restrict__ qtot, const long long *__restrict__ qchunk,
+                                                    int nq, int L, int *__restrict__ spos, float *__restrict__ sval) {
+    __shared__ float xs[kTcSelChunk];
+    const long long k = blockIdx.x;
+    int lo = 0, hi = nq - 1;  // query owning chunk k: last with qchunk <= k
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (qchunk[mid] <= k) lo = mid;
+        else hi = mid - 1;
+    }
+    const int qi = lo;
+    const int e0 = (int)(k - qchunk[qi]) * kTcSelChunk, m = min(kTcSelChunk, qtot[qi] - e0);
+    const float *x = cand + qbase[qi] + e0;
+    for (int e = threadIdx.x; e < m; e += 256) xs[e] = x[e];
+    __syncthreads();
+    int *po = spos + k * L;
+    float *vo = sval + k * L;
+    if (m <= L) {
+        for (int e = threadIdx.x; e < L; e += 256) {
+            po[e] = e < m ? e0 + e : INT_MAX;
+            vo[e] = e < m ? xs[e] : __int_as_float(0x7fffffff);
+        }
+        return;
+    }
+    select_smallest(m, L, [&](int e) { return dkey(xs[e]); },
+                    [&](int slot, int e) {
+                        po[slot] = e0 + e;
+                        vo[slot] = xs[e];
+                    });
+}
+
+// Phase 2: per query, the L smallest of its survivors (ties: earlier position),
+// in candidate order.
+__global__ void __launch_bounds__(256) k_tc_select2(const long long *__restrict__ qchunk, const int *__restrict__ qtot,
+                                                    int L, const int *__restrict__ spos, const float *__restrict__ sval,
+                                                    int *__restrict__ sl_pos, float *__restrict__ sl_apx,
+                                                    int *__restrict__ sl_cnt) {
+    const int qi = blockIdx.x;
+    const int M = qtot[qi];
+    const long long c0 = qchunk[qi];
+    const int n = (int)(qchunk[qi + 1] - c0) * L;
+    const int *pi = spos + c0 * L;
+    const float *vi = sval + c0 * L;
+    int *po = sl_pos + (size_t)qi * L;
+    float *ao = sl_apx + (size_t)qi * L;
+    const int take = min(L, M);
+    if (threadIdx.x == 0) sl_cnt[qi] = take;
+    if (M <= L) {  // one chunk holding every candidate, in order
+        for (int e = threadIdx.x; e < M; e += 256) {
+            po[e] = pi[e];
+            ao[e] = vi[e];
+        }
+        return;
+    }
+    // padding (INT_MAX, NaN) has the largest key and comes last on ties
+    select_smallest(n, L, [&](int e) { return dkey(vi[e]); },
+                    [&](int slot, int e) {
+                        po[slot] = pi[e];
+                        ao[slot] = vi[e];
+                    });
+}
+
+__global__ void k_tc_chunks(const int *__restrict__ qtot, int nq, int *__restrict__ nch) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nq) nch[i] = (qtot[i] + kTcSelChunk - 1) / kTcSelChunk;
 }
 
 }  // namespace
@@ -761,6 +819,30 @@ void launch_check(const char *what) {
 
 size_t a16(size_t x) { return (x + 15) & ~size_t(15); }
 
+int sm_count() {
+    static int n = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
+    });
+    return n;
+}
+
+CUtensorMap bf16_rows_map(void *base, int64_t cols, int64_t rows, int box_rows) {
+    CUtensorMap m;
+    const cuuint64_t gdim[2] = {(cuuint64_t)cols, (cuuint64_t)std::max<int64_t>(rows, 1)};
+    const cuuint64_t gstride[1] = {(cuuint64_t)cols * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, gdim, gstride, box, estr,
+                                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw Error{SAQG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r)};
+    return m;
+}
+
 }  // namespace
 
 void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, int64_t L, float m,
@@ -775,7 +857,7 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
                      "the tensor-core search needs every segment coded (bits >= 1) and 64-dim aligned");
     SAQG_REQUIRE(I.N < (int64_t)1 << 31 && nq * nprobe < (int64_t)1 << 31, "index or batch too large");
     if (nq == 0) return;
-    int BN = std::min(kTcMaxN, (kTcCols / ix.S) / 16 * 16);
+    const int BN = std::min(kTcMaxN, (kTcCols / ix.S) / 16 * 16);
     SAQG_REQUIRE(BN >= 16, "too many segments for the tensor-core search");
     ensure_tc_state(I, st);
 
@@ -783,6 +865,7 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     std::lock_guard<std::mutex> lock(C.mu);
     const bool host = mem == SAQG_MEM_HOST;
     const int64_t P = nq * nprobe;
+    // arena 1: sized by the call's shape
     size_t need = 0;
     auto add = [&](size_t b) { need += a16(b); };
     add(4 * (size_t)nq * I.D);                  // queries
@@ -795,13 +878,13 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     add(4 * (size_t)nq);                        // full-path list
     add(64);                                    // flags
     add(4 * (size_t)nq * (nprobe + 1));         // lp
-    add(4 * (size_t)nq);                        // qtot
-    add(8 * (size_t)(nq + 1));                  // qbase
+    add(4 * (size_t)nq * 2);                    // qtot, chunks per query
+    add(8 * (size_t)(nq + 1) * 2);              // qbase, qchunk
     add(4 * (size_t)I.K * 2);                   // bcnt, bfill
     add(8 * (size_t)(I.K + 1));                 // boff
     add(4 * (size_t)P * 2);                     // bucket, sorted
-    add(4 * (size_t)nq * L * 2);                // sl_pos, sl_apx
-    add(4 * (size_t)nq);                        // sl_cnt
+    add(4 * (size_t)nq * L * 5);                // sl_pos, sl_apx, sl_dist, groups, group probes
+    add(4 * (size_t)nq * 2);                    // sl_cnt, group counts
     add(4 * (size_t)nq * topk * 3);             // outputs (host io)
     add(16);                                    // error word
     char *base = static_cast<char *>(C.scratch_get(need + 256));
@@ -821,16 +904,22 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     int *fb = reinterpret_cast<int *>(take(4 * (size_t)nq));
     int *flags = reinterpret_cast<int *>(take(64));
     int *lp = reinterpret_cast<int *>(take(4 * (size_t)nq * (nprobe + 1)));
-    int *qtot = reinterpret_cast<int *>(take(4 * (size_t)nq));
-    long long *qbase = reinterpret_cast<long long *>(take(8 * (size_t)(nq + 1)));
+    int *qtot = reinterpret_cast<int *>(take(4 * (size_t)nq * 2));
+    int *nchk = qtot + nq;
+    long long *qbase = reinterpret_cast<long long *>(take(8 * (size_t)(nq + 1) * 2));
+    long long *qchunk = qbase + nq + 1;
     int *bcnt = reinterpret_cast<int *>(take(4 * (size_t)I.K * 2));
     int *bfill = bcnt + I.K;
     long long *boff = reinterpret_cast<long long *>(take(8 * (size_t)(I.K + 1)));
     int *bucket = reinterpret_cast<int *>(take(4 * (size_t)P * 2));
     int *sorted = bucket + P;
-    int *sl_pos = reinterpret_cast<int *>(take(4 * (size_t)nq * L * 2));
+    int *sl_pos = reinterpret_cast<int *>(take(4 * (size_t)nq * L * 5));
     float *sl_apx = reinterpret_cast<float *>(sl_pos + nq * L);
-    int *sl_cnt = reinterpret_cast<int *>(take(4 * (size_t)nq));
+    float *sl_dist = sl_apx + nq * L;
+    int *grp = reinterpret_cast<int *>(sl_dist + nq * L);
+    int *gj = grp + nq * L;
+    int *sl_cnt = reinterpret_cast<int *>(take(4 * (size_t)nq * 2));
+    int *ng = sl_cnt + nq;
     uint32_t *oid = reinterpret_cast<uint32_t *>(take(4 * (size_t)nq * topk * 3));
     float *od = reinterpret_cast<float *>(oid + nq * topk);
     float *oa = od + nq * topk;
@@ -858,12 +947,16 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     mark(0);
     tc_rank_rotate(I, C, qin, nq, nprobe, m, dist, work, probe, qrot, prune, full, fb, flags, st);
     mark(1);
-    // pairs: candidate offsets per query, buckets per cluster
+    // pairs: candidate offsets per query, buckets per cluster, selection chunks
     SAQG_CUDA_TRY(cudaMemsetAsync(bcnt, 0, 8 * (size_t)I.K, st));
     SAQG_CUDA_TRY(cudaMemsetAsync(err, 0, 16, st));
     k_tc_pairs<<<(unsigned)((nq + 7) / 8), 256, 0, st>>>(ix, probe, (int)nq, (int)nprobe, lp, qtot, bcnt);
     launch_check("k_tc_pairs");
     k_excl_scan<<<1, 1024, 0, st>>>(qtot, (int)nq, qbase);
+    launch_check("k_excl_scan");
+    k_tc_chunks<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(qtot, (int)nq, nchk);
+    launch_check("k_tc_chunks");
+    k_excl_scan<<<1, 1024, 0, st>>>(nchk, (int)nq, qchunk);
     launch_check("k_excl_scan");
     k_excl_scan<<<1, 1024, 0, st>>>(bcnt, (int)I.K, boff);
     launch_check("k_excl_scan");
@@ -871,49 +964,62 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     launch_check("k_tc_fill");
     k_tc_sort<<<(unsigned)I.K, 256, 0, st>>>(bcnt, boff, bucket, sorted);
     launch_check("k_tc_sort");
-    long long total = 0;
-    SAQG_CUDA_TRY(cudaMemcpyAsync(&total, qbase + nq, 8, cudaMemcpyDeviceToHost, st));
+    long long totals[2] = {0, 0};
+    SAQG_CUDA_TRY(cudaMemcpyAsync(&totals[0], qbase + nq, 8, cudaMemcpyDeviceToHost, st));
+    SAQG_CUDA_TRY(cudaMemcpyAsync(&totals[1], qchunk + nq, 8, cudaMemcpyDeviceToHost, st));
     SAQG_CUDA_TRY(cudaStreamSynchronize(st));
-    float *cand = static_cast<float *>(C.split_scratch_get(4 * (size_t)std::max<long long>(total, 1)));
+    const long long total = totals[0], nchunks = totals[1];
+    // arena 2: sized by the candidates
+    size_t need2 = a16(4 * (size_t)std::max<long long>(total, 1)) + a16(2 * (size_t)P * ix.Dtot) +
+                   a16(8 * (size_t)P * ix.S) + a16(8 * (size_t)P) + a16(8 * (size_t)std::max<long long>(nchunks, 1) * L);
+    char *base2 = static_cast<char *>(C.split_scratch_get(need2 + 256));
+    size_t off2 = 0;
+    auto take2 = [&](size_t b) {
+        char *p = base2 + off2;
+        off2 += a16(b);
+        return p;
+    };
+    float *cand = reinterpret_cast<float *>(take2(4 * (size_t)std::max<long long>(total, 1)));
+    __nv_bfloat16 *Bq = reinterpret_cast<__nv_bfloat16 *>(take2(2 * (size_t)P * ix.Dtot));
+    float2 *pscal = reinterpret_cast<float2 *>(take2(8 * (size_t)P * ix.S));
+    long long *cbase = reinterpret_cast<long long *>(take2(8 * (size_t)P));
+    int *spos = reinterpret_cast<int *>(take2(8 * (size_t)std::max<long long>(nchunks, 1) * L));
+    float *sval = reinterpret_cast<float *>(spos + std::max<long long>(nchunks, 1) * L);
+    k_tc_gather<<<(unsigned)((P * 32 + 255) / 256), 256, 0, st>>>(ix, probe, sorted, (int)P, (int)nprobe, qrot, qbase,
+                                                                 lp, Bq, pscal, cbase);
+    launch_check("k_tc_gather");
     mark(2);
-    // contraction
-    CUtensorMap tmA;
-    {
-        const cuuint64_t gdim[2] = {(cuuint64_t)ix.Dtot, (cuuint64_t)std::max<int64_t>(I.N, 1)};
-        const cuuint64_t gstride[1] = {(cuuint64_t)ix.Dtot * 2};
-        const cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)kTcBM};
-        const cuuint32_t estr[2] = {1, 1};
-        const CUresult r = tensor_map_encoder()(&tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, I.tc_codes, gdim, gstride,
-                                                box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (r != CUDA_SUCCESS) throw Error{SAQG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r)};
-    }
+    // contraction: persistent, one CTA per SM
+    const CUtensorMap tmA = bf16_rows_map(I.tc_codes, ix.Dtot, I.N, kTcBM);
+    const CUtensorMap tmB = bf16_rows_map(Bq, ix.Dtot, P, 16);
     TcWork wk;
     wk.tiles = static_cast<const int2 *>(I.tc_tiles);
+    wk.ntiles = (int)I.tc_ntiles;
     wk.bcnt = bcnt;
     wk.boff = boff;
-    wk.bucket = sorted;
-    wk.qrot = qrot;
-    wk.lp = lp;
-    wk.qbase = qbase;
+    wk.cbase = cbase;
+    wk.pscal = pscal;
     wk.cand = cand;
-    wk.nprobe = (int)nprobe;
     wk.BN = BN;
     wk.err = err;
     const size_t smem = tc_contract_smem();
     SAQG_CUDA_TRY(cudaFuncSetAttribute(k_tc_contract, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (I.tc_ntiles > 0) {
-        k_tc_contract<<<(unsigned)I.tc_ntiles, kTcThreads, smem, st>>>(tmA, ix, wk);
+        const unsigned grid = (unsigned)std::min<int64_t>(I.tc_ntiles, sm_count());
+        k_tc_contract<<<grid, kTcThreads, smem, st>>>(tmA, tmB, ix, wk);
         launch_check("k_tc_contract");
     }
     mark(3);
-    k_tc_select<<<(unsigned)nq, 256, 0, st>>>(cand, qbase, qtot, (int)L, sl_pos, sl_apx, sl_cnt);
-    launch_check("k_tc_select");
+    k_tc_select1<<<(unsigned)std::max<long long>(nchunks, 1), 256, 0, st>>>(cand, qbase, qtot, qchunk, (int)nq, (int)L,
+                                                                            spos, sval);
+    launch_check("k_tc_select1");
+    k_tc_select2<<<(unsigned)nq, 256, 0, st>>>(qchunk, qtot, (int)L, spos, sval, sl_pos, sl_apx, sl_cnt);
+    launch_check("k_tc_select2");
     mark(4);
-    tc_rerank(I, probe, nq, nprobe, qrot, prune, lp, sl_pos, sl_apx, sl_cnt, (int)L, topk, host ? oid : ids,
-              host ? od : dists, host ? oa : approx, st);
+    tc_rerank(I, probe, nq, nprobe, qrot, prune, lp, sl_pos, sl_apx, sl_cnt, (int)L, topk, grp, gj, ng, sl_dist,
+              host ? oid : ids, host ? od : dists, host ? oa : approx, st);
     mark(5);
-    count_launch(7);
+    count_launch(11);
     int herr = 0;
     SAQG_CUDA_TRY(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
     if (host) {
