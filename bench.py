@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[20000, 50000, 100000, 200000])
     ap.add_argument("--serve-seconds", type=float, default=0.3)
     ap.add_argument("--tc-shortlist", type=int, default=40)
+    ap.add_argument("--only", default="all", choices=["all", "precision"],
+                    help="precision: only the precision form's measurements (its own JSON line)")
     ap.add_argument("--precision-bits", type=int, nargs="*", default=[6, 8])
     ap.add_argument("--precision-n", type=int, default=1_000_000)
     ap.add_argument("--precision-dim", type=int, default=1536)
@@ -165,6 +167,13 @@ def precision_leg(a, torch, flush, log):
                                         ids_c.data_ptr(), d_c.data_ptr(), N.SAQG_MEM_DEVICE, sptr))
             ms_tc, _ = time_calls(torch, tc, flush, 5)
             ms_core, _ = time_calls(torch, core, flush, 5)
+            cst = N.SearchStats()
+            flush.zero_()
+            N.check(lib.saqg_search_ex(index._h, q.data_ptr(), B, 10, a.precision_nprobe, C.byref(scfg),
+                                       ids_c.data_ptr(), d_c.data_ptr(), N.SAQG_MEM_DEVICE, sptr, C.byref(cst), None))
+            core_stages = {"ms_probe": cst.ms_probe, "ms_qprep": cst.ms_qprep, "ms_scan": cst.ms_scan,
+                           "probe_full": cst.probe_full, "probe_full_ties": cst.probe_full_ties,
+                           "probe_exact": cst.probe_exact}
             flush.zero_()
             tc(True)
             torch.cuda.synchronize()
@@ -190,6 +199,7 @@ def precision_leg(a, torch, flush, log):
                    "tc_approx_rel_err_vs_fp32_estimator": {"median": float(np.median(rel_apx_est)),
                                                            "p99": float(np.percentile(rel_apx_est, 99))},
                    "stages_ms": {k: s[k] for k in ("ms_probe", "ms_pairs", "ms_contract", "ms_select", "ms_rerank")},
+                   "core_stages": core_stages,
                    "contract_roofline": {"tensor_tflops": tflops, "tensor_peak": peak_tf, "tensor_frac": tflops / peak_tf,
                                          "tensor_peak_kind": peak_tf_kind,
                                          "issued_tflops": s["mma_flops"] / (s["ms_contract"] / 1e3) / 1e12,
@@ -358,6 +368,12 @@ def main():
         dist.init_process_group("nccl")
     log = (lambda m: print(f"[bench] {m}", file=sys.stderr, flush=True)) if rank == 0 else (lambda m: None)
     t_start = time.time()
+    if a.only == "precision":
+        flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+        prec = precision_leg(a, torch, flush, log)
+        print(json.dumps({"metric": "precision form (tensor-core contraction) vs FP32 CUDA-core search",
+                          "precision": prec, "wall_s": time.time() - t_start}), flush=True)
+        return
     wl = build_workload(a, torch)
     log(f"workload {wl.name} generated in {time.time() - t_start:.1f}s")
     index, ipath, meta = get_index_and_meta(a, torch, wl, log)

@@ -740,60 +740,88 @@ __global__ void __launch_bounds__(256) k_qprep_small(DevIndexView ix, const floa
 // k_qprep for a tile of kQprepQT queries per CTA: each P element is read once
 // for the whole tile and drives kQprepQT independent chains, each in exactly
 // k_qprep's order (so the outputs are bit-identical); L2 traffic for the
-// rotations drops by the tile size.
+// rotations drops by the tile size.  A CTA computes kQprepSlice outputs (one
+// per thread; blockIdx.z picks the slice), and the P column of the next
+// 16-input block is loaded while the current block's chains run.
 constexpr int kQprepQT = 16;
-__global__ void __launch_bounds__(256) k_qprep_tiled(DevIndexView ix, const float *__restrict__ q, int nq, float m,
-                                                     float *__restrict__ qrot, float *__restrict__ prune) {
+constexpr int kQprepSlice = 256;
+__global__ void __launch_bounds__(kQprepSlice) k_qprep_tiled(DevIndexView ix, const float *__restrict__ q, int nq,
+                                                             float m, float *__restrict__ qrot,
+                                                             float *__restrict__ prune) {
     extern __shared__ __align__(16) float cqs[];  // [kQprepQT][dim]
     const int s = blockIdx.x, q0 = blockIdx.y * kQprepQT, nqt = min(kQprepQT, nq - q0);
     const SegDev &g = ix.seg[s];
     const int dim = g.dim, qoff = g.qoff;
+    const int i = blockIdx.z * kQprepSlice + threadIdx.x;
+    if (blockIdx.z * kQprepSlice >= dim) return;
     for (int e = threadIdx.x; e < kQprepQT * dim; e += blockDim.x) {
-        const int t = e / dim, i = e - t * dim, gi = qoff + i;
+        const int t = e / dim, ii = e - t * dim, gi = qoff + ii;
         cqs[e] = (t < nqt && gi < ix.D) ? q[(size_t)(q0 + t) * ix.D + gi] : 0.0f;
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5;
-    for (int t = warp; t < nqt; t += blockDim.x >> 5) {
-        const float *cq = cqs + t * dim, *var = ix.var + qoff;
-        const float v2 = warp_eigen_sum(dim, [&](int i) { return __fmul_rn(var[i], __fmul_rn(cq[i], cq[i])); });
-        if ((threadIdx.x & 31) == 0) prune[(size_t)(q0 + t) * ix.S + s] = __fmul_rn(sqrtf(v2), m);
-    }
-    if (!g.P) {
-        for (int e = threadIdx.x; e < nqt * dim; e += blockDim.x) {
-            const int t = e / dim, i = e - t * dim;
-            qrot[(size_t)(q0 + t) * ix.Dtot + qoff + i] = cqs[e];
+    if (blockIdx.z == 0)
+        for (int t = warp; t < nqt; t += blockDim.x >> 5) {
+            const float *cq = cqs + t * dim, *var = ix.var + qoff;
+            const float v2 = warp_eigen_sum(dim, [&](int k) { return __fmul_rn(var[k], __fmul_rn(cq[k], cq[k])); });
+            if ((threadIdx.x & 31) == 0) prune[(size_t)(q0 + t) * ix.S + s] = __fmul_rn(sqrtf(v2), m);
         }
+    if (i >= dim) return;
+    if (!g.P) {
+        for (int t = 0; t < nqt; ++t) qrot[(size_t)(q0 + t) * ix.Dtot + qoff + i] = cqs[t * dim + i];
         return;
     }
-    const int bc = dim < 128 ? dim : 16;
-    for (int i = threadIdx.x; i < dim; i += blockDim.x) {
-        float res[kQprepQT], c[kQprepQT];
+    float res[kQprepQT], c[kQprepQT];
 #pragma unroll
-        for (int t = 0; t < kQprepQT; ++t) res[t] = 0.0f;
-        for (int j2 = 0; j2 < dim; j2 += bc) {
+    for (int t = 0; t < kQprepQT; ++t) res[t] = 0.0f;
+    if (dim < 128) {  // one block of `dim` inputs (dims are multiples of 64)
+#pragma unroll
+        for (int t = 0; t < kQprepQT; ++t) c[t] = 0.0f;
+        for (int j = 0; j < dim; j += 4) {
+            const float p0 = g.P[(size_t)j * dim + i], p1 = g.P[(size_t)(j + 1) * dim + i];
+            const float p2 = g.P[(size_t)(j + 2) * dim + i], p3 = g.P[(size_t)(j + 3) * dim + i];
+#pragma unroll
+            for (int t = 0; t < kQprepQT; ++t) {
+                const float4 v = *reinterpret_cast<const float4 *>(cqs + t * dim + j);
+                c[t] = fmaf(p0, v.x, c[t]);
+                c[t] = fmaf(p1, v.y, c[t]);
+                c[t] = fmaf(p2, v.z, c[t]);
+                c[t] = fmaf(p3, v.w, c[t]);
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < kQprepQT; ++t) res[t] = fmaf(c[t], 1.0f, res[t]);
+    } else {  // blocks of 16 inputs, the next block's P column in flight
+        float pc[16], pn[16];
+#pragma unroll
+        for (int jj = 0; jj < 16; ++jj) pc[jj] = g.P[(size_t)jj * dim + i];
+        for (int j2 = 0; j2 < dim; j2 += 16) {
+            if (j2 + 16 < dim) {
+#pragma unroll
+                for (int jj = 0; jj < 16; ++jj) pn[jj] = g.P[(size_t)(j2 + 16 + jj) * dim + i];
+            }
 #pragma unroll
             for (int t = 0; t < kQprepQT; ++t) c[t] = 0.0f;
-            const int je = min(j2 + bc, dim);  // dims are multiples of 64: blocks split into groups of 4
-            for (int j = j2; j < je; j += 4) {
-                const float p0 = g.P[(size_t)j * dim + i], p1 = g.P[(size_t)(j + 1) * dim + i];
-                const float p2 = g.P[(size_t)(j + 2) * dim + i], p3 = g.P[(size_t)(j + 3) * dim + i];
+#pragma unroll
+            for (int jj = 0; jj < 16; jj += 4) {
 #pragma unroll
                 for (int t = 0; t < kQprepQT; ++t) {
-                    const float4 v = *reinterpret_cast<const float4 *>(cqs + t * dim + j);
-                    c[t] = fmaf(p0, v.x, c[t]);
-                    c[t] = fmaf(p1, v.y, c[t]);
-                    c[t] = fmaf(p2, v.z, c[t]);
-                    c[t] = fmaf(p3, v.w, c[t]);
+                    const float4 v = *reinterpret_cast<const float4 *>(cqs + t * dim + j2 + jj);
+                    c[t] = fmaf(pc[jj], v.x, c[t]);
+                    c[t] = fmaf(pc[jj + 1], v.y, c[t]);
+                    c[t] = fmaf(pc[jj + 2], v.z, c[t]);
+                    c[t] = fmaf(pc[jj + 3], v.w, c[t]);
                 }
             }
 #pragma unroll
             for (int t = 0; t < kQprepQT; ++t) res[t] = fmaf(c[t], 1.0f, res[t]);
-        }
 #pragma unroll
-        for (int t = 0; t < kQprepQT; ++t)
-            if (t < nqt) qrot[(size_t)(q0 + t) * ix.Dtot + qoff + i] = res[t];
+            for (int jj = 0; jj < 16; ++jj) pc[jj] = pn[jj];
+        }
     }
+#pragma unroll
+    for (int t = 0; t < kQprepQT; ++t)
+        if (t < nqt) qrot[(size_t)(q0 + t) * ix.Dtot + qoff + i] = res[t];
 }
 
 // ------------------------------------------------------------------ scan
@@ -2429,8 +2457,9 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         if (nq >= kQprepQT && kQprepQT * qsm <= 200 * 1024) {
             SAQG_CUDA_TRY(cudaFuncSetAttribute(k_qprep_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)(kQprepQT * qsm)));
-            k_qprep_tiled<<<dim3((unsigned)ix.S, (unsigned)((nq + kQprepQT - 1) / kQprepQT)), 256, kQprepQT * qsm,
-                            st>>>(ix, qin, (int)nq, m, qrot, prune);
+            k_qprep_tiled<<<dim3((unsigned)ix.S, (unsigned)((nq + kQprepQT - 1) / kQprepQT),
+                                 (unsigned)((qsm / 4 + kQprepSlice - 1) / kQprepSlice)),
+                            kQprepSlice, kQprepQT * qsm, st>>>(ix, qin, (int)nq, m, qrot, prune);
             check_launch("k_qprep_tiled");
         } else {
             int dmax = 0;
@@ -2800,15 +2829,22 @@ __device__ float searched_dist(const DevIndexView &ix, const ScanSmem &sm, int64
         v[s] = __shfl_sync(kFull, v[s], ln);
         f[s] = __shfl_sync(kFull, f[s], ln);
     }
+    // ex-code inner products by the 16 lanes of CodeHelper::compute_ip (each
+    // half-warp computes them; lane 0 holds the result)
+    float ex[kMaxSeg];
+    const unsigned half = lane < 16 ? 0x0000ffffu : 0xffff0000u;
+    for (int s = 0; s < S; ++s) {
+        const SegDev &g = ix.seg[s];
+        ex[s] = g.bits > 1 ? excode_ip_half(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim, g.bits - 1,
+                                            lane & 15, half)
+                           : 0.0f;
+    }
     float d = 0.0f;
     if (lane == 0) {
         float acc[kMaxSeg];
         for (int s = 0; s < S; ++s) {
             const SegDev &g = ix.seg[s];
-            const float ex = g.bits > 1 ? excode_ip_thread(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim,
-                                                           g.bits - 1)
-                                        : 0.0f;
-            acc[s] = accurate_dist(g.onorm[gb * 32 + ln], ipx[s], ex, g.exfac[gv].x, g.bits, sm.scal[s].sum_q,
+            acc[s] = accurate_dist(g.onorm[gb * 32 + ln], ipx[s], ex[s], g.exfac[gv].x, g.bits, sm.scal[s].sum_q,
                                    sm.scal[s].q_l2sqr);
         }
         if (S == 1) {
@@ -2963,8 +2999,9 @@ void tc_rank_rotate(const Index &I, SearchCtx &C, const float *q, int64_t nq, in
     if (nq >= kQprepQT && kQprepQT * qsm <= 200 * 1024) {
         SAQG_CUDA_TRY(cudaFuncSetAttribute(k_qprep_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)(kQprepQT * qsm)));
-        k_qprep_tiled<<<dim3((unsigned)ix.S, (unsigned)((nq + kQprepQT - 1) / kQprepQT)), 256, kQprepQT * qsm, st>>>(
-            ix, q, (int)nq, m, qrot, prune);
+        k_qprep_tiled<<<dim3((unsigned)ix.S, (unsigned)((nq + kQprepQT - 1) / kQprepQT),
+                             (unsigned)((qsm / 4 + kQprepSlice - 1) / kQprepSlice)),
+                        kQprepSlice, kQprepQT * qsm, st>>>(ix, q, (int)nq, m, qrot, prune);
         check_launch("k_qprep_tiled");
     } else {
         k_qprep<<<dim3((unsigned)ix.S, (unsigned)nq), 256, qsm, st>>>(ix, q, m, qrot, prune);
