@@ -641,7 +641,21 @@ def main():
         e1.synchronize()
         mixed_ms.append(e0.elapsed_time(e1))
     mixed_line = {"qps": B / (float(np.mean(mixed_ms)) / 1e3), "batch": B, "ms_per_batch": float(np.mean(mixed_ms)),
-                  "nprobe": "U[16,256] per query (mean %.0f)" % float(np_mix.mean()), "k": "10 or 100 per query"}
+                  "nprobe": "U[16,256] per query (mean %.0f)" % float(np_mix.mean()), "k": "10 or 100 per query",
+                  "form": "exact (saqg_search_batch)"}
+    # the same uneven batch through the tensor-core form (saqg_search_tc_batch), shortlist 4 x 100
+    ids_tm = torch.empty((B, 100), dtype=torch.int32, device="cuda")
+    d_tm = torch.empty((B, 100), dtype=torch.float32, device="cuda")
+
+    def mixed_tc():
+        N.check(lib.saqg_search_tc_batch(index._h, qdev.data_ptr(), B, np_mix.ctypes.data, k_mix.ctypes.data, 256, 100,
+                                         400, C.byref(scfg), ids_tm.data_ptr(), d_tm.data_ptr(), None,
+                                         N.SAQG_MEM_DEVICE, sptr, None))
+    mixed_tc_ms, _ = time_calls(torch, mixed_tc, flush, max(3, min(10, a.steps // 10)))
+    em, tm = ids_m.cpu().numpy().view(np.uint32), ids_tm.cpu().numpy().view(np.uint32)
+    hit = sum(len(set(em[i, :k_mix[i]].tolist()) & set(tm[i, :k_mix[i]].tolist())) for i in range(B))
+    mixed_line["tensor_core_form"] = {"qps": B / (mixed_tc_ms / 1e3), "ms_per_batch": mixed_tc_ms, "shortlist": 400,
+                                      "recall_vs_exact": hit / float(k_mix.sum())}
 
     # ---- serving: Poisson arrivals through the continuous-batching server ----
     serving = []

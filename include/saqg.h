@@ -213,6 +213,18 @@ int saqg_search_tc(const saqg_index *index, const float *queries, int64_t nq, in
                    int64_t shortlist, const saqg_searcher_config *cfg, uint32_t *ids, float *dists, float *approx,
                    int mem, void *stream, saqg_tc_stats *stats);
 
+/* No counterpart in the reference: saqg_search_tc for a batch whose queries
+ * carry their own nprobe and topk, host arrays of nq values (either may be
+ * NULL: then `nprobe` / `topk` for every query).  Rows of ids / dists / approx
+ * are max(topk) long; query i's first topk_i entries are its result and the
+ * rest id 0 / FLT_MAX.  Each query's answer equals its saqg_search_tc answer
+ * with its own nprobe and topk and the same shortlist (which must be at least
+ * the largest topk). */
+int saqg_search_tc_batch(const saqg_index *index, const float *queries, int64_t nq, const int32_t *nprobe_per_query,
+                         const int32_t *topk_per_query, int64_t nprobe, int64_t topk, int64_t shortlist,
+                         const saqg_searcher_config *cfg, uint32_t *ids, float *dists, float *approx, int mem,
+                         void *stream, saqg_tc_stats *stats);
+
 /* ---- graph-captured search ---------------------------------------------- */
 /* No counterpart in the reference: saqg_search for a fixed shape (nq, topk,
  * nprobe) on device buffers, captured into a CUDA graph.  Creation runs the

@@ -100,6 +100,9 @@ EXPORTS = {
                                      C.c_void_p, C.c_void_p]),
     "saqg_search_tc": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, I64, C.POINTER(SearcherConfig), C.c_void_p,
                                  C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(TcStats)]),
+    "saqg_search_tc_batch": (C.c_int, [C.c_void_p, C.c_void_p, I64, C.c_void_p, C.c_void_p, I64, I64, I64,
+                                       C.POINTER(SearcherConfig), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.c_void_p, C.POINTER(TcStats)]),
     "saqg_search_graph_create": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.POINTER(SearcherConfig),
                                            C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "saqg_search_graph_launch": (C.c_int, [C.c_void_p, C.c_void_p]),

@@ -186,6 +186,20 @@ int saqg_search_tc(const saqg_index *index, const float *queries, int64_t nq, in
     });
 }
 
+int saqg_search_tc_batch(const saqg_index *index, const float *queries, int64_t nq, const int32_t *nprobe_per_query,
+                         const int32_t *topk_per_query, int64_t nprobe, int64_t topk, int64_t shortlist,
+                         const saqg_searcher_config *cfg, uint32_t *ids, float *dists, float *approx, int mem,
+                         void *stream, saqg_tc_stats *stats) {
+    return guarded([&] {
+        SAQG_REQUIRE(index && (queries || nq == 0) && (ids || nq == 0), "null argument");
+        SAQG_REQUIRE(!cfg || cfg->dist_type == SAQG_DIST_L2, "only L2 search is supported");
+        SAQG_REQUIRE(mem == SAQG_MEM_HOST || mem == SAQG_MEM_DEVICE, "mem must be SAQG_MEM_HOST or SAQG_MEM_DEVICE");
+        const float m = cfg ? cfg->searcher_vars_bound_m : 4.0f;
+        run_search_tc(*index->impl, queries, nq, topk, nprobe, shortlist, m, ids, dists, approx, mem,
+                      (cudaStream_t)stream, stats, nprobe_per_query, topk_per_query);
+    });
+}
+
 int saqg_search_graph_create(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
                              const saqg_searcher_config *cfg, uint32_t *ids, float *dists, void *stream,
                              saqg_search_graph **out) {

@@ -165,18 +165,18 @@ int64_t run_estimate(const Index &idx, const float *q_host, int64_t nprobe, floa
 
 // Tensor-core form (search.cu): centroid ranking + query rotation of a batch,
 // and the exact re-rank of its shortlist.
-void tc_rank_rotate(const Index &idx, SearchCtx &ctx, const float *q, int64_t nq, int64_t nprobe, float m, float *dist,
-                    void *work, uint32_t *probe, float *qrot, float *prune, uint8_t *full, int *fb_list, int *flags,
-                    cudaStream_t st);
+void tc_rank_rotate(const Index &idx, SearchCtx &ctx, const float *q, int64_t nq, int64_t nprobe, const int *qnp,
+                    float m, float *dist, void *work, uint32_t *probe, float *qrot, float *prune, uint8_t *full,
+                    int *fb_list, int *flags, cudaStream_t st);
 size_t tc_probe_work_bytes(const Index &idx, int64_t nq);
 void tc_rerank(const Index &idx, const uint32_t *probe, int64_t nq, int64_t nprobe, const float *qrot,
                const float *prune, const int *lp, const int *sl_pos, const float *sl_apx, const int *sl_cnt, int L,
-               int64_t topk, int *grp, int *gj, int *ng, float *sl_dist, uint32_t *ids, float *dists, float *apx,
-               cudaStream_t st);
+               int64_t topk, const int *qk, int *grp, int *gj, int *ng, float *sl_dist, uint32_t *ids, float *dists,
+               float *apx, cudaStream_t st);
 // tc_search.cu
 void run_search_tc(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, int64_t shortlist,
                    float m, uint32_t *ids, float *dists, float *approx, int mem, cudaStream_t st,
-                   saqg_tc_stats *stats);
+                   saqg_tc_stats *stats, const int *np_host = nullptr, const int *k_host = nullptr);
 
 // graph.cpp
 struct SearchGraph;

@@ -2922,8 +2922,8 @@ __global__ void __launch_bounds__(kScanThreads) k_tc_topk(DevIndexView ix, const
                                                           const float *__restrict__ sl_apx,
                                                           const int *__restrict__ sl_cnt,
                                                           const float *__restrict__ sl_dist, int L, int L2, int topk,
-                                                          uint32_t *__restrict__ ids, float *__restrict__ dists,
-                                                          float *__restrict__ apx_out) {
+                                                          const int *__restrict__ qk, uint32_t *__restrict__ ids,
+                                                          float *__restrict__ dists, float *__restrict__ apx_out) {
     extern __shared__ __align__(16) char smem_raw[];
     unsigned long long *key = reinterpret_cast<unsigned long long *>(smem_raw);
     const int qi = blockIdx.x, tid = threadIdx.x;
@@ -2948,10 +2948,11 @@ __global__ void __launch_bounds__(kScanThreads) k_tc_topk(DevIndexView ix, const
             }
             __syncthreads();
         }
+    const int kq = qk ? qk[qi] : topk;  // this query's k; rows are topk long, padded with (0, FLT_MAX)
     for (int t = tid; t < topk; t += blockDim.x) {
         uint32_t id = 0;
         float d = FLT_MAX, a = FLT_MAX;
-        if (t < n) {
+        if (t < n && t < kq) {
             const int p = 0x7fffffff - (int)(unsigned)(key[t] & 0xffffffffull);
             int lo = 0, hi = n - 1;  // the shortlist entry of position p
             while (lo < hi) {
@@ -2978,20 +2979,21 @@ __global__ void __launch_bounds__(kScanThreads) k_tc_topk(DevIndexView ix, const
 
 }  // namespace
 
-void tc_rank_rotate(const Index &I, SearchCtx &C, const float *q, int64_t nq, int64_t nprobe, float m, float *dist,
-                    void *work, uint32_t *probe, float *qrot, float *prune, uint8_t *full, int *fb_list, int *flags,
-                    cudaStream_t st) {
+void tc_rank_rotate(const Index &I, SearchCtx &C, const float *q, int64_t nq, int64_t nprobe, const int *qnp, float m,
+                    float *dist, void *work, uint32_t *probe, float *qrot, float *prune, uint8_t *full, int *fb_list,
+                    int *flags, cudaStream_t st) {
     const DevIndexView &ix = I.view;
     SAQG_CUDA_TRY(cudaMemsetAsync(flags, 0, 64, st));
     Cand *wk = static_cast<Cand *>(work);
     const char *pm = std::getenv("SAQG_PROBE");
     const bool shortlist = nq >= kGemmMinQueries && nprobe <= kShortCap && !(pm && std::string(pm) == "exact");
     if (shortlist) {
-        probe_shortlist(I, C, q, nq, nprobe, nullptr, dist, probe, full, fb_list, flags, wk, nullptr, st);
+        probe_shortlist(I, C, q, nq, nprobe, qnp, dist, probe, full, fb_list, flags, wk, nullptr, st);
     } else {
         k_probe_dist<<<dim3((unsigned)((I.K + 7) / 8), (unsigned)nq), 256, 0, st>>>(ix, q, dist);
         check_launch("k_probe_dist");
-        k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, wk, flags);
+        k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, wk, flags, nullptr,
+                                                              qnp);
         check_launch("k_probe_select");
     }
     size_t qsm = 0;
@@ -3014,8 +3016,8 @@ size_t tc_probe_work_bytes(const Index &I, int64_t nq) { return sizeof(Cand) * (
 
 void tc_rerank(const Index &I, const uint32_t *probe, int64_t nq, int64_t nprobe, const float *qrot,
                const float *prune, const int *lp, const int *sl_pos, const float *sl_apx, const int *sl_cnt, int L,
-               int64_t topk, int *grp, int *gj, int *ng, float *sl_dist, uint32_t *ids, float *dists, float *apx,
-               cudaStream_t st) {
+               int64_t topk, const int *qk, int *grp, int *gj, int *ng, float *sl_dist, uint32_t *ids, float *dists,
+               float *apx, cudaStream_t st) {
     const DevIndexView &ix = I.view;
     int L2 = 1;
     while (L2 < L) L2 <<= 1;
@@ -3029,7 +3031,7 @@ void tc_rerank(const Index &I, const uint32_t *probe, int64_t nq, int64_t nprobe
                                                                              sl_pos, sl_cnt, grp, gj, ng, L, sl_dist);
     check_launch("k_tc_rerank");
     k_tc_topk<<<(unsigned)nq, kScanThreads, 8 * (size_t)L2, st>>>(ix, probe, (int)nprobe, lp, sl_pos, sl_apx, sl_cnt,
-                                                                  sl_dist, L, L2, (int)topk, ids, dists, apx);
+                                                                  sl_dist, L, L2, (int)topk, qk, ids, dists, apx);
     check_launch("k_tc_topk");
     count_launch(3);
 }

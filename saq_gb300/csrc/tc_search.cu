@@ -255,17 +255,20 @@ __global__ void k_tc_cluster_of(const int64_t *__restrict__ vec_off, int K, int3
 
 // ------------------------------------------------------------ pairs
 // One warp per query: candidate offsets of its probes in probe order
-// (lp[i][j] = sizes of probes 0..j-1; lp[i][nprobe] = its candidates) and the
-// per-cluster pair counts.
-__global__ void k_tc_pairs(DevIndexView ix, const uint32_t *__restrict__ probe, int nq, int nprobe, int *__restrict__ lp,
-                           int *__restrict__ qtot, int *__restrict__ bcnt) {
+// (lp[i][j] = sizes of probes 0..j-1; lp[i][j] for j >= the query's nprobe =
+// its candidate count) and the per-cluster pair counts.  qnp: per-query nprobe
+// (null: nprobe for every query); probe rows are nprobe long.
+__global__ void k_tc_pairs(DevIndexView ix, const uint32_t *__restrict__ probe, int nq, int nprobe,
+                           const int *__restrict__ qnp, int *__restrict__ lp, int *__restrict__ qtot,
+                           int *__restrict__ bcnt) {
     const int qi = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (qi >= nq) return;
+    const int npq = qnp ? qnp[qi] : nprobe;
     int run = 0;
-    for (int j0 = 0; j0 < nprobe; j0 += 32) {
+    for (int j0 = 0; j0 < npq; j0 += 32) {
         const int j = j0 + lane;
         int sz = 0;
-        if (j < nprobe) {
+        if (j < npq) {
             const uint32_t c = probe[(size_t)qi * nprobe + j];
             sz = (int)(ix.vec_off[c + 1] - ix.vec_off[c]);
             atomicAdd(&bcnt[c], 1);
@@ -276,13 +279,11 @@ __global__ void k_tc_pairs(DevIndexView ix, const uint32_t *__restrict__ probe, 
             const int y = __shfl_up_sync(kFullMask, x, o);
             if (lane >= o) x += y;
         }
-        if (j < nprobe) lp[(size_t)qi * (nprobe + 1) + j] = run + x - sz;
+        if (j < npq) lp[(size_t)qi * (nprobe + 1) + j] = run + x - sz;
         run += __shfl_sync(kFullMask, x, 31);
     }
-    if (lane == 0) {
-        lp[(size_t)qi * (nprobe + 1) + nprobe] = run;
-        qtot[qi] = run;
-    }
+    for (int j = npq + lane; j <= nprobe; j += 32) lp[(size_t)qi * (nprobe + 1) + j] = run;
+    if (lane == 0) qtot[qi] = run;
 }
 
 // Exclusive prefix sum of n ints into n + 1 int64s (the last is the total);
@@ -319,10 +320,11 @@ __global__ void __launch_bounds__(1024) k_excl_scan(const int *__restrict__ in, 
     if (tid == 1023) out[n] = run;
 }
 
-__global__ void k_tc_fill(const uint32_t *__restrict__ probe, int npairs, const long long *__restrict__ boff,
-                          int *__restrict__ bfill, int *__restrict__ bucket) {
+__global__ void k_tc_fill(const uint32_t *__restrict__ probe, int npairs, int nprobe, const int *__restrict__ qnp,
+                          const long long *__restrict__ boff, int *__restrict__ bfill, int *__restrict__ bucket) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npairs) return;
+    if (qnp && p % nprobe >= qnp[p / nprobe]) return;  // past this query's nprobe
     const uint32_t c = probe[p];
     const int slot = atomicAdd(&bfill[c], 1);
     bucket[boff[c] + slot] = p;
@@ -846,8 +848,25 @@ CUtensorMap bf16_rows_map(void *base, int64_t cols, int64_t rows, int box_rows) 
 }  // namespace
 
 void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, int64_t L, float m,
-                   uint32_t *ids, float *dists, float *approx, int mem, cudaStream_t st, saqg_tc_stats *stats) {
+                   uint32_t *ids, float *dists, float *approx, int mem, cudaStream_t st, saqg_tc_stats *stats,
+                   const int *np_host, const int *k_host) {
     const DevIndexView &ix = I.view;
+    // per-query nprobe / k (host arrays): the scalars become their maxima
+    int64_t pairs = nq * nprobe;
+    if (np_host || k_host) {
+        int64_t npm = 0, km = 0;
+        pairs = 0;
+        for (int64_t i = 0; i < nq; ++i) {
+            const int a = np_host ? np_host[i] : (int)nprobe, b = k_host ? k_host[i] : (int)topk;
+            SAQG_REQUIRE(a >= 1 && a <= I.K, "every nprobe must be in [1, number of clusters]");
+            SAQG_REQUIRE(b >= 1 && b <= kTcMaxShort, "every topk must be in [1, 1024]");
+            npm = std::max<int64_t>(npm, a);
+            km = std::max<int64_t>(km, b);
+            pairs += a;
+        }
+        if (np_host) nprobe = npm;
+        if (k_host) topk = km;
+    }
     SAQG_REQUIRE(nq >= 0 && nq <= kTcMaxBatch, "the tensor-core search takes at most 8192 queries per call");
     SAQG_REQUIRE(topk >= 1 && topk <= kTcMaxShort, "topk must be in [1, 1024]");
     SAQG_REQUIRE(L >= topk && L <= kTcMaxShort, "shortlist must be in [topk, 1024]");
@@ -864,7 +883,7 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     SearchCtx &C = I.ctx;
     std::lock_guard<std::mutex> lock(C.mu);
     const bool host = mem == SAQG_MEM_HOST;
-    const int64_t P = nq * nprobe;
+    const int64_t P = nq * nprobe;  // probe slots (rows of nprobe); `pairs` of them are used
     // arena 1: sized by the call's shape
     size_t need = 0;
     auto add = [&](size_t b) { need += a16(b); };
@@ -887,6 +906,7 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     add(4 * (size_t)nq * 2);                    // sl_cnt, group counts
     add(4 * (size_t)nq * topk * 3);             // outputs (host io)
     add(16);                                    // error word
+    add(4 * (size_t)nq * 2);                    // per-query nprobe / k
     char *base = static_cast<char *>(C.scratch_get(need + 256));
     size_t off = 0;
     auto take = [&](size_t b) {
@@ -924,6 +944,18 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     float *od = reinterpret_cast<float *>(oid + nq * topk);
     float *oa = od + nq * topk;
     int *err = reinterpret_cast<int *>(take(16));
+    int *qnp = nullptr, *qk = nullptr;
+    {
+        int *pk = reinterpret_cast<int *>(take(4 * (size_t)nq * 2));
+        if (np_host) {
+            qnp = pk;
+            SAQG_CUDA_TRY(cudaMemcpyAsync(qnp, np_host, 4 * (size_t)nq, cudaMemcpyHostToDevice, st));
+        }
+        if (k_host) {
+            qk = pk + nq;
+            SAQG_CUDA_TRY(cudaMemcpyAsync(qk, k_host, 4 * (size_t)nq, cudaMemcpyHostToDevice, st));
+        }
+    }
 
     cudaEvent_t ev[6] = {};
     struct EvGuard {
@@ -945,12 +977,12 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
         qin = dq;
     }
     mark(0);
-    tc_rank_rotate(I, C, qin, nq, nprobe, m, dist, work, probe, qrot, prune, full, fb, flags, st);
+    tc_rank_rotate(I, C, qin, nq, nprobe, qnp, m, dist, work, probe, qrot, prune, full, fb, flags, st);
     mark(1);
     // pairs: candidate offsets per query, buckets per cluster, selection chunks
     SAQG_CUDA_TRY(cudaMemsetAsync(bcnt, 0, 8 * (size_t)I.K, st));
     SAQG_CUDA_TRY(cudaMemsetAsync(err, 0, 16, st));
-    k_tc_pairs<<<(unsigned)((nq + 7) / 8), 256, 0, st>>>(ix, probe, (int)nq, (int)nprobe, lp, qtot, bcnt);
+    k_tc_pairs<<<(unsigned)((nq + 7) / 8), 256, 0, st>>>(ix, probe, (int)nq, (int)nprobe, qnp, lp, qtot, bcnt);
     launch_check("k_tc_pairs");
     k_excl_scan<<<1, 1024, 0, st>>>(qtot, (int)nq, qbase);
     launch_check("k_excl_scan");
@@ -960,7 +992,7 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     launch_check("k_excl_scan");
     k_excl_scan<<<1, 1024, 0, st>>>(bcnt, (int)I.K, boff);
     launch_check("k_excl_scan");
-    k_tc_fill<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(probe, (int)P, boff, bfill, bucket);
+    k_tc_fill<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(probe, (int)P, (int)nprobe, qnp, boff, bfill, bucket);
     launch_check("k_tc_fill");
     k_tc_sort<<<(unsigned)I.K, 256, 0, st>>>(bcnt, boff, bucket, sorted);
     launch_check("k_tc_sort");
@@ -970,8 +1002,8 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     SAQG_CUDA_TRY(cudaStreamSynchronize(st));
     const long long total = totals[0], nchunks = totals[1];
     // arena 2: sized by the candidates
-    size_t need2 = a16(4 * (size_t)std::max<long long>(total, 1)) + a16(2 * (size_t)P * ix.Dtot) +
-                   a16(8 * (size_t)P * ix.S) + a16(8 * (size_t)P) + a16(8 * (size_t)std::max<long long>(nchunks, 1) * L);
+    size_t need2 = a16(4 * (size_t)std::max<long long>(total, 1)) + a16(2 * (size_t)pairs * ix.Dtot) +
+                   a16(8 * (size_t)pairs * ix.S) + a16(8 * (size_t)pairs) + a16(8 * (size_t)std::max<long long>(nchunks, 1) * L);
     char *base2 = static_cast<char *>(C.split_scratch_get(need2 + 256));
     size_t off2 = 0;
     auto take2 = [&](size_t b) {
@@ -980,18 +1012,18 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
         return p;
     };
     float *cand = reinterpret_cast<float *>(take2(4 * (size_t)std::max<long long>(total, 1)));
-    __nv_bfloat16 *Bq = reinterpret_cast<__nv_bfloat16 *>(take2(2 * (size_t)P * ix.Dtot));
-    float2 *pscal = reinterpret_cast<float2 *>(take2(8 * (size_t)P * ix.S));
-    long long *cbase = reinterpret_cast<long long *>(take2(8 * (size_t)P));
+    __nv_bfloat16 *Bq = reinterpret_cast<__nv_bfloat16 *>(take2(2 * (size_t)pairs * ix.Dtot));
+    float2 *pscal = reinterpret_cast<float2 *>(take2(8 * (size_t)pairs * ix.S));
+    long long *cbase = reinterpret_cast<long long *>(take2(8 * (size_t)pairs));
     int *spos = reinterpret_cast<int *>(take2(8 * (size_t)std::max<long long>(nchunks, 1) * L));
     float *sval = reinterpret_cast<float *>(spos + std::max<long long>(nchunks, 1) * L);
-    k_tc_gather<<<(unsigned)((P * 32 + 255) / 256), 256, 0, st>>>(ix, probe, sorted, (int)P, (int)nprobe, qrot, qbase,
-                                                                 lp, Bq, pscal, cbase);
+    k_tc_gather<<<(unsigned)((pairs * 32 + 255) / 256), 256, 0, st>>>(ix, probe, sorted, (int)pairs, (int)nprobe, qrot,
+                                                                     qbase, lp, Bq, pscal, cbase);
     launch_check("k_tc_gather");
     mark(2);
     // contraction: persistent, one CTA per SM
     const CUtensorMap tmA = bf16_rows_map(I.tc_codes, ix.Dtot, I.N, kTcBM);
-    const CUtensorMap tmB = bf16_rows_map(Bq, ix.Dtot, P, 16);
+    const CUtensorMap tmB = bf16_rows_map(Bq, ix.Dtot, pairs, 16);
     TcWork wk;
     wk.tiles = static_cast<const int2 *>(I.tc_tiles);
     wk.ntiles = (int)I.tc_ntiles;
@@ -1016,7 +1048,7 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     k_tc_select2<<<(unsigned)nq, 256, 0, st>>>(qchunk, qtot, (int)L, spos, sval, sl_pos, sl_apx, sl_cnt);
     launch_check("k_tc_select2");
     mark(4);
-    tc_rerank(I, probe, nq, nprobe, qrot, prune, lp, sl_pos, sl_apx, sl_cnt, (int)L, topk, grp, gj, ng, sl_dist,
+    tc_rerank(I, probe, nq, nprobe, qrot, prune, lp, sl_pos, sl_apx, sl_cnt, (int)L, topk, qk, grp, gj, ng, sl_dist,
               host ? oid : ids, host ? od : dists, host ? oa : approx, st);
     mark(5);
     count_launch(11);
@@ -1050,7 +1082,7 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
             const int64_t nch = (hc[c] + BN - 1) / BN, npad = (nch - 1) * BN + (((hc[c] - (nch - 1) * BN) + 15) & ~15);
             padded += 2 * (int64_t)ix.Dtot * kTcBM * nt * npad;
         }
-        stats->pairs = P;
+        stats->pairs = pairs;
         stats->candidates = total;
         stats->tiles = tiles;
         stats->flops = flops;

@@ -179,37 +179,50 @@ class IVF:
                                                N.SAQG_MEM_HOST, _stream_ptr(stream), None))
         return (ids, dists) if return_dists else ids
 
-    def search_tc(self, query, topk: int, nprobe: int, shortlist: int | None = None,
+    def search_tc(self, query, topk, nprobe, shortlist: int | None = None,
                   searcher_cfg: SearcherConfig | None = None, return_dists: bool = False,
                   return_approx: bool = False, stats: bool = False, stream=None):
         """Tensor-core form of a batched search (saqg_search_tc): the approximate
         distances of every probed vector come from one dense BF16 product per
         cluster on the tensor cores, the `shortlist` (default 4 * topk) smallest
-        per query are re-ranked with the exact search's distance.  Returns ids
-        [, dists] [, approx] [, stats dict]."""
+        per query are re-ranked with the exact search's distance.  `topk` /
+        `nprobe` may be per-query sequences (saqg_search_tc_batch; rows are then
+        max(topk) long, padded with id 0 / FLT_MAX).  Returns ids [, dists]
+        [, approx] [, stats dict]."""
         cfg = (searcher_cfg or SearcherConfig()).to_c()
-        L = int(shortlist if shortlist is not None else max(4 * topk, topk))
+        mixed = not (np.isscalar(topk) and np.isscalar(nprobe))
         st = N.TcStats()
         sp = C.byref(st) if stats else None
         if _is_cuda_tensor(query):
             import torch
             q = query.contiguous().view(-1, self.num_dim)
             nq = q.shape[0]
-            ids = torch.empty((nq, topk), dtype=torch.int32, device=q.device)
-            dists = torch.empty((nq, topk), dtype=torch.float32, device=q.device)
-            apx = torch.empty((nq, topk), dtype=torch.float32, device=q.device)
-            N.check(self.lib.saqg_search_tc(self._h, q.data_ptr(), nq, topk, nprobe, L, C.byref(cfg), ids.data_ptr(),
-                                            dists.data_ptr(), apx.data_ptr(), N.SAQG_MEM_DEVICE, _stream_ptr(stream),
-                                            sp))
         else:
             q = np.ascontiguousarray(query, np.float32).reshape(-1, self.num_dim)
             nq = q.shape[0]
-            ids = np.zeros((nq, topk), np.uint32)
-            dists = np.zeros((nq, topk), np.float32)
-            apx = np.zeros((nq, topk), np.float32)
-            N.check(self.lib.saqg_search_tc(self._h, q.ctypes.data, nq, topk, nprobe, L, C.byref(cfg), ids.ctypes.data,
-                                            dists.ctypes.data, apx.ctypes.data, N.SAQG_MEM_HOST, _stream_ptr(stream),
-                                            sp))
+        if mixed:
+            ks = np.broadcast_to(np.asarray(topk, np.int32), (nq,)).copy()
+            nps = np.broadcast_to(np.asarray(nprobe, np.int32), (nq,)).copy()
+            kmax, npmax = int(ks.max()), int(nps.max())
+        else:
+            kmax, npmax = int(topk), int(nprobe)
+        L = int(shortlist if shortlist is not None else 4 * kmax)
+        if _is_cuda_tensor(query):
+            ids = torch.empty((nq, kmax), dtype=torch.int32, device=q.device)
+            dists = torch.empty((nq, kmax), dtype=torch.float32, device=q.device)
+            apx = torch.empty((nq, kmax), dtype=torch.float32, device=q.device)
+            qp, ip, dp, ap, mem = q.data_ptr(), ids.data_ptr(), dists.data_ptr(), apx.data_ptr(), N.SAQG_MEM_DEVICE
+        else:
+            ids = np.zeros((nq, kmax), np.uint32)
+            dists = np.zeros((nq, kmax), np.float32)
+            apx = np.zeros((nq, kmax), np.float32)
+            qp, ip, dp, ap, mem = q.ctypes.data, ids.ctypes.data, dists.ctypes.data, apx.ctypes.data, N.SAQG_MEM_HOST
+        if mixed:
+            N.check(self.lib.saqg_search_tc_batch(self._h, qp, nq, nps.ctypes.data, ks.ctypes.data, npmax, kmax, L,
+                                                  C.byref(cfg), ip, dp, ap, mem, _stream_ptr(stream), sp))
+        else:
+            N.check(self.lib.saqg_search_tc(self._h, qp, nq, kmax, npmax, L, C.byref(cfg), ip, dp, ap, mem,
+                                            _stream_ptr(stream), sp))
         out = [ids]
         if return_dists:
             out.append(dists)

@@ -91,6 +91,23 @@ def test_batch_equals_single_queries(built):
         assert np.array_equal(si[0], ids[i]) and np.array_equal(sd[0], d[i]), i
 
 
+def test_uneven_batch_equals_single_queries(built):
+    """Queries with their own nprobe and k in one call (saqg_search_tc_batch):
+    each row equals that query searched alone with its own arguments and the
+    same shortlist; rows are padded to the largest k with id 0 / FLT_MAX."""
+    index, _, q, _ = built
+    nq, L = 100, 48
+    rng = np.random.default_rng(17)
+    nps = rng.integers(2, 21, size=nq).astype(np.int32)
+    ks = rng.choice([5, 10, 12], size=nq).astype(np.int32)
+    ids, d = index.search_tc(q[:nq], ks, nps, shortlist=L, return_dists=True)
+    assert ids.shape == (nq, 12)
+    for i in range(0, nq, 9):
+        si, sd = index.search_tc(q[i:i + 1], int(ks[i]), int(nps[i]), shortlist=L, return_dists=True)
+        assert np.array_equal(si[0], ids[i, :ks[i]]) and np.array_equal(sd[0], d[i, :ks[i]]), i
+        assert np.all(ids[i, ks[i]:] == 0) and np.all(d[i, ks[i]:] == np.float32(3.4028235e38)), i
+
+
 def test_device_buffers_match_host(built):
     torch = pytest.importorskip("torch")
     index, _, q, _ = built
