@@ -654,8 +654,14 @@ def main():
     mixed_tc_ms, _ = time_calls(torch, mixed_tc, flush, max(3, min(10, a.steps // 10)))
     em, tm = ids_m.cpu().numpy().view(np.uint32), ids_tm.cpu().numpy().view(np.uint32)
     hit = sum(len(set(em[i, :k_mix[i]].tolist()) & set(tm[i, :k_mix[i]].tolist())) for i in range(B))
+    # recall@10 against FP64 ground truth of both forms, over the queries with k = 10 that have ground truth
+    sel = [i for i in range(min(B, len(meta["gt"]))) if k_mix[i] == 10]
+    gt10 = meta["gt"][sel]
+    mixed_line["recall@10_fp64_k10_queries"] = round(workloads.recall_at(em[sel, :10], gt10, 10), 4)
     mixed_line["tensor_core_form"] = {"qps": B / (mixed_tc_ms / 1e3), "ms_per_batch": mixed_tc_ms, "shortlist": 400,
-                                      "recall_vs_exact": hit / float(k_mix.sum())}
+                                      "recall_vs_exact": hit / float(k_mix.sum()),
+                                      "recall@10_fp64_k10_queries": round(workloads.recall_at(tm[sel, :10], gt10, 10), 4),
+                                      "k10_queries": len(sel)}
 
     # ---- serving: Poisson arrivals through the continuous-batching server ----
     serving = []
