@@ -491,12 +491,10 @@ def main():
             vec_counts.append(stats.vectors)
         torch.cuda.synchronize()
 
+    from saq_gb300.replicas import max_over_ranks
+
     def world_max(x):
-        if world > 1:
-            t = torch.tensor([x], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return float(t.item())
-        return x
+        return max_over_ranks(x, "cuda")
     tot_ms = world_max(float(sum(step_ms)))
     exact_value = world * B * a.steps / (tot_ms / 1e3)
     tc_tot_ms = world_max(float(sum(tc_step_ms)))
