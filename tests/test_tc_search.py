@@ -151,3 +151,66 @@ def test_rejects_uncoded_segments(golden_case_by_name):
     index = ivf.IVF.load(golden_case_by_name("aniso_b15_seg_0bit"))
     with pytest.raises(N.SaqgError, match="every segment coded"):
         index.search_tc(z["q"][:4], 10, 4)
+
+
+@pytest.fixture(scope="module")
+def with_empty(tmp_path_factory):
+    """12 clusters, two of them empty and far away (as in test_edge_cases)."""
+    from saq_gb300 import ivf
+    tmp = tmp_path_factory.mktemp("tc_edge")
+    x, q = data.gaussian_mixture(3000, 128, 40, sigma=0.6, seed=13, n_query=80)
+    cent, cids = data.kmeans(x, 10, iters=5, seed=5)
+    far = np.full((2, 128), 50.0, np.float32)
+    far[1] *= -1
+    cent = np.concatenate([cent, far])
+    rng = np.random.default_rng(21)
+    plan = O.plan(O.colwise_var(x), 6.0, False, 0)
+    rots = np.concatenate([data.random_orthogonal(d, rng).astype(np.float32).reshape(-1) for d, _ in plan])
+    index = ivf.IVF(x.shape[0], 128, cent.shape[0], ivf.QuantizeConfig(avg_bits=6.0, enable_segmentation=False))
+    index.construct(x, cent, cids.astype(np.uint32), rotations=rots)
+    opath = str(tmp / "o.index")
+    O.build_index(opath, x, cent, cids.astype(np.uint32), 6.0, False, 0, rots)
+    return index, O.OracleIndex(opath), q
+
+
+@pytest.mark.parametrize("nq", [80, 6])
+def test_edge_empty_clusters_and_unfilled_rows(with_empty, nq):
+    """nprobe = every cluster (two empty), topk 1, and topk beyond the probed
+    vectors (rows padded with id 0 / FLT_MAX); a query whose only probe is an
+    empty cluster gets a row of padding."""
+    index, oi, q = with_empty
+    qq = q[:nq]
+    for topk, nprobe, L in [(10, 12, 40), (1, 3, 4), (1000, 1, 1000)]:
+        ids, d = index.search_tc(qq, topk, nprobe, shortlist=L, return_dists=True)
+        for i in range(nq):
+            oid, od, accmap, m = _full_topk(oi, qq[i], nprobe, topk)
+            n = min(topk, m)
+            for j in range(n):
+                assert accmap[int(ids[i, j])] == d[i, j], (topk, nprobe, i, j)
+            if m <= L:  # the shortlist holds every candidate: the oracle's top-k exactly
+                assert np.array_equal(ids[i, :n], oid[:n]) and np.array_equal(d[i, :n], od[:n].astype(np.float32))
+            assert np.all(ids[i, n:] == 0) and np.all(d[i, n:] == np.float32(3.4028235e38))
+    far_q = np.full((1, 128), 50.0, np.float32)  # nearest centroid: an empty cluster
+    ids, d = index.search_tc(far_q, 5, 1, return_dists=True)
+    assert np.all(ids == 0) and np.all(d == np.float32(3.4028235e38))
+
+
+def test_edge_one_cluster_and_no_queries(tmp_path):
+    from saq_gb300 import ivf
+    x, q = data.gaussian_mixture(700, 64, 5, sigma=0.5, seed=3, n_query=5)
+    cent = x.mean(axis=0, keepdims=True).astype(np.float32)
+    cids = np.zeros(x.shape[0], np.uint32)
+    rng = np.random.default_rng(22)
+    plan = O.plan(O.colwise_var(x), 6.0, False, 0)
+    rots = np.concatenate([data.random_orthogonal(dd, rng).astype(np.float32).reshape(-1) for dd, _ in plan])
+    index = ivf.IVF(x.shape[0], 64, 1, ivf.QuantizeConfig(avg_bits=6.0, enable_segmentation=False))
+    index.construct(x, cent, cids, rotations=rots)
+    opath = str(tmp_path / "one.index")
+    O.build_index(opath, x, cent, cids, 6.0, False, 0, rots)
+    oi = O.OracleIndex(opath)
+    ids, d = index.search_tc(q, 20, 1, shortlist=1000, return_dists=True)
+    for i in range(q.shape[0]):
+        oid, od, _, _ = _full_topk(oi, q[i], 1, 20)
+        assert np.array_equal(ids[i], oid) and np.array_equal(d[i], od.astype(np.float32)), i
+    empty = index.search_tc(np.zeros((0, 64), np.float32), 10, 1)
+    assert empty.shape == (0, 10)
