@@ -23,6 +23,7 @@ i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 u16p = np.ctypeslib.ndpointer(dtype=np.uint16, flags="C_CONTIGUOUS")
 u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 L = C.c_long
 
 
@@ -63,6 +64,8 @@ def lib():
         l.orc_search.argtypes = [C.c_void_p, f32p, L, L, L, C.c_float, u32p, C.c_void_p, C.c_int]
         l.orc_estimate.restype = L
         l.orc_estimate.argtypes = [C.c_void_p, f32p, L, C.c_float, u32p, f32p, f32p, f32p, L]
+        l.orc_tc_approx.restype = L
+        l.orc_tc_approx.argtypes = [C.c_void_p, f32p, L, C.c_float, u32p, f64p, L]
         l.orc_build_index.restype = C.c_int
         l.orc_build_index.argtypes = [f32p, L, L, f32p, L, u32p, C.c_float, C.c_int, C.c_int, C.c_int, C.c_float,
                                       C.c_int, C.c_void_p, C.c_void_p, C.c_char_p]
@@ -198,6 +201,15 @@ class OracleIndex:
         d = np.zeros((q.shape[0], topk), np.float32) if with_dists else None
         lib().orc_search(self.h, q, q.shape[0], topk, nprobe, m, ids, None if d is None else d.ctypes.data, threads)
         return (ids, d) if with_dists else ids
+
+    def tc_approx(self, q, nprobe, m=4.0, cap=None):
+        """Model of the tensor-core form's approximate distance (exact codes, double):
+        (ids, approx) for every vector of the probed clusters, in estimate's order."""
+        cap = cap or self.N
+        ids = np.zeros(cap, np.uint32)
+        apx = np.zeros(cap, np.float64)
+        n = lib().orc_tc_approx(self.h, _f32(q), nprobe, m, ids, apx, cap)
+        return ids[:n], apx[:n]
 
     def estimate(self, q, nprobe, m=4.0, cap=None):
         cap = cap or self.N

@@ -1197,6 +1197,59 @@ long orc_estimate(void *h, const float *q, long nprobe, float m, uint32_t *ids, 
     return w;
 }
 
+// Model of the tensor-core form's approximate distance (the reference has no
+// such form): per segment |o|^2 + |r|^2 - 2 rescale (delta <r, u> + (delta/2 - 1) sum r),
+// r the rotated residual query, u the full B-bit code ((1-bit code << (B-1)) |
+// ex-code), delta = 2 / 2^B, all in double; for every vector of the probed
+// clusters in the order of orc_estimate.  It is CaqCluEstimator::compAccurateDist
+// (caq_estimator.hpp:190-217) with the 1-bit part's u16 LUT replaced by the
+// exact code.
+long orc_tc_approx(void *h, const float *q, long nprobe, float m, uint32_t *ids, double *approx, long cap) {
+    auto *ix = static_cast<Index *>(h);
+    auto cd = probe(ix, q, nprobe);
+    Query Q(ix, q, m);
+    const long S = (long)ix->segs.size();
+    long w = 0;
+    std::vector<uint16_t> ex;
+    for (auto &cc : cd) {
+        const Clu &c = ix->clus[cc.id];
+        for (long s = 0; s < S; ++s) Q.se[s].prepare(c.cent[s].data());
+        for (long v = 0; v < c.n; ++v) {
+            const long b = v / kFS;
+            const int j = (int)(v % kFS);
+            double a = 0;
+            for (long s = 0; s < S; ++s) {
+                const SegEst &e = Q.se[s];
+                const double on = ix->onorm(c, s, b)[j];
+                double sq = 0, sr = 0, ip = 0;
+                for (long d = 0; d < e.D; ++d) {
+                    sq += (double)e.q[d] * e.q[d];
+                    sr += e.q[d];
+                }
+                if (e.bits == 0) {
+                    a += on * on + sq;
+                    continue;
+                }
+                ex.assign(e.D, 0);
+                if (e.bits > 1) unpack_excode(ix->lcode(c, s, v), e.D, (int)e.bits - 1, ex.data());
+                const uint8_t *blk = ix->codes(c, s, b);
+                for (long d = 0; d < e.D; ++d) {
+                    const long msb = (block_nibble(blk, d / 4, j) >> (3 - d % 4)) & 1;
+                    ip += (double)((msb << (e.bits - 1)) | ex[d]) * e.q[d];
+                }
+                const double dl = 2.0 / (double)(1L << e.bits);
+                a += on * on + sq - 2.0 * ix->lfac(c, s, v)[0] * (dl * ip + (dl / 2 - 1.0) * sr);
+            }
+            if (w < cap) {
+                ids[w] = c.ids[v];
+                approx[w] = a;
+            }
+            ++w;
+        }
+    }
+    return w;
+}
+
 int orc_build_index(const float *data, long N, long D, const float *cent, long K, const uint32_t *cids, float avg_bits,
                     int seg, int eqseg, int rdlmt, float eps, int rotate, const float *vars, const float *rots,
                     const char *path) {
