@@ -55,3 +55,36 @@ def test_invalid_arguments_return_status(lib):
     with pytest.raises(SaqgError, match="multiple of 64"):
         ivf.plan(np.ones(100, np.float32), 4.0)
     assert lib.saqg_version() == 1
+
+
+def test_integration_adapter_compiles_and_links(tmp_path, lib):
+    """The C++ adapter that INTEGRATION.md shows a reference application (GpuIVF,
+    same member signature as IVF::search) compiles against include/saqg.h and
+    links against the library, with a stand-in for the reference's row vector
+    and searcher config (only .data() and searcher_vars_bound_m are used)."""
+    import shutil
+    import subprocess
+    from saq_gb300.build import LIB
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("no C++ compiler")
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    block = re.search(r"```cpp\n(.*?)```", text, flags=re.S).group(1)
+    src = tmp_path / "adapter.cpp"
+    src.write_text("#include <stdexcept>\n#include <vector>\n" + block + """
+struct RowVec { std::vector<float> v; const float *data() const { return v.data(); } };
+struct Cfg { float searcher_vars_bound_m = 4.0f; };
+int main(int argc, char **argv) {
+    if (argc < 2) return 0;  // construction needs an index file and a GPU
+    GpuIVF ivf(argv[1]);
+    RowVec q{std::vector<float>(128, 0.0f)};
+    uint32_t ids[10];
+    ivf.search(q, 10, 4, Cfg{}, ids);
+    return 0;
+}
+""")
+    exe = tmp_path / "adapter"
+    r = subprocess.run([gxx, "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                        LIB, "-Wl,-rpath," + os.path.dirname(LIB)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert subprocess.run([str(exe)]).returncode == 0
