@@ -691,9 +691,11 @@ def main():
         qnp = wl.q.cpu().numpy()
         r, ns, dt, cids_cpu, _ = cpu_search_rate(ipath, qnp, a.topk, nprobe, a.cpu_seconds, threads)
         same = bool(np.array_equal(cids_cpu[:min(ns, B)], got[:min(ns, B)]))
+        r1, ns1, dt1, _, _ = cpu_search_rate(ipath, qnp, a.topk, nprobe, min(2.0, a.cpu_seconds), 1)
         cpu = {"value": r, "unit": "queries/s", "cores": threads, "kind": "port",
                "sample": f"{ns} queries of the batch on the same index ({dt:.1f}s, {threads} threads)",
-               "ids_equal_gpu": same}
+               "ids_equal_gpu": same,
+               "single_thread": {"value": r1, "sample": f"{ns1} queries ({dt1:.1f}s, 1 thread)"}}
 
     precision = None
     if rank == 0 and a.precision_bits:
