@@ -4,21 +4,32 @@ Workload (default): 10M x 1024 unit-norm vectors, anisotropic spectrum, PCA,
 16,384 clusters with Zipf(1.1) sizes, SAQ B=4 with segmentation, k=10, the
 smallest nprobe that reaches recall@10 >= 0.95 against exact FP64 ground truth.
 
-  value   batched QPS: one search call answers a batch of 4096 queries that are
-          already in HBM (each query answered exactly as an independent
-          IVF::search call); the L2 cache is flushed between timed steps.
+  value   batched QPS of the exact form (saqg_search): one call answers a batch
+          of 4096 queries already in HBM, every answer bit-identical to an
+          independent IVF::search call; the L2 cache is flushed between steps.
   e2e     the same batch through the C ABI with host buffers: host->device copy
           of the queries and device->host copy of ids + distances inside the
           timed region.
+  roofline  the exact form's scan phase: compulsory bytes (each distinct probed
+          cluster's codes once + every re-rank) / its CUDA-event duration.
+  batched_tc  the batched tensor-core form (saqg_search_tc, a stated-recall
+          variant: dense contraction, shortlist, exact re-rank) with the
+          contraction's roofline on the codes' own (packed) bytes.
   plain   the plain single-query drop-in: one query per call (QPS, p50, p99).
-  roofline  the scan kernel's algorithmic bytes / its CUDA-event duration.
+  c1, c2  the single-query configurations: 100k x 960 Gaussian mixture (nprobe
+          32) and 1M x 1024 anisotropic (B 1.5 / 4, with and without
+          segmentation, nprobe 16-128): plain QPS, p50 / p99, recall@10 against
+          FP64, GPU encode vectors/s, and the CPU oracle's search and encode
+          rates on the same data beside them.
   cpu_baseline  the CPU oracle (a port of the reference's search) on the host
           cores, on a bounded sample of the same queries and index.
 
---impl reference times the CPU implementation alone (same index, same
-queries, all host threads) and prints its line with "impl": "reference".
-Multi-GPU (--gpus N via torchrun) runs N independent replicas (the search
-has no exchange step): value = all ranks' queries / the slowest rank's time.
+--impl reference times the CPU implementation alone on an index that the CPU
+oracle's builder writes (same data, plan and rotations, so the same file; this
+process never loads the GPU library) and prints its line with
+"impl": "reference".  Multi-GPU (--gpus N via torchrun) runs N independent
+replicas (the search has no exchange step): value = all ranks' queries / the
+slowest rank's time.
 """
 from __future__ import annotations
 
@@ -39,7 +50,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "QPS at recall@10≥0.95 (10M×1024, B=4): batched vs plain GPU; p99 ms; HBM %"
 NPROBE_GRID = [16, 24, 32, 48, 64, 96, 128, 160, 192, 256]
-CACHE_VERSION = 3
+CACHE_VERSION = 4
 
 
 def parse():
@@ -65,8 +76,12 @@ def parse():
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[20000, 50000, 100000, 200000])
     ap.add_argument("--serve-seconds", type=float, default=0.3)
     ap.add_argument("--tc-shortlist", type=int, default=40)
-    ap.add_argument("--only", default="all", choices=["all", "precision"],
-                    help="precision: only the precision form's measurements (its own JSON line)")
+    ap.add_argument("--only", default="all", choices=["all", "precision", "c1", "c2"],
+                    help="precision / c1 / c2: only that leg's measurements (its own JSON line)")
+    ap.add_argument("--configs", type=int, default=1, help="0: skip the c1 / c2 legs in the full run")
+    ap.add_argument("--c2-n", type=int, default=1_000_000)
+    ap.add_argument("--c2-queries", type=int, default=400, help="single queries timed per (B, seg, nprobe)")
+    ap.add_argument("--c1-queries", type=int, default=1000)
     ap.add_argument("--precision-bits", type=int, nargs="*", default=[6, 8])
     ap.add_argument("--precision-n", type=int, default=1_000_000)
     ap.add_argument("--precision-dim", type=int, default=1536)
@@ -284,10 +299,13 @@ def dist_env():
     return rank, world, local
 
 
-def cache_paths(a):
+def cache_paths(a, builder):
+    """Per-box cache of the built index; `builder` is "gpu" (this library) or
+    "oracle" (the CPU oracle's builder, used by the reference arm).  Both write
+    the same bytes from the same data, plan and rotations."""
     key = (f"v{CACHE_VERSION}_n{a.n}_d{a.dim}_k{a.clusters}_b{a.bits}_s{a.sigma}_na{a.noise_alpha}"
            f"_q{a.query_clusters}_seed0")
-    d = os.path.join(a.cache, key)
+    d = os.path.join(a.cache, key, builder)
     os.makedirs(d, exist_ok=True)
     return d, os.path.join(d, "index.saq"), os.path.join(d, "meta.json")
 
@@ -298,39 +316,47 @@ def build_workload(a, torch):
                                 sigma=a.sigma, noise_alpha=a.noise_alpha, query_clusters=a.query_clusters)
 
 
+ROT_SEED = 1
+
+
+def tune_nprobe(search, gt, topk, clusters, target):
+    """Smallest nprobe on the grid whose recall@topk reaches the target."""
+    from saq_gb300 import workloads
+    curve = {}
+    for npb in NPROBE_GRID:
+        if npb > clusters:
+            break
+        r = workloads.recall_at(search(npb), gt, topk)
+        curve[npb] = r
+        if r >= target:
+            return npb, r, curve
+    return max(curve), curve[max(curve)], curve
+
+
 def get_index_and_meta(a, torch, wl, log):
     """Index built on the GPU (or loaded from this box's cache), ground truth and the tuned nprobe."""
     from saq_gb300 import ivf, workloads
-    cdir, ipath, mpath = cache_paths(a)
+    cdir, ipath, mpath = cache_paths(a, "gpu")
     meta = json.load(open(mpath)) if os.path.exists(mpath) and os.path.exists(ipath) else None
     t0 = time.time()
     if meta:
         index = ivf.IVF.load(ipath)
         log(f"index loaded from cache in {time.time() - t0:.1f}s")
     else:
+        plan = ivf.plan(wl.variance, a.bits, True)
+        rots = workloads.rotations(plan, ROT_SEED)
         cfg = ivf.QuantizeConfig(avg_bits=a.bits, enable_segmentation=True)
         index = ivf.IVF(a.n, a.dim, a.clusters, cfg)
         index.set_variance(wl.variance)
-        index.construct(wl.x, wl.centroids.cpu().numpy(), wl.cids.cpu().numpy().astype(np.uint32), seed=1)
+        index.construct(wl.x, wl.centroids.cpu().numpy(), wl.cids.cpu().numpy().astype(np.uint32), rotations=rots)
         torch.cuda.synchronize()
         build_s = time.time() - t0
         log(f"index built on the GPU in {build_s:.1f}s plan={index.info()['plan']}")
         gt = workloads.ground_truth(wl.x, wl.q[: a.gt_queries], a.topk)
         np.save(os.path.join(cdir, "gt.npy"), gt)
-        # nprobe: smallest on the grid reaching the target recall@10
-        nprobe, rec, curve = None, None, {}
         qg = wl.q[: a.gt_queries].contiguous()
-        for npb in NPROBE_GRID:
-            if npb > a.clusters:
-                break
-            ids = index.search(qg, a.topk, npb).cpu().numpy().view(np.uint32)
-            r = workloads.recall_at(ids, gt, a.topk)
-            curve[npb] = r
-            if r >= a.target_recall:
-                nprobe, rec = npb, r
-                break
-        if nprobe is None:
-            nprobe, rec = max(curve), curve[max(curve)]
+        nprobe, rec, curve = tune_nprobe(lambda npb: index.search(qg, a.topk, npb).cpu().numpy().view(np.uint32),
+                                         gt, a.topk, a.clusters, a.target_recall)
         index.save(ipath)
         meta = dict(nprobe=nprobe, recall=rec, curve=curve, build_s=build_s, plan=index.info()["plan"])
         json.dump(meta, open(mpath, "w"))
@@ -339,11 +365,46 @@ def get_index_and_meta(a, torch, wl, log):
     return index, ipath, meta
 
 
-def cpu_search_rate(ipath, q, topk, nprobe, seconds, threads):
-    """Oracle (CPU port of the reference search) QPS on a bounded sample."""
+def get_oracle_index(a, torch, wl, log):
+    """The reference arm's index: written by the CPU oracle's builder on every
+    host thread (same data, plan and rotations as the GPU arm, so the same
+    bytes); nprobe tuned with the oracle's own search.  Nothing here touches
+    the GPU library."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    oi = O.OracleIndex(ipath)
+    from saq_gb300 import workloads
+    cdir, ipath, mpath = cache_paths(a, "oracle")
+    meta = json.load(open(mpath)) if os.path.exists(mpath) and os.path.exists(ipath) else None
+    if not meta:
+        t0 = time.time()
+        plan = O.plan(wl.variance, a.bits, True, 0)
+        rots = workloads.rotations(plan, ROT_SEED)
+        xh = wl.x.cpu().numpy()
+        O.build_index(ipath, xh, wl.centroids.cpu().numpy(), wl.cids.cpu().numpy().astype(np.uint32), a.bits, True,
+                      0, rots, variance=wl.variance, threads=0)
+        del xh
+        build_s = time.time() - t0
+        log(f"index built by the CPU oracle in {build_s:.1f}s ({os.cpu_count()} threads) plan={plan}")
+        gt = workloads.ground_truth(wl.x, wl.q[: a.gt_queries], a.topk)
+        np.save(os.path.join(cdir, "gt.npy"), gt)
+        oi = O.OracleIndex(ipath)
+        qg = wl.q[: a.gt_queries].cpu().numpy()
+        nprobe, rec, curve = tune_nprobe(lambda npb: oi.search(qg, a.topk, npb, threads=os.cpu_count() or 1),
+                                         gt, a.topk, a.clusters, a.target_recall)
+        del oi
+        meta = dict(nprobe=nprobe, recall=rec, curve=curve, build_s=build_s, plan=plan)
+        json.dump(meta, open(mpath, "w"))
+        log(f"nprobe={nprobe} recall@{a.topk}={rec:.4f} curve={curve}")
+    meta["gt"] = np.load(os.path.join(cdir, "gt.npy"))
+    return ipath, meta
+
+
+def cpu_search_rate(ipath, q, topk, nprobe, seconds, threads, oi=None):
+    """Oracle (CPU port of the reference search) QPS on a bounded sample: single-query
+    tasks on `threads` host threads (src/test_qps.cpp's thread pool)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    oi = oi or O.OracleIndex(ipath)
     probe = q[:threads]
     t0 = time.time()
     oi.search(probe, topk, nprobe, threads=threads)
@@ -356,6 +417,143 @@ def cpu_search_rate(ipath, q, topk, nprobe, seconds, threads):
     return nsamp / dt, nsamp, dt, ids, oi
 
 
+def plain_latencies(torch, lib, index, q, topk, nprobe):
+    """Device time (CUDA events, synchronised per call) of one saqg_search call
+    per query with nq = 1, the plain drop-in; returns (ms per query, ids)."""
+    import ctypes as C
+    from saq_gb300 import _native as N, ivf
+    stream = torch.cuda.current_stream()
+    sptr = C.c_void_p(stream.cuda_stream)
+    scfg = ivf.SearcherConfig().to_c()
+    P = q.shape[0]
+    ids = torch.empty((P, topk), dtype=torch.int32, device="cuda")
+    dd = torch.empty((P, topk), dtype=torch.float32, device="cuda")
+
+    def one(i):
+        N.check(lib.saqg_search(index._h, q[i].data_ptr(), 1, topk, nprobe, C.byref(scfg), ids[i].data_ptr(),
+                                dd[i].data_ptr(), N.SAQG_MEM_DEVICE, sptr))
+    for i in range(min(8, P)):
+        one(i)
+    torch.cuda.synchronize()
+    lat = []
+    for i in range(P):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        one(i)
+        e1.record(stream)
+        e1.synchronize()
+        lat.append(e0.elapsed_time(e1))
+    return np.array(lat), ids.cpu().numpy().view(np.uint32)
+
+
+def cpu_encode_rate(xh, cent, cids, var, bits, seg, rots, want, tmpdir):
+    """The CPU oracle's builder (IVF::construct restated) on every host thread,
+    on the first clusters holding at least `want` vectors: vectors/s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    sizes = np.bincount(cids, minlength=cent.shape[0])
+    kk = int(np.searchsorted(np.cumsum(sizes), min(want, len(cids)))) + 1
+    kk = min(kk, cent.shape[0])
+    sel = cids < kk
+    xs = np.ascontiguousarray(xh[sel])
+    path = os.path.join(tmpdir, "cpu_encode.index")
+    t0 = time.time()
+    O.build_index(path, xs, cent[:kk], cids[sel], bits, seg, 0, rots, variance=var, threads=0)
+    dt = time.time() - t0
+    os.remove(path)
+    return {"value": len(xs) / dt, "unit": "vectors/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{len(xs)} vectors ({kk} clusters) built into an index file in {dt:.1f}s"}
+
+
+def single_query_config(a, torch, log, wl, name, variants, nprobes, nq_time, tmpdir):
+    """One single-query configuration: per (B, segmentation) a GPU-built index,
+    per nprobe the plain drop-in's QPS / p50 / p99 / recall@10 against FP64, and
+    the CPU oracle's search (all host threads, single-query tasks) and encode
+    rates on the same data."""
+    from saq_gb300 import ivf, workloads
+    threads = os.cpu_count() or 1
+    gt = workloads.ground_truth(wl.x, wl.q[:nq_time], 10)
+    qd = wl.q[:nq_time].contiguous()
+    qh = qd.cpu().numpy()
+    xh = None
+    cent = wl.centroids.cpu().numpy()
+    cids = wl.cids.cpu().numpy().astype(np.uint32)
+    out = {"workload": wl.name, "n": int(wl.x.shape[0]), "dim": int(wl.x.shape[1]),
+           "clusters": int(cent.shape[0]), "k": 10, "queries_timed": nq_time,
+           "timing": "plain single-query saqg_search per call (CUDA events, synchronised per call); "
+                     "QPS = queries / sum of latencies", "variants": []}
+    for bits, seg in variants:
+        plan = ivf.plan(wl.variance, bits, seg)
+        rots = workloads.rotations(plan, ROT_SEED)
+        t0 = time.time()
+        index = ivf.IVF(wl.x.shape[0], wl.x.shape[1], cent.shape[0],
+                        ivf.QuantizeConfig(avg_bits=bits, enable_segmentation=seg))
+        index.set_variance(wl.variance)
+        index.construct(wl.x, cent, cids, rotations=rots)
+        torch.cuda.synchronize()
+        enc_s = time.time() - t0
+        ipath = os.path.join(tmpdir, f"{name}_{bits}_{int(seg)}.index")
+        index.save(ipath)
+        row = {"bits": bits, "segmentation": seg, "plan": plan,
+               "encode_gpu": {"value": wl.x.shape[0] / enc_s, "unit": "vectors/s",
+                              "note": "saqg_index_construct from device-resident data, rotation included"},
+               "nprobe": []}
+        if xh is None:
+            xh = wl.x.cpu().numpy()
+        row["encode_cpu_baseline"] = cpu_encode_rate(xh, cent, cids, wl.variance, bits, seg, rots,
+                                                     min(100_000, wl.x.shape[0]), tmpdir)
+        oi = None
+        for npb in nprobes:
+            lat, ids = plain_latencies(torch, index.lib, index, qd, 10, npb)
+            r, ns, dt, cids_cpu, oi = cpu_search_rate(ipath, qh, 10, npb, a.cpu_seconds / 10, threads, oi)
+            pt = {"nprobe": npb, "qps": len(lat) / (lat.sum() / 1e3), "p50_ms": float(np.median(lat)),
+                  "p99_ms": float(np.percentile(lat, 99)), "recall@10": round(workloads.recall_at(ids, gt, 10), 4),
+                  "cpu_baseline": {"value": r, "unit": "queries/s", "cores": threads, "kind": "port",
+                                   "sample": f"{ns} single-query tasks in {dt:.2f}s"},
+                  "ids_equal_cpu": bool(np.array_equal(cids_cpu[:ns], ids[:ns]))}
+            row["nprobe"].append(pt)
+            log(f"{name} B={bits} seg={seg} nprobe={npb}: {pt['qps']:.0f} q/s p50 {pt['p50_ms']:.3f} ms "
+                f"p99 {pt['p99_ms']:.3f} ms recall {pt['recall@10']:.4f} cpu {r:.0f} q/s")
+        r1, ns1, dt1, _, _ = cpu_search_rate(ipath, qh, 10, nprobes[0], 1.0, 1, oi)
+        del oi
+        row["cpu_single_thread"] = {"value": r1, "nprobe": nprobes[0], "sample": f"{ns1} queries in {dt1:.2f}s"}
+        row["encode_over_cpu"] = row["encode_gpu"]["value"] / row["encode_cpu_baseline"]["value"]
+        log(f"{name} B={bits} seg={seg}: encode GPU {row['encode_gpu']['value']:.0f} v/s, "
+            f"CPU {row['encode_cpu_baseline']['value']:.0f} v/s")
+        out["variants"].append(row)
+        os.remove(ipath)
+        del index
+        torch.cuda.empty_cache()
+    return out
+
+
+def c1_leg(a, torch, log, tmpdir):
+    from saq_gb300 import workloads
+    t0 = time.time()
+    wl = workloads.gaussian_mixture_ivf(100_000, 960, 1024, 0.5, nq=a.c1_queries, k=1024, iters=20, seed=0)
+    log(f"c1 workload (k-means 1024 x 20 iterations on the GPU) in {time.time() - t0:.1f}s")
+    out = single_query_config(a, torch, log, wl, "c1", [(4.0, True)], [32], a.c1_queries, tmpdir)
+    out["data"] = ("Gaussian mixture: 1,024 centres ~ N(0,1)^960, point = centre + N(0, 0.5^2), seed 0; PCA; "
+                   "k-means 1,024 clusters x 20 iterations; queries from the same mixture")
+    del wl
+    torch.cuda.empty_cache()
+    return out
+
+
+def c2_leg(a, torch, log, tmpdir):
+    from saq_gb300 import workloads
+    t0 = time.time()
+    wl = workloads.aniso_ivf(a.c2_n, 1024, 0.8, nq=a.c2_queries, k=4096, iters=8, seed=0)
+    log(f"c2 workload (k-means 4096 x 8 iterations on the GPU) in {time.time() - t0:.1f}s")
+    out = single_query_config(a, torch, log, wl, "c2", [(1.5, True), (1.5, False), (4.0, True), (4.0, False)],
+                              [16, 32, 64, 128], a.c2_queries, tmpdir)
+    out["data"] = ("unit-norm rows, random orthogonal basis, per-axis variance ~ i^-0.8, seed 0; PCA; "
+                   "k-means 4,096 clusters x 8 iterations")
+    del wl
+    torch.cuda.empty_cache()
+    return out
+
+
 def main():
     a = parse()
     rank, world, local = dist_env()
@@ -363,7 +561,7 @@ def main():
         return
     import torch
     torch.cuda.set_device(local)
-    if world > 1:
+    if world > 1 and a.impl != "reference":
         import torch.distributed as dist
         dist.init_process_group("nccl")
     log = (lambda m: print(f"[bench] {m}", file=sys.stderr, flush=True)) if rank == 0 else (lambda m: None)
@@ -374,9 +572,18 @@ def main():
         print(json.dumps({"metric": "precision form (tensor-core contraction) vs FP32 CUDA-core search",
                           "precision": prec, "wall_s": time.time() - t_start}), flush=True)
         return
+    if a.only in ("c1", "c2"):
+        with tempfile.TemporaryDirectory() as td:
+            out = (c1_leg if a.only == "c1" else c2_leg)(a, torch, log, td)
+        print(json.dumps({"metric": "plain single-query QPS, p50/p99, recall@10 and encode vectors/s",
+                          a.only: out, "wall_s": time.time() - t_start}), flush=True)
+        return
     wl = build_workload(a, torch)
     log(f"workload {wl.name} generated in {time.time() - t_start:.1f}s")
-    index, ipath, meta = get_index_and_meta(a, torch, wl, log)
+    if a.impl == "reference":
+        ipath, meta = get_oracle_index(a, torch, wl, log)
+    else:
+        index, ipath, meta = get_index_and_meta(a, torch, wl, log)
     nprobe = meta["nprobe"]
     threads = os.cpu_count() or 1
     config = {"workload": f"{a.n // 1_000_000}M x {a.dim}, B={a.bits:g} SAQ (segmented), {a.clusters} clusters "
@@ -385,33 +592,34 @@ def main():
               "l2": "flushed between timed steps (256 MiB write)", "queries": "same distribution as the base set",
               "data_model": f"unit-norm; centre spectrum i^-0.8, within-cluster spectrum i^-{a.noise_alpha:g}, "
                             f"sigma {a.sigma:g}; query clusters {a.query_clusters}",
-              "form": f"batched tensor-core search (saqg_search_tc): BF16 code contraction, shortlist "
-                      f"{a.tc_shortlist}, re-ranked with the exact search's distance"}
+              "form": "batched exact search (saqg_search): every id and distance equal to the reference's "
+                      "IVF::search on the same index, bit for bit"}
 
     if a.impl == "reference":
         qh = wl.q.cpu().numpy()
-        rates = []
+        oi = None
         for _ in range(a.warmup):
-            cpu_search_rate(ipath, qh, a.topk, nprobe, 2.0, threads)
+            _, _, _, _, oi = cpu_search_rate(ipath, qh, a.topk, nprobe, 2.0, threads, oi)
         step_q = None
         times = []
         for _ in range(a.steps):
-            r, ns, dt, _, _ = cpu_search_rate(ipath, qh, a.topk, nprobe, 3.0, threads)
-            rates.append(r)
+            r, ns, dt, _, oi = cpu_search_rate(ipath, qh, a.topk, nprobe, 3.0, threads, oi)
             times.append(dt)
             step_q = ns
-        v = float(sum(step_q for _ in rates) / sum(times))
+        v = float(step_q * len(times) / sum(times))
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "queries/s", "n_gpus": world,
                 "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32",
                 "data": "synthetic (seeded, generated on the GPU)", "config": config,
                 "cpu_baseline": {"value": v, "unit": "queries/s", "cores": threads, "kind": "port",
-                                 "sample": f"{step_q} queries per step on the same 10M index"},
+                                 "sample": f"{step_q} single-query tasks per step on the same 10M index "
+                                           f"(written by the CPU oracle's builder in "
+                                           f"{meta.get('build_s', 0.0):.0f}s)"},
                 "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
 
-    from saq_gb300 import _native as N, ivf
+    from saq_gb300 import _native as N, ivf, workloads
     import ctypes as C
     lib = index.lib
     stream = torch.cuda.current_stream()
@@ -431,14 +639,6 @@ def main():
                                    C.byref(stats) if with_stats else None,
                                    probes.data_ptr() if with_stats else None))
 
-    # ---- exact batched form (saqg_search: every answer the reference's), device-resident ----
-    for _ in range(a.warmup):
-        batched(True)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    step_ms, scan_ms, fast_b, rr_b, spec, rr, probe_ms, qprep_ms, split_ms = [], [], [], [], [], [], [], [], []
-    vec_counts = []
     ids_t = torch.empty((B, a.topk), dtype=torch.int32, device="cuda")
     d_t = torch.empty((B, a.topk), dtype=torch.float32, device="cuda")
     tst = N.TcStats()
@@ -448,30 +648,19 @@ def main():
                                    ids_t.data_ptr(), d_t.data_ptr(), None, N.SAQG_MEM_DEVICE, sptr,
                                    C.byref(tst) if with_stats else None))
     for _ in range(a.warmup):
+        batched(True)
+    for _ in range(a.warmup):
         tcb()
     torch.cuda.synchronize()
+    step_ms, scan_ms, fast_b, rr_b, spec, rr, probe_ms, qprep_ms, split_ms = [], [], [], [], [], [], [], [], []
+    vec_counts = []
     with ClockSampler(local) as clk:
         time.sleep(0.3)  # first sample before the timed region
-        # ---- headline: the batched tensor-core form (saqg_search_tc), device-resident ----
+        # ---- headline: the exact batched form (saqg_search), device-resident ----
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
         launches0 = lib.saqg_kernel_launches()
-        tc_step_ms = []
-        for _ in range(a.steps):
-            flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            tcb()
-            e1.record(stream)
-            e1.synchronize()
-            tc_step_ms.append(e0.elapsed_time(e1))
-        torch.cuda.synchronize()
-        launches = lib.saqg_kernel_launches() - launches0
-        if world > 1:
-            torch.distributed.barrier()
-        # ---- exact batched form ----
-        torch.cuda.synchronize()
         for _ in range(a.steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -490,22 +679,35 @@ def main():
             rr.append(stats.reranked)
             vec_counts.append(stats.vectors)
         torch.cuda.synchronize()
+        launches = lib.saqg_kernel_launches() - launches0
+        if world > 1:
+            torch.distributed.barrier()
+        # ---- the batched tensor-core form (saqg_search_tc) on the same batch ----
+        tc_step_ms = []
+        for _ in range(a.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            tcb()
+            e1.record(stream)
+            e1.synchronize()
+            tc_step_ms.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
 
     from saq_gb300.replicas import max_over_ranks
 
     def world_max(x):
         return max_over_ranks(x, "cuda")
     tot_ms = world_max(float(sum(step_ms)))
-    exact_value = world * B * a.steps / (tot_ms / 1e3)
+    value = world * B * a.steps / (tot_ms / 1e3)
     tc_tot_ms = world_max(float(sum(tc_step_ms)))
-    value = world * B * a.steps / (tc_tot_ms / 1e3)
+    tc_value = world * B * a.steps / (tc_tot_ms / 1e3)
     got = ids.cpu().numpy().view(np.uint32)
-    from saq_gb300 import workloads
     gt = meta["gt"]
     ng = min(len(gt), B)
     batch_recall = workloads.recall_at(got[:ng], gt[:ng], a.topk)
 
-    # compulsory bytes: each distinct probed cluster once + every re-rank
+    # compulsory bytes of the exact form: each distinct probed cluster once + every re-rank
     info = index.info()
     sizes = np.bincount(wl.cids.cpu().numpy(), minlength=a.clusters)
     nblk = (sizes + 31) // 32
@@ -537,9 +739,15 @@ def main():
     it_ = ids_t.cpu().numpy().view(np.uint32)
     ts = tc_stats[-1]
     contract_ms = float(np.mean([x["ms_contract"] for x in tc_stats]))
-    # algorithmic bytes of one contraction launch: the codes of every probed
-    # cluster once (BF16), the gathered query rows, the approximate distances written
-    tc_bytes = int(ts["code_bytes"] + 2 * ts["pairs"] * sum(d for d, _ in info["plan"]) + 4 * ts["candidates"])
+    # algorithmic bytes of one contraction launch (the unit of the codes' own width):
+    # every distinct probed cluster's codes once at their packed width (sum over
+    # segments of dim x bits / 8) with |o| and the rescale factor per coded
+    # segment, the queries' rows (BF16) of every (query, cluster) pair, and the
+    # approximate distances written
+    dtot = sum(d for d, _ in info["plan"])
+    packed_pv = sum(d * b / 8 + (8 if b else 4) for d, b in info["plan"])
+    n_distinct = int(sizes[distinct].sum())
+    tc_bytes = int(n_distinct * packed_pv + 2 * ts["pairs"] * dtot + 4 * ts["candidates"])
     tc_achieved = tc_bytes / (contract_ms / 1e3) / 1e9
     tc_traffic = None
     tf2 = os.path.join(ROOT, "profiles", "k_tc_contract_traffic.json")
@@ -549,7 +757,7 @@ def main():
             tc_traffic = tj.get("dram_bytes_per_launch")
     tc_recall = workloads.recall_at(it_[:ng], gt[:ng], a.topk)
 
-    # ---- e2e: host buffers through the C ABI ----
+    # ---- e2e: host buffers through the C ABI (exact form; the tensor-core form beside it) ----
     qh = torch.empty((B, a.dim), dtype=torch.float32).pin_memory()
     qh.copy_(qdev.cpu())
     ih = torch.empty((B, a.topk), dtype=torch.int32).pin_memory()
@@ -565,7 +773,8 @@ def main():
         N.check(lib.saqg_search(index._h, qh.data_ptr(), B, a.topk, nprobe, C.byref(scfg), ih.data_ptr(),
                                 dh.data_ptr(), N.SAQG_MEM_HOST, sptr))
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    e2e_exact = world * B * a.steps / (world_max(sum(e2e_ms)) / 1e3)
+    e2e_v = world * B * a.steps / (world_max(sum(e2e_ms)) / 1e3)
+    e2e_same = bool(np.array_equal(ih.numpy().view(np.uint32), got))
     for _ in range(max(1, a.warmup)):
         N.check(lib.saqg_search_tc(index._h, qh.data_ptr(), B, a.topk, nprobe, a.tc_shortlist, C.byref(scfg),
                                    ih.data_ptr(), dh.data_ptr(), None, N.SAQG_MEM_HOST, sptr, None))
@@ -577,25 +786,12 @@ def main():
         N.check(lib.saqg_search_tc(index._h, qh.data_ptr(), B, a.topk, nprobe, a.tc_shortlist, C.byref(scfg),
                                    ih.data_ptr(), dh.data_ptr(), None, N.SAQG_MEM_HOST, sptr, None))
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    e2e_v = world * B * a.steps / (world_max(sum(e2e_ms)) / 1e3)
+    e2e_tc = world * B * a.steps / (world_max(sum(e2e_ms)) / 1e3)
 
     # ---- plain single-query drop-in ----
     P = a.plain_queries
     qp = wl.q[:P].contiguous()
-    lat = []
-    for i in range(min(8, P)):
-        N.check(lib.saqg_search(index._h, qp[i].data_ptr(), 1, a.topk, nprobe, C.byref(scfg), ids.data_ptr(),
-                                dd.data_ptr(), N.SAQG_MEM_DEVICE, sptr))
-    torch.cuda.synchronize()
-    for i in range(P):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        N.check(lib.saqg_search(index._h, qp[i].data_ptr(), 1, a.topk, nprobe, C.byref(scfg), ids.data_ptr(),
-                                dd.data_ptr(), N.SAQG_MEM_DEVICE, sptr))
-        e1.record(stream)
-        e1.synchronize()
-        lat.append(e0.elapsed_time(e1))
-    lat = np.array(lat)
+    lat, _ = plain_latencies(torch, lib, index, qp, a.topk, nprobe)
     plain_qps = P / (lat.sum() / 1e3)
 
     # ---- plain single query through a captured graph (query copied into the bound buffer) ----
@@ -689,13 +885,22 @@ def main():
     cpu = None
     if rank == 0:
         qnp = wl.q.cpu().numpy()
-        r, ns, dt, cids_cpu, _ = cpu_search_rate(ipath, qnp, a.topk, nprobe, a.cpu_seconds, threads)
+        r, ns, dt, cids_cpu, oi = cpu_search_rate(ipath, qnp, a.topk, nprobe, a.cpu_seconds, threads)
         same = bool(np.array_equal(cids_cpu[:min(ns, B)], got[:min(ns, B)]))
-        r1, ns1, dt1, _, _ = cpu_search_rate(ipath, qnp, a.topk, nprobe, min(2.0, a.cpu_seconds), 1)
+        r1, ns1, dt1, _, _ = cpu_search_rate(ipath, qnp, a.topk, nprobe, min(2.0, a.cpu_seconds), 1, oi)
+        del oi
         cpu = {"value": r, "unit": "queries/s", "cores": threads, "kind": "port",
                "sample": f"{ns} queries of the batch on the same index ({dt:.1f}s, {threads} threads)",
                "ids_equal_gpu": same,
                "single_thread": {"value": r1, "sample": f"{ns1} queries ({dt1:.1f}s, 1 thread)"}}
+
+    del index, wl
+    torch.cuda.empty_cache()
+    configs = {}
+    if rank == 0 and a.configs:
+        with tempfile.TemporaryDirectory() as td:
+            configs["c1"] = c1_leg(a, torch, log, td)
+            configs["c2"] = c2_leg(a, torch, log, td)
 
     precision = None
     if rank == 0 and a.precision_bits:
@@ -704,56 +909,60 @@ def main():
     clocks = clk.summary()
     line = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": a.steps,
-        "warmup": a.warmup, "ms_per_step": tc_tot_ms / a.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "bf16+f32", "data": "synthetic (seeded, generated on the GPU)",
+        "warmup": a.warmup, "ms_per_step": tot_ms / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic (seeded, generated on the GPU)",
         "config": config,
-        "batched": {"form": "tensor-core (saqg_search_tc)", "qps": value, "batch": B,
-                    "p50_ms": float(np.median(tc_step_ms)), "p99_ms": float(np.percentile(tc_step_ms, 99)),
-                    f"recall@{a.topk}": round(tc_recall, 4),
-                    f"recall@{a.topk}_vs_exact_search": round(overlap(it_, got, a.topk), 4),
-                    "shortlist": a.tc_shortlist,
-                    "stages_ms": {k: float(np.mean([x[k] for x in tc_stats]))
-                                  for k in ("ms_probe", "ms_pairs", "ms_contract", "ms_select", "ms_rerank")}},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "kernel": "scan phase (k_scan beside the split pass)",
+                     "peak_kind": peak_kind,
+                     "bytes_per_launch": compulsory, "effective_bytes_per_launch": effective,
+                     "effective_gbs": effective / (mean_scan / 1e3) / 1e9, "scan_ms": mean_scan,
+                     "reranked_per_query": float(np.mean(rr)) / B,
+                     "speculative_per_query": float(np.mean(spec)) / B,
+                     "probe_ms": float(np.mean(probe_ms)), "qprep_ms": float(np.mean(qprep_ms)),
+                     "split_pass_ms": float(np.mean(split_ms)),
+                     # what bounds the scan: one shared-memory LUT lookup per 4 coded dims per
+                     # (query, vector); peak one 32-lane lookup per SM per cycle
+                     "lut_lookups_per_s": lookups / (mean_scan / 1e3),
+                     "lut_lookup_peak_per_s": lookup_peak,
+                     "lut_lookup_frac": lookups / (mean_scan / 1e3) / lookup_peak},
+        "batched": {"form": "exact (saqg_search)", "qps": value, "batch": B,
+                    "p50_ms": float(np.median(step_ms)), "p99_ms": float(np.percentile(step_ms, 99)),
+                    f"recall@{a.topk}": round(batch_recall, 4)},
+        "batched_tc": {
+            "form": "tensor-core (saqg_search_tc): dense BF16 code contraction, shortlist "
+                    f"{a.tc_shortlist}, re-ranked with the exact search's distance; a stated-recall variant",
+            "qps": tc_value, "e2e_qps": e2e_tc, "p50_ms": float(np.median(tc_step_ms)),
+            "p99_ms": float(np.percentile(tc_step_ms, 99)), f"recall@{a.topk}": round(tc_recall, 4),
+            f"recall@{a.topk}_vs_exact_search": round(overlap(it_, got, a.topk), 4),
+            "stages_ms": {k: float(np.mean([x[k] for x in tc_stats]))
+                          for k in ("ms_probe", "ms_pairs", "ms_contract", "ms_select", "ms_rerank")},
+            "roofline": {"bound": "hbm", "achieved": tc_achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": tc_achieved / hbm, "traffic": tc_traffic, "peak_kind": peak_kind,
+                         "kernel": "k_tc_contract (tcgen05.mma BF16, TMA-fed, persistent)",
+                         "bytes_per_launch": tc_bytes,
+                         "bytes_note": "packed codes of each distinct probed cluster once + query rows + outputs",
+                         "bf16_operand_bytes": ts["code_bytes"], "contract_ms": contract_ms,
+                         "tiles": ts["tiles"], "tensor_tflops": ts["flops"] / (contract_ms / 1e3) / 1e12,
+                         "tensor_peak_tflops": bf16_peak()[0]}},
         "plain": {"qps": plain_qps, "queries": P, "p50_ms": float(np.median(lat)),
                   "p99_ms": float(np.percentile(lat, 99)),
                   "graph": {"qps": P / (glat.sum() / 1e3), "p50_ms": float(np.median(glat)),
                             "p99_ms": float(np.percentile(glat, 99)),
                             "note": "saqg_search_graph_launch of a captured single-query search"}},
         "batched_over_plain": value / world / plain_qps,
-        "p99_ms": float(np.percentile(tc_step_ms, 99)),
-        "roofline": {"bound": "hbm", "achieved": tc_achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": tc_achieved / hbm, "traffic": tc_traffic, "peak_kind": peak_kind,
-                     "kernel": "k_tc_contract (tcgen05.mma BF16, TMA-fed, persistent)",
-                     "bytes_per_launch": tc_bytes, "contract_ms": contract_ms,
-                     "code_bytes": ts["code_bytes"], "tiles": ts["tiles"],
-                     "tensor_tflops": ts["flops"] / (contract_ms / 1e3) / 1e12,
-                     "tensor_peak_tflops": bf16_peak()[0]},
-        "batched_exact": {
-            "form": "CUDA-core exact replay (saqg_search): every answer the reference's, bit for bit",
-            "qps": exact_value, "p50_ms": float(np.median(step_ms)), "p99_ms": float(np.percentile(step_ms, 99)),
-            f"recall@{a.topk}": round(batch_recall, 4), "e2e_qps": e2e_exact, "over_plain": exact_value / world / plain_qps,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": traffic, "kernel": "scan phase (k_scan beside the split pass)",
-                         "peak_kind": peak_kind,
-                         "bytes_per_launch": compulsory, "effective_bytes_per_launch": effective,
-                         "effective_gbs": effective / (mean_scan / 1e3) / 1e9, "scan_ms": mean_scan,
-                         "reranked_per_query": float(np.mean(rr)) / B,
-                         "speculative_per_query": float(np.mean(spec)) / B,
-                         "probe_ms": float(np.mean(probe_ms)), "qprep_ms": float(np.mean(qprep_ms)),
-                         "split_pass_ms": float(np.mean(split_ms)),
-                         # what bounds the scan: one shared-memory LUT lookup per 4 coded dims per
-                         # (query, vector); peak one 32-lane lookup per SM per cycle
-                         "lut_lookups_per_s": lookups / (mean_scan / 1e3),
-                         "lut_lookup_peak_per_s": lookup_peak,
-                         "lut_lookup_frac": lookups / (mean_scan / 1e3) / lookup_peak}},
+        "batched_tc_over_plain": tc_value / world / plain_qps,
+        "p99_ms": float(np.percentile(step_ms, 99)),
         "uneven_batch": mixed_line,
+        "c1": configs.get("c1"),
+        "c2": configs.get("c2"),
         "precision": precision,
         "serving": {"server": "continuous batching, 2 batches in flight, max batch %d" % B,
                     "nprobe": "U[16,256] per query", "k": "10 or 100 per query", "arrivals": "Poisson",
                     "rates": serving},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_v, "unit": "queries/s", "h2d_bytes_per_step": B * a.dim * 4,
-                "d2h_bytes_per_step": B * a.topk * 8},
+                "d2h_bytes_per_step": B * a.topk * 8, "ids_equal_device_run": e2e_same},
         "clocks": clocks,
         "gpu_launches": int(launches),
         "wall_s": time.time() - t_start,

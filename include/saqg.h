@@ -165,7 +165,11 @@ int saqg_search_ex(const saqg_index *index, const float *queries, int64_t nq, in
  * array's address (cudaGetSymbolAddress) and may make the driver load the
  * kernels: make it before any stream capture.  Every call on a device shares
  * the array, so calls that overlap on the GPU (other streams, other threads)
- * race: order them on one stream. */
+ * race: order them on one stream.  The array lives in the module of the search
+ * kernels: any process that runs a search kernel of this library on a device
+ * holds its 16 MiB there until exit, whether or not it calls this entry point
+ * (count it in device-memory budgets).  A host pointer, or one on another
+ * device, is rejected with SAQG_ERR_INVALID before any work. */
 #define SAQG_STATIC_SCRATCH_BYTES (16u << 20)
 int saqg_search_static(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
                        const saqg_searcher_config *cfg, uint32_t *ids, float *dists, void *stream);

@@ -68,7 +68,7 @@ def lib():
         l.orc_tc_approx.argtypes = [C.c_void_p, f32p, L, C.c_float, u32p, f64p, L]
         l.orc_build_index.restype = C.c_int
         l.orc_build_index.argtypes = [f32p, L, L, f32p, L, u32p, C.c_float, C.c_int, C.c_int, C.c_int, C.c_float,
-                                      C.c_int, C.c_void_p, C.c_void_p, C.c_char_p]
+                                      C.c_int, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int]
         _lib = l
     return _lib
 
@@ -145,8 +145,9 @@ def caq_encode(resid, bits, cent_unrot=None, rdlmt=6, eps=1e-8):
 
 
 def build_index(path, data, centroids, cids, avg_bits, enable_seg=True, eqseg=0, rotations=None, variance=None,
-                rdlmt=6, eps=1e-8):
-    """IVF::construct + IVF::save with the given rotations (concatenated per segment; None = no rotation)."""
+                rdlmt=6, eps=1e-8, threads=0):
+    """IVF::construct + IVF::save with the given rotations (concatenated per segment; None = no rotation).
+    threads <= 0: every host thread (the file is the same for any thread count)."""
     x = _f32(data)
     c = _f32(centroids)
     v = None if variance is None else _f32(variance)
@@ -154,7 +155,7 @@ def build_index(path, data, centroids, cids, avg_bits, enable_seg=True, eqseg=0,
     rc = lib().orc_build_index(x, x.shape[0], x.shape[1], c, c.shape[0], np.ascontiguousarray(cids, np.uint32),
                                avg_bits, int(enable_seg), eqseg, rdlmt, eps, int(r is not None),
                                None if v is None else v.ctypes.data, None if r is None else r.ctypes.data,
-                               path.encode())
+                               path.encode(), int(threads))
     if rc != 0:
         raise RuntimeError(f"oracle build failed ({rc})")
 

@@ -97,20 +97,45 @@ inline float eigen_var_q2(const float *var, const float *q, long n) {
     return eigen_redux_sum(n, [&](long i) { return var[i] * (q[i] * q[i]); });
 }
 
-// out = q (1 x D) * P (D x D, row-major)
-void gemv_rowvec(const float *q, const float *P, long D, float *out) {
+// out = Q * P for m row vectors Q (m x D) and P (D x D, row-major).  Per
+// output (r, i) the arithmetic is
+//   res = 0; for each block b of bc inputs: c = 0; c = fma(P[j][i], Q[r][j], c)
+//   for j ascending in b; res = fma(c, 1, res)
+// i.e. Eigen's GEMV order for each row.  The loops run input-row-major (all
+// outputs of all m rows advance together over one row of P, which is read once
+// per m vectors); every output still sees exactly the sequence above.  `out`
+// must not alias `Q`.
+void gemv_rows(const float *Q, long m, const float *P, long D, float *out) {
     const long bc = D < 128 ? D : 16;
-    for (long i = 0; i < D; ++i) {
-        float res = 0.0f;
-        for (long j2 = 0; j2 < D; j2 += bc) {
-            long je = std::min(j2 + bc, D);
-            float c = 0.0f;
-            for (long j = j2; j < je; ++j) c = std::fma(P[j * D + i], q[j], c);
-            res = std::fma(c, 1.0f, res);
+    constexpr long kW = 64;  // outputs held in registers across one block's inputs
+    for (long i = 0; i < m * D; ++i) out[i] = 0.0f;
+    for (long j2 = 0; j2 < D; j2 += bc) {
+        const long je = std::min(j2 + bc, D);
+        for (long r = 0; r < m; ++r) {
+            const float *q = Q + r * D;
+            float *o = out + r * D;
+            long i0 = 0;
+            for (; i0 + kW <= D; i0 += kW) {
+                float c[kW];
+                for (long t = 0; t < kW; ++t) c[t] = 0.0f;
+                for (long j = j2; j < je; ++j) {
+                    const float qj = q[j];
+                    const float *row = P + j * D + i0;
+                    for (long t = 0; t < kW; ++t) c[t] = std::fma(row[t], qj, c[t]);
+                }
+                for (long t = 0; t < kW; ++t) o[i0 + t] = std::fma(c[t], 1.0f, o[i0 + t]);
+            }
+            for (long i = i0; i < D; ++i) {
+                float c = 0.0f;
+                for (long j = j2; j < je; ++j) c = std::fma(P[j * D + i], q[j], c);
+                o[i] = std::fma(c, 1.0f, o[i]);
+            }
         }
-        out[i] = res;
     }
 }
+
+// out = q (1 x D) * P (D x D, row-major), Eigen's GEMV order (gemv_rows with m = 1).
+void gemv_rowvec(const float *q, const float *P, long D, float *out) { gemv_rows(q, 1, P, D, out); }
 
 // x86 minps semantics: (a < b) ? a : b
 inline float minps(float a, float b) { return a < b ? a : b; }
@@ -913,6 +938,23 @@ void colwise_mean_var(const float *x, long N, long D, std::vector<float> &var) {
 // vector and centroid uses the GEMV order above (the reference's GEMM order for
 // whole clusters depends on the host's cache-blocking sizes; its GEMV order is
 // what it uses for the centroid and for single-vector clusters).
+// fn(i) for i in [0, n) on `threads` threads, dynamically in chunks of 64.
+template <class F>
+void parallel_for(long n, int threads, F fn) {
+    if (threads <= 1 || n < 128) {
+        for (long i = 0; i < n; ++i) fn(i);
+        return;
+    }
+    std::atomic<long> next{0};
+    std::vector<std::thread> th;
+    for (int t = 0; t < threads; ++t)
+        th.emplace_back([&]() {
+            for (long a; (a = next.fetch_add(64)) < n;)
+                for (long i = a; i < std::min(n, a + 64); ++i) fn(i);
+        });
+    for (auto &t : th) t.join();
+}
+
 struct BuildCfg {
     float avg_bits;
     int seg, eqseg, rdlmt, rotate;
@@ -940,7 +982,7 @@ void put_cfg_bytes(const BuildCfg &c, uint8_t *q32, uint8_t *s20) {
 }
 
 int build_index(const float *data, long N, long D, const float *cent, long K, const uint32_t *cids, const BuildCfg &cfg,
-                const float *vars_in, const float *rots, const char *path) {
+                const float *vars_in, const float *rots, const char *path, int threads) {
     if (D % 64) return 1;
     std::vector<float> var;
     if (vars_in) var.assign(vars_in, vars_in + D);
@@ -983,61 +1025,108 @@ int build_index(const float *data, long N, long D, const float *cent, long K, co
     for (long s = 0; s < S; ++s) meta.segs.push_back(Seg{plan.segs[s].first, plan.segs[s].second, {}});
     std::memcpy(meta.qcfg, q32, 32);
     meta.derive();
+    // Vectors in file order (cluster by cluster), cluster starts in vectors and in 32-vector blocks.
+    std::vector<long> cstart(K + 1, 0), bstart(K + 1, 0), seg_off(S + 1, 0);
     for (long c = 0; c < K; ++c) {
-        const long n = (long)lists[c].size(), nb = (n + kFS - 1) / kFS;
-        std::vector<float> sfac(S > 1 ? 64 * S * nb : 0, 0.0f);
-        std::vector<uint8_t> scode(meta.block_bytes * nb, 0), lc(meta.long_stride * n, 0);
-        std::vector<float> lfac(2 * S * n, 0.0f);
-        std::vector<std::vector<float>> rc(S);
-        long off = 0;
+        cstart[c + 1] = cstart[c] + (long)lists[c].size();
+        bstart[c + 1] = bstart[c] + ((long)lists[c].size() + kFS - 1) / kFS;
+    }
+    for (long s = 0; s < S; ++s) seg_off[s + 1] = seg_off[s] + plan.segs[s].first;
+    std::vector<uint32_t> order(N), clu_of(N);
+    for (long c = 0; c < K; ++c)
+        for (long v = 0; v < (long)lists[c].size(); ++v) {
+            order[cstart[c] + v] = lists[c][v];
+            clu_of[cstart[c] + v] = (uint32_t)c;
+        }
+    // Per-segment centroid slices (zero-padded) and their rotations.
+    std::vector<std::vector<float>> cseg_all(K * S), rc_all(K * S);
+    parallel_for(K, threads, [&](long c) {
         for (long s = 0; s < S; ++s) {
-            const long d = plan.segs[s].first, bits = plan.segs[s].second;
-            std::vector<float> cseg(d, 0.0f), xs(d), xr(d), o(d);
-            for (long i = 0; i < d && off + i < D; ++i) cseg[i] = cent[c * D + off + i];
-            rc[s].resize(d);
-            if (cfg.rotate) gemv_rowvec(cseg.data(), rots + roff[s], d, rc[s].data());
-            else rc[s] = cseg;
-            std::vector<uint8_t> shortc(nb * kFS * (d / 8), 0);
-            CaqOut out;
-            for (long v = 0; v < n; ++v) {
-                const float *x = data + (size_t)lists[c][v] * D;
-                for (long i = 0; i < d; ++i) xs[i] = off + i < D ? x[off + i] : 0.0f;
-                if (cfg.rotate) gemv_rowvec(xs.data(), rots + roff[s], d, xr.data());
-                else xr = xs;
-                for (long i = 0; i < d; ++i) o[i] = xr[i] - rc[s][i];
-                caq_encode(o.data(), d, (int)bits, cseg.data(), cfg.rdlmt, cfg.eps, out);
-                const long b = v / kFS, j = v % kFS;
-                float *fac = S == 1 ? reinterpret_cast<float *>(scode.data() + b * meta.block_bytes)
-                                    : sfac.data() + (b * S + s) * 64;
-                fac[j] = out.o_l2norm;
+            const long d = plan.segs[s].first, off = seg_off[s];
+            std::vector<float> &cs = cseg_all[c * S + s], &rc = rc_all[c * S + s];
+            cs.assign(d, 0.0f);
+            for (long i = 0; i < d && off + i < D; ++i) cs[i] = cent[c * D + off + i];
+            rc.resize(d);
+            if (cfg.rotate) gemv_rowvec(cs.data(), rots + roff[s], d, rc.data());
+            else rc = cs;
+        }
+    });
+    // Every vector encoded independently: factors, 1-bit codes (MSB-first bytes,
+    // in block-padded slots) and ex-codes at their final places.
+    const long nslots = bstart[K] * kFS;
+    std::vector<float> onorm_all(N * S, 0.0f), ipco_all(N * S, 0.0f), lfac_all(2 * S * N, 0.0f);
+    std::vector<std::vector<uint8_t>> shortc(S);
+    for (long s = 0; s < S; ++s) shortc[s].assign(nslots * (plan.segs[s].first / 8), 0);
+    std::vector<uint8_t> lc_all((size_t)meta.long_stride * N, 0);
+    constexpr long kGroup = 8;  // vectors rotated together (one pass over P per group)
+    parallel_for((N + kGroup - 1) / kGroup, threads, [&](long grp) {
+        const long p0 = grp * kGroup, m = std::min(kGroup, N - p0);
+        thread_local std::vector<float> xs, xr, o;
+        thread_local std::vector<uint16_t> low;
+        thread_local CaqOut out;
+        for (long s = 0; s < S; ++s) {
+            const long d = plan.segs[s].first, bits = plan.segs[s].second, off = seg_off[s];
+            xs.assign((size_t)m * d, 0.0f);
+            xr.resize((size_t)m * d);
+            o.resize(d);
+            for (long r = 0; r < m; ++r) {
+                const float *x = data + (size_t)order[p0 + r] * D;
+                for (long i = 0; i < d && off + i < D; ++i) xs[r * d + i] = x[off + i];
+            }
+            if (cfg.rotate) gemv_rows(xs.data(), m, rots + roff[s], d, xr.data());
+            else xr = xs;
+            for (long r = 0; r < m; ++r) {
+                const long p = p0 + r, c = clu_of[p], v = p - cstart[c];
+                const std::vector<float> &rc = rc_all[c * S + s];
+                for (long i = 0; i < d; ++i) o[i] = xr[r * d + i] - rc[i];
+                caq_encode(o.data(), d, (int)bits, cseg_all[c * S + s].data(), cfg.rdlmt, cfg.eps, out);
+                onorm_all[p * S + s] = out.o_l2norm;
                 if (bits == 0) continue;
-                fac[kFS + j] = out.ip_cent_oa;
-                lfac[(v * S + s) * 2] = out.rescale;
-                lfac[(v * S + s) * 2 + 1] = out.error;
+                ipco_all[p * S + s] = out.ip_cent_oa;
+                lfac_all[(p * S + s) * 2] = out.rescale;
+                lfac_all[(p * S + s) * 2 + 1] = out.error;
                 const int sb = 1 << (bits - 1);
-                uint8_t *sc = &shortc[v * (d / 8)];
+                uint8_t *sc = &shortc[s][(size_t)(bstart[c] * kFS + v) * (d / 8)];
                 for (long i = 0; i < d; ++i)
                     if (out.code[i] & sb) sc[i / 8] |= (uint8_t)(0x80 >> (i % 8));
                 if (bits > 1) {
-                    std::vector<uint16_t> low(d);
+                    low.resize(d);
                     for (long i = 0; i < d; ++i) low[i] = (uint16_t)(out.code[i] & (sb - 1));
-                    uint8_t *dst = S == 1 ? lc.data() + v * meta.long_pv[0] : lc.data() + v * meta.long_stride + meta.long_off[s];
-                    pack_excode(low.data(), d, (int)bits - 1, dst);
+                    pack_excode(low.data(), d, (int)bits - 1,
+                                lc_all.data() + (size_t)p * meta.long_stride + meta.long_off[s]);
                 }
             }
-            if (bits)
-                for (long b = 0; b < nb; ++b) {
-                    uint8_t *blk = S == 1 ? scode.data() + b * meta.block_bytes + 256 : scode.data() + b * meta.block_bytes + meta.sc_off[s];
-                    pack_block(&shortc[b * kFS * (d / 8)], d, blk);
-                }
-            off += d;
+        }
+    });
+    // Clusters in order: factor blocks and FastScan-packed 1-bit blocks, then the
+    // per-vector arrays (IVF::save, ivf.hpp:197-233).
+    for (long c = 0; c < K; ++c) {
+        const long n = cstart[c + 1] - cstart[c], nb = bstart[c + 1] - bstart[c], p0 = cstart[c];
+        std::vector<float> sfac(S > 1 ? 64 * S * nb : 0, 0.0f);
+        std::vector<uint8_t> scode(meta.block_bytes * nb, 0);
+        for (long v = 0; v < n; ++v) {
+            const long b = v / kFS, j = v % kFS;
+            for (long s = 0; s < S; ++s) {
+                float *fac = S == 1 ? reinterpret_cast<float *>(scode.data() + b * meta.block_bytes)
+                                    : sfac.data() + (b * S + s) * 64;
+                fac[j] = onorm_all[(p0 + v) * S + s];
+                if (plan.segs[s].second) fac[kFS + j] = ipco_all[(p0 + v) * S + s];
+            }
+        }
+        for (long s = 0; s < S; ++s) {
+            const long d = plan.segs[s].first;
+            if (!plan.segs[s].second) continue;
+            for (long b = 0; b < nb; ++b) {
+                uint8_t *blk = S == 1 ? scode.data() + b * meta.block_bytes + 256 : scode.data() + b * meta.block_bytes + meta.sc_off[s];
+                pack_block(&shortc[s][(size_t)(bstart[c] + b) * kFS * (d / 8)], d, blk);
+            }
         }
         if (S > 1) w(sfac.data(), 4 * sfac.size());
         w(scode.data(), scode.size());
-        w(lc.data(), lc.size());
-        w(lfac.data(), 4 * lfac.size());
+        w(lc_all.data() + (size_t)p0 * meta.long_stride, (size_t)n * meta.long_stride);
+        w(lfac_all.data() + (size_t)p0 * 2 * S, 4 * (size_t)n * 2 * S);
         w(lists[c].data(), 4 * n);
-        for (long s = 0; s < S; ++s) w(rc[s].data(), 4 * rc[s].size());
+        for (long s = 0; s < S; ++s) w(rc_all[c * S + s].data(), 4 * rc_all[c * S + s].size());
     }
     std::fclose(f);
     return 0;
@@ -1250,11 +1339,13 @@ long orc_tc_approx(void *h, const float *q, long nprobe, float m, uint32_t *ids,
     return w;
 }
 
+// threads <= 0: every hardware thread.  The file does not depend on the thread count.
 int orc_build_index(const float *data, long N, long D, const float *cent, long K, const uint32_t *cids, float avg_bits,
                     int seg, int eqseg, int rdlmt, float eps, int rotate, const float *vars, const float *rots,
-                    const char *path) {
+                    const char *path, int threads) {
     BuildCfg c{avg_bits, seg, eqseg, rdlmt, rotate, eps};
-    return build_index(data, N, D, cent, K, cids, c, vars, rots, path);
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    return build_index(data, N, D, cent, K, cids, c, vars, rots, path, threads);
 }
 
 }  // extern "C"

@@ -2709,6 +2709,9 @@ int64_t run_estimate(const Index &I, const float *q_host, int64_t nprobe, float 
 // per device, placed by the driver when it loads this file's kernels), shared by
 // every call on that device.  Nothing in it needs to start at zero except the
 // 64-byte flag words, which each call clears on its stream before its kernels.
+// Because it belongs to this file's module, every process that runs any search
+// kernel of the library on a device holds these 16 MiB there until it exits,
+// whether or not it calls saqg_search_static.
 static __device__ __align__(256) unsigned char g_static_scratch[SAQG_STATIC_SCRATCH_BYTES];
 
 namespace {
@@ -2758,6 +2761,25 @@ void run_search_static(const Index &I, const float *q, int64_t nq, int64_t topk,
                      " clusters and nprobe " + std::to_string(nprobe) + " need " + std::to_string(need) +
                      " bytes of scratch, above the static maximum of " +
                      std::to_string((size_t)SAQG_STATIC_SCRATCH_BYTES) + " bytes; split the batch");
+    // The kernels would fault on a host pointer or one on another device; a
+    // wrong pointer is reported instead (this call takes device memory only).
+    auto require_device_ptr = [&](const void *p, const char *what) {
+        cudaPointerAttributes a{};
+        const cudaError_t e = cudaPointerGetAttributes(&a, p);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            throw Error{SAQG_ERR_INVALID, std::string("saqg_search_static: ") + what +
+                                              " is not a pointer the CUDA runtime knows: " + cudaGetErrorString(e)};
+        }
+        if (a.type == cudaMemoryTypeManaged) return;
+        if (a.type != cudaMemoryTypeDevice || a.device != I.device)
+            throw Error{SAQG_ERR_INVALID, std::string("saqg_search_static: ") + what +
+                                              " must be device memory on the index's device (" +
+                                              std::to_string(I.device) + ")"};
+    };
+    require_device_ptr(q, "queries");
+    require_device_ptr(ids, "ids");
+    if (dists) require_device_ptr(dists, "dists");
     const DevIndexView &ix = I.view;
     const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xstride_of(ix));
     SAQG_REQUIRE(smem <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");

@@ -12,6 +12,12 @@ the configuration's sizes and value distributions:
   PCA: mean-centred, components by descending eigenvalue (the reference's
       python/pca.py workflow), applied to base, queries and centroids.
 
+  gaussian_mixture_ivf (100k x 960, 1,024 clusters): centres ~ N(0,1)^d,
+      point = centre + N(0, sigma^2) per coordinate; PCA over the base set;
+      IVF centroids from k-means (Lloyd, 20 iterations).
+  aniso_ivf (1M x 1024, 4,096 clusters): unit-norm rows with per-axis
+      variance ~ i^-alpha in a random orthogonal basis; PCA; k-means.
+
 Queries follow the base distribution (their clusters drawn with the same
 Zipf weights).  Ground truth is exact: an FP32 shortlist followed by an FP64
 re-rank.
@@ -101,6 +107,127 @@ def zipf_aniso(n: int, d: int, k: int, nq: int, s: float = 1.1, alpha: float = 0
         sumsq += (x[a:b] * x[a:b]).sum(0, dtype=torch.float64)
     var = (sumsq / n - (colsum / n) ** 2).float().cpu().numpy()
     return Workload(f"zipf_aniso_{n}x{d}_k{k}", x, q.contiguous(), cent, labels, var, sizes)
+
+
+@torch.no_grad()
+def kmeans(x: torch.Tensor, k: int, iters: int, seed: int = 0, chunk: int = 1 << 18):
+    """Lloyd's k-means (L2) on the device, the role faiss plays in the reference's
+    python/ivf.py: seeded by k distinct points, `iters` updates (FP64 sums, empty
+    clusters keep their centre), then every point assigned to its nearest centre.
+    Returns (centroids k x d float32, cluster id per point int64)."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n, d = x.shape
+    g = torch.Generator(device=x.device)
+    g.manual_seed(seed)
+    cent = x[torch.randperm(n, generator=g, device=x.device)[:k]].clone()
+    assign = torch.empty(n, dtype=torch.int64, device=x.device)
+
+    def nearest():
+        cn = (cent * cent).sum(1)
+        for a in range(0, n, chunk):
+            b = min(n, a + chunk)
+            assign[a:b] = torch.argmin(cn[None, :] - 2.0 * x[a:b] @ cent.T, dim=1)
+    for _ in range(iters):
+        nearest()
+        sums = torch.zeros(k, d, dtype=torch.float64, device=x.device)
+        for a in range(0, n, chunk):
+            b = min(n, a + chunk)
+            sums.index_add_(0, assign[a:b], x[a:b].double())
+        cnt = torch.bincount(assign, minlength=k)
+        nz = cnt > 0
+        cent[nz] = (sums[nz] / cnt[nz, None]).float()
+    nearest()
+    return cent.contiguous(), assign
+
+
+def _pca(x: torch.Tensor, q: torch.Tensor, g: torch.Generator, chunk: int = 1 << 20):
+    """Mean-centred full-rank PCA (python/pca.py): covariance of (a sample of) the
+    base set, components by descending eigenvalue, applied in place to x and q."""
+    n = x.shape[0]
+    samp = x[torch.randperm(n, generator=g, device=x.device)[: min(n, 1 << 20)]]
+    mean = samp.mean(0)
+    xc = samp - mean
+    cov = (xc.T @ xc / samp.shape[0]).double().cpu().numpy()
+    evals, evecs = np.linalg.eigh(cov)
+    comp = torch.as_tensor(evecs[:, np.argsort(-evals, kind="stable")].T.astype(np.float32), device=x.device)
+    del samp, xc
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        x[a:b] = (x[a:b] - mean) @ comp.T
+    return (q - mean) @ comp.T
+
+
+def _column_variance(x: torch.Tensor, chunk: int = 1 << 20) -> np.ndarray:
+    n, d = x.shape
+    colsum = torch.zeros(d, device=x.device, dtype=torch.float64)
+    sumsq = torch.zeros(d, device=x.device, dtype=torch.float64)
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        colsum += x[a:b].sum(0, dtype=torch.float64)
+        sumsq += (x[a:b].double() ** 2).sum(0)
+    return (sumsq / n - (colsum / n) ** 2).float().cpu().numpy()
+
+
+@torch.no_grad()
+def gaussian_mixture_ivf(n: int = 100_000, d: int = 960, centers: int = 1024, sigma: float = 0.5, nq: int = 1000,
+                         k: int = 1024, iters: int = 20, seed: int = 0, device: str = "cuda") -> Workload:
+    """Gaussian mixture: centres ~ N(0,1)^d, point = centre + N(0, sigma^2) per
+    coordinate, queries from the same mixture; PCA over the base set; k-means
+    with k clusters for `iters` iterations gives the IVF centroids and ids."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    dev = torch.device(device)
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    ctr = torch.randn(centers, d, generator=g, device=dev)
+    lab = torch.randint(0, centers, (n,), generator=g, device=dev)
+    x = ctr[lab] + sigma * torch.randn(n, d, generator=g, device=dev)
+    ql = torch.randint(0, centers, (nq,), generator=g, device=dev)
+    q = ctr[ql] + sigma * torch.randn(nq, d, generator=g, device=dev)
+    q = _pca(x, q, g)
+    cent, cids = kmeans(x, k, iters, seed=seed + 1)
+    sizes = torch.bincount(cids, minlength=k).cpu().numpy()
+    return Workload(f"gmix_{n}x{d}_k{k}", x, q.contiguous(), cent, cids, _column_variance(x), sizes)
+
+
+@torch.no_grad()
+def aniso_ivf(n: int = 1_000_000, d: int = 1024, alpha: float = 0.8, nq: int = 10_000, k: int = 4096,
+              iters: int = 10, seed: int = 0, device: str = "cuda", chunk: int = 1 << 20) -> Workload:
+    """Unit-norm rows with per-axis variance ~ i^-alpha in a random orthogonal
+    basis (queries from the same distribution); PCA; k-means with k clusters."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    dev = torch.device(device)
+    rng = np.random.default_rng(seed)
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    q_, r_ = np.linalg.qr(rng.standard_normal((d, d)))
+    basis = torch.as_tensor((q_ * np.sign(np.diag(r_))[None, :]).astype(np.float32), device=dev)
+    scale = _spectrum(d, alpha, dev)
+
+    def draw(m):
+        out = torch.empty(m, d, device=dev)
+        for a in range(0, m, chunk):
+            b = min(m, a + chunk)
+            v = (torch.randn(b - a, d, generator=g, device=dev) * scale) @ basis.T
+            out[a:b] = v / v.norm(dim=1, keepdim=True)
+        return out
+    x = draw(n)
+    q = _pca(x, draw(nq), g)
+    cent, cids = kmeans(x, k, iters, seed=seed + 1)
+    sizes = torch.bincount(cids, minlength=k).cpu().numpy()
+    return Workload(f"aniso_{n}x{d}_k{k}", x, q.contiguous(), cent, cids, _column_variance(x), sizes)
+
+
+def rotations(plan, seed: int) -> np.ndarray:
+    """Random orthogonal matrices (numpy, seeded), one per segment of `plan`,
+    concatenated row-major: the rotations both builders are given, so that the
+    GPU builder and the CPU oracle write the same index."""
+    rng = np.random.default_rng(seed)
+    mats = []
+    for dim, _ in plan:
+        a = rng.standard_normal((dim, dim))
+        q_, r_ = np.linalg.qr(a)
+        mats.append((q_ * np.sign(np.diag(r_))[None, :]).astype(np.float32).reshape(-1))
+    return np.concatenate(mats)
 
 
 @torch.no_grad()

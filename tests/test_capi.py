@@ -58,7 +58,7 @@ def test_invalid_arguments_return_status(lib):
 
 
 def test_integration_adapter_compiles_and_links(tmp_path, lib):
-    """The C++ adapter that INTEGRATION.md shows a reference application (GpuIVF,
+    """The C++ adapter a reference application uses (include/saqg_ivf.hpp: GpuIVF,
     same member signature as IVF::search) compiles against include/saqg.h and
     links against the library, with a stand-in for the reference's row vector
     and searcher config (only .data() and searcher_vars_bound_m are used)."""
@@ -68,10 +68,9 @@ def test_integration_adapter_compiles_and_links(tmp_path, lib):
     gxx = shutil.which("g++")
     if not gxx:
         pytest.skip("no C++ compiler")
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    block = re.search(r"```cpp\n(.*?)```", text, flags=re.S).group(1)
     src = tmp_path / "adapter.cpp"
-    src.write_text("#include <stdexcept>\n#include <vector>\n" + block + """
+    src.write_text("""#include <vector>
+#include "saqg_ivf.hpp"
 struct RowVec { std::vector<float> v; const float *data() const { return v.data(); } };
 struct Cfg { float searcher_vars_bound_m = 4.0f; };
 int main(int argc, char **argv) {
@@ -80,11 +79,12 @@ int main(int argc, char **argv) {
     RowVec q{std::vector<float>(128, 0.0f)};
     uint32_t ids[10];
     ivf.search(q, 10, 4, Cfg{}, ids);
+    ivf.search_batch(q.data(), 1, 10, 4, Cfg{}, ids);
     return 0;
 }
 """)
     exe = tmp_path / "adapter"
-    r = subprocess.run([gxx, "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
-                        LIB, "-Wl,-rpath," + os.path.dirname(LIB)], capture_output=True, text=True)
+    r = subprocess.run([gxx, "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                        str(exe), LIB, "-Wl,-rpath," + os.path.dirname(LIB)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     assert subprocess.run([str(exe)]).returncode == 0

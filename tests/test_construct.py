@@ -162,3 +162,20 @@ def test_batched_scan_with_deferred_queries(defer, tmp_path, monkeypatch):
         oids, od = O.OracleIndex(opath).search(q, topk, nprobe, with_dists=True)
         assert np.array_equal(ids, oids)
         assert np.array_equal(d.view(np.uint32), od.view(np.uint32))
+
+
+@pytest.mark.parametrize("case", [(4.0, True, 0, 256), (1.5, True, 0, 192), (9.0, False, 0, 128)])
+def test_oracle_build_independent_of_threads(case, tmp_path):
+    """The oracle's builder encodes vectors on many threads; the file must be the
+    same for any thread count (every vector's arithmetic is independent)."""
+    bits, seg, eqseg, D = case
+    x, _ = data.anisotropic(2500, D, 0.8, seed=11)
+    cent, cids = data.kmeans(x, 9, iters=3, seed=4)
+    plan = O.plan(O.colwise_var(x), bits, seg, eqseg)
+    rots = _rotations(plan, 13)
+    files = []
+    for th in (1, 3, 8):
+        path = str(tmp_path / f"t{th}.index")
+        O.build_index(path, x, cent, cids, bits, seg, eqseg, rots, threads=th)
+        files.append(open(path, "rb").read())
+    assert files[0] == files[1] == files[2]
