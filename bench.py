@@ -446,6 +446,44 @@ def plain_latencies(torch, lib, index, q, topk, nprobe):
     return np.array(lat), ids.cpu().numpy().view(np.uint32)
 
 
+def plain_threads(torch, lib, index, qh, topk, nprobe, threads, seconds=1.0):
+    """The plain drop-in driven the way the reference's drivers drive IVF::search
+    (src/test_qps.cpp:77-84): `threads` host threads, each answering one query
+    per call on its own stream, with host buffers (the call copies the query in
+    and the result out).  Returns (queries/s over the wall clock, queries)."""
+    import ctypes as C
+    import threading
+    from saq_gb300 import _native as N, ivf
+    scfg = ivf.SearcherConfig().to_c()
+    streams = [torch.cuda.Stream() for _ in range(threads)]
+    qpin = torch.from_numpy(np.ascontiguousarray(qh)).pin_memory()
+    n_all = qpin.shape[0]
+    outs = [(torch.empty((1, topk), dtype=torch.int32).pin_memory(),
+             torch.empty((1, topk), dtype=torch.float32).pin_memory()) for _ in range(threads)]
+
+    def run(count):
+        done = [0] * threads
+
+        def worker(t):
+            sp = C.c_void_p(streams[t].cuda_stream)
+            ih, dh = outs[t]
+            for j in range(t, count, threads):
+                N.check(lib.saqg_search(index._h, qpin[j % n_all].data_ptr(), 1, topk, nprobe, C.byref(scfg),
+                                        ih.data_ptr(), dh.data_ptr(), N.SAQG_MEM_HOST, sp))
+                done[t] += 1
+        th = [threading.Thread(target=worker, args=(t,)) for t in range(threads)]
+        t0 = time.perf_counter()
+        for x in th:
+            x.start()
+        for x in th:
+            x.join()
+        return time.perf_counter() - t0, sum(done)
+    dt, n = run(threads * 4)  # warm-up: every thread's context and stream
+    count = max(threads * 8, int(n / max(dt, 1e-6) * seconds))
+    dt, n = run(count)
+    return n / dt, n
+
+
 def cpu_encode_rate(xh, cent, cids, var, bits, seg, rots, want, tmpdir):
     """The CPU oracle's builder (IVF::construct restated) on every host thread,
     on the first clusters holding at least `want` vectors: vectors/s."""
@@ -480,8 +518,10 @@ def single_query_config(a, torch, log, wl, name, variants, nprobes, nq_time, tmp
     cids = wl.cids.cpu().numpy().astype(np.uint32)
     out = {"workload": wl.name, "n": int(wl.x.shape[0]), "dim": int(wl.x.shape[1]),
            "clusters": int(cent.shape[0]), "k": 10, "queries_timed": nq_time,
-           "timing": "plain single-query saqg_search per call (CUDA events, synchronised per call); "
-                     "QPS = queries / sum of latencies", "variants": []}
+           "timing": "qps / p50 / p99: plain single-query saqg_search per call on one stream (CUDA events, "
+                     "synchronised per call), QPS = queries / sum of latencies; threads_qps: one query per call "
+                     "from as many host threads as the CPU baseline uses, each on its own stream, host buffers "
+                     "(src/test_qps.cpp's driver), over the wall clock", "variants": []}
     for bits, seg in variants:
         plan = ivf.plan(wl.variance, bits, seg)
         rots = workloads.rotations(plan, ROT_SEED)
@@ -506,14 +546,18 @@ def single_query_config(a, torch, log, wl, name, variants, nprobes, nq_time, tmp
         for npb in nprobes:
             lat, ids = plain_latencies(torch, index.lib, index, qd, 10, npb)
             r, ns, dt, cids_cpu, oi = cpu_search_rate(ipath, qh, 10, npb, a.cpu_seconds / 10, threads, oi)
+            tq, tn = plain_threads(torch, index.lib, index, qh, 10, npb, threads)
             pt = {"nprobe": npb, "qps": len(lat) / (lat.sum() / 1e3), "p50_ms": float(np.median(lat)),
                   "p99_ms": float(np.percentile(lat, 99)), "recall@10": round(workloads.recall_at(ids, gt, 10), 4),
+                  "threads_qps": tq, "threads": threads, "threads_over_cpu": None,
                   "cpu_baseline": {"value": r, "unit": "queries/s", "cores": threads, "kind": "port",
                                    "sample": f"{ns} single-query tasks in {dt:.2f}s"},
                   "ids_equal_cpu": bool(np.array_equal(cids_cpu[:ns], ids[:ns]))}
+            pt["threads_over_cpu"] = tq / r
             row["nprobe"].append(pt)
             log(f"{name} B={bits} seg={seg} nprobe={npb}: {pt['qps']:.0f} q/s p50 {pt['p50_ms']:.3f} ms "
-                f"p99 {pt['p99_ms']:.3f} ms recall {pt['recall@10']:.4f} cpu {r:.0f} q/s")
+                f"p99 {pt['p99_ms']:.3f} ms recall {pt['recall@10']:.4f}; {threads} threads {tq:.0f} q/s; "
+                f"cpu {r:.0f} q/s")
         r1, ns1, dt1, _, _ = cpu_search_rate(ipath, qh, 10, nprobes[0], 1.0, 1, oi)
         del oi
         row["cpu_single_thread"] = {"value": r1, "nprobe": nprobes[0], "sample": f"{ns1} queries in {dt1:.2f}s"}
@@ -793,6 +837,7 @@ def main():
     qp = wl.q[:P].contiguous()
     lat, _ = plain_latencies(torch, lib, index, qp, a.topk, nprobe)
     plain_qps = P / (lat.sum() / 1e3)
+    plain_thr_qps, plain_thr_n = plain_threads(torch, lib, index, wl.q[:B].cpu().numpy(), a.topk, nprobe, threads)
 
     # ---- plain single query through a captured graph (query copied into the bound buffer) ----
     gq = torch.empty((1, a.dim), dtype=torch.float32, device="cuda")
@@ -947,6 +992,9 @@ def main():
                          "tensor_peak_tflops": bf16_peak()[0]}},
         "plain": {"qps": plain_qps, "queries": P, "p50_ms": float(np.median(lat)),
                   "p99_ms": float(np.percentile(lat, 99)),
+                  "threads": {"qps": plain_thr_qps, "threads": threads, "queries": plain_thr_n,
+                              "note": "one query per saqg_search call from host threads on their own streams, "
+                                      "host buffers, wall clock (the reference drivers' thread pool)"},
                   "graph": {"qps": P / (glat.sum() / 1e3), "p50_ms": float(np.median(glat)),
                             "p99_ms": float(np.percentile(glat, 99)),
                             "note": "saqg_search_graph_launch of a captured single-query search"}},

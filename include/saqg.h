@@ -13,9 +13,13 @@
  * caller's buffers are used in place, nothing is copied).  `stream` is a
  * cudaStream_t passed as void* (NULL = the legacy default stream).
  *
- * Threading: an index handle is read-only after load/construct; concurrent
- * searches on one handle are serialised by a per-handle lock around its
- * device scratch arena.
+ * Threading: an index handle is read-only after load/construct.  Searches on
+ * one handle may be called from many host threads at once (as the reference's
+ * drivers call IVF::search from a thread pool): each call leases a scratch
+ * context from the handle's pool (the pool grows to the number of calls in
+ * flight), and calls on different streams overlap on the device.  A context
+ * reused from a call on another stream first makes the new stream wait for
+ * that call's end, so no two calls ever share scratch on the device.
  */
 #ifndef SAQG_H
 #define SAQG_H
@@ -299,6 +303,14 @@ int saqg_estimate(const saqg_index *index, const float *query_host, int64_t npro
  * plan for a padded dimension.  Writes up to `cap` (dim, bits) pairs. */
 int saqg_plan(const float *variance_host, int64_t dim_padded, float avg_bits, int enable_segmentation, int seg_eqseg,
               int64_t *dims, int64_t *bits, int cap, int *num_segments);
+
+/* The same plan computed on the GPU (SaqDataMaker::dynamic_programming,
+ * saq_data.hpp:147-227, one thread per DP state of a level, in the reference's
+ * visit order; the plan equals saqg_plan's).  `variance` is host or device
+ * memory per `mem`; runs on `stream` and returns when the plan is known.
+ * saqg_index_construct plans this way. */
+int saqg_plan_gpu(const float *variance, int64_t dim_padded, float avg_bits, int enable_segmentation, int seg_eqseg,
+                  int mem, void *stream, int64_t *dims, int64_t *bits, int cap, int *num_segments);
 
 /* CAQEncoder::encode_and_fac (quantization/caq/caq_encoder.hpp:172-247) for n
  * residual vectors of one segment: codes (n x dim int32) and factors

@@ -119,6 +119,8 @@ EXPORTS = {
                                 C.c_void_p, C.c_void_p, I64, C.POINTER(I64)]),
     "saqg_plan": (C.c_int, [C.c_void_p, I64, C.c_float, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                             C.POINTER(C.c_int)]),
+    "saqg_plan_gpu": (C.c_int, [C.c_void_p, I64, C.c_float, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "saqg_caq_encode": (C.c_int, [C.c_void_p, I64, I64, C.c_int, C.c_void_p, C.c_int, C.c_float, C.c_void_p,
                                   C.c_void_p, C.c_int, C.c_void_p]),
 }

@@ -304,6 +304,24 @@ int saqg_plan(const float *variance_host, int64_t dim_padded, float avg_bits, in
     });
 }
 
+int saqg_plan_gpu(const float *variance, int64_t dim_padded, float avg_bits, int enable_segmentation, int seg_eqseg,
+                  int mem, void *stream, int64_t *dims, int64_t *bits, int cap, int *num_segments) {
+    return guarded([&] {
+        SAQG_REQUIRE(num_segments && (cap == 0 || (dims && bits)), "null argument");
+        SAQG_REQUIRE(dim_padded > 0 && dim_padded % 64 == 0, "dim_padded must be a positive multiple of 64");
+        SAQG_REQUIRE(avg_bits >= 0 && avg_bits <= kMaxBits, "avg_bits out of range");
+        SAQG_REQUIRE(mem == SAQG_MEM_HOST || mem == SAQG_MEM_DEVICE, "mem must be SAQG_MEM_HOST or SAQG_MEM_DEVICE");
+        SAQG_REQUIRE(!enable_segmentation || seg_eqseg > 0 || variance, "variance required for the DP planner");
+        auto p = make_plan_gpu(variance, dim_padded, avg_bits, enable_segmentation != 0, seg_eqseg,
+                               mem == SAQG_MEM_DEVICE, (cudaStream_t)stream);
+        *num_segments = (int)p.size();
+        for (int i = 0; i < (int)p.size() && i < cap; ++i) {
+            dims[i] = p[i].first;
+            bits[i] = p[i].second;
+        }
+    });
+}
+
 int saqg_caq_encode(const float *resid, int64_t n, int64_t dim, int bits, const float *centroid, int rd_lmt, float eps,
                     int32_t *codes, float *factors, int mem, void *stream) {
     return guarded([&] {

@@ -533,16 +533,19 @@ Index *construct_index(const float *data, int64_t n, int64_t dim, const float *c
         ddata = data_buf->as<float>();
     }
     // variance
+    // variance and the segment plan (the planner runs on the device)
     I->var.resize(dim);
+    std::vector<std::pair<int64_t, int64_t>> plan;
     if (variance) {
         std::memcpy(I->var.data(), variance, 4 * dim);
+        plan = make_plan_gpu(variance, dim, cfg.avg_bits, cfg.enable_segmentation != 0, cfg.seg_eqseg, false, 0);
     } else {
         DevBuf dv(4 * dim);
         k_colwise_var<<<(unsigned)((dim + 127) / 128), 128>>>(ddata, n, (int)dim, dv.as<float>());
         launch_check("k_colwise_var");
+        plan = make_plan_gpu(dv.as<float>(), dim, cfg.avg_bits, cfg.enable_segmentation != 0, cfg.seg_eqseg, true, 0);
         SAQG_CUDA_TRY(cudaMemcpy(I->var.data(), dv.p, 4 * dim, cudaMemcpyDeviceToHost));
     }
-    auto plan = make_plan(I->var.data(), dim, cfg.avg_bits, cfg.enable_segmentation != 0, cfg.seg_eqseg);
     SAQG_REQUIRE(!plan.empty() && plan.size() <= (size_t)kMaxSeg, "planner produced an unsupported plan");
     int64_t roff = 0;
     for (auto &pr : plan) {

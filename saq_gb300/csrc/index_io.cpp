@@ -93,6 +93,7 @@ Index::~Index() {
     int cur = 0;
     cudaGetDevice(&cur);
     cudaSetDevice(device);
+    ctx_pool.clear();  // on this index's device
     for (void *p : allocations) cudaFree(p);
     if (cnorm2) cudaFree(cnorm2);
     if (tc_codes) cudaFree(tc_codes);
@@ -100,7 +101,44 @@ Index::~Index() {
     cudaSetDevice(cur);
 }
 
+CtxLease::CtxLease(const Index &I, cudaStream_t stream) : st(stream) {
+    {
+        std::lock_guard<std::mutex> lk(I.pool_mu);
+        for (int pass = 0; pass < 2 && !c; ++pass)  // an idle context last used on this stream, else any idle one
+            for (auto &p : I.ctx_pool)
+                if ((pass == 1 || p->last_stream == stream) && p->mu.try_lock()) {
+                    c = p.get();
+                    break;
+                }
+        if (!c) {
+            I.ctx_pool.push_back(std::make_unique<SearchCtx>());
+            c = I.ctx_pool.back().get();
+            c->mu.lock();
+        }
+    }
+    try {
+        if (!c->ev_done) SAQG_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming));
+        if (c->used && c->last_stream != stream) SAQG_CUDA_TRY(cudaStreamWaitEvent(stream, c->ev_done, 0));
+    } catch (...) {
+        c->mu.unlock();
+        throw;
+    }
+}
+
+CtxLease::~CtxLease() {
+    if (cudaEventRecord(c->ev_done, st) == cudaSuccess) {
+        c->last_stream = st;
+        c->used = true;
+    } else {  // the next call cannot order itself after this one: let it wait for the device
+        cudaGetLastError();
+        cudaDeviceSynchronize();
+        c->used = false;
+    }
+    c->mu.unlock();
+}
+
 SearchCtx::~SearchCtx() {
+    if (ev_done) cudaEventDestroy(ev_done);
     if (scratch) cudaFree(scratch);
     if (split_scratch) cudaFree(split_scratch);
     if (aux) cudaStreamDestroy(aux);

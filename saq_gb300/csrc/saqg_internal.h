@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -89,6 +90,11 @@ struct SearchCtx {
     void *blas = nullptr;
     void *blas_ws = nullptr;  // cuBLAS workspace owned by the context (graph capture needs one)
     size_t blas_ws_bytes = 0;
+    // pooled contexts: the stream of the last call and an event recorded at its
+    // end, so a call on another stream waits for that work before reusing the arenas
+    cudaStream_t last_stream = nullptr;
+    cudaEvent_t ev_done = nullptr;
+    bool used = false;
     SearchCtx() = default;
     SearchCtx(const SearchCtx &) = delete;
     SearchCtx &operator=(const SearchCtx &) = delete;
@@ -121,8 +127,10 @@ struct Index {
     std::vector<void *> allocations;
     int64_t device_bytes = 0;
     int device = 0;
-    // the search context of ordinary calls (serialised by its mutex)
-    mutable SearchCtx ctx;
+    // search contexts of ordinary calls: a pool that grows with the number of
+    // calls in flight at once (each call leases one, see CtxLease)
+    mutable std::mutex pool_mu;
+    mutable std::vector<std::unique_ptr<SearchCtx>> ctx_pool;
     // probe shortlist: squared centroid norms (built on first use, under init_mu)
     mutable std::mutex init_mu;
     mutable float *cnorm2 = nullptr;
@@ -146,6 +154,20 @@ void save_index_v2(const Index &idx, const std::string &path);
 // Host-only conversion between the reference format and v2 (either direction;
 // the source format is detected).
 void convert_index_file(const std::string &src, const std::string &dst, int format);
+
+// A search context leased from an index's pool for one call on `st`: an idle
+// context (one last used on `st` first), or a new one.  The context's arenas may
+// still be read by the previous call's kernels on another stream, so `st` first
+// waits for the event recorded at that call's end; the lease records it again on
+// release.  Concurrent calls on one index thus overlap on their own streams.
+struct CtxLease {
+    SearchCtx *c = nullptr;
+    cudaStream_t st = nullptr;
+    CtxLease(const Index &I, cudaStream_t stream);
+    ~CtxLease();
+    CtxLease(const CtxLease &) = delete;
+    CtxLease &operator=(const CtxLease &) = delete;
+};
 
 // search.cu
 void run_search(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,
@@ -202,8 +224,12 @@ Index *construct_index(const float *data, int64_t n, int64_t dim, const float *c
                        const uint32_t *cids, const saqg_quantize_config &cfg, const float *variance,
                        const float *rotations, uint64_t seed, int data_mem);
 
-// plan.cpp
+// plan.cpp (host) and plan_gpu.cu (device; the same plans)
 std::vector<std::pair<int64_t, int64_t>> make_plan(const float *var, int64_t dpad, float avg_bits, bool seg,
                                                    int eqseg);
+std::vector<std::pair<int64_t, int64_t>> make_plan_device(const float *dvar, int64_t dpad, float avg_bits,
+                                                          cudaStream_t st);
+std::vector<std::pair<int64_t, int64_t>> make_plan_gpu(const float *var, int64_t dpad, float avg_bits, bool seg,
+                                                       int eqseg, bool var_on_device, cudaStream_t st);
 
 }  // namespace saqg

@@ -22,6 +22,7 @@
 #include <climits>
 #include <cstdio>
 #include <cstdlib>
+#include <memory>
 #include <string>
 
 #include <cublas_v2.h>
@@ -2359,7 +2360,12 @@ size_t search_bytes_estimate(const Index &I, int64_t nq, int64_t topk, int64_t n
 void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,
                 float *dists, int mem, cudaStream_t st, saqg_search_stats *stats, uint32_t *probes_out,
                 const int *np_host, const int *k_host, SearchCtx *ctx) {
-    SearchCtx &C = ctx ? *ctx : I.ctx;
+    std::unique_ptr<CtxLease> lease;
+    if (!ctx) {
+        lease = std::make_unique<CtxLease>(I, st);  // locked; ordered after its previous call
+        ctx = lease->c;
+    }
+    SearchCtx &C = *ctx;
     // per-query nprobe / k (host arrays): the scalars become their maxima
     int64_t sum_np = nq * nprobe;
     if (np_host || k_host) {
@@ -2380,7 +2386,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
     SAQG_REQUIRE(nprobe >= 1 && nprobe <= I.K, "nprobe must be in [1, number of clusters]");
     if (nq == 0) return;
     const DevIndexView &ix = I.view;
-    std::lock_guard<std::mutex> lock(C.mu);
+    std::unique_lock<std::mutex> lock(C.mu, std::defer_lock);
+    if (!lease) lock.lock();  // a caller's own context (graph, serving slot)
     const bool host = mem == SAQG_MEM_HOST;
     Bump bp{(char *)C.scratch_get(search_scratch_bytes(I, nq, topk, nprobe, host))};
     QueryShape qsh;
@@ -2645,9 +2652,9 @@ int64_t run_estimate(const Index &I, const float *q_host, int64_t nprobe, float 
                      float *fast, float *vars, int64_t cap) {
     SAQG_REQUIRE(nprobe >= 1 && nprobe <= I.K, "nprobe must be in [1, number of clusters]");
     const DevIndexView &ix = I.view;
-    std::lock_guard<std::mutex> lock(I.ctx.mu);
     cudaStream_t st = 0;
-    Bump bp{(char *)I.ctx.scratch_get(search_scratch_bytes(I, 1, 1, nprobe, true))};
+    CtxLease lease(I, st);
+    Bump bp{(char *)lease.c->scratch_get(search_scratch_bytes(I, 1, 1, nprobe, true))};
     float *dq = bp.take<float>(I.D);
     float *dist = bp.take<float>(I.K);
     Cand *work = bp.take<Cand>(I.K);

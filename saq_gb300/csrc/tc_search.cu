@@ -880,8 +880,8 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     SAQG_REQUIRE(BN >= 16, "too many segments for the tensor-core search");
     ensure_tc_state(I, st);
 
-    SearchCtx &C = I.ctx;
-    std::lock_guard<std::mutex> lock(C.mu);
+    CtxLease lease(I, st);  // locked; ordered after its previous call
+    SearchCtx &C = *lease.c;
     const bool host = mem == SAQG_MEM_HOST;
     const int64_t P = nq * nprobe;  // probe slots (rows of nprobe); `pairs` of them are used
     // arena 1: sized by the call's shape

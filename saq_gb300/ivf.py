@@ -326,6 +326,24 @@ def plan(variance, avg_bits: float, enable_segmentation: bool = True, seg_eqseg:
     return [(int(dims[i]), int(bits[i])) for i in range(ns.value)]
 
 
+def plan_gpu(variance, avg_bits: float, enable_segmentation: bool = True, seg_eqseg: int = 0, stream=None):
+    """SaqDataMaker::analyze_plan with the dynamic program on the GPU (the same plan
+    as `plan`).  `variance` is a numpy array or a CUDA tensor."""
+    lib = N.load()
+    if _is_cuda_tensor(variance):
+        v = variance.contiguous().float()
+        ptr, mem, size = v.data_ptr(), N.SAQG_MEM_DEVICE, v.numel()
+    else:
+        v = np.ascontiguousarray(variance, np.float32).reshape(-1)
+        ptr, mem, size = v.ctypes.data, N.SAQG_MEM_HOST, v.size
+    dims = np.zeros(64, np.int64)
+    bits = np.zeros(64, np.int64)
+    ns = C.c_int()
+    N.check(lib.saqg_plan_gpu(ptr, size, avg_bits, int(enable_segmentation), seg_eqseg, mem, _stream_ptr(stream),
+                              dims.ctypes.data, bits.ctypes.data, 64, C.byref(ns)))
+    return [(int(dims[i]), int(bits[i])) for i in range(ns.value)]
+
+
 def caq_encode(resid, bits: int, centroid=None, rd_lmt: int = 6, eps: float = 1e-8):
     """CAQEncoder::encode_and_fac on the GPU for n residual vectors (host arrays)."""
     lib = N.load()

@@ -7,9 +7,10 @@
 
 For each: the GPU builder and the CPU oracle's builder are given the same data,
 centroids, ids, variance and rotations and must write byte-identical index
-files; then 200 queries are searched on the GPU (as one batch and one query per
-call, the plain drop-in) and by the oracle, and ids and distances must be equal
-bit for bit.  The oracle is pinned to the reference by the golden fixtures.
+files (a NaN factor's sign bit aside, see _same_index); then 200 queries
+are searched on the GPU (as one batch and one query per call, the plain
+drop-in) and by the oracle, and ids and distances must be equal bit for bit.
+The oracle is pinned to the reference by the golden fixtures.
 """
 import os
 
@@ -42,15 +43,41 @@ def _build_both(wl, bits, seg, tmp, tag):
     return index, gpath, opath
 
 
-def _same_file(a, b):
-    sa, sb = os.path.getsize(a), os.path.getsize(b)
-    assert sa == sb
-    with open(a, "rb") as fa, open(b, "rb") as fb:
-        while True:
-            x, y = fa.read(1 << 24), fb.read(1 << 24)
-            assert x == y
-            if not x:
-                break
+def _same_index(a, b):
+    """Byte-identical files, except that a NaN factor may differ in its sign bit.
+
+    A vector equal to its centroid (a one-vector cluster) has a zero residual;
+    the reference's error factor is then 0 * sqrt(0/0 - 1) (caq_encoder.hpp:
+    230-232), a NaN whose sign is the host's default NaN: negative on x86 (and on
+    the GPU), positive on Arm.  Such NaNs compare equal here; every other byte
+    must match."""
+    from saq_gb300 import index_format as F
+    if os.path.getsize(a) == os.path.getsize(b):
+        with open(a, "rb") as fa, open(b, "rb") as fb:
+            while True:
+                x, y = fa.read(1 << 24), fb.read(1 << 24)
+                if x != y:
+                    break
+                if not x:
+                    return
+    A, B = F.load(a), F.load(b)
+    assert A.N == B.N and A.D == B.D and A.K == B.K
+    assert A.centroids.tobytes() == B.centroids.tobytes()
+    assert A.variance.tobytes() == B.variance.tobytes()
+    assert A.quantize_cfg == B.quantize_cfg
+    for sa, sb in zip(A.segments, B.segments):
+        assert (sa.dim, sa.bits) == (sb.dim, sb.bits)
+        assert (sa.P is None and sb.P is None) or sa.P.tobytes() == sb.P.tobytes()
+    for ca, cb in zip(A.clusters, B.clusters):
+        assert ca.num_vec == cb.num_vec
+        for fld in ("ids", "short_factors", "short_code", "long_code"):
+            assert np.ascontiguousarray(getattr(ca, fld)).tobytes() == np.ascontiguousarray(getattr(cb, fld)).tobytes()
+        for x, y in zip(ca.centroids, cb.centroids):
+            assert x.tobytes() == y.tobytes()
+        fa, fb = ca.long_factors.view(np.uint32), cb.long_factors.view(np.uint32)
+        nan = np.isnan(ca.long_factors)
+        assert np.array_equal(nan, np.isnan(cb.long_factors))
+        assert np.array_equal(fa[~nan], fb[~nan])
 
 
 def _check_search(index, opath, q, nprobes, topk=10, single=True):
@@ -81,7 +108,7 @@ def test_c1_gaussian_mixture_100k_x_960(c1_workload, tmp_path):
     wl = c1_workload
     assert wl.x.shape == (100_000, 960)
     index, gpath, opath = _build_both(wl, 4.0, True, str(tmp_path), "c1")
-    _same_file(gpath, opath)
+    _same_index(gpath, opath)
     q = wl.q[:NQ].cpu().numpy()
     _check_search(index, opath, q, [32])
 
@@ -101,7 +128,7 @@ def test_c2_aniso_1m_x_1024(c2_workload, bits, seg, tmp_path):
     import torch
     wl = c2_workload
     index, gpath, opath = _build_both(wl, bits, seg, str(tmp_path), f"c2_{bits}_{int(seg)}")
-    _same_file(gpath, opath)
+    _same_index(gpath, opath)
     q = wl.q[:NQ].cpu().numpy()
     _check_search(index, opath, q, [16, 64, 128], single=(bits == 4.0 and seg))
     del index
