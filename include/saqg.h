@@ -248,6 +248,56 @@ int saqg_search_graph_create(const saqg_index *index, const float *queries, int6
 int saqg_search_graph_launch(saqg_search_graph *graph, void *stream);
 int saqg_search_graph_free(saqg_search_graph *graph);
 
+/* No counterpart in the reference.  Launch shapes of the batched search picked
+ * by timing (saqg_autotune) and graphs of either form with per-query nprobe /
+ * topk (saqg_search_graph_create_ex). */
+#define SAQG_FORM_EXACT 0 /* saqg_search: every answer the reference's */
+#define SAQG_FORM_TC 1    /* saqg_search_tc: the tensor-core form */
+
+typedef struct saqg_tune_report {
+    int form;            /* SAQG_FORM_EXACT or SAQG_FORM_TC */
+    int scan_mode;       /* exact: 0 CTA per query (+ split pass for the largest probes), 1 split pass, 2 warp per query; -1 built-in */
+    int defer_blocks;    /* exact, mode 0: blocks above which a query takes the split pass (-1 built-in) */
+    int first_blocks;    /* exact: blocks the split pass scans before speculating (-1 built-in) */
+    int pairs_per_chunk; /* tensor-core form: the MMA's N (-1 built-in) */
+    int candidates;      /* shapes timed (each one's answers checked equal to the built-in shapes') */
+    float default_ms;    /* one call with the built-in shapes (best of 3, CUDA events) */
+    float tuned_ms;      /* one call with the chosen shapes */
+} saqg_tune_report;
+
+/* Times every candidate launch shape of a call (`queries`: nq x dim, device
+ * memory, on `stream`) and keeps the fastest in the index: later calls whose
+ * batch size rounds up to the same power of two, with the same topk and nprobe,
+ * use it.  `shortlist` is read for SAQG_FORM_TC only.  Allocates and synchronises;
+ * call it outside any stream capture. */
+int saqg_autotune(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
+                  int64_t shortlist, int form, const saqg_searcher_config *cfg, void *stream,
+                  saqg_tune_report *report);
+
+typedef struct saqg_graph_config {
+    int form;                         /* SAQG_FORM_EXACT or SAQG_FORM_TC */
+    const int32_t *nprobe_per_query;  /* device, nq values, each clamped to [1, nprobe]; NULL: nprobe for all */
+    const int32_t *topk_per_query;    /* device, nq values, each clamped to [1, topk]; NULL: topk for all */
+    int64_t shortlist;                /* SAQG_FORM_TC: as saqg_search_tc's (>= topk) */
+    int64_t candidate_capacity;       /* SAQG_FORM_TC: approximate distances a launch may hold (0: twice the
+                                         creation batch's, at least 4096 per query) */
+    int autotune;                     /* 1: saqg_autotune this shape before the capture */
+} saqg_graph_config;
+
+/* saqg_search_graph_create for either form, with per-query nprobe / topk read
+ * from device arrays at every launch (rows of ids / dists are topk long, padded
+ * with id 0 / FLT_MAX past a query's own topk).  The tensor-core form is
+ * captured with a fixed candidate capacity and reads nothing back to the host;
+ * after a launch has completed, saqg_search_graph_status reports whether it
+ * fitted (SAQG_ERR_NOMEM: the batch needed more candidates, its results are
+ * void) or a contraction wait timed out (SAQG_ERR_INTERNAL).  `report` (may be
+ * NULL) receives the autotuner's choice. */
+int saqg_search_graph_create_ex(const saqg_index *index, const float *queries, int64_t nq, int64_t topk,
+                                int64_t nprobe, const saqg_searcher_config *cfg, const saqg_graph_config *gcfg,
+                                uint32_t *ids, float *dists, void *stream, saqg_search_graph **out,
+                                saqg_tune_report *report);
+int saqg_search_graph_status(saqg_search_graph *graph, void *stream);
+
 /* ---- serving ----------------------------------------------------------- */
 /* No counterpart in the reference (its drivers call IVF::search from a thread
  * pool): a serving loop with continuous batching on one index.  Submitted

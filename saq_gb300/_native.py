@@ -56,6 +56,24 @@ class TcStats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class TuneReport(C.Structure):
+    _fields_ = [("form", C.c_int), ("scan_mode", C.c_int), ("defer_blocks", C.c_int), ("first_blocks", C.c_int),
+                ("pairs_per_chunk", C.c_int), ("candidates", C.c_int), ("default_ms", C.c_float),
+                ("tuned_ms", C.c_float)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class GraphConfig(C.Structure):
+    _fields_ = [("form", C.c_int), ("nprobe_per_query", C.c_void_p), ("topk_per_query", C.c_void_p),
+                ("shortlist", I64), ("candidate_capacity", I64), ("autotune", C.c_int)]
+
+
+SAQG_FORM_EXACT = 0
+SAQG_FORM_TC = 1
+
+
 class SaqgError(RuntimeError):
     pass
 
@@ -119,6 +137,11 @@ EXPORTS = {
                                 C.c_void_p, C.c_void_p, I64, C.POINTER(I64)]),
     "saqg_plan": (C.c_int, [C.c_void_p, I64, C.c_float, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                             C.POINTER(C.c_int)]),
+    "saqg_autotune": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, I64, C.c_int, C.c_void_p, C.c_void_p,
+                                C.c_void_p]),
+    "saqg_search_graph_create_ex": (C.c_int, [C.c_void_p, C.c_void_p, I64, I64, I64, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "saqg_search_graph_status": (C.c_int, [C.c_void_p, C.c_void_p]),
     "saqg_plan_gpu": (C.c_int, [C.c_void_p, I64, C.c_float, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                 C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "saqg_caq_encode": (C.c_int, [C.c_void_p, I64, I64, C.c_int, C.c_void_p, C.c_int, C.c_float, C.c_void_p,

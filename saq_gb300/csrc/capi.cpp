@@ -208,8 +208,68 @@ int saqg_search_graph_create(const saqg_index *index, const float *queries, int6
         SAQG_REQUIRE(!cfg || cfg->dist_type == SAQG_DIST_L2, "only L2 search is supported");
         *out = nullptr;
         const float m = cfg ? cfg->searcher_vars_bound_m : 4.0f;
-        SearchGraph *g = graph_create(*index->impl, nq, topk, nprobe, m, queries, ids, dists, (cudaStream_t)stream);
+        SearchGraph *g = graph_create(*index->impl, nq, topk, nprobe, m, queries, ids, dists, (cudaStream_t)stream,
+                                      GraphCfg{});
         *out = new saqg_search_graph{g};
+    });
+}
+
+namespace {
+void fill_report(saqg_tune_report *r, int form, const TuneReport &t) {
+    if (!r) return;
+    r->form = form;
+    r->scan_mode = t.scan.mode;
+    r->defer_blocks = t.scan.defer_blocks;
+    r->first_blocks = t.scan.first_blocks;
+    r->pairs_per_chunk = t.tc.bn;
+    r->candidates = t.candidates;
+    r->default_ms = t.default_ms;
+    r->tuned_ms = t.tuned_ms;
+}
+}  // namespace
+
+int saqg_autotune(const saqg_index *index, const float *queries, int64_t nq, int64_t topk, int64_t nprobe,
+                  int64_t shortlist, int form, const saqg_searcher_config *cfg, void *stream,
+                  saqg_tune_report *report) {
+    return guarded([&] {
+        SAQG_REQUIRE(index && queries, "null argument");
+        SAQG_REQUIRE(form == SAQG_FORM_EXACT || form == SAQG_FORM_TC, "unknown search form");
+        SAQG_REQUIRE(!cfg || cfg->dist_type == SAQG_DIST_L2, "only L2 search is supported");
+        const float m = cfg ? cfg->searcher_vars_bound_m : 4.0f;
+        const TuneReport t =
+            form == SAQG_FORM_EXACT
+                ? autotune_exact(*index->impl, queries, nq, topk, nprobe, m, (cudaStream_t)stream)
+                : autotune_tc(*index->impl, queries, nq, topk, nprobe, shortlist, m, (cudaStream_t)stream);
+        fill_report(report, form, t);
+    });
+}
+
+int saqg_search_graph_create_ex(const saqg_index *index, const float *queries, int64_t nq, int64_t topk,
+                                int64_t nprobe, const saqg_searcher_config *cfg, const saqg_graph_config *gcfg,
+                                uint32_t *ids, float *dists, void *stream, saqg_search_graph **out,
+                                saqg_tune_report *report) {
+    return guarded([&] {
+        SAQG_REQUIRE(index && queries && ids && out && gcfg, "null argument");
+        SAQG_REQUIRE(!cfg || cfg->dist_type == SAQG_DIST_L2, "only L2 search is supported");
+        *out = nullptr;
+        const float m = cfg ? cfg->searcher_vars_bound_m : 4.0f;
+        GraphCfg gc;
+        gc.form = gcfg->form;
+        gc.np_dev = gcfg->nprobe_per_query;
+        gc.k_dev = gcfg->topk_per_query;
+        gc.shortlist = gcfg->shortlist;
+        gc.cand_cap = gcfg->candidate_capacity;
+        gc.autotune = gcfg->autotune;
+        SearchGraph *g = graph_create(*index->impl, nq, topk, nprobe, m, queries, ids, dists, (cudaStream_t)stream, gc);
+        fill_report(report, gc.form, graph_tune(g));
+        *out = new saqg_search_graph{g};
+    });
+}
+
+int saqg_search_graph_status(saqg_search_graph *graph, void *stream) {
+    return guarded([&] {
+        SAQG_REQUIRE(graph, "null argument");
+        graph_status(graph->impl, (cudaStream_t)stream);
     });
 }
 

@@ -120,7 +120,10 @@ __global__ void k_plan_answer(const double *__restrict__ fv, const uint32_t *__r
         }
     int ns = ans_ns, i = i_end, B = ans_b, n = 0;
     long long tmp[2 * 64];
-    while (i > 0 && n < 64 && ns > 0 && B >= 0) {  // a corrupt table ends the walk (out[0] = -1)
+    // (as the reference: with no segment possible the walk reads the table's
+    // untouched state and yields one 0-bit segment; a corrupt table ends the
+    // walk with out[0] = -1)
+    while (i > 0 && n < 64 && ns >= 0 && B >= 0) {
         const uint32_t s = fs[at(ns, i, B)];
         const int pi = (int)(s >> 4), bits = (int)(s & 0xf);
         if (pi >= i) break;

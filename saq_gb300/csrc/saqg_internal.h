@@ -3,7 +3,9 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <cstdint>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -107,6 +109,22 @@ struct SearchCtx {
     size_t held_bytes() const { return scratch_bytes + split_scratch_bytes; }
 };
 
+// Launch shapes of the exact batched search (values < 0: the built-in choice).
+// Every choice returns the same answers; the autotuner picks one per shape.
+struct ScanTune {
+    int mode = -1;          // 0: CTA per query, split pass for the largest probes; 1: split pass; 2: warp per query
+    int defer_blocks = -1;  // mode 0: a query probing more blocks than this takes the split pass
+    int first_blocks = -1;  // split pass: blocks scanned exactly before the speculation
+};
+// Launch shape of the tensor-core form: (query, cluster) pairs per MMA chunk
+// (the MMA's N; a multiple of 16).  The approximate distances do not depend on it.
+struct TcTune {
+    int bn = -1;
+};
+// Key of a tuned shape: (form, batch-size bucket (next power of two), topk, nprobe).
+using TuneKey = std::array<int64_t, 4>;
+int64_t tune_bucket(int64_t nq);
+
 struct Index {
     // metadata
     int64_t N = 0, D = 0, K = 0;
@@ -138,6 +156,10 @@ struct Index {
     mutable void *tc_codes = nullptr;
     mutable void *tc_tiles = nullptr;
     mutable int64_t tc_ntiles = 0;
+    // launch shapes chosen by the autotuner (saqg_autotune), by shape
+    mutable std::mutex tune_mu;
+    mutable std::map<TuneKey, ScanTune> scan_tunes;
+    mutable std::map<TuneKey, TcTune> tc_tunes;
     ~Index();
     void *dalloc(size_t bytes);
     void upload(void *dst, const void *src, size_t bytes);
@@ -169,11 +191,22 @@ struct CtxLease {
     CtxLease &operator=(const CtxLease &) = delete;
 };
 
+// Options of the exact search beyond the reference's arguments.
+struct SearchOpts {
+    const ScanTune *tune = nullptr;  // launch shapes (null: the index's tuned choice for the shape, else built-in)
+    const int *np_dev = nullptr;     // per-query nprobe / topk in device memory (graph launches), each
+    const int *k_dev = nullptr;      // clamped to [1, nprobe] / [1, topk]
+};
+
 // search.cu
 void run_search(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,
                 float *dists, int mem, cudaStream_t st, saqg_search_stats *stats = nullptr,
                 uint32_t *probes_out = nullptr, const int *np_host = nullptr, const int *k_host = nullptr,
-                SearchCtx *ctx = nullptr);
+                SearchCtx *ctx = nullptr, const SearchOpts *opts = nullptr);
+// Copies of per-query nprobe / topk (device arrays, may be null) clamped to
+// [1, np_max] / [1, k_max], into np_out / k_out (device, nq each).
+void clamp_shape(const int *np, const int *k, int64_t nq, int np_max, int k_max, int *np_out, int *k_out,
+                 cudaStream_t st);
 // Scratch bytes a batch of this shape needs (both arenas), for admission by memory.
 size_t search_bytes_estimate(const Index &idx, int64_t nq, int64_t topk, int64_t nprobe);
 // Grows a context's arenas (and creates its stream, events and BLAS handle)
@@ -195,17 +228,58 @@ void tc_rerank(const Index &idx, const uint32_t *probe, int64_t nq, int64_t npro
                const float *prune, const int *lp, const int *sl_pos, const float *sl_apx, const int *sl_cnt, int L,
                int64_t topk, const int *qk, int *grp, int *gj, int *ng, float *sl_dist, uint32_t *ids, float *dists,
                float *apx, cudaStream_t st);
+// Options of the tensor-core form beyond its arguments.
+struct TcOpts {
+    const TcTune *tune = nullptr;  // null: the index's tuned choice for the shape, else built-in
+    const int *np_dev = nullptr;   // per-query nprobe / topk in device memory, clamped as for the exact search
+    const int *k_dev = nullptr;
+    // > 0: capacity in approximate distances.  The call then never reads sizes
+    // back to the host (it can be captured in a graph); a batch needing more
+    // sets bit 2 of the error word and returns no candidates.
+    int64_t cand_cap = 0;
+    SearchCtx *ctx = nullptr;      // a caller's own context (graphs); null: one leased from the index
+    int **err_word = nullptr;      // receives the device address of the call's error word
+    int64_t *candidates = nullptr; // receives the call's candidate count (calls without cand_cap)
+};
 // tc_search.cu
 void run_search_tc(const Index &idx, const float *q, int64_t nq, int64_t topk, int64_t nprobe, int64_t shortlist,
                    float m, uint32_t *ids, float *dists, float *approx, int mem, cudaStream_t st,
-                   saqg_tc_stats *stats, const int *np_host = nullptr, const int *k_host = nullptr);
+                   saqg_tc_stats *stats, const int *np_host = nullptr, const int *k_host = nullptr,
+                   const TcOpts *opts = nullptr);
+// Device scratch bytes of a tensor-core call of this shape with a candidate capacity.
+void presize_tc_ctx(const Index &idx, SearchCtx &ctx, int64_t nq, int64_t topk, int64_t nprobe, int64_t shortlist,
+                    int64_t cand_cap);
+
+// autotune.cpp: time every candidate launch shape of this call on the device
+// (outputs checked equal to the built-in shapes'), keep the fastest in the index.
+struct TuneReport {
+    ScanTune scan;
+    TcTune tc;
+    int candidates = 0;
+    float default_ms = 0, tuned_ms = 0;
+};
+TuneReport autotune_exact(const Index &idx, const float *q_dev, int64_t nq, int64_t topk, int64_t nprobe, float m,
+                          cudaStream_t st);
+TuneReport autotune_tc(const Index &idx, const float *q_dev, int64_t nq, int64_t topk, int64_t nprobe,
+                       int64_t shortlist, float m, cudaStream_t st);
 
 // graph.cpp
+struct GraphCfg {
+    int form = SAQG_FORM_EXACT;
+    const int *np_dev = nullptr, *k_dev = nullptr;  // per-query arrays in device memory (bound)
+    int64_t shortlist = 0;                          // tensor-core form
+    int64_t cand_cap = 0;                           // tensor-core form (0: from the warm-up call)
+    int autotune = 0;
+};
 struct SearchGraph;
 SearchGraph *graph_create(const Index &idx, int64_t nq, int64_t topk, int64_t nprobe, float m, const float *q_dev,
-                          uint32_t *ids_dev, float *dists_dev, cudaStream_t st);
+                          uint32_t *ids_dev, float *dists_dev, cudaStream_t st, const GraphCfg &cfg);
 void graph_launch(SearchGraph *g, cudaStream_t st);
+int graph_status(SearchGraph *g, cudaStream_t st);
+const TuneReport &graph_tune(const SearchGraph *g);
 void graph_free(SearchGraph *g);
+// A context's BLAS handle with a workspace of its own (so captured calls allocate nothing).
+void ctx_blas_ready(SearchCtx &ctx);
 
 // serve.cpp
 struct Server;

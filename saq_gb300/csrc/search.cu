@@ -22,8 +22,10 @@
 #include <climits>
 #include <cstdio>
 #include <cstdlib>
+#include <map>
 #include <memory>
 #include <string>
+#include <tuple>
 
 #include <cublas_v2.h>
 
@@ -2258,15 +2260,43 @@ int64_t split_positions(const Index &I, int64_t want) {
 }
 
 // Which exact scan serves a call: the split scan for latency-bound calls (few
-// queries), one CTA per query for batches.  SAQG_SCAN_MODE=seq|split|warp forces one.
+// queries), one CTA per query for batches, unless the tuned shape says
+// otherwise.  SAQG_SCAN_MODE=seq|split|warp forces one (tests).
 // 0: one CTA per query, 1: split scan, 2: one warp per query.
-int scan_mode(int64_t nq, int64_t topk) {
+int scan_mode(int64_t nq, int64_t topk, const ScanTune &t) {
     const char *m = std::getenv("SAQG_SCAN_MODE");
     if (m && std::string(m) == "seq") return 0;
     if (m && std::string(m) == "split") return 1;
     if (m && std::string(m) == "warp") return topk <= 256 ? 2 : 0;
+    if (t.mode == 0 || t.mode == 1) return t.mode;
+    if (t.mode == 2) return topk <= 256 ? 2 : 0;
     if (nq <= 16) return 1;
     return 0;
+}
+
+// The deferral threshold of mode 0 (blocks of a query's probes above which it
+// takes the split pass; 0: never).
+int defer_threshold(const ScanTune &t) {
+    int defer = t.defer_blocks >= 0 ? t.defer_blocks : kDeferBlocks;
+    if (const char *e = std::getenv("SAQG_DEFER_BLOCKS")) defer = std::max(0, std::atoi(e));
+    return defer;
+}
+
+// Whether no query of a mode-0 call can be deferred: its nprobe largest
+// clusters hold no more blocks than the threshold.
+bool no_deferral(const Index &I, int64_t nprobe, const ScanTune &t) {
+    const int defer = defer_threshold(t);
+    return defer == 0 || I.max_blocks_of_probes(nprobe) <= defer;
+}
+
+// Per-query nprobe / k copies clamped to the call's maxima (graph launches read
+// caller-written device arrays; an out-of-range value must not index past a row).
+__global__ void k_clamp_shape(const int *__restrict__ np, const int *__restrict__ k, int nq, int np_max, int k_max,
+                              int *__restrict__ np_out, int *__restrict__ k_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    if (np) np_out[i] = min(max(np[i], 1), np_max);
+    if (k) k_out[i] = min(max(k[i], 1), k_max);
 }
 
 int xstride_of(const DevIndexView &) { return 0; }  // re-rank reads ex-codes in place (no staging buffer)
@@ -2275,6 +2305,55 @@ void check_launch(const char *what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) throw Error{SAQG_ERR_CUDA, std::string(what) + " launch failed: " + cudaGetErrorString(e)};
 }
+
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per (kernel, device)
+// and size: a call's host time matters for single queries.
+void ensure_smem(const void *fn, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, size_t> have;
+    int dev = 0;
+    SAQG_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    size_t &h = have[{fn, dev}];
+    if (bytes <= h) return;
+    SAQG_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    h = bytes;
+}
+
+// SMs x resident CTAs of a kernel (per device and shared-memory size), cached.
+int full_grid(const void *fn, int threads, size_t smem) {
+    static std::mutex mu;
+    static std::map<std::tuple<const void *, int, size_t>, int> have;
+    int dev = 0;
+    SAQG_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = have.find({fn, dev, smem});
+    if (it != have.end()) return it->second;
+    int sms = 0, per_sm = 0;
+    SAQG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SAQG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+    const int g = std::max(1, sms * std::max(1, per_sm));
+    have[{fn, dev, smem}] = g;
+    return g;
+}
+
+}  // namespace
+
+int64_t tune_bucket(int64_t nq) {
+    int64_t b = 1;
+    while (b < nq) b <<= 1;
+    return b;
+}
+
+void clamp_shape(const int *np, const int *k, int64_t nq, int np_max, int k_max, int *np_out, int *k_out,
+                 cudaStream_t st) {
+    if (nq <= 0 || (!np && !k)) return;
+    k_clamp_shape<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(np, k, (int)nq, np_max, k_max, np_out, k_out);
+    check_launch("k_clamp_shape");
+    count_launch(1);
+}
+
+namespace {
 
 void blas_try(cublasStatus_t e, const char *what) {
     if (e != CUBLAS_STATUS_SUCCESS) throw Error{SAQG_ERR_CUDA, std::string(what) + " failed (cuBLAS status " +
@@ -2317,7 +2396,7 @@ void probe_shortlist(const Index &I, SearchCtx &C, const float *q, int64_t nq, i
     sb.e2 = (float)((2.0 * (double)I.D + 32.0) * u);
     const size_t smem = 12 * (size_t)kShortCap + 4 * (size_t)I.D + (I.K <= kShortKeys ? 4 * (size_t)I.K : 0);
     SAQG_REQUIRE(smem <= 220 * 1024, "dimension too large for the probe shortlist's shared memory");
-    SAQG_CUDA_TRY(cudaFuncSetAttribute(k_probe_shortlist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ensure_smem((const void *)k_probe_shortlist, (size_t)smem);
     k_probe_shortlist<<<(unsigned)nq, kShortThreads, smem, st>>>(ix, q, dist, reinterpret_cast<const float2 *>(I.cnorm2),
                                                                  sb, (int)nprobe, qnp, probe, full,
                                                                  fb_list, flags + 2, cnt);
@@ -2338,6 +2417,10 @@ void presize_ctx(const Index &I, SearchCtx &C, int64_t nq, int64_t topk, int64_t
     C.aux_stream();
     C.fork_event();
     C.join_event();
+    ctx_blas_ready(C);
+}
+
+void ctx_blas_ready(SearchCtx &C) {
     if (!C.blas) {
         cublasHandle_t h = nullptr;
         blas_try(cublasCreate(&h), "cublasCreate");
@@ -2359,7 +2442,7 @@ size_t search_bytes_estimate(const Index &I, int64_t nq, int64_t topk, int64_t n
 
 void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, float m, uint32_t *ids,
                 float *dists, int mem, cudaStream_t st, saqg_search_stats *stats, uint32_t *probes_out,
-                const int *np_host, const int *k_host, SearchCtx *ctx) {
+                const int *np_host, const int *k_host, SearchCtx *ctx, const SearchOpts *opts) {
     std::unique_ptr<CtxLease> lease;
     if (!ctx) {
         lease = std::make_unique<CtxLease>(I, st);  // locked; ordered after its previous call
@@ -2403,6 +2486,22 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         SAQG_CUDA_TRY(cudaMemcpyAsync(d, k_host, 4 * (size_t)nq, cudaMemcpyHostToDevice, st));
         qsh.k = d;
     }
+    if (!np_host && !k_host && opts && (opts->np_dev || opts->k_dev)) {  // device arrays: clamped copies
+        int *dn = opts->np_dev ? bp.take<int>(nq) : nullptr;
+        int *dk = opts->k_dev ? bp.take<int>(nq) : nullptr;
+        clamp_shape(opts->np_dev, opts->k_dev, nq, (int)nprobe, (int)topk, dn, dk, st);
+        qsh.np = dn;
+        qsh.k = dk;
+    }
+    // launch shapes: the caller's, else the autotuner's choice for this shape, else built-in
+    ScanTune tune;
+    if (opts && opts->tune) {
+        tune = *opts->tune;
+    } else {
+        std::lock_guard<std::mutex> lk(I.tune_mu);
+        const auto it = I.scan_tunes.find(TuneKey{0, tune_bucket(nq), topk, nprobe});
+        if (it != I.scan_tunes.end()) tune = it->second;
+    }
     float *dq = bp.take<float>((size_t)nq * I.D);
     float *dist = bp.take<float>((size_t)nq * I.K);
     Cand *work = bp.take<Cand>((size_t)nq * I.K);
@@ -2444,7 +2543,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                             stats ? counters : nullptr, st);
         } else if (nq >= 8 && I.D % 32 == 0 && I.D <= 32 * kProbeRegs) {
             const size_t qsm = 4 * (size_t)kProbeQT * I.D;
-            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_probe_dist_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm));
+            ensure_smem((const void *)k_probe_dist_tiled, (size_t)qsm);
             const unsigned gx = (unsigned)std::min<int64_t>((I.K + kProbeWarps - 1) / kProbeWarps, 304);
             k_probe_dist_tiled<<<dim3(gx, (unsigned)((nq + kProbeQT - 1) / kProbeQT)), kProbeWarps * 32, qsm, st>>>(
                 ix, qin, (int)nq, dist);
@@ -2462,8 +2561,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         size_t qsm = 0;
         for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
         if (nq >= kQprepQT && kQprepQT * qsm <= 200 * 1024) {
-            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_qprep_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)(kQprepQT * qsm)));
+            ensure_smem((const void *)k_qprep_tiled, (size_t)(kQprepQT * qsm));
             k_qprep_tiled<<<dim3((unsigned)ix.S, (unsigned)((nq + kQprepQT - 1) / kQprepQT),
                                  (unsigned)((qsm / 4 + kQprepSlice - 1) / kQprepSlice)),
                             kQprepSlice, kQprepQT * qsm, st>>>(ix, qin, (int)nq, m, qrot, prune);
@@ -2483,14 +2581,25 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         uint32_t *ids_out = host ? oid : ids;
         float *d_out = host ? od : dists;
         unsigned long long *cnt = stats ? counters : nullptr;
-        const int mode = (qsh.np || qsh.k) && scan_mode(nq, topk) == 2 ? 0 : scan_mode(nq, topk);
+        const int mode0 = scan_mode(nq, topk, tune);
+        const int mode = (qsh.np || qsh.k) && mode0 == 2 ? 0 : mode0;
         if (mode == 2) {
             const size_t per_warp = align16(warp_smem_bytes(ix.Dtot, ix.S, (int)topk));
             const size_t wsm = per_warp * kWarpsPerCta;
-            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+            ensure_smem((const void *)k_scan_warp, (size_t)wsm);
             k_scan_warp<<<(unsigned)((nq + kWarpsPerCta - 1) / kWarpsPerCta), kWarpsPerCta * 32, wsm, st>>>(
                 ix, probe, (int)nprobe, (int)nq, qrot, prune, (int)topk, ids_out, d_out, cnt, per_warp);
             check_launch("k_scan_warp");
+            count_launch(4);
+        } else if (mode == 0 && no_deferral(I, nprobe, tune)) {
+            // no query of this call can probe more blocks than the deferral
+            // threshold: the CTA scan answers every query, no split pass
+            const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs, kScanOverlap);
+            SAQG_REQUIRE(smem_k <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
+            ensure_smem((const void *)k_scan, (size_t)smem_k);
+            k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, qsh, qrot, prune, ids_out, d_out, flags + 1,
+                                                                cnt, xs, nullptr);
+            check_launch("k_scan");
             count_launch(4);
         } else {
             // split-pass state: every query (mode 1), or the deferred giant-cluster queries (mode 0)
@@ -2522,7 +2631,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             ss.qsh = qsh;
             // heavy queries beside a batch: a longer prefix for a tighter bound; a
             // few queries alone: the speculative part has the GPU, so only the pool must fill
-            ss.first_blocks = mode == 0 ? kFirstBlocks : 1;
+            ss.first_blocks = tune.first_blocks > 0 ? tune.first_blocks : (mode == 0 ? kFirstBlocks : 1);
             ss.t_lo = 0;
             ss.t_hi = INT_MAX;
             ss.final_level = 1;
@@ -2531,10 +2640,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.summ, 0xff, 8 * (size_t)pos_cap, st));  // NaN: no record
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 16, st));
             int defer = -1;  // mode 1: every query
-            if (mode == 0) {
-                defer = kDeferBlocks;
-                if (const char *e = std::getenv("SAQG_DEFER_BLOCKS")) defer = std::max(0, std::atoi(e));
-            }
+            if (mode == 0) defer = defer_threshold(tune);
             k_defer<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(ix, probe, (int)nq, defer, ss, deferred);
             check_launch("k_defer");
             cudaStream_t sp = st;  // stream of the split pass
@@ -2548,7 +2654,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                 }
                 const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs, kScanOverlap);
                 SAQG_REQUIRE(smem_k <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
-                SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_k));
+                ensure_smem((const void *)k_scan, (size_t)smem_k);
                 k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, qsh, qrot, prune, ids_out, d_out,
                                                                     flags + 1, cnt, xs, deferred);
                 check_launch("k_scan");
@@ -2556,17 +2662,13 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
             const size_t smem_r = smem + 2 * 4 * (size_t)kReplayRecs * ss.rec_words;
             SAQG_REQUIRE(smem_r <= 220 * 1024, "dimension / topk too large for the replay kernel's shared memory");
-            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_first, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_spec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
-            SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
+            ensure_smem((const void *)k_scan_first, (size_t)smem);
+            ensure_smem((const void *)k_scan_spec, (size_t)smem1);
+            ensure_smem((const void *)k_scan_replay, (size_t)smem_r);
             k_scan_first<<<(unsigned)cap, kScanThreads, smem, sp>>>(ix, probe, qrot, prune, ss, flags + 1, cnt, xs);
             check_launch("k_scan_first");
             if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[5], sp));
-            int dev = 0, sms = 0, per_sm = 0;
-            SAQG_CUDA_TRY(cudaGetDevice(&dev));
-            SAQG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-            SAQG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scan_spec, kScanThreads, smem1));
-            const unsigned grid = (unsigned)std::max(1, sms * std::max(1, per_sm));
+            const unsigned grid = (unsigned)full_grid((const void *)k_scan_spec, kScanThreads, smem1);
             // levels of speculation (tiles after the split point): each level's
             // replay leaves the exact pool, whose distk bounds the next level
             const int nlev = mode == 0 ? (int)(sizeof(kSpecLevels) / sizeof(kSpecLevels[0])) : 1;
@@ -2692,7 +2794,7 @@ int64_t run_estimate(const Index &I, const float *q_host, int64_t nprobe, float 
         SAQG_CUDA_TRY(cudaMemcpy(doff, off.data(), 8 * (nprobe + 1), cudaMemcpyHostToDevice));
         const int xs = xstride_of(ix);
         const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
-        SAQG_CUDA_TRY(cudaFuncSetAttribute(k_estimate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        ensure_smem((const void *)k_estimate, (size_t)smem);
         k_estimate<<<(unsigned)nprobe, kScanThreads, smem, st>>>(ix, probe, doff, qrot, prune, oids, oacc, ofast, ovars,
                                                                  xs);
         check_launch("k_estimate");
@@ -2809,7 +2911,7 @@ void run_search_static(const Index &I, const float *q, int64_t nq, int64_t topk,
     SAQG_CUDA_TRY(cudaMemsetAsync(flags, 0, 64, st));
     if (nq >= 8 && I.D % 32 == 0 && I.D <= 32 * kProbeRegs) {
         const size_t qsm = 4 * (size_t)kProbeQT * I.D;
-        SAQG_CUDA_TRY(cudaFuncSetAttribute(k_probe_dist_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm));
+        ensure_smem((const void *)k_probe_dist_tiled, (size_t)qsm);
         const unsigned gx = (unsigned)std::min<int64_t>((I.K + kProbeWarps - 1) / kProbeWarps, 304);
         k_probe_dist_tiled<<<dim3(gx, (unsigned)((nq + kProbeQT - 1) / kProbeQT)), kProbeWarps * 32, qsm, st>>>(
             ix, q, (int)nq, dist);
@@ -2827,7 +2929,7 @@ void run_search_static(const Index &I, const float *q, int64_t nq, int64_t topk,
     check_launch("k_qprep");
     const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xstride_of(ix), kScanOverlap);
     SAQG_REQUIRE(smem_k <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
-    SAQG_CUDA_TRY(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_k));
+    ensure_smem((const void *)k_scan, (size_t)smem_k);
     QueryShape qsh;
     qsh.np_max = (int)nprobe;
     qsh.k_max = (int)topk;
@@ -3028,8 +3130,7 @@ void tc_rank_rotate(const Index &I, SearchCtx &C, const float *q, int64_t nq, in
     size_t qsm = 0;
     for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
     if (nq >= kQprepQT && kQprepQT * qsm <= 200 * 1024) {
-        SAQG_CUDA_TRY(cudaFuncSetAttribute(k_qprep_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)(kQprepQT * qsm)));
+        ensure_smem((const void *)k_qprep_tiled, (size_t)(kQprepQT * qsm));
         k_qprep_tiled<<<dim3((unsigned)ix.S, (unsigned)((nq + kQprepQT - 1) / kQprepQT),
                              (unsigned)((qsm / 4 + kQprepSlice - 1) / kQprepSlice)),
                         kQprepSlice, kQprepQT * qsm, st>>>(ix, q, (int)nq, m, qrot, prune);
@@ -3055,7 +3156,7 @@ void tc_rerank(const Index &I, const uint32_t *probe, int64_t nq, int64_t nprobe
     check_launch("k_tc_groups");
     const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, 1, 0);
     SAQG_REQUIRE(smem <= 200 * 1024, "dimension too large for the re-rank kernel's shared memory");
-    SAQG_CUDA_TRY(cudaFuncSetAttribute(k_tc_rerank, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ensure_smem((const void *)k_tc_rerank, (size_t)smem);
     k_tc_rerank<<<dim3((unsigned)L, (unsigned)nq), kScanThreads, smem, st>>>(ix, probe, (int)nprobe, qrot, prune, lp,
                                                                              sl_pos, sl_cnt, grp, gj, ng, L, sl_dist);
     check_launch("k_tc_rerank");

@@ -41,6 +41,7 @@
 #include <cfloat>
 #include <climits>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -357,9 +358,9 @@ __global__ void __launch_bounds__(256) k_tc_sort(const int *__restrict__ bcnt, c
 __global__ void k_tc_gather(DevIndexView ix, const uint32_t *__restrict__ probe, const int *__restrict__ sorted,
                             int P, int nprobe, const float *__restrict__ qrot, const long long *__restrict__ qbase,
                             const int *__restrict__ lp, __nv_bfloat16 *__restrict__ Bq, float2 *__restrict__ pscal,
-                            long long *__restrict__ cbase) {
+                            long long *__restrict__ cbase, const long long *__restrict__ ptot) {
     const int b = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (b >= P) return;
+    if (b >= P || (ptot && b >= *ptot)) return;  // ptot: the pairs actually bucketed (P an upper bound)
     const int p = sorted[b], qi = p / nprobe, j = p - qi * nprobe;
     const int c = (int)probe[p];
     if (lane == 0) cbase[b] = qbase[qi] + lp[(size_t)qi * (nprobe + 1) + j];
@@ -405,6 +406,7 @@ struct TcWork {
     const float2 *pscal;        // [P][S] residual sum / squared norm per segment
     float *cand;                // approximate distances
     int BN;                     // pairs per chunk (multiple of 16)
+    long long cand_cap;         // approximate distances the cand array holds
     int *err;
 };
 
@@ -591,7 +593,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_contract(const __grid_cons
                     if (vrow) {
 #pragma unroll
                         for (int i = 0; i < 16; ++i)
-                            if (n0 + i < nh) w.cand[w.cbase[rb + n0 + i] + rl] = d[i];
+                            if (n0 + i < nh) {
+                                const long long at = w.cbase[rb + n0 + i] + rl;
+                                if (at < w.cand_cap) w.cand[at] = d[i];
+                            }
                     }
                 }
                 tc_fence_before();
@@ -693,6 +698,7 @@ __global__ void __launch_bounds__(256) k_tc_select1(const float *__restrict__ ca
                                                     int nq, int L, int *__restrict__ spos, float *__restrict__ sval) {
     __shared__ float xs[kTcSelChunk];
     const long long k = blockIdx.x;
+    if (k >= qchunk[nq]) return;  // a grid sized by a capacity (graph launches)
     int lo = 0, hi = nq - 1;  // query owning chunk k: last with qchunk <= k
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -749,6 +755,20 @@ __global__ void __launch_bounds__(256) k_tc_select2(const long long *__restrict_
                         po[slot] = pi[e];
                         ao[slot] = vi[e];
                     });
+}
+
+// Calls without a host round trip (graph launches): when the batch needs more
+// approximate distances than `cap` or more selection chunks than `chunk_cap`,
+// record it (bit 2 of the error word) and empty every bucket and candidate
+// count, so that no later kernel reads or writes past the arrays.
+__global__ void k_tc_guard(const long long *__restrict__ qbase, const long long *__restrict__ qchunk, int nq, int K,
+                           long long cap, long long chunk_cap, int *__restrict__ bcnt, int *__restrict__ qtot,
+                           int *__restrict__ err) {
+    if (qbase[nq] <= cap && qchunk[nq] <= chunk_cap) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    if (i == 0) atomicOr(err, 2);
+    for (int c = i; c < K; c += stride) bcnt[c] = 0;
+    for (int q = i; q < nq; q += stride) qtot[q] = 0;
 }
 
 __global__ void k_tc_chunks(const int *__restrict__ qtot, int nq, int *__restrict__ nch) {
@@ -847,44 +867,21 @@ CUtensorMap bf16_rows_map(void *base, int64_t cols, int64_t rows, int box_rows) 
 
 }  // namespace
 
-void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, int64_t L, float m,
-                   uint32_t *ids, float *dists, float *approx, int mem, cudaStream_t st, saqg_tc_stats *stats,
-                   const int *np_host, const int *k_host) {
-    const DevIndexView &ix = I.view;
-    // per-query nprobe / k (host arrays): the scalars become their maxima
-    int64_t pairs = nq * nprobe;
-    if (np_host || k_host) {
-        int64_t npm = 0, km = 0;
-        pairs = 0;
-        for (int64_t i = 0; i < nq; ++i) {
-            const int a = np_host ? np_host[i] : (int)nprobe, b = k_host ? k_host[i] : (int)topk;
-            SAQG_REQUIRE(a >= 1 && a <= I.K, "every nprobe must be in [1, number of clusters]");
-            SAQG_REQUIRE(b >= 1 && b <= kTcMaxShort, "every topk must be in [1, 1024]");
-            npm = std::max<int64_t>(npm, a);
-            km = std::max<int64_t>(km, b);
-            pairs += a;
-        }
-        if (np_host) nprobe = npm;
-        if (k_host) topk = km;
-    }
-    SAQG_REQUIRE(nq >= 0 && nq <= kTcMaxBatch, "the tensor-core search takes at most 8192 queries per call");
-    SAQG_REQUIRE(topk >= 1 && topk <= kTcMaxShort, "topk must be in [1, 1024]");
-    SAQG_REQUIRE(L >= topk && L <= kTcMaxShort, "shortlist must be in [topk, 1024]");
-    SAQG_REQUIRE(nprobe >= 1 && nprobe <= I.K, "nprobe must be in [1, number of clusters]");
-    for (int s = 0; s < ix.S; ++s)
-        SAQG_REQUIRE(ix.seg[s].bits >= 1 && ix.seg[s].dim % kTcBK == 0,
-                     "the tensor-core search needs every segment coded (bits >= 1) and 64-dim aligned");
-    SAQG_REQUIRE(I.N < (int64_t)1 << 31 && nq * nprobe < (int64_t)1 << 31, "index or batch too large");
-    if (nq == 0) return;
-    const int BN = std::min(kTcMaxN, (kTcCols / ix.S) / 16 * 16);
-    SAQG_REQUIRE(BN >= 16, "too many segments for the tensor-core search");
-    ensure_tc_state(I, st);
+namespace {
 
-    CtxLease lease(I, st);  // locked; ordered after its previous call
-    SearchCtx &C = *lease.c;
-    const bool host = mem == SAQG_MEM_HOST;
-    const int64_t P = nq * nprobe;  // probe slots (rows of nprobe); `pairs` of them are used
-    // arena 1: sized by the call's shape
+// Pairs per MMA chunk: the tuned value when given (a multiple of 16), at most
+// what two accumulators of S segments fit in TMEM.
+int tc_bn(const DevIndexView &ix, int tuned) {
+    const int cap = std::min(kTcMaxN, (kTcCols / ix.S) / 16 * 16);
+    if (tuned >= 16) return std::min(cap, tuned / 16 * 16);
+    return cap;
+}
+
+// Scratch layout of one call: arena 1 by the call's shape, arena 2 by its
+// candidates (the exact count, or a capacity for calls without a host round trip).
+size_t tc_arena1_bytes(const Index &I, int64_t nq, int64_t topk, int64_t nprobe, int64_t L) {
+    const DevIndexView &ix = I.view;
+    const int64_t P = nq * nprobe;
     size_t need = 0;
     auto add = [&](size_t b) { need += a16(b); };
     add(4 * (size_t)nq * I.D);                  // queries
@@ -907,7 +904,83 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     add(4 * (size_t)nq * topk * 3);             // outputs (host io)
     add(16);                                    // error word
     add(4 * (size_t)nq * 2);                    // per-query nprobe / k
-    char *base = static_cast<char *>(C.scratch_get(need + 256));
+    return need + 256;
+}
+
+size_t tc_arena2_bytes(const DevIndexView &ix, int64_t total, int64_t pairs, int64_t nchunks, int64_t L) {
+    return a16(4 * (size_t)std::max<int64_t>(total, 1)) + a16(2 * (size_t)pairs * ix.Dtot) +
+           a16(8 * (size_t)pairs * ix.S) + a16(8 * (size_t)pairs) +
+           a16(8 * (size_t)std::max<int64_t>(nchunks, 1) * L) + 256;
+}
+
+}  // namespace
+
+void presize_tc_ctx(const Index &I, SearchCtx &C, int64_t nq, int64_t topk, int64_t nprobe, int64_t L,
+                    int64_t cand_cap) {
+    std::lock_guard<std::mutex> lock(C.mu);
+    C.scratch_get(tc_arena1_bytes(I, nq, topk, nprobe, L));
+    C.split_scratch_get(tc_arena2_bytes(I.view, cand_cap, nq * nprobe, cand_cap / kTcSelChunk + nq, L));
+    ctx_blas_ready(C);
+}
+
+void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, int64_t L, float m,
+                   uint32_t *ids, float *dists, float *approx, int mem, cudaStream_t st, saqg_tc_stats *stats,
+                   const int *np_host, const int *k_host, const TcOpts *opts) {
+    const DevIndexView &ix = I.view;
+    const TcOpts none;
+    const TcOpts &o = opts ? *opts : none;
+    const bool dev_shape = !np_host && !k_host && (o.np_dev || o.k_dev);
+    // per-query nprobe / k (host arrays): the scalars become their maxima
+    int64_t pairs = nq * nprobe;
+    if (np_host || k_host) {
+        int64_t npm = 0, km = 0;
+        pairs = 0;
+        for (int64_t i = 0; i < nq; ++i) {
+            const int a = np_host ? np_host[i] : (int)nprobe, b = k_host ? k_host[i] : (int)topk;
+            SAQG_REQUIRE(a >= 1 && a <= I.K, "every nprobe must be in [1, number of clusters]");
+            SAQG_REQUIRE(b >= 1 && b <= kTcMaxShort, "every topk must be in [1, 1024]");
+            npm = std::max<int64_t>(npm, a);
+            km = std::max<int64_t>(km, b);
+            pairs += a;
+        }
+        if (np_host) nprobe = npm;
+        if (k_host) topk = km;
+    }
+    SAQG_REQUIRE(nq >= 0 && nq <= kTcMaxBatch, "the tensor-core search takes at most 8192 queries per call");
+    SAQG_REQUIRE(topk >= 1 && topk <= kTcMaxShort, "topk must be in [1, 1024]");
+    SAQG_REQUIRE(L >= topk && L <= kTcMaxShort, "shortlist must be in [topk, 1024]");
+    SAQG_REQUIRE(nprobe >= 1 && nprobe <= I.K, "nprobe must be in [1, number of clusters]");
+    SAQG_REQUIRE(o.cand_cap >= 0 && o.cand_cap < ((int64_t)1 << 40), "candidate capacity out of range");
+    for (int s = 0; s < ix.S; ++s)
+        SAQG_REQUIRE(ix.seg[s].bits >= 1 && ix.seg[s].dim % kTcBK == 0,
+                     "the tensor-core search needs every segment coded (bits >= 1) and 64-dim aligned");
+    SAQG_REQUIRE(I.N < (int64_t)1 << 31 && nq * nprobe < (int64_t)1 << 31, "index or batch too large");
+    if (nq == 0) return;
+    TcTune tune;
+    if (o.tune) {
+        tune = *o.tune;
+    } else {
+        std::lock_guard<std::mutex> lk(I.tune_mu);
+        const auto it = I.tc_tunes.find(TuneKey{1, tune_bucket(nq), topk, nprobe});
+        if (it != I.tc_tunes.end()) tune = it->second;
+    }
+    const int BN = tc_bn(ix, tune.bn);
+    SAQG_REQUIRE(BN >= 16, "too many segments for the tensor-core search");
+    ensure_tc_state(I, st);
+
+    std::unique_ptr<CtxLease> lease;
+    SearchCtx *ctxp = o.ctx;
+    if (!ctxp) {
+        lease = std::make_unique<CtxLease>(I, st);  // locked; ordered after its previous call
+        ctxp = lease->c;
+    }
+    SearchCtx &C = *ctxp;
+    std::unique_lock<std::mutex> lock(C.mu, std::defer_lock);
+    if (!lease) lock.lock();  // the caller's own context (graph)
+    const bool host = mem == SAQG_MEM_HOST;
+    const bool capped = o.cand_cap > 0;  // no host round trip
+    const int64_t P = nq * nprobe;  // probe slots (rows of nprobe); `pairs` of them are used
+    char *base = static_cast<char *>(C.scratch_get(tc_arena1_bytes(I, nq, topk, nprobe, L)));
     size_t off = 0;
     auto take = [&](size_t b) {
         char *p = base + off;
@@ -944,6 +1017,7 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     float *od = reinterpret_cast<float *>(oid + nq * topk);
     float *oa = od + nq * topk;
     int *err = reinterpret_cast<int *>(take(16));
+    if (o.err_word) *o.err_word = err;
     int *qnp = nullptr, *qk = nullptr;
     {
         int *pk = reinterpret_cast<int *>(take(4 * (size_t)nq * 2));
@@ -954,6 +1028,11 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
         if (k_host) {
             qk = pk + nq;
             SAQG_CUDA_TRY(cudaMemcpyAsync(qk, k_host, 4 * (size_t)nq, cudaMemcpyHostToDevice, st));
+        }
+        if (dev_shape) {
+            qnp = o.np_dev ? pk : nullptr;
+            qk = o.k_dev ? pk + nq : nullptr;
+            clamp_shape(o.np_dev, o.k_dev, nq, (int)nprobe, (int)topk, qnp, qk, st);
         }
     }
 
@@ -996,15 +1075,25 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     launch_check("k_tc_fill");
     k_tc_sort<<<(unsigned)I.K, 256, 0, st>>>(bcnt, boff, bucket, sorted);
     launch_check("k_tc_sort");
-    long long totals[2] = {0, 0};
-    SAQG_CUDA_TRY(cudaMemcpyAsync(&totals[0], qbase + nq, 8, cudaMemcpyDeviceToHost, st));
-    SAQG_CUDA_TRY(cudaMemcpyAsync(&totals[1], qchunk + nq, 8, cudaMemcpyDeviceToHost, st));
-    SAQG_CUDA_TRY(cudaStreamSynchronize(st));
-    const long long total = totals[0], nchunks = totals[1];
+    long long total = 0, nchunks = 0;
+    if (capped) {  // sized by the capacity; a batch beyond it is emptied and reported
+        total = o.cand_cap;
+        nchunks = o.cand_cap / kTcSelChunk + nq;
+        pairs = P;
+        k_tc_guard<<<64, 256, 0, st>>>(qbase, qchunk, (int)nq, (int)I.K, total, nchunks, bcnt, qtot, err);
+        launch_check("k_tc_guard");
+    } else {
+        long long totals[2] = {0, 0};
+        SAQG_CUDA_TRY(cudaMemcpyAsync(&totals[0], qbase + nq, 8, cudaMemcpyDeviceToHost, st));
+        SAQG_CUDA_TRY(cudaMemcpyAsync(&totals[1], qchunk + nq, 8, cudaMemcpyDeviceToHost, st));
+        SAQG_CUDA_TRY(cudaStreamSynchronize(st));
+        total = totals[0];
+        nchunks = totals[1];
+        if (dev_shape) pairs = P;
+        if (o.candidates) *o.candidates = total;
+    }
     // arena 2: sized by the candidates
-    size_t need2 = a16(4 * (size_t)std::max<long long>(total, 1)) + a16(2 * (size_t)pairs * ix.Dtot) +
-                   a16(8 * (size_t)pairs * ix.S) + a16(8 * (size_t)pairs) + a16(8 * (size_t)std::max<long long>(nchunks, 1) * L);
-    char *base2 = static_cast<char *>(C.split_scratch_get(need2 + 256));
+    char *base2 = static_cast<char *>(C.split_scratch_get(tc_arena2_bytes(ix, total, pairs, nchunks, L)));
     size_t off2 = 0;
     auto take2 = [&](size_t b) {
         char *p = base2 + off2;
@@ -1018,7 +1107,9 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     int *spos = reinterpret_cast<int *>(take2(8 * (size_t)std::max<long long>(nchunks, 1) * L));
     float *sval = reinterpret_cast<float *>(spos + std::max<long long>(nchunks, 1) * L);
     k_tc_gather<<<(unsigned)((pairs * 32 + 255) / 256), 256, 0, st>>>(ix, probe, sorted, (int)pairs, (int)nprobe, qrot,
-                                                                     qbase, lp, Bq, pscal, cbase);
+                                                                     qbase, lp, Bq, pscal, cbase,
+                                                                     pairs == P && (capped || dev_shape) ? boff + I.K
+                                                                                                          : nullptr);
     launch_check("k_tc_gather");
     mark(2);
     // contraction: persistent, one CTA per SM
@@ -1033,6 +1124,7 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     wk.pscal = pscal;
     wk.cand = cand;
     wk.BN = BN;
+    wk.cand_cap = std::max<long long>(total, 1);
     wk.err = err;
     const size_t smem = tc_contract_smem();
     SAQG_CUDA_TRY(cudaFuncSetAttribute(k_tc_contract, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1051,16 +1143,19 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     tc_rerank(I, probe, nq, nprobe, qrot, prune, lp, sl_pos, sl_apx, sl_cnt, (int)L, topk, qk, grp, gj, ng, sl_dist,
               host ? oid : ids, host ? od : dists, host ? oa : approx, st);
     mark(5);
-    count_launch(11);
-    int herr = 0;
-    SAQG_CUDA_TRY(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+    count_launch(capped ? 12 : 11);
     if (host) {
         SAQG_CUDA_TRY(cudaMemcpyAsync(ids, oid, 4 * (size_t)nq * topk, cudaMemcpyDeviceToHost, st));
         if (dists) SAQG_CUDA_TRY(cudaMemcpyAsync(dists, od, 4 * (size_t)nq * topk, cudaMemcpyDeviceToHost, st));
         if (approx) SAQG_CUDA_TRY(cudaMemcpyAsync(approx, oa, 4 * (size_t)nq * topk, cudaMemcpyDeviceToHost, st));
     }
+    if (capped && !host && !stats) return;  // the caller reads the error word (graph status)
+    int herr = 0;
+    SAQG_CUDA_TRY(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
     SAQG_CUDA_TRY(cudaStreamSynchronize(st));
-    if (herr) throw Error{SAQG_ERR_INTERNAL, "tensor-core contraction: a pipeline wait timed out"};
+    if (herr & 1) throw Error{SAQG_ERR_INTERNAL, "tensor-core contraction: a pipeline wait timed out"};
+    if (herr & 2) throw Error{SAQG_ERR_NOMEM, "tensor-core search: the batch needs more approximate distances than "
+                                               "the candidate capacity"};
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         float t[5] = {0, 0, 0, 0, 0};
@@ -1072,18 +1167,21 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
         stats->ms_rerank = t[4];
         std::vector<int> hc((size_t)I.K);
         SAQG_CUDA_TRY(cudaMemcpy(hc.data(), bcnt, 4 * (size_t)I.K, cudaMemcpyDeviceToHost));
-        int64_t flops = 0, bytes = 0, tiles = 0, padded = 0;
+        int64_t flops = 0, bytes = 0, tiles = 0, padded = 0, npairs = 0;
         for (int64_t c = 0; c < I.K; ++c) {
             if (!hc[c]) continue;
             const int64_t nt = (I.sizes[c] + kTcBM - 1) / kTcBM;
             flops += 2 * (int64_t)ix.Dtot * hc[c] * I.sizes[c];
             bytes += 2 * (int64_t)ix.Dtot * I.sizes[c];
             tiles += nt;
+            npairs += hc[c];
             const int64_t nch = (hc[c] + BN - 1) / BN, npad = (nch - 1) * BN + (((hc[c] - (nch - 1) * BN) + 15) & ~15);
             padded += 2 * (int64_t)ix.Dtot * kTcBM * nt * npad;
         }
-        stats->pairs = pairs;
-        stats->candidates = total;
+        long long tot = total;
+        if (capped) SAQG_CUDA_TRY(cudaMemcpy(&tot, qbase + nq, 8, cudaMemcpyDeviceToHost));
+        stats->pairs = npairs;
+        stats->candidates = tot;
         stats->tiles = tiles;
         stats->flops = flops;
         stats->mma_flops = padded;
