@@ -691,6 +691,15 @@ def main():
         N.check(lib.saqg_search_tc(index._h, qdev.data_ptr(), B, a.topk, nprobe, a.tc_shortlist, C.byref(scfg),
                                    ids_t.data_ptr(), d_t.data_ptr(), None, N.SAQG_MEM_DEVICE, sptr,
                                    C.byref(tst) if with_stats else None))
+    # autotuner: time every candidate launch shape of this batch once; later
+    # calls of the shape (the timed ones) use the fastest
+    tune = {}
+    for form, name in ((N.SAQG_FORM_EXACT, "exact"), (N.SAQG_FORM_TC, "tensor_core")):
+        rep = N.TuneReport()
+        N.check(lib.saqg_autotune(index._h, qdev.data_ptr(), B, a.topk, nprobe, a.tc_shortlist, form, C.byref(scfg),
+                                  sptr, C.byref(rep)))
+        tune[name] = rep.as_dict()
+        log(f"autotune {name}: default {rep.default_ms:.3f} ms, tuned {rep.tuned_ms:.3f} ms ({rep.candidates} shapes)")
     for _ in range(a.warmup):
         batched(True)
     for _ in range(a.warmup):
@@ -973,7 +982,10 @@ def main():
                      "lut_lookup_frac": lookups / (mean_scan / 1e3) / lookup_peak},
         "batched": {"form": "exact (saqg_search)", "qps": value, "batch": B,
                     "p50_ms": float(np.median(step_ms)), "p99_ms": float(np.percentile(step_ms, 99)),
-                    f"recall@{a.topk}": round(batch_recall, 4)},
+                    f"recall@{a.topk}": round(batch_recall, 4),
+                    "autotune": {"note": "saqg_autotune on this batch before the timed steps (best of 3 per "
+                                         "shape, answers checked equal); the timed calls use the chosen shapes",
+                                 **tune}},
         "batched_tc": {
             "form": "tensor-core (saqg_search_tc): dense BF16 code contraction, shortlist "
                     f"{a.tc_shortlist}, re-ranked with the exact search's distance; a stated-recall variant",

@@ -62,7 +62,7 @@ def build(verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, headers, verbose), srcs))
     if _stale(LIB, objs):
-        cmd = [NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-lcublas", "-lpthread",
+        cmd = [NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-lpthread",
                "-Xlinker", "-rpath", "-Xlinker", os.path.join(os.path.dirname(os.path.dirname(NVCC)), "lib64")]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

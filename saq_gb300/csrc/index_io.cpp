@@ -17,8 +17,6 @@
 #include <functional>
 #include <memory>
 
-#include <cublas_v2.h>
-
 #include "saqg_internal.h"
 
 namespace saqg {
@@ -144,8 +142,6 @@ SearchCtx::~SearchCtx() {
     if (aux) cudaStreamDestroy(aux);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
-    if (blas) cublasDestroy(static_cast<cublasHandle_t>(blas));
-    if (blas_ws) cudaFree(blas_ws);
 }
 
 void *Index::dalloc(size_t bytes) {

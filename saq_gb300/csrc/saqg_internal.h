@@ -78,8 +78,8 @@ struct DevIndexView {  // passed to kernels by value
     SegDev seg[kMaxSeg];
 };
 
-// What one in-flight search owns: scratch arenas, the auxiliary stream of the
-// split pass with its fork / join events, and a BLAS handle.  Searches on
+// What one in-flight search owns: scratch arenas and the auxiliary stream of
+// the split pass with its fork / join events.  Searches on
 // different contexts may run concurrently on different streams.
 struct SearchCtx {
     std::mutex mu;
@@ -89,9 +89,6 @@ struct SearchCtx {
     size_t split_scratch_bytes = 0;
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    void *blas = nullptr;
-    void *blas_ws = nullptr;  // cuBLAS workspace owned by the context (graph capture needs one)
-    size_t blas_ws_bytes = 0;
     // pooled contexts: the stream of the last call and an event recorded at its
     // end, so a call on another stream waits for that work before reusing the arenas
     cudaStream_t last_stream = nullptr;
@@ -278,8 +275,10 @@ void graph_launch(SearchGraph *g, cudaStream_t st);
 int graph_status(SearchGraph *g, cudaStream_t st);
 const TuneReport &graph_tune(const SearchGraph *g);
 void graph_free(SearchGraph *g);
-// A context's BLAS handle with a workspace of its own (so captured calls allocate nothing).
-void ctx_blas_ready(SearchCtx &ctx);
+// probe_gemm.cu: ip (row-major nq x K) = Q C^T with TF32 tensor-core products and
+// FP32 accumulation; *err is set (device) if a pipeline wait timed out.
+void probe_ip_gemm(const float *q, int64_t nq, const float *cent, int64_t K, int64_t D, float *ip, int *err,
+                   cudaStream_t st);
 
 // serve.cpp
 struct Server;

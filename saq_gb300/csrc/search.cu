@@ -27,8 +27,6 @@
 #include <string>
 #include <tuple>
 
-#include <cublas_v2.h>
-
 #include "device_common.cuh"
 #include "saqg_internal.h"
 
@@ -426,7 +424,8 @@ __global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView 
                                                                    uint32_t *__restrict__ probe,
                                                                    uint8_t *__restrict__ full, int *__restrict__ fb_list,
                                                                    int *__restrict__ fb_count,
-                                                                   unsigned long long *__restrict__ counters) {
+                                                                   unsigned long long *__restrict__ counters,
+                                                                   const int *__restrict__ ip_err) {
     extern __shared__ __align__(16) char smem_raw[];
     unsigned long long *keys = reinterpret_cast<unsigned long long *>(smem_raw);  // [kShortCap]
     uint32_t *cand = reinterpret_cast<uint32_t *>(keys + kShortCap);             // [kShortCap]
@@ -493,6 +492,7 @@ __global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView 
         __syncthreads();
     }
     const float T = key_to_float(s_prefix);
+    if (*ip_err) s_bad = 1;  // the inner products are incomplete: the full exact path ranks every query
     // the shortlist: lower end not above T
     if (!s_bad)
         for (int c = tid; c < K; c += kShortThreads) {
@@ -2355,10 +2355,6 @@ void clamp_shape(const int *np, const int *k, int64_t nq, int np_max, int k_max,
 
 namespace {
 
-void blas_try(cublasStatus_t e, const char *what) {
-    if (e != CUBLAS_STATUS_SUCCESS) throw Error{SAQG_ERR_CUDA, std::string(what) + " failed (cuBLAS status " +
-                                                                   std::to_string((int)e) + ")"};
-}
 
 // Centroid ranking of a batch: TF32 GEMM of inner products, the shortlist
 // kernel, and the full exact path for the queries it hands back.
@@ -2377,19 +2373,10 @@ void probe_shortlist(const Index &I, SearchCtx &C, const float *q, int64_t nq, i
             I.cnorm2 = p;
         }
     }
-    if (!C.blas) {
-        cublasHandle_t h = nullptr;
-        blas_try(cublasCreate(&h), "cublasCreate");
-        C.blas = h;
-    }
-    cublasHandle_t h = static_cast<cublasHandle_t>(C.blas);
-    blas_try(cublasSetStream(h, st), "cublasSetStream");
-    const float one = 1.0f, zero = 0.0f;
-    // dist (row-major nq x K) = Q C^T, i.e. column-major K x nq = C^T(op T) * Q^T
-    blas_try(cublasGemmEx(h, CUBLAS_OP_T, CUBLAS_OP_N, (int)I.K, (int)nq, (int)I.D, &one, ix.centroids, CUDA_R_32F,
-                          (int)I.D, q, CUDA_R_32F, (int)I.D, &zero, dist, CUDA_R_32F, (int)I.K,
-                          CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT),
-             "cublasGemmEx");
+    (void)C;
+    // dist (row-major nq x K) = Q C^T on the tensor cores (TF32 operands, FP32
+    // accumulation); flags[3] is set if a pipeline wait of the GEMM timed out
+    probe_ip_gemm(q, nq, ix.centroids, I.K, I.D, dist, flags + 3, st);
     const double u = 1.0 / 16777216.0;
     ShortBound sb;
     sb.e1 = (float)(2.0 * (1.0 / 512 + 1.0 / 1048576 + (double)(I.D + 2) * u));
@@ -2399,7 +2386,7 @@ void probe_shortlist(const Index &I, SearchCtx &C, const float *q, int64_t nq, i
     ensure_smem((const void *)k_probe_shortlist, (size_t)smem);
     k_probe_shortlist<<<(unsigned)nq, kShortThreads, smem, st>>>(ix, q, dist, reinterpret_cast<const float2 *>(I.cnorm2),
                                                                  sb, (int)nprobe, qnp, probe, full,
-                                                                 fb_list, flags + 2, cnt);
+                                                                 fb_list, flags + 2, cnt, flags + 3);
     check_launch("k_probe_shortlist");
     k_probe_dist_list<<<608, 256, 0, st>>>(ix, q, dist, fb_list, flags + 2);
     check_launch("k_probe_dist_list");
@@ -2417,22 +2404,9 @@ void presize_ctx(const Index &I, SearchCtx &C, int64_t nq, int64_t topk, int64_t
     C.aux_stream();
     C.fork_event();
     C.join_event();
-    ctx_blas_ready(C);
 }
 
-void ctx_blas_ready(SearchCtx &C) {
-    if (!C.blas) {
-        cublasHandle_t h = nullptr;
-        blas_try(cublasCreate(&h), "cublasCreate");
-        C.blas = h;
-    }
-    if (!C.blas_ws) {  // a workspace of its own: cuBLAS then allocates nothing inside a call
-        C.blas_ws_bytes = 32u << 20;
-        SAQG_CUDA_TRY(cudaMalloc(&C.blas_ws, C.blas_ws_bytes));
-        blas_try(cublasSetWorkspace(static_cast<cublasHandle_t>(C.blas), C.blas_ws, C.blas_ws_bytes),
-                 "cublasSetWorkspace");
-    }
-}
+
 
 size_t search_bytes_estimate(const Index &I, int64_t nq, int64_t topk, int64_t nprobe) {
     const int64_t max_pos = I.max_blocks_of_probes(nprobe);

@@ -47,10 +47,13 @@
 #include <vector>
 
 #include "saqg_internal.h"
+#include "tcgen05.cuh"
 
 namespace saqg {
 
 namespace {
+
+using namespace tc;
 
 constexpr int kTcBM = 128;           // vectors per tile: the MMA's M
 constexpr int kTcBK = 64;            // dims per pipeline stage: one 128-byte BF16 row
@@ -61,109 +64,11 @@ constexpr int kTcCols = 256;         // TMEM columns of one accumulator (segment
 constexpr int kTcMaxN = 128;         // pairs per chunk at most (the MMA's N)
 constexpr int kTcMaxShort = 1024;    // shortlist length at most
 constexpr int kTcMaxBatch = 8192;    // queries per call at most (bucket sort in shared memory)
-constexpr unsigned kFullMask = 0xffffffffu;
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ uint64_t gtimer() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Waits for the phase of parity `parity` of `bar`.  Gives up after one second,
-// or at once when another role of the CTA gave up (`abort`), so that no wait
-// outlives a lost arrival; the caller then records the failure.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort) {
-    if (mbar_try(bar, parity)) return true;
-    const uint64_t t0 = gtimer();
-    for (;;) {
-        if (mbar_try(bar, parity)) return true;
-        if (*abort) return false;
-        if (gtimer() - t0 > 1000000000ull) {
-            *abort = 1;
-            return false;
-        }
-    }
-}
-
-// Bounded wait that ignores `abort` (draining copies in flight before exit).
-__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
-    const uint64_t t0 = gtimer();
-    while (!mbar_try(bar, parity))
-        if (gtimer() - t0 > 1000000000ull) return;
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int x, int y) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
-            dst),
-        "l"((uint64_t)map), "r"(bar), "r"(x), "r"(y)
-        : "memory");
-}
-
-// Shared-memory matrix descriptor (tcgen05): K-major operand in the 128-byte
-// swizzle layout, rows of 128 bytes, 8-row groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
-    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
 
 // Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
 // K-major, M = 128, N = n.
 __device__ __forceinline__ uint32_t idesc_bf16(int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-            tmem),
-        "l"(a), "l"(b), "r"(idesc), "r"(acc)
-        : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// 16 consecutive FP32 columns of this thread's TMEM lane.
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-        "tcgen05.wait::ld.sync.aligned;\n"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr)
-        : "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
-    __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<uint32_t *>(&h);
 }
 
 // ------------------------------------------------------------ code matrix
@@ -920,7 +825,6 @@ void presize_tc_ctx(const Index &I, SearchCtx &C, int64_t nq, int64_t topk, int6
     std::lock_guard<std::mutex> lock(C.mu);
     C.scratch_get(tc_arena1_bytes(I, nq, topk, nprobe, L));
     C.split_scratch_get(tc_arena2_bytes(I.view, cand_cap, nq * nprobe, cand_cap / kTcSelChunk + nq, L));
-    ctx_blas_ready(C);
 }
 
 void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int64_t nprobe, int64_t L, float m,
