@@ -94,6 +94,7 @@ Index::~Index() {
     ctx_pool.clear();  // on this index's device
     for (void *p : allocations) cudaFree(p);
     if (cnorm2) cudaFree(cnorm2);
+    if (cent_bf16) cudaFree(cent_bf16);
     if (tc_codes) cudaFree(tc_codes);
     if (tc_tiles) cudaFree(tc_tiles);
     cudaSetDevice(cur);

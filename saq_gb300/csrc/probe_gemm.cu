@@ -1,19 +1,21 @@
 // Inner products of a query batch with every centroid on the tensor cores:
-// ip[q][c] = sum_d Q[q][d] C[c][d] with TF32 operands and FP32 accumulation,
-// the first step of the batched centroid ranking (FlatInitializer::
-// centroids_distances, initializer.hpp:52-76, for a batch).  k_probe_shortlist
-// turns each product into a distance interval that provably holds the
-// reference's float distance, so the ranking stays exact.
+// ip[q][c] = sum_d Q[q][d] C[c][d] with BF16 operands (rounded to nearest) and
+// FP32 accumulation, the first step of the batched centroid ranking
+// (FlatInitializer::centroids_distances, initializer.hpp:52-76, for a batch).
+// k_probe_shortlist turns each product into a distance interval that provably
+// holds the reference's float distance, so the ranking stays exact.  BF16 halves
+// the operand bytes that every tile streams from L2 (the bound of this GEMM at
+// these shapes) against TF32, for a four times wider interval.
 //
 // k_probe_gemm is persistent, one CTA of 192 threads per SM, over 128 x 256
 // output tiles (queries x centroids), tiles taken round-robin:
-//   warp 0 (one thread)  TMA: per 32-dim stage the 128-row query tile and the
-//                        256-row centroid tile (FP32, 128-byte swizzle) into a
+//   warp 0 (one thread)  TMA: per 64-dim stage the 128-row query tile and the
+//                        256-row centroid tile (BF16, 128-byte swizzle) into a
 //                        4-stage ring (48 KB per stage)
-//   warp 1 (one thread)  tcgen05.mma kind::tf32 (M = 128, N = 256, K = 8 per
-//                        instruction) into one of two TMEM accumulators of 256
-//                        columns; commits free a stage / publish an accumulator;
-//                        warp 1 also owns the 512 TMEM columns
+//   warp 1 (one thread)  tcgen05.mma kind::f16 (BF16; M = 128, N = 256, K = 16
+//                        per instruction) into one of two TMEM accumulators of
+//                        256 columns; commits free a stage / publish an
+//                        accumulator; warp 1 also owns the 512 TMEM columns
 //   warps 2-5            epilogue: tcgen05.ld of their 32 lanes (query rows),
 //                        row-major FP32 stores of the products
 // Tile t uses accumulator t & 1, so the MMAs of the next tile overlap the
@@ -38,17 +40,23 @@ using namespace tc;
 
 constexpr int kGmBM = 128;                 // queries per tile (the MMA's M)
 constexpr int kGmBN = 256;                 // centroids per tile (the MMA's N)
-constexpr int kGmBK = 32;                  // dims per stage: one 128-byte FP32 row
+constexpr int kGmBK = 64;                  // dims per stage: one 128-byte BF16 row
 constexpr int kGmStages = 4;
 constexpr int kGmThreads = 192;
 constexpr int kGmStageA = kGmBM * 128;     // 16 KB
 constexpr int kGmStageB = kGmBN * 128;     // 32 KB
 constexpr int kGmCols = 512;               // two accumulators of 256 FP32 columns
 
-// Instruction descriptor of kind::tf32: FP32 accumulator, TF32 A and B, both
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
 // K-major, M = 128, N = 256.
-__device__ __forceinline__ uint32_t idesc_tf32() {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kGmBN >> 3) << 17) | ((uint32_t)(kGmBM >> 4) << 24);
+__device__ __forceinline__ uint32_t idesc_gemm() {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kGmBN >> 3) << 17) | ((uint32_t)(kGmBM >> 4) << 24);
+}
+
+// x (n floats) -> BF16, rounded to nearest even.
+__global__ void k_to_bf16(const float *__restrict__ x, int64_t n, __nv_bfloat16 *__restrict__ y) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = __float2bfloat16_rn(x[i]);
 }
 
 struct GemmArgs {
@@ -134,7 +142,7 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_probe_gemm(const __grid_const
         if (lane == 0) {
             int it = 0, lt = 0;
             bool ok = true;
-            const uint32_t idesc = idesc_tf32();
+            const uint32_t idesc = idesc_gemm();
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++lt) {
                 const int buf = lt & 1;
                 if (!mbar_wait(acce(buf), (((uint32_t)lt >> 1) & 1u) ^ 1u, abort)) {
@@ -153,8 +161,8 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_probe_gemm(const __grid_const
                     tc_fence_after();
                     const uint64_t da = sw128_desc(sA + st * kGmStageA), db = sw128_desc(sB + st * kGmStageB);
 #pragma unroll
-                    for (int kk = 0; kk < kGmBK / 8; ++kk)  // 8 TF32 = 32 bytes per instruction
-                        mma_tf32(dacc, da + 2 * kk, db + 2 * kk, idesc, (kc == 0 && kk == 0) ? 0u : 1u);
+                    for (int kk = 0; kk < kGmBK / 16; ++kk)  // 16 BF16 = 32 bytes per instruction
+                        mma_bf16(dacc, da + 2 * kk, db + 2 * kk, idesc, (kc == 0 && kk == 0) ? 0u : 1u);
                     mma_commit(empty(st));
                 }
                 if (ok) mma_commit(accf(buf));
@@ -227,14 +235,14 @@ PFN_cuTensorMapEncodeTiled_v12000 map_encoder() {
     return fn;
 }
 
-// Row-major FP32 matrix [rows][cols] read in (32 x box_rows) boxes, 128-byte swizzle.
-CUtensorMap f32_rows_map(const float *base, int64_t cols, int64_t rows, int box_rows) {
+// Row-major BF16 matrix [rows][cols] read in (64 x box_rows) boxes, 128-byte swizzle.
+CUtensorMap bf16_map(const __nv_bfloat16 *base, int64_t cols, int64_t rows, int box_rows) {
     CUtensorMap m;
     const cuuint64_t gdim[2] = {(cuuint64_t)cols, (cuuint64_t)std::max<int64_t>(rows, 1)};
-    const cuuint64_t gstride[1] = {(cuuint64_t)cols * 4};
+    const cuuint64_t gstride[1] = {(cuuint64_t)cols * 2};
     const cuuint32_t box[2] = {(cuuint32_t)kGmBK, (cuuint32_t)box_rows};
     const cuuint32_t estr[2] = {1, 1};
-    const CUresult r = map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), gdim, gstride,
+    const CUresult r = map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16 *>(base), gdim, gstride,
                                      box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) throw Error{SAQG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r)};
@@ -254,14 +262,24 @@ int sms() {
 
 }  // namespace
 
-void probe_ip_gemm(const float *q, int64_t nq, const float *cent, int64_t K, int64_t D, float *ip, int *err,
+void to_bf16(const float *x, int64_t n, void *y, cudaStream_t st) {
+    if (n <= 0) return;
+    const unsigned grid = (unsigned)std::min<int64_t>((n + 255) / 256, 4 * (int64_t)sms() * 8);
+    k_to_bf16<<<grid, 256, 0, st>>>(x, n, static_cast<__nv_bfloat16 *>(y));
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw Error{SAQG_ERR_CUDA, std::string("k_to_bf16 launch failed: ") + cudaGetErrorString(e)};
+    count_launch(1);
+}
+
+void probe_ip_gemm(const void *q_bf16, int64_t nq, const void *cent_bf16, int64_t K, int64_t D, float *ip, int *err,
                    cudaStream_t st) {
-    SAQG_REQUIRE(D % 4 == 0 && D > 0, "the probe GEMM needs a dimension that is a multiple of 4");
+    SAQG_REQUIRE(D % 8 == 0 && D > 0, "the probe GEMM needs a dimension that is a multiple of 8");
     SAQG_REQUIRE(nq < (int64_t)1 << 31 && K < (int64_t)1 << 31, "probe GEMM too large");
-    SAQG_REQUIRE(((uintptr_t)q & 15) == 0 && ((uintptr_t)cent & 15) == 0, "probe GEMM operands must be 16-byte aligned");
+    SAQG_REQUIRE(((uintptr_t)q_bf16 & 15) == 0 && ((uintptr_t)cent_bf16 & 15) == 0,
+                 "probe GEMM operands must be 16-byte aligned");
     if (nq == 0 || K == 0) return;
-    const CUtensorMap tmQ = f32_rows_map(q, D, nq, kGmBM);
-    const CUtensorMap tmC = f32_rows_map(cent, D, K, kGmBN);
+    const CUtensorMap tmQ = bf16_map(static_cast<const __nv_bfloat16 *>(q_bf16), D, nq, kGmBM);
+    const CUtensorMap tmC = bf16_map(static_cast<const __nv_bfloat16 *>(cent_bf16), D, K, kGmBN);
     GemmArgs g;
     g.M = (int)nq;
     g.N = (int)K;
@@ -271,10 +289,7 @@ void probe_ip_gemm(const float *q, int64_t nq, const float *cent, int64_t K, int
     g.out = ip;
     g.ldo = K;
     g.err = err;
-    static std::once_flag attr_once;
-    std::call_once(attr_once, [] {
-        cudaFuncSetAttribute(k_probe_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem());
-    });
+    SAQG_CUDA_TRY(cudaFuncSetAttribute(k_probe_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem()));
     const int64_t ntiles = (int64_t)g.tiles_m * g.tiles_n;
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, sms());
     k_probe_gemm<<<grid, kGmThreads, gemm_smem(), st>>>(tmQ, tmC, g);

@@ -149,6 +149,7 @@ struct Index {
     // probe shortlist: squared centroid norms (built on first use, under init_mu)
     mutable std::mutex init_mu;
     mutable float *cnorm2 = nullptr;
+    mutable void *cent_bf16 = nullptr;  // centroids rounded to BF16 (the probe GEMM's operand)
     // tensor-core form: BF16 code matrix [N][Dtot] and the (cluster, tile) list (built on first use, under init_mu)
     mutable void *tc_codes = nullptr;
     mutable void *tc_tiles = nullptr;
@@ -219,7 +220,7 @@ int64_t run_estimate(const Index &idx, const float *q_host, int64_t nprobe, floa
 // and the exact re-rank of its shortlist.
 void tc_rank_rotate(const Index &idx, SearchCtx &ctx, const float *q, int64_t nq, int64_t nprobe, const int *qnp,
                     float m, float *dist, void *work, uint32_t *probe, float *qrot, float *prune, uint8_t *full,
-                    int *fb_list, int *flags, cudaStream_t st);
+                    int *fb_list, int *flags, void *qbf, cudaStream_t st);
 size_t tc_probe_work_bytes(const Index &idx, int64_t nq);
 void tc_rerank(const Index &idx, const uint32_t *probe, int64_t nq, int64_t nprobe, const float *qrot,
                const float *prune, const int *lp, const int *sl_pos, const float *sl_apx, const int *sl_cnt, int L,
@@ -275,10 +276,12 @@ void graph_launch(SearchGraph *g, cudaStream_t st);
 int graph_status(SearchGraph *g, cudaStream_t st);
 const TuneReport &graph_tune(const SearchGraph *g);
 void graph_free(SearchGraph *g);
-// probe_gemm.cu: ip (row-major nq x K) = Q C^T with TF32 tensor-core products and
-// FP32 accumulation; *err is set (device) if a pipeline wait timed out.
-void probe_ip_gemm(const float *q, int64_t nq, const float *cent, int64_t K, int64_t D, float *ip, int *err,
+// probe_gemm.cu: ip (row-major nq x K) = Q C^T with BF16 operands (row-major,
+// nq x D and K x D) and FP32 accumulation on the tensor cores; *err is set
+// (device) if a pipeline wait timed out.  to_bf16 rounds n floats to nearest.
+void probe_ip_gemm(const void *q_bf16, int64_t nq, const void *cent_bf16, int64_t K, int64_t D, float *ip, int *err,
                    cudaStream_t st);
+void to_bf16(const float *x, int64_t n, void *y_bf16, cudaStream_t st);
 
 // serve.cpp
 struct Server;

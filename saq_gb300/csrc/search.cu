@@ -375,12 +375,12 @@ __global__ void __launch_bounds__(kSelThreads) k_probe_select(const float *__res
 }
 
 // ------------------------------------------------------ probe: GEMM shortlist
-// Batches rank centroids from inner products q.c computed by a TF32
-// tensor-core GEMM.  Each approximate distance a = |q|^2 + |c|^2 - 2 q.c gets
-// a rigorous bound b on its distance from the reference's float distance
-// (TF32 operands are within 2^-10 of their FP32 values, so |q.c error| <=
-// (2^-9 + accumulation) |q||c|; the norms and the reference's own sum add
-// (2D + 32) * 2^-24 (|q| + |c|)^2).  Every centroid of the exact top-nprobe has
+// Batches rank centroids from inner products q.c computed by a BF16
+// tensor-core GEMM (probe_gemm.cu).  Each approximate distance a = |q|^2 +
+// |c|^2 - 2 q.c gets a rigorous bound b on its distance from the reference's
+// float distance (operands rounded to BF16 are within 2^-9 of their FP32
+// values, so |q.c error| <= (2^-8 + 2^-18 + accumulation) |q||c|; the norms and
+// the reference's own sum add (2D + 32) * 2^-24 (|q| + |c|)^2).  Every centroid of the exact top-nprobe has
 // a - b <= T, T the nprobe-th smallest a + b, so only those centroids get the
 // exact Eigen-order distance and the ranking is the exact one.  A query with
 // equal distances among its first nprobe + 1 (where the standard library's
@@ -2220,6 +2220,7 @@ size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t np
     add(4 * (size_t)nq * nprobe);              // probe ids
     add(4 * (size_t)nq * I.view.Dtot);         // rotated queries
     add(4 * (size_t)nq * I.view.S);            // prune bounds
+    add(2 * (size_t)nq * I.D);                 // BF16 queries (probe GEMM)
     add((size_t)nq);                           // shortlist: queries on the full exact path
     add(4 * (size_t)nq);                       // ... and their list
     add(4 * (size_t)nq * topk * 2);            // outputs (host io)
@@ -2360,7 +2361,7 @@ namespace {
 // kernel, and the full exact path for the queries it hands back.
 void probe_shortlist(const Index &I, SearchCtx &C, const float *q, int64_t nq, int64_t nprobe, const int *qnp,
                      float *dist, uint32_t *probe, uint8_t *full, int *fb_list, int *flags, Cand *work,
-                     unsigned long long *cnt, cudaStream_t st) {
+                     unsigned long long *cnt, void *qbf, cudaStream_t st) {
     const DevIndexView &ix = I.view;
     {
         std::lock_guard<std::mutex> lk(I.init_mu);
@@ -2374,12 +2375,24 @@ void probe_shortlist(const Index &I, SearchCtx &C, const float *q, int64_t nq, i
         }
     }
     (void)C;
-    // dist (row-major nq x K) = Q C^T on the tensor cores (TF32 operands, FP32
-    // accumulation); flags[3] is set if a pipeline wait of the GEMM timed out
-    probe_ip_gemm(q, nq, ix.centroids, I.K, I.D, dist, flags + 3, st);
+    {
+        std::lock_guard<std::mutex> lk(I.init_mu);
+        if (!I.cent_bf16) {
+            void *p = nullptr;
+            SAQG_CUDA_TRY(cudaMalloc(&p, 2 * (size_t)I.K * I.D));
+            to_bf16(ix.centroids, I.K * I.D, p, st);
+            SAQG_CUDA_TRY(cudaStreamSynchronize(st));  // other contexts read it on their own streams
+            I.cent_bf16 = p;
+        }
+    }
+    // dist (row-major nq x K) = Q C^T on the tensor cores (BF16 operands rounded
+    // to nearest, FP32 accumulation); flags[3] is set if a GEMM wait timed out
+    to_bf16(q, nq * I.D, qbf, st);
+    probe_ip_gemm(qbf, nq, I.cent_bf16, I.K, I.D, dist, flags + 3, st);
     const double u = 1.0 / 16777216.0;
     ShortBound sb;
-    sb.e1 = (float)(2.0 * (1.0 / 512 + 1.0 / 1048576 + (double)(I.D + 2) * u));
+    // BF16 operands lie within 2^-9 of their values: |q.c error| <= (2^-8 + 2^-18) |q||c| + accumulation
+    sb.e1 = (float)(2.0 * (1.0 / 256 + 1.0 / 262144 + (double)(I.D + 2) * u));
     sb.e2 = (float)((2.0 * (double)I.D + 32.0) * u);
     const size_t smem = 12 * (size_t)kShortCap + 4 * (size_t)I.D + (I.K <= kShortKeys ? 4 * (size_t)I.K : 0);
     SAQG_REQUIRE(smem <= 220 * 1024, "dimension too large for the probe shortlist's shared memory");
@@ -2482,6 +2495,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
     uint32_t *probe = bp.take<uint32_t>((size_t)nq * nprobe);
     float *qrot = bp.take<float>((size_t)nq * ix.Dtot);
     float *prune = bp.take<float>((size_t)nq * ix.S);
+    void *qbf = bp.take<uint16_t>((size_t)nq * I.D);
     uint8_t *full = bp.take<uint8_t>((size_t)nq);
     int *fb_list = bp.take<int>((size_t)nq);
     uint32_t *oid = bp.take<uint32_t>((size_t)nq * topk);
@@ -2514,7 +2528,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         shortlist = nq >= kGemmMinQueries && nprobe <= kShortCap && !(pm && std::string(pm) == "exact");
         if (shortlist) {
             probe_shortlist(I, C, qin, nq, nprobe, qsh.np, dist, probe, full, fb_list, flags, work,
-                            stats ? counters : nullptr, st);
+                            stats ? counters : nullptr, qbf, st);
         } else if (nq >= 8 && I.D % 32 == 0 && I.D <= 32 * kProbeRegs) {
             const size_t qsm = 4 * (size_t)kProbeQT * I.D;
             ensure_smem((const void *)k_probe_dist_tiled, (size_t)qsm);
@@ -3086,14 +3100,14 @@ __global__ void __launch_bounds__(kScanThreads) k_tc_topk(DevIndexView ix, const
 
 void tc_rank_rotate(const Index &I, SearchCtx &C, const float *q, int64_t nq, int64_t nprobe, const int *qnp, float m,
                     float *dist, void *work, uint32_t *probe, float *qrot, float *prune, uint8_t *full, int *fb_list,
-                    int *flags, cudaStream_t st) {
+                    int *flags, void *qbf, cudaStream_t st) {
     const DevIndexView &ix = I.view;
     SAQG_CUDA_TRY(cudaMemsetAsync(flags, 0, 64, st));
     Cand *wk = static_cast<Cand *>(work);
     const char *pm = std::getenv("SAQG_PROBE");
     const bool shortlist = nq >= kGemmMinQueries && nprobe <= kShortCap && !(pm && std::string(pm) == "exact");
     if (shortlist) {
-        probe_shortlist(I, C, q, nq, nprobe, qnp, dist, probe, full, fb_list, flags, wk, nullptr, st);
+        probe_shortlist(I, C, q, nq, nprobe, qnp, dist, probe, full, fb_list, flags, wk, nullptr, qbf, st);
     } else {
         k_probe_dist<<<dim3((unsigned)((I.K + 7) / 8), (unsigned)nq), 256, 0, st>>>(ix, q, dist);
         check_launch("k_probe_dist");

@@ -795,6 +795,7 @@ size_t tc_arena1_bytes(const Index &I, int64_t nq, int64_t topk, int64_t nprobe,
     add(4 * (size_t)P);                         // probes
     add(4 * (size_t)nq * ix.Dtot);              // rotated queries
     add(4 * (size_t)nq * ix.S);                 // prune bounds
+    add(2 * (size_t)nq * I.D);                  // BF16 queries (probe GEMM)
     add((size_t)nq);                            // full-path flags
     add(4 * (size_t)nq);                        // full-path list
     add(64);                                    // flags
@@ -897,6 +898,7 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     uint32_t *probe = reinterpret_cast<uint32_t *>(take(4 * (size_t)P));
     float *qrot = reinterpret_cast<float *>(take(4 * (size_t)nq * ix.Dtot));
     float *prune = reinterpret_cast<float *>(take(4 * (size_t)nq * ix.S));
+    void *qbf = take(2 * (size_t)nq * I.D);
     uint8_t *full = reinterpret_cast<uint8_t *>(take((size_t)nq));
     int *fb = reinterpret_cast<int *>(take(4 * (size_t)nq));
     int *flags = reinterpret_cast<int *>(take(64));
@@ -960,7 +962,7 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
         qin = dq;
     }
     mark(0);
-    tc_rank_rotate(I, C, qin, nq, nprobe, qnp, m, dist, work, probe, qrot, prune, full, fb, flags, st);
+    tc_rank_rotate(I, C, qin, nq, nprobe, qnp, m, dist, work, probe, qrot, prune, full, fb, flags, qbf, st);
     mark(1);
     // pairs: candidate offsets per query, buckets per cluster, selection chunks
     SAQG_CUDA_TRY(cudaMemsetAsync(bcnt, 0, 8 * (size_t)I.K, st));
