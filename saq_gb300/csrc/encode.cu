@@ -4,8 +4,10 @@
 // accepted move changes the running <o,o_a> and |o_a|^2 read by the next
 // dimension (caq_encoder.hpp:57-142); bit-exact codes need the reference's
 // exact FP64 operation sequence, so one thread owns one vector and walks its
-// dimensions in order.  This file is compiled with --fmad=false: no multiply
-// is fused into an add unless written as fma().
+// dimensions in order.  In index construction the 32 lanes of a warp encode
+// 32 vectors whose residuals and codes are interleaved by dimension, so every
+// step of the 32 chains is one coalesced access.  This file is compiled with
+// --fmad=false: no multiply is fused into an add unless written as fma().
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -56,31 +58,38 @@ __device__ float thread_eigen_sum(int n, F f) {
     return r;
 }
 
-// encode + code_adjustment + encode_and_fac (caq_encoder.hpp:57-247) for one vector.
-__device__ void caq_encode_one(const float *__restrict__ o, int D, int bits, const float *__restrict__ cent, int rdlmt,
-                               float eps, int32_t *__restrict__ code, float *__restrict__ fac) {
+// encode + code_adjustment + encode_and_fac (caq_encoder.hpp:57-247) for one
+// vector whose dimension j lies at o_[j * STR] (its code at code_[j * STR]):
+// STR = 1 for a row-major vector, 32 for a vector of a warp-interleaved group,
+// where the 32 lanes of a warp encode 32 vectors and every load and store of
+// the warp at dimension j is one contiguous 128-byte access.
+template <int STR>
+__device__ void caq_encode_one(const float *__restrict__ o_, int D, int bits, const float *__restrict__ cent, int rdlmt,
+                               float eps, int32_t *__restrict__ code_, float *__restrict__ fac) {
+    auto o = [&](int j) { return o_[(int64_t)j * STR]; };
+    auto code = [&](int j) -> int32_t & { return code_[(int64_t)j * STR]; };
     double v_mx = 0, v_mi = 0, delta = 0, ip = 0, oa2 = 0;
     if (bits > 0) {
         const int cmax = (1 << bits) - 1;
-        float mx = o[0], mn = o[0];
+        float mx = o(0), mn = o(0);
         for (int j = 1; j < D; ++j) {
-            mx = fmaxf(mx, o[j]);
-            mn = fminf(mn, o[j]);
+            mx = fmaxf(mx, o(j));
+            mn = fminf(mn, o(j));
         }
         v_mx = (double)fmaxf(mx, -mn);
         v_mi = -v_mx;
         delta = __ddiv_rn(__dsub_rn(v_mx, v_mi), (double)(cmax + 1));
-        const double vec_sum = (double)thread_eigen_sum(D, [&](int i) { return o[i]; });
+        const double vec_sum = (double)thread_eigen_sum(D, [&](int i) { return o(i); });
         double ip_o_code = 0;
         uint64_t code_l2 = 0;
         uint32_t code_sum = 0;
         const float vmi_f = (float)v_mi, d_f = (float)delta;
         for (int j = 0; j < D; ++j) {
             float cf = 0.0f;
-            if (delta != 0) cf = fminf(floorf(__fdiv_rn(__fsub_rn(o[j], vmi_f), d_f)), (float)cmax);
-            ip_o_code = __dadd_rn(ip_o_code, (double)__fmul_rn(cf, o[j]));
+            if (delta != 0) cf = fminf(floorf(__fdiv_rn(__fsub_rn(o(j), vmi_f), d_f)), (float)cmax);
+            ip_o_code = __dadd_rn(ip_o_code, (double)__fmul_rn(cf, o(j)));
             const int c = (int)cf;
-            code[j] = c;
+            code(j) = c;
             code_l2 += (uint64_t)(c * c);
             code_sum += (uint32_t)c;
         }
@@ -97,9 +106,9 @@ __device__ void caq_encode_one(const float *__restrict__ o, int D, int bits, con
                 adj = 0;
                 for (int j = 0; j < D; ++j) {
                     int cur = 0;
-                    const float ov = o[j];
-                    double oa = __dadd_rn(__dmul_rn(__dadd_rn((double)code[j], 0.5), delta), v_mi);
-                    int c = code[j];
+                    const float ov = o(j);
+                    double oa = __dadd_rn(__dmul_rn(__dadd_rn((double)code(j), 0.5), delta), v_mi);
+                    int c = code(j);
                     const double tmp = __dsub_rn(oa2, __dmul_rn(oa, oa));
                     const double ipd = __dmul_rn(delta, (double)ov);
                     while (c < cmax) {
@@ -122,16 +131,16 @@ __device__ void caq_encode_one(const float *__restrict__ o, int D, int bits, con
                         oa2 = nl;
                         cur++;
                     }
-                    if (code[j] != c) {
-                        code[j] = c;
+                    if (code(j) != c) {
+                        code(j) = c;
                         adj += cur;
                     }
                 }
                 if (rdlmt && round >= rdlmt) break;
                 double ci = 0, co = 0;
                 for (int j = 0; j < D; ++j) {
-                    const double qv = __dadd_rn(__dmul_rn(__dadd_rn((double)code[j], 0.5), delta), v_mi);
-                    ci = __dadd_rn(ci, __dmul_rn(qv, (double)o[j]));
+                    const double qv = __dadd_rn(__dmul_rn(__dadd_rn((double)code(j), 0.5), delta), v_mi);
+                    ci = __dadd_rn(ci, __dmul_rn(qv, (double)o(j)));
                     co = __dadd_rn(co, __dmul_rn(qv, qv));
                 }
                 oa2 = co;
@@ -139,9 +148,9 @@ __device__ void caq_encode_one(const float *__restrict__ o, int D, int bits, con
             }
         }
     } else {
-        for (int j = 0; j < D; ++j) code[j] = 0;
+        for (int j = 0; j < D; ++j) code(j) = 0;
     }
-    const double o_l2sqr = (double)thread_eigen_sum(D, [&](int i) { return __fmul_rn(o[i], o[i]); });
+    const double o_l2sqr = (double)thread_eigen_sum(D, [&](int i) { return __fmul_rn(o(i), o(i)); });
     const double o_l2norm = __dsqrt_rn(o_l2sqr);
     double rescale = ip != 0 ? __ddiv_rn(o_l2sqr, ip) : 0.0;
     const double err = __dmul_rn(
@@ -156,7 +165,7 @@ __device__ void caq_encode_one(const float *__restrict__ o, int D, int bits, con
     float ipc = 0.0f;
     if (bits > 1 && cent) {
         const float df = (float)delta, vf = (float)v_mi;
-        ipc = thread_eigen_sum(D, [&](int i) { return __fmul_rn(cent[i], __fadd_rn(__fmul_rn((float)code[i], df), vf)); });
+        ipc = thread_eigen_sum(D, [&](int i) { return __fmul_rn(cent[i], __fadd_rn(__fmul_rn((float)code(i), df), vf)); });
     }
     fac[0] = (float)o_l2norm;
     fac[1] = ipc;
@@ -168,7 +177,7 @@ __global__ void k_caq_encode(const float *__restrict__ resid, int64_t n, int D, 
                              int rdlmt, float eps, int32_t *__restrict__ codes, float *__restrict__ facs) {
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n) return;
-    caq_encode_one(resid + v * D, D, bits, cent, rdlmt, eps, codes + v * D, facs + v * 4);
+    caq_encode_one<1>(resid + v * D, D, bits, cent, rdlmt, eps, codes + v * D, facs + v * 4);
 }
 
 }  // namespace
@@ -247,7 +256,7 @@ constexpr int kRT = 64, kRK = 16;
 __global__ void __launch_bounds__(256) k_rotate(const float *__restrict__ data, int D, const int64_t *__restrict__ rows,
                                                 int64_t nv, int off, int dim, const float *__restrict__ P,
                                                 const float *__restrict__ rc, const int32_t *__restrict__ cid,
-                                                float *__restrict__ out) {
+                                                float *__restrict__ out, int interleaved) {
     __shared__ float xs[kRK][kRT + 1];
     __shared__ float ps[kRK][kRT];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -303,7 +312,7 @@ __global__ void __launch_bounds__(256) k_rotate(const float *__restrict__ data, 
             const int o = o0 + tx * 4 + b;
             if (o >= dim) continue;
             const float r = rc ? __fsub_rn(res[a][b], rc[(int64_t)cid[v] * dim + o]) : res[a][b];
-            out[v * dim + o] = r;
+            out[interleaved ? (v >> 5) * (int64_t)dim * 32 + (int64_t)o * 32 + (v & 31) : v * dim + o] = r;
         }
     }
 }
@@ -320,19 +329,26 @@ __global__ void k_centroid_slices(const float *__restrict__ cent, int64_t K, int
 }
 
 // CAQEncoder::encode_and_fac for the vectors of a chunk, each with its own
-// cluster's un-rotated centroid slice.
+// cluster's un-rotated centroid slice.  Residuals and codes are warp-interleaved
+// ([v / 32][dim][v % 32]): lane l of a warp encodes vector 32 w + l, and each
+// step of the 32 sequential FP64 chains reads one coalesced line.
+__device__ __forceinline__ int64_t inter_at(int64_t v, int D) { return (v >> 5) * (int64_t)D * 32 + (v & 31); }
+
 __global__ void k_caq_encode_clustered(const float *__restrict__ resid, int64_t n, int D, int bits,
                                        const float *__restrict__ cslices, const int32_t *__restrict__ cid, int rdlmt,
                                        float eps, int32_t *__restrict__ codes, float *__restrict__ facs) {
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n) return;
-    caq_encode_one(resid + v * D, D, bits, cslices + (int64_t)cid[v] * D, rdlmt, eps, codes + v * D, facs + v * 4);
+    caq_encode_one<32>(resid + inter_at(v, D), D, bits, cslices + (int64_t)cid[v] * D, rdlmt, eps,
+                       codes + inter_at(v, D), facs + v * 4);
 }
 
-// CodeHelper<B>::compacted_code8/16 (code_helper.hpp) for one vector.
+// CodeHelper<B>::compacted_code8/16 (code_helper.hpp) for one vector (code of
+// dimension d at v[d * STR]).
+template <int STR>
 __device__ void pack_bits8_dev(const int32_t *__restrict__ v, int D, int bits, int shift, int mask,
                                uint8_t *__restrict__ y) {
-    auto val = [&](int d) { return (uint32_t)((v[d] >> shift) & mask); };
+    auto val = [&](int d) { return (uint32_t)((v[(int64_t)d * STR] >> shift) & mask); };
     switch (bits) {
     case 1:
         for (int i = 0; i < D / 8; ++i) {
@@ -388,22 +404,23 @@ __device__ void pack_bits8_dev(const int32_t *__restrict__ v, int D, int bits, i
     }
 }
 
+template <int STR>
 __device__ void pack_excode_dev(const int32_t *__restrict__ code, int D, int exb, uint8_t *__restrict__ y) {
     const int lowmask = (1 << exb) - 1;
     if (exb > 8) {  // compacted_code16: low bytes, then the remaining bits in their own layout
-        for (int d = 0; d < D; ++d) y[d] = (uint8_t)(code[d] & lowmask & 0xFF);
+        for (int d = 0; d < D; ++d) y[d] = (uint8_t)(code[(int64_t)d * STR] & lowmask & 0xFF);
         const int hb = exb - 8;
         if (hb == 5) {
-            pack_bits8_dev(code, D, 4, 9, 15, y + D);
-            pack_bits8_dev(code, D, 1, 8, 1, y + D + D / 2);
+            pack_bits8_dev<STR>(code, D, 4, 9, 15, y + D);
+            pack_bits8_dev<STR>(code, D, 1, 8, 1, y + D + D / 2);
         } else {
-            pack_bits8_dev(code, D, hb, 8, (1 << hb) - 1, y + D);
+            pack_bits8_dev<STR>(code, D, hb, 8, (1 << hb) - 1, y + D);
         }
     } else if (exb == 5) {  // CodeHelper<5>: 4-bit layout of code>>1, then the low bit
-        pack_bits8_dev(code, D, 4, 1, 15, y);
-        pack_bits8_dev(code, D, 1, 0, 1, y + D / 2);
+        pack_bits8_dev<STR>(code, D, 4, 1, 15, y);
+        pack_bits8_dev<STR>(code, D, 1, 0, 1, y + D / 2);
     } else {
-        pack_bits8_dev(code, D, exb, 0, lowmask, y);
+        pack_bits8_dev<STR>(code, D, exb, 0, lowmask, y);
     }
 }
 
@@ -424,15 +441,15 @@ __global__ void k_pack(const int32_t *__restrict__ codes, const float *__restric
     if (g.bits == 0) return;
     g.ipcent[gb * 32 + lane] = f[1];
     g.exfac[gv] = make_float2(f[2], f[3]);
-    const int32_t *code = codes + v * g.dim;
+    const int32_t *code = codes + inter_at(v, g.dim);  // warp-interleaved codes: dimension d at code[32 d]
     const int sb = 1 << (g.bits - 1);
     uint8_t *cb = reinterpret_cast<uint8_t *>(g.codes) + (size_t)gb * (g.dim / 8) * 32;
     for (int i = 0; i < g.dim / 8; ++i) {
         uint32_t byte = 0;
-        for (int k = 0; k < 8; ++k) byte |= (code[i * 8 + k] & sb) ? (0x80u >> k) : 0u;
+        for (int k = 0; k < 8; ++k) byte |= (code[(int64_t)(i * 8 + k) * 32] & sb) ? (0x80u >> k) : 0u;
         cb[((size_t)(i / 8) * 32 + lane) * 8 + (i % 8)] = (uint8_t)byte;
     }
-    if (g.bits > 1) pack_excode_dev(code, g.dim, g.bits - 1, g.lcode + (size_t)gv * g.lstride);
+    if (g.bits > 1) pack_excode_dev<32>(code, g.dim, g.bits - 1, g.lcode + (size_t)gv * g.lstride);
 }
 
 // Random orthogonal matrix (modified Gram-Schmidt on a Gaussian matrix, FP64,
@@ -622,8 +639,10 @@ Index *construct_index(const float *data, int64_t n, int64_t dim, const float *c
     }
     int64_t maxd = 0;
     for (auto &sg : X.segs) maxd = std::max(maxd, sg.dim);
-    const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(n, (int64_t)(1u << 30) / (8 * maxd)));
-    DevBuf resid(4 * (size_t)chunk * maxd), codes(4 * (size_t)chunk * maxd), facs(16 * (size_t)chunk);
+    // chunks of whole 32-vector groups (residuals and codes are warp-interleaved)
+    const int64_t chunk = std::max<int64_t>(32, std::min<int64_t>(n, (int64_t)(1u << 30) / (8 * maxd)) / 32 * 32);
+    const int64_t chunk_pad = (std::min(chunk, n) + 31) / 32 * 32;
+    DevBuf resid(4 * (size_t)chunk_pad * maxd), codes(4 * (size_t)chunk_pad * maxd), facs(16 * (size_t)chunk_pad);
     DevBuf cslice(4 * (size_t)k * maxd);
     int off = 0;
     for (size_t s = 0; s < S; ++s) {
@@ -654,7 +673,8 @@ Index *construct_index(const float *data, int64_t n, int64_t dim, const float *c
         {
             dim3 grid((unsigned)((d + kRT - 1) / kRT), (unsigned)((k + kRT - 1) / kRT));
             if (dP) {
-                k_rotate<<<grid, 256>>>(dcent, (int)dim, didx.as<int64_t>(), k, off, (int)d, dP, nullptr, nullptr, g.cent);
+                k_rotate<<<grid, 256>>>(dcent, (int)dim, didx.as<int64_t>(), k, off, (int)d, dP, nullptr, nullptr, g.cent,
+                                        0);
                 launch_check("k_rotate(centroids)");
             }
             k_centroid_slices<<<(unsigned)((k * d + 255) / 256), 256>>>(dcent, k, (int)dim, off, (int)d,
@@ -676,7 +696,7 @@ Index *construct_index(const float *data, int64_t n, int64_t dim, const float *c
             const int64_t nv = std::min(chunk, n - v0);
             dim3 grid((unsigned)((d + kRT - 1) / kRT), (unsigned)((nv + kRT - 1) / kRT));
             k_rotate<<<grid, 256>>>(ddata, (int)dim, drows.as<int64_t>() + v0, nv, off, (int)d,
-                                    dP ? dP : idP->as<float>(), g.cent, dcid.as<int32_t>() + v0, resid.as<float>());
+                                    dP ? dP : idP->as<float>(), g.cent, dcid.as<int32_t>() + v0, resid.as<float>(), 1);
             launch_check("k_rotate");
             k_caq_encode_clustered<<<(unsigned)((nv + 63) / 64), 64>>>(
                 resid.as<float>(), nv, (int)d, g.bits, cslice.as<float>(), dcid.as<int32_t>() + v0, cfg.caq_adj_rd_lmt,
