@@ -425,14 +425,15 @@ __global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView 
                                                                    uint8_t *__restrict__ full, int *__restrict__ fb_list,
                                                                    int *__restrict__ fb_count,
                                                                    unsigned long long *__restrict__ counters,
-                                                                   const int *__restrict__ ip_err) {
+                                                                   const int *__restrict__ ip_err, int keep_keys) {
     extern __shared__ __align__(16) char smem_raw[];
     unsigned long long *keys = reinterpret_cast<unsigned long long *>(smem_raw);  // [kShortCap]
     uint32_t *cand = reinterpret_cast<uint32_t *>(keys + kShortCap);             // [kShortCap]
     float *qs = reinterpret_cast<float *>(cand + kShortCap);                      // [D]
-    uint32_t *hk = reinterpret_cast<uint32_t *>(qs + ix.D);                       // [K] when K <= kShortKeys
-    const bool keep = ix.K <= kShortKeys;
+    uint32_t *hk = reinterpret_cast<uint32_t *>(qs + ix.D);                       // [K] when keep_keys
+    const bool keep = keep_keys != 0;
     __shared__ uint32_t hist[256];
+    __shared__ uint32_t tmin[kShortThreads];
     __shared__ uint32_t s_prefix, s_mask, s_rem, s_n;
     __shared__ int s_bad;
     __shared__ float s_red[kShortThreads / 32];
@@ -459,24 +460,45 @@ __global__ void __launch_bounds__(kShortThreads) k_probe_shortlist(DevIndexView 
     float qn2 = 0.0f;
     for (int i = 0; i < kShortThreads / 32; ++i) qn2 += s_red[i];
     const float qn = sqrtf(qn2);
-    // T: the nprobe-th smallest upper end (radix select on the order-preserving keys)
+    // T: the nprobe-th smallest upper end (radix select on the order-preserving
+    // keys).  For nprobe <= threads / 2, each thread contributes the smallest
+    // upper end of its strided share of the centroids and T is the nprobe-th
+    // smallest of those: the nprobe-th smallest of a subset of the upper ends is
+    // at least the nprobe-th smallest of all, so the shortlist below still holds
+    // every centroid of the exact top-nprobe (it may hold a few more).
+    const bool by_thread = nprobe <= kShortThreads / 2;
+    if (by_thread) {
+        uint32_t m = 0xffffffffu;
+        for (int c = tid; c < K; c += kShortThreads) {
+            float lo, hi;
+            approx_bounds(qn2, qn, ipq[c], cn2[c], sb, lo, hi);
+            if (!(isfinite(lo) && isfinite(hi))) s_bad = 1;
+            m = min(m, fkey(hi));
+        }
+        tmin[tid] = m;
+    }
     for (int pass = 0; pass < 4; ++pass) {
         const int shift = 24 - 8 * pass;
         for (int i = tid; i < 256; i += kShortThreads) hist[i] = 0;
         __syncthreads();
         const uint32_t prefix = s_prefix, mask = s_mask;
-        for (int c = tid; c < K; c += kShortThreads) {
-            uint32_t k;
-            if (pass == 0 || !keep) {
-                float lo, hi;
-                approx_bounds(qn2, qn, ipq[c], cn2[c], sb, lo, hi);
-                if (pass == 0 && !(isfinite(lo) && isfinite(hi))) s_bad = 1;
-                k = fkey(hi);
-                if (keep) hk[c] = k;
-            } else {
-                k = hk[c];
-            }
+        if (by_thread) {
+            const uint32_t k = tmin[tid];
             if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255u], 1u);
+        } else {
+            for (int c = tid; c < K; c += kShortThreads) {
+                uint32_t k;
+                if (pass == 0 || !keep) {
+                    float lo, hi;
+                    approx_bounds(qn2, qn, ipq[c], cn2[c], sb, lo, hi);
+                    if (pass == 0 && !(isfinite(lo) && isfinite(hi))) s_bad = 1;
+                    k = fkey(hi);
+                    if (keep) hk[c] = k;
+                } else {
+                    k = hk[c];
+                }
+                if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255u], 1u);
+            }
         }
         __syncthreads();
         if (tid < 32) {
@@ -2394,12 +2416,15 @@ void probe_shortlist(const Index &I, SearchCtx &C, const float *q, int64_t nq, i
     // BF16 operands lie within 2^-9 of their values: |q.c error| <= (2^-8 + 2^-18) |q||c| + accumulation
     sb.e1 = (float)(2.0 * (1.0 / 256 + 1.0 / 262144 + (double)(I.D + 2) * u));
     sb.e2 = (float)((2.0 * (double)I.D + 32.0) * u);
-    const size_t smem = 12 * (size_t)kShortCap + 4 * (size_t)I.D + (I.K <= kShortKeys ? 4 * (size_t)I.K : 0);
+    // upper-end keys kept in shared memory for the full radix select, which only
+    // a query with nprobe > kShortThreads / 2 runs
+    const bool keep = I.K <= kShortKeys && nprobe > kShortThreads / 2;
+    const size_t smem = 12 * (size_t)kShortCap + 4 * (size_t)I.D + (keep ? 4 * (size_t)I.K : 0);
     SAQG_REQUIRE(smem <= 220 * 1024, "dimension too large for the probe shortlist's shared memory");
     ensure_smem((const void *)k_probe_shortlist, (size_t)smem);
     k_probe_shortlist<<<(unsigned)nq, kShortThreads, smem, st>>>(ix, q, dist, reinterpret_cast<const float2 *>(I.cnorm2),
                                                                  sb, (int)nprobe, qnp, probe, full,
-                                                                 fb_list, flags + 2, cnt, flags + 3);
+                                                                 fb_list, flags + 2, cnt, flags + 3, keep ? 1 : 0);
     check_launch("k_probe_shortlist");
     k_probe_dist_list<<<608, 256, 0, st>>>(ix, q, dist, fb_list, flags + 2);
     check_launch("k_probe_dist_list");

@@ -40,6 +40,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <climits>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -313,6 +314,10 @@ struct TcWork {
     int BN;                     // pairs per chunk (multiple of 16)
     long long cand_cap;         // approximate distances the cand array holds
     int *err;
+    // every pipeline wait gives up after wait_ns; skip_it >= 0 (tests of the
+    // timeout path only): CTA 0's producer issues no copy for its stage skip_it
+    unsigned long long wait_ns;
+    int skip_it;
 };
 
 // Persistent contraction, one CTA per SM, tiles round-robin.  Roles:
@@ -389,10 +394,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_contract(const __grid_cons
                     for (int kc = 0; kc < kch; ++kc, ++it) {
                         const int st = it % kTcStages;
                         const uint32_t ph = (uint32_t)(it / kTcStages) & 1u;
-                        if (!mbar_wait(empty(st), ph ^ 1u, abort)) {
+                        if (!mbar_wait(empty(st), ph ^ 1u, abort, w.wait_ns)) {
                             ok = false;
                             break;
                         }
+                        if (it == w.skip_it && blockIdx.x == 0) continue;  // test hook: this stage never fills
                         mbar_expect_tx(full(st), kTcStageBytes + npad * 128);
                         tma_load_2d(sA + st * kTcStageBytes, &tmA, full(st), kc * kTcBK, row0);
                         for (int bx = 0; bx < npad / 16; ++bx)
@@ -403,7 +409,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_contract(const __grid_cons
             if (!ok) {
                 atomicExch(w.err, 1);
                 for (int k = max(0, it - kTcStages); k < it; ++k)  // copies possibly in flight
-                    mbar_drain(full(k % kTcStages), (uint32_t)(k / kTcStages) & 1u);
+                    mbar_drain(full(k % kTcStages), (uint32_t)(k / kTcStages) & 1u, w.wait_ns);
             }
         }
         __syncwarp();
@@ -418,7 +424,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_contract(const __grid_cons
                     const int nh = min(BN, cnt - ch * BN), npad = (nh + 15) & ~15;
                     const uint32_t idesc = idesc_bf16(npad);
                     const int buf = g & 1;
-                    if (!mbar_wait(acce(buf), (((uint32_t)g >> 1) & 1u) ^ 1u, abort)) {
+                    if (!mbar_wait(acce(buf), (((uint32_t)g >> 1) & 1u) ^ 1u, abort, w.wait_ns)) {
                         ok = false;
                         break;
                     }
@@ -427,7 +433,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_contract(const __grid_cons
                     for (int kc = 0; kc < kch; ++kc, ++it) {
                         const int st = it % kTcStages;
                         const uint32_t ph = (uint32_t)(it / kTcStages) & 1u;
-                        if (!mbar_wait(full(st), ph, abort)) {
+                        if (!mbar_wait(full(st), ph, abort, w.wait_ns)) {
                             ok = false;
                             break;
                         }
@@ -448,7 +454,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_contract(const __grid_cons
             }
             if (!ok) atomicExch(w.err, 1);
             mma_commit(done);  // every MMA issued has finished once `done` completes
-            mbar_drain(done, 0);
+            mbar_drain(done, 0, w.wait_ns);
         }
         __syncwarp();
     } else {
@@ -469,7 +475,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_contract(const __grid_cons
             for (int ch = 0; ch * BN < cnt; ++ch, ++g) {
                 const int nh = min(BN, cnt - ch * BN), npad = (nh + 15) & ~15;
                 const int buf = g & 1;
-                if (ok && !mbar_wait(accf(buf), ((uint32_t)g >> 1) & 1u, abort)) ok = false;
+                if (ok && !mbar_wait(accf(buf), ((uint32_t)g >> 1) & 1u, abort, w.wait_ns)) ok = false;
                 tc_fence_after();
                 if (!__all_sync(kFullMask, ok)) {
                     ok = false;
@@ -1032,6 +1038,12 @@ void run_search_tc(const Index &I, const float *q, int64_t nq, int64_t topk, int
     wk.BN = BN;
     wk.cand_cap = std::max<long long>(total, 1);
     wk.err = err;
+    wk.wait_ns = 1000000000ull;
+    wk.skip_it = -1;
+    // test hooks of the timeout path (tests/test_tc_search.py): a shorter wait
+    // limit and one stage of CTA 0 that never fills
+    if (const char *e = std::getenv("SAQG_TEST_TC_WAIT_MS")) wk.wait_ns = 1000000ull * (unsigned long long)std::max(1, std::atoi(e));
+    if (const char *e = std::getenv("SAQG_TEST_TC_SKIP_STAGE")) wk.skip_it = std::max(0, std::atoi(e));
     const size_t smem = tc_contract_smem();
     SAQG_CUDA_TRY(cudaFuncSetAttribute(k_tc_contract, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (I.tc_ntiles > 0) {

@@ -45,13 +45,14 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
 // Waits for the phase of parity `parity` of `bar`.  Gives up after one second,
 // or at once when another role of the CTA gave up (`abort`), so that no wait
 // outlives a lost arrival; the caller then records the failure.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort,
+                                          uint64_t limit_ns = 1000000000ull) {
     if (mbar_try(bar, parity)) return true;
     const uint64_t t0 = gtimer();
     for (;;) {
         if (mbar_try(bar, parity)) return true;
         if (*abort) return false;
-        if (gtimer() - t0 > 1000000000ull) {
+        if (gtimer() - t0 > limit_ns) {
             *abort = 1;
             return false;
         }
@@ -59,10 +60,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
 }
 
 // Bounded wait that ignores `abort` (draining copies in flight before exit).
-__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity, uint64_t limit_ns = 1000000000ull) {
     const uint64_t t0 = gtimer();
     while (!mbar_try(bar, parity))
-        if (gtimer() - t0 > 1000000000ull) return;
+        if (gtimer() - t0 > limit_ns) return;
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, uint32_t bar, int x, int y) {

@@ -214,3 +214,25 @@ def test_edge_one_cluster_and_no_queries(tmp_path):
         assert np.array_equal(ids[i], oid) and np.array_equal(d[i], od.astype(np.float32)), i
     empty = index.search_tc(np.zeros((0, 64), np.float32), 10, 1)
     assert empty.shape == (0, 10)
+
+
+def test_contraction_wait_timeout_is_reported_and_the_context_recovers(built, monkeypatch):
+    """The contraction's bounded pipeline waits: with a 20 ms limit and one stage
+    of CTA 0 that never fills (the test hooks SAQG_TEST_TC_WAIT_MS and
+    SAQG_TEST_TC_SKIP_STAGE), the waits run out, the CTA drains and frees its
+    tensor memory, and the call returns SAQG_ERR_INTERNAL; the next call on the
+    same index returns the same answers as before, bit for bit."""
+    index, _, q, _ = built
+    nq, topk = 64, 10
+    nprobe = index.num_cen  # every cluster: CTA 0 has work
+    want_ids, want_d = index.search_tc(q[:nq], topk, nprobe, shortlist=40, return_dists=True)
+    monkeypatch.setenv("SAQG_TEST_TC_WAIT_MS", "20")
+    monkeypatch.setenv("SAQG_TEST_TC_SKIP_STAGE", "1")
+    from saq_gb300._native import SaqgError
+    with pytest.raises(SaqgError, match="timed out"):
+        index.search_tc(q[:nq], topk, nprobe, shortlist=40, return_dists=True)
+    monkeypatch.delenv("SAQG_TEST_TC_WAIT_MS")
+    monkeypatch.delenv("SAQG_TEST_TC_SKIP_STAGE")
+    ids, d = index.search_tc(q[:nq], topk, nprobe, shortlist=40, return_dists=True)
+    assert np.array_equal(ids, want_ids)
+    assert np.array_equal(np.asarray(d).view(np.uint32), np.asarray(want_d).view(np.uint32))
