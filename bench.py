@@ -911,29 +911,35 @@ def main():
                                       "recall@10_fp64_k10_queries": round(workloads.recall_at(tm[sel, :10], gt10, 10), 4),
                                       "k10_queries": len(sel)}
 
-    # ---- serving: Poisson arrivals through the continuous-batching server ----
-    serving = []
+    # ---- serving: Poisson arrivals through the continuous-batching server (both forms) ----
+    serving, serving_tc = [], []
     if a.serve_seconds > 0:
-        srv = ivf.Server(index, max_batch=B, max_inflight=2, max_topk=100, max_nprobe=256, max_wait_us=200)
         qpool = wl.q.cpu().numpy()
-        for rate in a.serve_rates:
-            n = max(1000, int(rate * a.serve_seconds))
-            arr = np.cumsum(rng.exponential(1.0 / rate, size=n))
-            qs = qpool[np.arange(n) % qpool.shape[0]]
-            nps = rng.integers(16, 257, size=n).astype(np.int32)
-            ks = rng.choice([10, 100], size=n).astype(np.int32)
-            before = srv.stats()
-            t0 = time.perf_counter()
-            _, _, lat_s = srv.run_trace(qs, arr, nps, ks)
-            wall = time.perf_counter() - t0
-            after = srv.stats()
-            nb = after["batches"] - before["batches"]
-            serving.append({"offered_qps": rate, "achieved_qps": n / wall, "queries": n,
+        gt_all = meta["gt"]
+        for form, out in (("exact", serving), ("tc", serving_tc)):
+            srv = ivf.Server(index, max_batch=B, max_inflight=2, max_topk=100, max_nprobe=256, max_wait_us=200,
+                             form=form)
+            for rate in a.serve_rates:
+                n = max(1000, int(rate * a.serve_seconds))
+                arr = np.cumsum(rng.exponential(1.0 / rate, size=n))
+                qi = np.arange(n) % qpool.shape[0]
+                qs = qpool[qi]
+                nps = rng.integers(16, 257, size=n).astype(np.int32)
+                ks = rng.choice([10, 100], size=n).astype(np.int32)
+                before = srv.stats()
+                t0 = time.perf_counter()
+                sids, _, lat_s = srv.run_trace(qs, arr, nps, ks)
+                wall = time.perf_counter() - t0
+                after = srv.stats()
+                nb = after["batches"] - before["batches"]
+                sel = [i for i in range(n) if ks[i] == 10 and qi[i] < len(gt_all)]
+                rec = workloads.recall_at(sids[sel, :10], gt_all[qi[sel]], 10) if sel else None
+                out.append({"offered_qps": rate, "achieved_qps": n / wall, "queries": n,
                             "p50_ms": float(np.percentile(lat_s, 50)), "p99_ms": float(np.percentile(lat_s, 99)),
-                            "mean_batch": n / max(1, nb)})
-            log(f"serving {rate}/s: p50 {serving[-1]['p50_ms']:.2f} ms p99 {serving[-1]['p99_ms']:.2f} ms "
-                f"achieved {serving[-1]['achieved_qps']:.0f}/s")
-        srv.close()
+                            "mean_batch": n / max(1, nb), "recall@10_fp64_k10_queries": rec})
+                log(f"serving ({form}) {rate}/s: p50 {out[-1]['p50_ms']:.2f} ms p99 {out[-1]['p99_ms']:.2f} ms "
+                    f"achieved {out[-1]['achieved_qps']:.0f}/s")
+            srv.close()
 
     # ---- CPU baseline (oracle port) on a bounded sample ----
     cpu = None
@@ -1019,7 +1025,11 @@ def main():
         "precision": precision,
         "serving": {"server": "continuous batching, 2 batches in flight, max batch %d" % B,
                     "nprobe": "U[16,256] per query", "k": "10 or 100 per query", "arrivals": "Poisson",
-                    "rates": serving},
+                    "rates": serving,
+                    "tensor_core_form": {"shortlist": 800, "rates": serving_tc,
+                                         "note": "the same trace through the tensor-core form (saqg_search_tc_batch "
+                                                 "per batch); recall against FP64 on the k = 10 queries with "
+                                                 "ground truth"}},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_v, "unit": "queries/s", "h2d_bytes_per_step": B * a.dim * 4,
                 "d2h_bytes_per_step": B * a.topk * 8, "ids_equal_device_run": e2e_same},

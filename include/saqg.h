@@ -316,6 +316,10 @@ typedef struct saqg_server_config {
     int32_t max_wait_us;      /* how long a partial batch waits for arrivals while others run */
     float searcher_vars_bound_m; /* SearcherConfig::searcher_vars_bound_m (0: 4) */
     int64_t mem_budget_bytes; /* device scratch for in-flight batches (0: half the free memory) */
+    int32_t form;             /* SAQG_FORM_EXACT (saqg_search_batch: every answer the reference's) or
+                                 SAQG_FORM_TC (saqg_search_tc_batch: the tensor-core form) */
+    int32_t shortlist;        /* SAQG_FORM_TC: approximate distances re-ranked per query (0: 8 x max_topk,
+                                 at most 1024) */
 } saqg_server_config;
 
 typedef struct saqg_server_stats {

@@ -83,7 +83,7 @@ _lib = None
 class ServerConfig(C.Structure):
     _fields_ = [("max_batch", C.c_int32), ("max_inflight", C.c_int32), ("max_topk", C.c_int32),
                 ("max_nprobe", C.c_int32), ("max_wait_us", C.c_int32), ("searcher_vars_bound_m", C.c_float),
-                ("mem_budget_bytes", I64)]
+                ("mem_budget_bytes", I64), ("form", C.c_int32), ("shortlist", C.c_int32)]
 
 
 class ServerStats(C.Structure):

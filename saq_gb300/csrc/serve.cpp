@@ -1,4 +1,6 @@
 // Serving loop: continuous batching of single queries on one index.
+// Batches run the exact form (every answer the reference's) or, by
+// configuration, the tensor-core form (saqg_search_tc_batch's path).
 //
 // Requests (one query each, with its own nprobe and k) queue on the host.  A
 // dispatcher thread forms a batch from everything pending whenever one of the
@@ -98,8 +100,15 @@ void Server::launch(Slot &s) {
         s.kmax = std::max(s.kmax, s.k[i]);
     }
     SAQG_CUDA_TRY(cudaMemcpyAsync(s.d_q, s.h_q, 4 * (size_t)n * I.D, cudaMemcpyHostToDevice, s.stream));
-    run_search(I, s.d_q, n, s.kmax, npmax, cfg.searcher_vars_bound_m, s.d_ids, s.d_d, SAQG_MEM_DEVICE, s.stream,
-               nullptr, nullptr, s.np.data(), s.k.data(), &s.ctx);
+    if (cfg.form == SAQG_FORM_TC) {
+        TcOpts o;
+        o.ctx = &s.ctx;
+        run_search_tc(I, s.d_q, n, s.kmax, npmax, std::max<int64_t>(cfg.shortlist, s.kmax), cfg.searcher_vars_bound_m,
+                      s.d_ids, s.d_d, nullptr, SAQG_MEM_DEVICE, s.stream, nullptr, s.np.data(), s.k.data(), &o);
+    } else {
+        run_search(I, s.d_q, n, s.kmax, npmax, cfg.searcher_vars_bound_m, s.d_ids, s.d_d, SAQG_MEM_DEVICE, s.stream,
+                   nullptr, nullptr, s.np.data(), s.k.data(), &s.ctx);
+    }
     SAQG_CUDA_TRY(cudaMemcpyAsync(s.h_ids, s.d_ids, 4 * (size_t)n * s.kmax, cudaMemcpyDeviceToHost, s.stream));
     SAQG_CUDA_TRY(cudaMemcpyAsync(s.h_d, s.d_d, 4 * (size_t)n * s.kmax, cudaMemcpyDeviceToHost, s.stream));
     SAQG_CUDA_TRY(cudaEventRecord(s.done_ev, s.stream));
@@ -213,6 +222,13 @@ Server *server_create(const Index &I, const saqg_server_config *c) {
     if (cfg.max_nprobe <= 0) cfg.max_nprobe = (int)std::min<int64_t>(256, I.K);
     if (cfg.max_wait_us < 0) cfg.max_wait_us = 0;
     if (cfg.searcher_vars_bound_m <= 0.0f) cfg.searcher_vars_bound_m = 4.0f;
+    SAQG_REQUIRE(cfg.form == SAQG_FORM_EXACT || cfg.form == SAQG_FORM_TC, "unknown search form");
+    if (cfg.form == SAQG_FORM_TC) {
+        if (cfg.shortlist <= 0) cfg.shortlist = std::min(1024, 8 * cfg.max_topk);
+        SAQG_REQUIRE(cfg.max_topk <= 1024 && cfg.shortlist >= cfg.max_topk && cfg.shortlist <= 1024,
+                     "tensor-core serving: max_topk <= shortlist <= 1024");
+        SAQG_REQUIRE(cfg.max_batch <= 8192, "tensor-core serving: at most 8192 queries per batch");
+    }
     SAQG_REQUIRE(cfg.max_topk <= 4096 && cfg.max_nprobe <= I.K, "server bounds beyond the index");
     SAQG_REQUIRE(cfg.max_inflight <= 16, "at most 16 batches in flight");
     int prev = 0;
@@ -240,7 +256,10 @@ Server *server_create(const Index &I, const saqg_server_config *c) {
         while (n > 1 && search_bytes_estimate(I, n, cfg.max_topk, cfg.max_nprobe) * cfg.max_inflight >
                             (size_t)cfg.mem_budget_bytes)
             n = (n + 1) / 2;
-        presize_ctx(I, s->ctx, n, cfg.max_topk, cfg.max_nprobe);
+        if (cfg.form == SAQG_FORM_TC)  // the candidate arena grows with the batches it meets
+            presize_tc_ctx(I, s->ctx, n, cfg.max_topk, cfg.max_nprobe, cfg.shortlist, 0);
+        else
+            presize_ctx(I, s->ctx, n, cfg.max_topk, cfg.max_nprobe);
         sv->slots.push_back(std::move(s));
     }
     if (prev != I.device) cudaSetDevice(prev);

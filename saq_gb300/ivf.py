@@ -254,11 +254,14 @@ class Server:
 
     def __init__(self, index: IVF, max_batch: int = 4096, max_inflight: int = 2, max_topk: int = 100,
                  max_nprobe: int = 0, max_wait_us: int = 200, mem_budget_bytes: int = 0,
-                 searcher_cfg: SearcherConfig | None = None):
+                 searcher_cfg: SearcherConfig | None = None, form: str = "exact", shortlist: int = 0):
+        """form "exact": batches answered as saqg_search_batch (every answer the
+        reference's); "tc": as saqg_search_tc_batch with `shortlist` (0: 8 x max_topk)."""
         self.index = index
         self.lib = index.lib
         cfg = N.ServerConfig(max_batch, max_inflight, max_topk, max_nprobe, max_wait_us,
-                             (searcher_cfg or SearcherConfig()).searcher_vars_bound_m, mem_budget_bytes)
+                             (searcher_cfg or SearcherConfig()).searcher_vars_bound_m, mem_budget_bytes,
+                             {"exact": N.SAQG_FORM_EXACT, "tc": N.SAQG_FORM_TC}[form], shortlist)
         self._h = C.c_void_p()
         N.check(self.lib.saqg_server_create(index._h, C.byref(cfg), C.byref(self._h)))
 

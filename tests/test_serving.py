@@ -66,3 +66,39 @@ def test_submit_wait_and_admission_by_memory(index_and_queries):
         assert np.array_equal(ids, aid)
         assert np.array_equal(d.view(np.uint32), ad.view(np.uint32))
     assert st["completed"] == 40
+
+
+@pytest.fixture(scope="module")
+def coded_index_and_queries():
+    """An index whose every segment is coded (the tensor-core form needs it)."""
+    from saq_gb300 import ivf
+    x, q = data.gaussian_mixture(60000, 128, 400, sigma=0.6, seed=12, n_query=200)
+    cent, cids = data.kmeans(x, 192, iters=4, seed=5)
+    index = ivf.IVF(x.shape[0], 128, 192, ivf.QuantizeConfig(avg_bits=6.0, enable_segmentation=False))
+    index.construct(x, cent, cids, seed=6)
+    return index, q
+
+
+def test_served_tensor_core_answers_equal_alone(coded_index_and_queries):
+    """Tensor-core serving: every answer equals the same query searched alone by
+    saqg_search_tc with the server's shortlist, bit for bit, whichever batch it
+    landed in."""
+    from saq_gb300 import ivf
+    index, q = coded_index_and_queries
+    rng = np.random.default_rng(2)
+    n, L = 200, 200
+    nps = rng.integers(4, 65, size=n).astype(np.int32)
+    ks = rng.choice([10, 100], size=n).astype(np.int32)
+    srv = ivf.Server(index, max_batch=40, max_inflight=2, max_topk=100, max_nprobe=64, max_wait_us=500, form="tc",
+                     shortlist=L)
+    try:
+        arrival = np.concatenate([np.zeros(120), 0.002 + 0.0003 * np.arange(80)])
+        ids, d, lat = srv.run_trace(q[:n], arrival, nps, ks)
+        st = srv.stats()
+    finally:
+        srv.close()
+    for i in range(n):
+        aid, ad = index.search_tc(q[i], int(ks[i]), int(nps[i]), shortlist=L, return_dists=True)
+        assert np.array_equal(ids[i, :ks[i]], aid[0]), i
+        assert np.array_equal(d[i, :ks[i]].view(np.uint32), ad[0].view(np.uint32)), i
+    assert st["completed"] == n and st["batches"] < n and st["max_batch_seen"] > 1
