@@ -76,8 +76,10 @@ def parse():
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[20000, 50000, 100000, 200000])
     ap.add_argument("--serve-seconds", type=float, default=0.3)
     ap.add_argument("--tc-shortlist", type=int, default=40)
-    ap.add_argument("--only", default="all", choices=["all", "precision", "c1", "c2"],
-                    help="precision / c1 / c2: only that leg's measurements (its own JSON line)")
+    ap.add_argument("--only", default="all", choices=["all", "precision", "c1", "c2", "kernels"],
+                    help="precision / c1 / c2: only that leg's measurements (its own JSON line); kernels: the "
+                         "workload at --n / --clusters, two exact batched calls then two tensor-core calls and "
+                         "nothing else (the command the kernel profiles capture)")
     ap.add_argument("--configs", type=int, default=1, help="0: skip the c1 / c2 legs in the full run")
     ap.add_argument("--c2-n", type=int, default=1_000_000)
     ap.add_argument("--c2-queries", type=int, default=400, help="single queries timed per (B, seg, nprobe)")
@@ -150,11 +152,14 @@ def precision_leg(a, torch, flush, log):
            "operands": "codes BF16 (exact integers), queries BF16, FP32 accumulation in TMEM (tcgen05.mma kind::f16)",
            "configs": []}
     for bits in a.precision_bits:
+        # the rotation (one orthogonal matrix per segment, as the reference's Rotator
+        # draws at index set-up) is made before the timed build, as for the other legs
+        rots = workloads.rotations(ivf.plan(wl.variance, float(bits), False), ROT_SEED)
         t0 = time.time()
         index = ivf.IVF(a.precision_n, a.precision_dim, a.precision_clusters,
                         ivf.QuantizeConfig(avg_bits=float(bits), enable_segmentation=False))
         index.set_variance(wl.variance)
-        index.construct(wl.x, wl.centroids.cpu().numpy(), wl.cids.cpu().numpy().astype(np.uint32), seed=1)
+        index.construct(wl.x, wl.centroids.cpu().numpy(), wl.cids.cpu().numpy().astype(np.uint32), rotations=rots)
         torch.cuda.synchronize()
         build_s = time.time() - t0
         lib = index.lib
@@ -598,6 +603,47 @@ def c2_leg(a, torch, log, tmpdir):
     return out
 
 
+def kernels_leg(a, torch, log):
+    """The batched calls alone, for kernel profiles: the index of the workload
+    (raw vectors freed once it is built), two exact calls (saqg_search) and two
+    tensor-core calls (saqg_search_tc) on one batch, in that order, with the
+    built-in launch shapes.  Prints their CUDA-event times."""
+    import ctypes as C
+    from saq_gb300 import _native as N, ivf, workloads
+    wl = build_workload(a, torch)
+    plan = ivf.plan(wl.variance, a.bits, True)
+    index = ivf.IVF(a.n, a.dim, a.clusters, ivf.QuantizeConfig(avg_bits=a.bits, enable_segmentation=True))
+    index.set_variance(wl.variance)
+    index.construct(wl.x, wl.centroids.cpu().numpy(), wl.cids.cpu().numpy().astype(np.uint32),
+                    rotations=workloads.rotations(plan, ROT_SEED))
+    q = wl.q[:a.batch].contiguous()
+    del wl
+    torch.cuda.empty_cache()
+    B, k, npb = q.shape[0], a.topk, 16
+    ids = torch.empty((B, k), dtype=torch.int32, device="cuda")
+    dd = torch.empty((B, k), dtype=torch.float32, device="cuda")
+    scfg = ivf.SearcherConfig().to_c()
+    stream = torch.cuda.current_stream()
+    sptr = C.c_void_p(stream.cuda_stream)
+    out = {"workload": f"{a.n} x {a.dim}, {a.clusters} clusters, B={a.bits:g} segmented, batch {B}, nprobe {npb}",
+           "plan": plan, "exact_ms": [], "tc_ms": []}
+    for form in ("exact", "tc"):
+        for _ in range(2):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            if form == "exact":
+                N.check(index.lib.saqg_search(index._h, q.data_ptr(), B, k, npb, C.byref(scfg), ids.data_ptr(),
+                                              dd.data_ptr(), N.SAQG_MEM_DEVICE, sptr))
+            else:
+                N.check(index.lib.saqg_search_tc(index._h, q.data_ptr(), B, k, npb, a.tc_shortlist, C.byref(scfg),
+                                                 ids.data_ptr(), dd.data_ptr(), None, N.SAQG_MEM_DEVICE, sptr, None))
+            e1.record(stream)
+            e1.synchronize()
+            out[f"{form}_ms"].append(e0.elapsed_time(e1))
+    log(f"kernels: exact {out['exact_ms']} ms, tensor-core {out['tc_ms']} ms")
+    return out
+
+
 def main():
     a = parse()
     rank, world, local = dist_env()
@@ -621,6 +667,9 @@ def main():
             out = (c1_leg if a.only == "c1" else c2_leg)(a, torch, log, td)
         print(json.dumps({"metric": "plain single-query QPS, p50/p99, recall@10 and encode vectors/s",
                           a.only: out, "wall_s": time.time() - t_start}), flush=True)
+        return
+    if a.only == "kernels":
+        print(json.dumps(kernels_leg(a, torch, log)), flush=True)
         return
     wl = build_workload(a, torch)
     log(f"workload {wl.name} generated in {time.time() - t_start:.1f}s")
