@@ -256,10 +256,12 @@ int saqg_search_graph_free(saqg_search_graph *graph);
 
 typedef struct saqg_tune_report {
     int form;            /* SAQG_FORM_EXACT or SAQG_FORM_TC */
-    int scan_mode;       /* exact: 0 CTA per query (+ split pass for the largest probes), 1 split pass, 2 warp per query; -1 built-in */
+    int scan_mode;       /* exact: 0 CTA per query (+ split pass for the largest probes), 1 split pass, 2 warp per query,
+                            3 as 0 with the warp-specialised CTA scan; -1 built-in */
     int defer_blocks;    /* exact, mode 0: blocks above which a query takes the split pass (-1 built-in) */
     int first_blocks;    /* exact: blocks the split pass scans before speculating (-1 built-in) */
     int pairs_per_chunk; /* tensor-core form: the MMA's N (-1 built-in) */
+    int spec_levels;     /* exact, mode 0: the split pass's set of speculation levels (-1 built-in) */
     int candidates;      /* shapes timed (each one's answers checked equal to the built-in shapes') */
     float default_ms;    /* one call with the built-in shapes (best of 3, CUDA events) */
     float tuned_ms;      /* one call with the chosen shapes */

@@ -58,7 +58,8 @@ class TcStats(C.Structure):
 
 class TuneReport(C.Structure):
     _fields_ = [("form", C.c_int), ("scan_mode", C.c_int), ("defer_blocks", C.c_int), ("first_blocks", C.c_int),
-                ("pairs_per_chunk", C.c_int), ("candidates", C.c_int), ("default_ms", C.c_float),
+                ("pairs_per_chunk", C.c_int), ("spec_levels", C.c_int), ("candidates", C.c_int),
+                ("default_ms", C.c_float),
                 ("tuned_ms", C.c_float)]
 
     def as_dict(self):

@@ -9,8 +9,10 @@
 // shape, and graphs captured from them, use it.
 //
 //   exact form   scan mode (CTA per query with the split pass for the largest
-//                probes / split pass for every query / warp per query), the
-//                deferral threshold and the split pass's exact prefix
+//                probes, its CTA scan plain or warp-specialised / split pass
+//                for every query / warp per query), the
+//                deferral threshold, the split pass's exact prefix and its
+//                speculation levels
 //   tensor-core  (query, cluster) pairs per MMA chunk (the MMA's N)
 #include <cuda_runtime.h>
 
@@ -87,9 +89,11 @@ TuneReport autotune_exact(const Index &I, const float *q, int64_t nq, int64_t to
     ScanTune dflt;  // built-in
     cands.push_back(dflt);
     for (int defer : {256, 1024, 4096})
-        for (int first : {16, 64}) cands.push_back(ScanTune{0, defer, first});
-    cands.push_back(ScanTune{1, -1, -1});
-    if (topk <= 256) cands.push_back(ScanTune{2, -1, -1});
+        for (int first : {16, 64}) cands.push_back(ScanTune{0, defer, first, -1});
+    for (int lv = 1; lv < 5; ++lv) cands.push_back(ScanTune{0, 1024, 16, lv});  // the speculation level sets
+    for (int defer : {-1, 4096}) cands.push_back(ScanTune{3, defer, -1, -1});  // warp-specialised CTA scan
+    cands.push_back(ScanTune{1, -1, -1, -1});
+    if (topk <= 256) cands.push_back(ScanTune{2, -1, -1, -1});
     DevOut ref((size_t)nq * topk), out((size_t)nq * topk);
     Events ev;
     TuneReport rep;

@@ -221,6 +221,7 @@ void fill_report(saqg_tune_report *r, int form, const TuneReport &t) {
     r->scan_mode = t.scan.mode;
     r->defer_blocks = t.scan.defer_blocks;
     r->first_blocks = t.scan.first_blocks;
+    r->spec_levels = t.scan.spec_levels;
     r->pairs_per_chunk = t.tc.bn;
     r->candidates = t.candidates;
     r->default_ms = t.default_ms;

@@ -109,9 +109,11 @@ struct SearchCtx {
 // Launch shapes of the exact batched search (values < 0: the built-in choice).
 // Every choice returns the same answers; the autotuner picks one per shape.
 struct ScanTune {
-    int mode = -1;          // 0: CTA per query, split pass for the largest probes; 1: split pass; 2: warp per query
+    int mode = -1;          // 0: CTA per query, split pass for the largest probes; 1: split pass; 2: warp per query;
+                            // 3: mode 0 with the warp-specialised CTA scan
     int defer_blocks = -1;  // mode 0: a query probing more blocks than this takes the split pass
     int first_blocks = -1;  // split pass: blocks scanned exactly before the speculation
+    int spec_levels = -1;   // mode 0: which set of speculation levels the split pass uses
 };
 // Launch shape of the tensor-core form: (query, cluster) pairs per MMA chunk
 // (the MMA's N; a multiple of 16).  The approximate distances do not depend on it.

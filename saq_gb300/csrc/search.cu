@@ -1111,22 +1111,30 @@ __device__ __forceinline__ bool stages_pass(const float *st, int n, float tau) {
     return true;
 }
 
-// Steps 1-3 of a tile of up to kTileB blocks (warp w <-> blocks t0 + w + k * kScanWarps
+// Steps 1-3 of a tile of up to kTileB blocks (warp w <-> blocks t0 + w + k * nwarps
 // of the cluster): estimates, candidate masks under `tau`, and the accurate
 // distances (multi-segment: accurate - estimate per segment) of every
 // candidate lane.  Ends with the partials in sm.part and the masks in sm.cmask.
+// The threads [tbase, tbase + nthr) take part (whole warps; a tile then has
+// nthr / 32 * kBlocksPerWarp slots); they synchronise on __syncthreads when
+// barid is 0, else on the named barrier barid.
 __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0, int64_t v0, int nb, int n, int t0,
-                                int t_end, float tau) {
-    const int S = ix.S, tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+                                int t_end, float tau, int tbase = 0, int nthr = kScanThreads, int barid = 0) {
+    const int S = ix.S, tid = (int)threadIdx.x - tbase, w = tid >> 5, lane = tid & 31;
+    const int nwarps = nthr >> 5, nslots = nwarps * kBlocksPerWarp;
+    auto sync = [&]() {
+        if (barid) asm volatile("bar.sync %0, %1;" ::"r"(barid), "r"(nthr) : "memory");
+        else __syncthreads();
+    };
 #pragma unroll
     for (int k = 0; k < kBlocksPerWarp; ++k) {
-        const int slot = w + k * kScanWarps, b = t0 + slot;
+        const int slot = w + k * nwarps, b = t0 + slot;
         if (b < t_end) block_estimates(ix, b0 + b, sm, slot, lane, tau);
     }
-    __syncthreads();
+    sync();
 #pragma unroll
     for (int k = 0; k < kBlocksPerWarp; ++k) {
-        const int slot = w + k * kScanWarps, b = t0 + slot;
+        const int slot = w + k * nwarps, b = t0 + slot;
         if (b < t_end) {
             bool cand;
             if (S == 1) {
@@ -1142,12 +1150,12 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
             sm.cmask[slot] = 0;
         }
     }
-    __syncthreads();
+    sync();
     // accurate distances: one thread per (candidate vector, segment); the
     // tasks of a segment start on a warp boundary, so a warp's lanes run the
     // same code (one ex-code width and length) instead of diverging over all
     int ncand = 0;
-    for (int i = 0; i < kTileB; ++i) ncand += __popc(sm.cmask[i]);
+    for (int i = 0; i < nslots; ++i) ncand += __popc(sm.cmask[i]);
     const int P = (ncand + 31) & ~31;
     const int total = S * P;
     auto decode = [&](int r, int &ww, int &j) {
@@ -1162,7 +1170,7 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
     };
     // first pull every task's ex-code row into L1, so the chains below do not
     // wait on memory group by group
-    for (int t = tid; t < total; t += blockDim.x) {
+    for (int t = tid; t < total; t += nthr) {
         const int s = t / P, r = t - s * P;
         if (r >= ncand) continue;
         int ww, j;
@@ -1173,7 +1181,7 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
             for (int o = 0; o < g.lstride; o += 128) asm volatile("prefetch.global.L1 [%0];" ::"l"(row + o));
         }
     }
-    for (int t = tid; t < total; t += blockDim.x) {
+    for (int t = tid; t < total; t += nthr) {
         const int s = t / P, r = t - s * P;
         if (r >= ncand) continue;
         int ww, j;
@@ -1187,7 +1195,7 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
                                         sc.sum_q, sc.q_l2sqr);
         sm.part[(ww * S + s) * 32 + j] = S == 1 ? acc : __fsub_rn(acc, sm.cd[(ww * S + s) * 32 + j]);
     }
-    __syncthreads();
+    sync();
 }
 
 // The reference's sequential decisions for one block (single thread):
@@ -1425,6 +1433,148 @@ __device__ void write_results(const ScanSmem &sm, int pool_size, int topk, int k
         out_ids[i] = i < topk ? sm.pool_id[i] : 0u;
         if (out_d) out_d[i] = i < pool_size && i < topk ? sm.pool_d[i] : FLT_MAX;
     }
+}
+
+// ------------------------------------------------------------------ warp-specialised scan
+// k_scan with the replay overlapped: warp 0 replays tile t (the reference's
+// decisions, the pool, distk) while warps 1-7 compute the estimates, masks and
+// accurate distances of tile t + 1 into the other of two tile buffers.  The
+// workers' bound for a tile is the distk the replay had published when the tile
+// began, which is at least every distk the tile will meet in the replay (distk
+// only shrinks), so the candidate lanes remain a superset and the answers are
+// k_scan's.  Named barriers: 1 among the workers (224 threads); 2 + b "tile in
+// buffer b written" (workers arrive, warp 0 waits); 4 + b "buffer b replayed"
+// (warp 0 arrives, the workers wait before they overwrite it).
+constexpr int kWsWorkers = kScanThreads - 32;
+constexpr int kWsSlots = (kWsWorkers / 32) * kBlocksPerWarp;  // blocks per tile
+
+struct WsTile {
+    int64_t v0;  // first vector of the tile's cluster
+    int t0;      // first block of the tile within the cluster
+};
+
+__host__ __device__ inline size_t ws_tile_bytes(int S) {
+    return 3 * align16(sizeof(float) * kTileB * S * 32) + align16(sizeof(float) * kTileB * 32) +
+           align16(sizeof(float) * kTileB * (S + 1)) + align16(sizeof(uint32_t) * kTileB) +
+           align16(sizeof(int) * kTileB);
+}
+
+__host__ __device__ inline size_t ws_smem_bytes(int Dtot, int S, int topk, int xstride) {
+    return scan_smem_bytes(Dtot, S, topk, xstride, false) + ws_tile_bytes(S);
+}
+
+// The tile buffer `b` of a warp-specialised layout: buffer 0 is the base
+// layout's, buffer 1 the arrays appended at `extra`.
+__device__ __forceinline__ ScanSmem ws_view(const ScanSmem &sm, char *extra, int S, int b) {
+    if (!b) return sm;
+    ScanSmem v = sm;
+    size_t o = 0;
+    v.cd = (float *)(extra + o);
+    o += align16(sizeof(float) * kTileB * S * 32);
+    v.ipx = (float *)(extra + o);
+    o += align16(sizeof(float) * kTileB * S * 32);
+    v.part = (float *)(extra + o);
+    o += align16(sizeof(float) * kTileB * S * 32);
+    v.cur = (float *)(extra + o);
+    o += align16(sizeof(float) * kTileB * 32);
+    v.stage = (float *)(extra + o);
+    o += align16(sizeof(float) * kTileB * (S + 1));
+    v.cmask = (uint32_t *)(extra + o);
+    o += align16(sizeof(uint32_t) * kTileB);
+    v.nstage = (int *)(extra + o);
+    return v;
+}
+
+__device__ __forceinline__ void named_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ __forceinline__ void named_arrive(int id, int n) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_ws(DevIndexView ix, const uint32_t *__restrict__ probe,
+                                                          QueryShape qsh, const float *__restrict__ qrot_all,
+                                                          const float *__restrict__ prune_all,
+                                                          uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
+                                                          unsigned long long *__restrict__ counters, int xstride,
+                                                          const uint8_t *__restrict__ deferred) {
+    extern __shared__ __align__(16) char smem_raw[];
+    const int qi = blockIdx.x;
+    if (deferred && deferred[qi]) return;  // answered by the split pass
+    const int np = qsh.np_of(qi), topk = qsh.k_of(qi), S = ix.S, tid = threadIdx.x;
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, qsh.k_max, xstride, false);
+    char *extra = smem_raw + scan_smem_bytes(ix.Dtot, S, qsh.k_max, xstride, false);
+    __shared__ WsTile meta[2];
+    __shared__ int pool_size;
+    __shared__ float distk;
+    volatile float *vdistk = &distk;
+    init_pool(sm, topk, pool_size, distk);
+    const uint32_t *pr = probe + (size_t)qi * qsh.np_max;
+    const float *qrot = qrot_all + (size_t)qi * ix.Dtot, *prune = prune_all + (size_t)qi * ix.S;
+    int ntiles = 0;
+    if (tid >= 32) {
+        // ---- workers: LUTs, estimates, masks, accurate distances
+        unsigned long long blocks = 0, vecs = 0;
+        for (int p = 0; p < np; ++p) {
+            const int c = (int)pr[p];
+            const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
+            const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
+            blocks += nb;
+            vecs += n;
+            if (nb == 0) continue;
+            prepare_cluster(ix, qrot, prune, c, sm, 32, 1);
+            for (int t0 = 0; t0 < nb; t0 += kWsSlots, ++ntiles) {
+                const int b = ntiles & 1;
+                if (ntiles >= 2) named_sync(4 + b, kScanThreads);  // the replay of tile ntiles - 2 is done
+                ScanSmem v = ws_view(sm, extra, S, b);
+                if (tid == 32) meta[b] = WsTile{v0, t0};
+                const float tau = __shfl_sync(kFull, *vdistk, 0);  // warp-uniform, as block_estimates wants
+                tile_candidates(ix, v, b0, v0, nb, n, t0, min(nb, t0 + kWsSlots), tau, 32, kWsWorkers, 1);
+                __threadfence_block();
+                named_arrive(2 + b, kScanThreads);
+            }
+        }
+        for (int t = max(0, ntiles - 2); t < ntiles; ++t) named_sync(4 + (t & 1), kScanThreads);  // the last replays
+        if (tid == 32 && counters) {
+            atomicAdd(counters + 0, blocks);
+            atomicAdd(counters + 1, vecs);
+        }
+    } else {
+        // ---- warp 0: the reference's decisions, in order
+        unsigned long long rr = 0, spec = 0;
+        float dk = distk;
+        int sz = pool_size;
+        for (int p = 0; p < np; ++p) {
+            const int c = (int)pr[p];
+            const int nb = (int)(ix.blk_off[c + 1] - ix.blk_off[c]);
+            for (int t0 = 0; t0 < nb; t0 += kWsSlots, ++ntiles) {
+                const int b = ntiles & 1;
+                named_sync(2 + b, kScanThreads);  // tile ntiles written
+                const ScanSmem v = ws_view(sm, extra, S, b);
+                const WsTile mt = meta[b];
+                const int cnt = min(kWsSlots, nb - mt.t0);
+                if (tid == 0)
+                    for (int i = 0; i < cnt; ++i) spec += __popc(v.cmask[i]);
+                for (int ww = 0; ww < cnt; ++ww)
+                    replay_block_warp(S, mt.t0 + ww, v.cur + ww * 32,
+                                      S == 1 ? 0.0f : stage_max(v.stage + ww * (S + 1), v.nstage[ww]),
+                                      S == 1 ? v.part + ww * 32 : v.part + ww * S * 32, v.cmask[ww], ix.ids + mt.v0,
+                                      sm.pool_id, sm.pool_d, sz, topk, dk, rr);
+                if (tid == 0) {
+                    *vdistk = dk;
+                    pool_size = sz;
+                }
+                __threadfence_block();
+                __syncwarp();
+                named_arrive(4 + b, kScanThreads);  // buffer b may be overwritten
+            }
+        }
+        if (tid == 0 && counters) {
+            atomicAdd(counters + 2, rr);
+            atomicAdd(counters + 3, spec);
+        }
+    }
+    __syncthreads();
+    write_results(sm, pool_size, topk, qsh.k_max, out_ids + (size_t)qi * qsh.k_max,
+                  out_d ? out_d + (size_t)qi * qsh.k_max : nullptr);
 }
 
 // ------------------------------------------------------------------ warp scan
@@ -1668,8 +1818,18 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_scan_warp(DevIndexView ix
 constexpr int kTileBlocks = 16;
 constexpr int kFirstBlocks = 16;  // exact prefix of a deferred query (its distk bounds the first level)
 // Levels of the speculation for deferred queries, in tiles after the split
-// point: [0, 8), [8, 64), [64, end).
-constexpr int kSpecLevels[] = {0, 8, 64};
+// point: [0, 8), [8, 64), [64, end) by default; the autotuner may pick another
+// set (each level's replay leaves the exact pool whose distk bounds the next
+// level's speculation: more levels, tighter bounds, more launches).
+constexpr int kMaxSpecLevels = 5;
+constexpr int kSpecLevelSets[][kMaxSpecLevels] = {
+    {0, 8, 64, -1, -1},
+    {0, 4, 32, 256, -1},
+    {0, 16, 128, -1, -1},
+    {0, 8, 64, 512, -1},
+    {0, 64, -1, -1, -1},
+};
+constexpr int kNumSpecLevelSets = (int)(sizeof(kSpecLevelSets) / sizeof(kSpecLevelSets[0]));
 constexpr int kDeferBlocks = 1024;  // a query scanning more blocks than this takes the split pass
                                      // (SAQG_DEFER_BLOCKS overrides it; 0 disables deferral)
 
@@ -2291,10 +2451,18 @@ int scan_mode(int64_t nq, int64_t topk, const ScanTune &t) {
     if (m && std::string(m) == "seq") return 0;
     if (m && std::string(m) == "split") return 1;
     if (m && std::string(m) == "warp") return topk <= 256 ? 2 : 0;
+    if (m && std::string(m) == "ws") return 0;
     if (t.mode == 0 || t.mode == 1) return t.mode;
+    if (t.mode == 3) return 0;
     if (t.mode == 2) return topk <= 256 ? 2 : 0;
     if (nq <= 16) return 1;
     return 0;
+}
+
+// Whether mode 0's CTA scan runs warp-specialised (scan mode 3).
+bool scan_ws(const ScanTune &t) {
+    if (const char *m = std::getenv("SAQG_SCAN_MODE")) return std::string(m) == "ws";
+    return t.mode == 3;
 }
 
 // The deferral threshold of mode 0 (blocks of a query's probes above which it
@@ -2341,6 +2509,26 @@ void ensure_smem(const void *fn, size_t bytes) {
     if (bytes <= h) return;
     SAQG_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     h = bytes;
+}
+
+// The CTA-per-query scan of `nq` queries (deferred ones skipped): k_scan, or
+// its warp-specialised form k_scan_ws, which gives the same answers.
+void launch_cta_scan(bool ws, const DevIndexView &ix, const uint32_t *probe, const QueryShape &qsh, const float *qrot,
+                     const float *prune, uint32_t *ids, float *d, int *err, unsigned long long *cnt, int xs,
+                     const uint8_t *deferred, int64_t nq, cudaStream_t st) {
+    if (ws) {
+        const size_t smem = ws_smem_bytes(ix.Dtot, ix.S, qsh.k_max, xs);
+        SAQG_REQUIRE(smem <= 220 * 1024, "dimension / topk too large for the scan kernel's shared memory");
+        ensure_smem((const void *)k_scan_ws, smem);
+        k_scan_ws<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, qsh, qrot, prune, ids, d, cnt, xs, deferred);
+        check_launch("k_scan_ws");
+        return;
+    }
+    const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, qsh.k_max, xs, kScanOverlap);
+    SAQG_REQUIRE(smem <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
+    ensure_smem((const void *)k_scan, smem);
+    k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, qsh, qrot, prune, ids, d, err, cnt, xs, deferred);
+    check_launch("k_scan");
 }
 
 // SMs x resident CTAs of a kernel (per device and shared-memory size), cached.
@@ -2607,12 +2795,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         } else if (mode == 0 && no_deferral(I, nprobe, tune)) {
             // no query of this call can probe more blocks than the deferral
             // threshold: the CTA scan answers every query, no split pass
-            const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs, kScanOverlap);
-            SAQG_REQUIRE(smem_k <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
-            ensure_smem((const void *)k_scan, (size_t)smem_k);
-            k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, qsh, qrot, prune, ids_out, d_out, flags + 1,
-                                                                cnt, xs, nullptr);
-            check_launch("k_scan");
+            launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, flags + 1, cnt, xs, nullptr, nq,
+                            st);
             count_launch(4);
         } else {
             // split-pass state: every query (mode 1), or the deferred giant-cluster queries (mode 0)
@@ -2665,12 +2849,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                     SAQG_CUDA_TRY(cudaEventRecord(C.fork_event(), st));
                     SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, C.fork_event(), 0));
                 }
-                const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs, kScanOverlap);
-                SAQG_REQUIRE(smem_k <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
-                ensure_smem((const void *)k_scan, (size_t)smem_k);
-                k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, qsh, qrot, prune, ids_out, d_out,
-                                                                    flags + 1, cnt, xs, deferred);
-                check_launch("k_scan");
+                launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, flags + 1, cnt, xs,
+                                deferred, nq, st);
             }
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
             const size_t smem_r = smem + 2 * 4 * (size_t)kReplayRecs * ss.rec_words;
@@ -2684,11 +2864,15 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             const unsigned grid = (unsigned)full_grid((const void *)k_scan_spec, kScanThreads, smem1);
             // levels of speculation (tiles after the split point): each level's
             // replay leaves the exact pool, whose distk bounds the next level
-            const int nlev = mode == 0 ? (int)(sizeof(kSpecLevels) / sizeof(kSpecLevels[0])) : 1;
+            const int *levels = kSpecLevelSets[tune.spec_levels >= 0 && tune.spec_levels < kNumSpecLevelSets
+                                                   ? tune.spec_levels : 0];
+            int nlev = 1;
+            if (mode == 0)
+                while (nlev < kMaxSpecLevels && levels[nlev] >= 0) ++nlev;
             for (int L = 0; L < nlev; ++L) {
                 SplitState sl = ss;
-                sl.t_lo = mode == 0 ? kSpecLevels[L] : 0;
-                sl.t_hi = L + 1 < nlev ? kSpecLevels[L + 1] : INT_MAX;
+                sl.t_lo = mode == 0 ? levels[L] : 0;
+                sl.t_hi = L + 1 < nlev ? levels[L + 1] : INT_MAX;
                 sl.final_level = L + 1 == nlev;
                 k_tile_prefix<<<1, 32, 0, sp>>>(sl);
                 check_launch("k_tile_prefix");

@@ -27,7 +27,7 @@ def built(tmp_path_factory):
     return index, O.OracleIndex(opath), q
 
 
-@pytest.mark.parametrize("mode,defer", [(None, None), ("seq", "1"), ("seq", "0"), ("split", None)])
+@pytest.mark.parametrize("mode,defer", [(None, None), ("seq", "1"), ("seq", "0"), ("split", None), ("ws", "1"), ("ws", "0")])
 @pytest.mark.parametrize("nq", [40, 120])
 def test_mixed_nprobe_and_k(built, mode, defer, nq, monkeypatch):
     index, oi, q = built

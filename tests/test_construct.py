@@ -127,7 +127,7 @@ def test_gpu_construct_matches_oracle_and_searches(case, tmp_path):
     O.build_index(opath, x, cent, cids, bits, seg, eqseg, rots)
     assert open(gpath, "rb").read() == open(opath, "rb").read()
     oids, od = O.OracleIndex(opath).search(q, 10, 5, with_dists=True)
-    for mode in ("seq", "split", "warp"):
+    for mode in ("seq", "split", "warp", "ws"):
         os.environ["SAQG_SCAN_MODE"] = mode
         try:
             ids, d = index.search(q, 10, 5, return_dists=True)

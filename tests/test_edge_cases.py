@@ -35,7 +35,7 @@ def with_empty(tmp_path_factory):
     return _build(x, cent, cids.astype(np.uint32), tmp) + (q,)
 
 
-@pytest.mark.parametrize("mode", ["seq", "split", "warp"])
+@pytest.mark.parametrize("mode", ["seq", "split", "warp", "ws"])
 @pytest.mark.parametrize("topk,nprobe", [(1, 3), (10, 12), (2000, 2), (4000, 12)])
 def test_against_oracle(with_empty, mode, topk, nprobe, monkeypatch):
     index, oi, q = with_empty

@@ -26,9 +26,10 @@ def saqg():
     return ivf
 
 
-@pytest.fixture(params=["seq", "split", "warp"])
+@pytest.fixture(params=["seq", "split", "warp", "ws"])
 def scan_mode(request, monkeypatch):
-    """The three exact scan implementations: CTA per query, split scan, warp per query."""
+    """The exact scan implementations: CTA per query, split scan, warp per query,
+    and CTA per query with the replay on its own warp (warp-specialised)."""
     monkeypatch.setenv("SAQG_SCAN_MODE", request.param)
     return request.param
 
