@@ -603,6 +603,28 @@ def c2_leg(a, torch, log, tmpdir):
     return out
 
 
+def exact_bytes(plan, sizes, probes, rerank_bytes, dim):
+    """Compulsory bytes of one exact batched search: per scanned block of each
+    distinct probed cluster 32 x (dim/8 over the coded segments + 4 bytes of |o|
+    per segment), 4 x dim per distinct probed centroid, and the re-rank's bytes."""
+    nblk = (sizes + 31) // 32
+    per_lane = sum(4 + (d // 8 if b else 0) for d, b in plan)
+    distinct = np.unique(probes)
+    return int((nblk[distinct] * 32 * per_lane).sum() + len(distinct) * 4 * dim + rerank_bytes)
+
+
+def contraction_bytes(plan, sizes, probes, pairs, candidates):
+    """Algorithmic bytes of one contraction launch (the codes' own width): every
+    distinct probed cluster's codes once at their packed width (sum over segments
+    of dim x bits / 8) with |o| and the rescale factor per coded segment, the
+    queries' rows (BF16) of every (query, cluster) pair, and the approximate
+    distances written."""
+    dtot = sum(d for d, _ in plan)
+    packed_pv = sum(d * b / 8 + (8 if b else 4) for d, b in plan)
+    n_distinct = int(sizes[np.unique(probes)].sum())
+    return int(n_distinct * packed_pv + 2 * pairs * dtot + 4 * candidates)
+
+
 def kernels_leg(a, torch, log):
     """The batched calls alone, for kernel profiles: the index of the workload
     (raw vectors freed once it is built), two exact calls (saqg_search) and two
@@ -617,6 +639,7 @@ def kernels_leg(a, torch, log):
     index.construct(wl.x, wl.centroids.cpu().numpy(), wl.cids.cpu().numpy().astype(np.uint32),
                     rotations=workloads.rotations(plan, ROT_SEED))
     q = wl.q[:a.batch].contiguous()
+    sizes = np.bincount(wl.cids.cpu().numpy(), minlength=a.clusters)
     del wl
     torch.cuda.empty_cache()
     B, k, npb = q.shape[0], a.topk, 16
@@ -640,6 +663,19 @@ def kernels_leg(a, torch, log):
             e1.record(stream)
             e1.synchronize()
             out[f"{form}_ms"].append(e0.elapsed_time(e1))
+    # byte counts of these calls (one more call of each form with statistics,
+    # after the ones a capture skips and takes), to scale a capture's DRAM bytes
+    # to the full workload
+    st, tst = N.SearchStats(), N.TcStats()
+    probes = torch.empty((B, npb), dtype=torch.int32, device="cuda")
+    N.check(index.lib.saqg_search_ex(index._h, q.data_ptr(), B, k, npb, C.byref(scfg), ids.data_ptr(), dd.data_ptr(),
+                                     N.SAQG_MEM_DEVICE, sptr, C.byref(st), probes.data_ptr()))
+    N.check(index.lib.saqg_search_tc(index._h, q.data_ptr(), B, k, npb, a.tc_shortlist, C.byref(scfg), ids.data_ptr(),
+                                     dd.data_ptr(), None, N.SAQG_MEM_DEVICE, sptr, C.byref(tst)))
+    torch.cuda.synchronize()
+    pr = probes.cpu().numpy()
+    out["exact_compulsory_bytes"] = exact_bytes(plan, sizes, pr, st.rerank_bytes, a.dim)
+    out["contraction_bytes"] = contraction_bytes(plan, sizes, pr, tst.pairs, tst.candidates)
     log(f"kernels: exact {out['exact_ms']} ms, tensor-core {out['tc_ms']} ms")
     return out
 
@@ -812,10 +848,8 @@ def main():
     # compulsory bytes of the exact form: each distinct probed cluster once + every re-rank
     info = index.info()
     sizes = np.bincount(wl.cids.cpu().numpy(), minlength=a.clusters)
-    nblk = (sizes + 31) // 32
-    per_lane = sum(4 + (d // 8 if b else 0) for d, b in info["plan"])
-    distinct = np.unique(probes.cpu().numpy())
-    compulsory = int((nblk[distinct] * 32 * per_lane).sum() + len(distinct) * 4 * a.dim + rr_b[-1])
+    probes_np = probes.cpu().numpy()
+    compulsory = exact_bytes(info["plan"], sizes, probes_np, rr_b[-1], a.dim)
     effective = fast_b[-1] + rr_b[-1]
     mean_scan = float(np.mean(scan_ms))
     coded_dims = sum(d for d, b in info["plan"] if b)
@@ -841,15 +875,7 @@ def main():
     it_ = ids_t.cpu().numpy().view(np.uint32)
     ts = tc_stats[-1]
     contract_ms = float(np.mean([x["ms_contract"] for x in tc_stats]))
-    # algorithmic bytes of one contraction launch (the unit of the codes' own width):
-    # every distinct probed cluster's codes once at their packed width (sum over
-    # segments of dim x bits / 8) with |o| and the rescale factor per coded
-    # segment, the queries' rows (BF16) of every (query, cluster) pair, and the
-    # approximate distances written
-    dtot = sum(d for d, _ in info["plan"])
-    packed_pv = sum(d * b / 8 + (8 if b else 4) for d, b in info["plan"])
-    n_distinct = int(sizes[distinct].sum())
-    tc_bytes = int(n_distinct * packed_pv + 2 * ts["pairs"] * dtot + 4 * ts["candidates"])
+    tc_bytes = contraction_bytes(info["plan"], sizes, probes_np, ts["pairs"], ts["candidates"])
     tc_achieved = tc_bytes / (contract_ms / 1e3) / 1e9
     tc_traffic = None
     tf2 = os.path.join(ROOT, "profiles", "k_tc_contract_traffic.json")

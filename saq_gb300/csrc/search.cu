@@ -39,6 +39,7 @@ constexpr int kScanThreads = kScanWarps * 32;
 constexpr int kBlocksPerWarp = 2;
 constexpr int kTileB = kScanWarps * kBlocksPerWarp;  // blocks per tile
 constexpr int kMaxTopK = 4096;
+constexpr int kScanMinCtas = 4;  // resident scan CTAs per SM the register budget is sized for
 
 struct SegScal {
     float delta, vl, sum_vl, sum_q, q_l2sqr, q_l2norm, c1, c2, vfac;
@@ -1014,21 +1015,25 @@ __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict_
         }
     }
     sync();
-    if (tid < S) {
+    if (tid < S) {  // what the quantizer needs
         SegScal &sc = sm.scal[tid];
-        const int dim = ix.seg[tid].dim, ncb = dim / 4;
         const float vl = key_to_float(sm.mm[2 * tid]), vr = key_to_float(sm.mm[2 * tid + 1]);
         const float delta = (float)__ddiv_rn((double)__fsub_rn(vr, vl), 65536.0 - 0.01);
         sc.delta = delta;
         sc.rdelta = __frcp_rn(delta);
         sc.vl = vl;
-        sc.sum_vl = (float)__dmul_rn(__dadd_rn((double)vl, __dmul_rn(0.5, (double)delta)), (double)(float)ncb);
-        sc.q_l2norm = sqrtf(sc.q_l2sqr);
-        sc.c1 = (float)__dsub_rn(__dmul_rn(0.5, (double)sc.sum_q), (double)__fmul_rn(0.58f, sc.q_l2norm));
-        sc.c2 = ix.seg[tid].c2;
-        sc.vfac = __fsub_rn(sc.q_l2sqr, __fmul_rn(2.0f, prune[tid]));
     }
     sync();
+    if (tid >= nt - S) {  // the epilogue constants, beside the quantization (the last warp's last lanes)
+        const int s = tid - (nt - S);
+        SegScal &sc = sm.scal[s];
+        const int ncb = ix.seg[s].dim / 4;
+        sc.sum_vl = (float)__dmul_rn(__dadd_rn((double)sc.vl, __dmul_rn(0.5, (double)sc.delta)), (double)(float)ncb);
+        sc.q_l2norm = sqrtf(sc.q_l2sqr);
+        sc.c1 = (float)__dsub_rn(__dmul_rn(0.5, (double)sc.sum_q), (double)__fmul_rn(0.58f, sc.q_l2norm));
+        sc.c2 = ix.seg[s].c2;
+        sc.vfac = __fsub_rn(sc.q_l2sqr, __fmul_rn(2.0f, prune[s]));
+    }
     for (int cb = tid; cb < ncb_all; cb += nt) {
         int s = 0;
         while (s + 1 < S && cb * 4 >= ix.seg[s + 1].qoff) ++s;
@@ -1047,6 +1052,31 @@ __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict_
         dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
     }
     sync();
+}
+
+// The block's minimum estimate for a pruning stage.  Only its comparisons with
+// distk / tau are ever used; without NaN lanes every reduction order gives the
+// same minimum (up to the sign of a zero, which no comparison sees), so a
+// single key reduction stands in for the reference's min tree.  With a NaN lane
+// the tree's order decides the result, and the tree runs.
+__device__ __forceinline__ float block_min(float cur) {
+    if (!__any_sync(kFull, cur != cur)) return key_to_float(__reduce_min_sync(kFull, fkey(cur)));
+    return warp_min_tree(cur);
+}
+
+// Pulls cluster c's rotated centroid rows (every segment, 4 * Dtot bytes) into
+// L2 ahead of its prepare_cluster: thread tid of nt takes the 128-byte lines
+// tid, tid + nt, ... of the rows laid end to end.
+__device__ __forceinline__ void prefetch_centroid(const DevIndexView &ix, int c, int tid, int nt) {
+    for (int s = 0, first = 0; s < ix.S; ++s) {
+        const SegDev &g = ix.seg[s];
+        const char *row = reinterpret_cast<const char *>(g.cent + (size_t)c * g.dim);
+        const int lines = (4 * g.dim + 127) / 128;
+        int l = tid - first;  // first line of this row that is the thread's
+        if (l < 0) l += (-l + nt - 1) / nt * nt;
+        for (; l < lines; l += nt) asm volatile("prefetch.global.L2 [%0];" ::"l"(row + 128 * l));
+        first += lines;
+    }
 }
 
 // Estimates of one block (this warp, lane = vector).  Fills cd/ipx for every
@@ -1076,7 +1106,7 @@ __device__ void block_estimates(const DevIndexView &ix, int64_t gb, ScanSmem &sm
         cur = __fadd_rn(cur, v);
     }
     int k = 0;
-    float mi = warp_min_tree(cur);
+    float mi = block_min(cur);
     if (lane == 0) sm.stage[w * (S + 1) + k] = mi;
     ++k;
     for (int s = 0; s < S && !(mi > tau); ++s) {  // mi is warp-uniform
@@ -1089,7 +1119,7 @@ __device__ void block_estimates(const DevIndexView &ix, int64_t gb, ScanSmem &sm
         sm.cd[(w * S + s) * 32 + lane] = f;
         sm.ipx[(w * S + s) * 32 + lane] = ipx;
         cur = __fadd_rn(cur, f);
-        mi = warp_min_tree(cur);
+        mi = block_min(cur);
         if (lane == 0) sm.stage[w * (S + 1) + k] = mi;
         ++k;
     }
@@ -1341,6 +1371,34 @@ __device__ __forceinline__ void replay_block_warp(int S, int bb, const float *cu
     }
 }
 
+// The reference's decisions for the nblk (<= 32) blocks of a tile, in order, by
+// one warp: lane i first reads block i's candidate mask and (several segments)
+// the largest of its stage minima, and a ballot keeps the blocks that can
+// change the pool under the distk at the tile's start.  distk only decreases,
+// so a block dropped here (no candidate lane, or a stage minimum above distk)
+// would be skipped by replay_block_warp as well; the rest are replayed in order.
+// Returns the tile's candidate lanes (for the tally).
+__device__ __forceinline__ unsigned replay_tile_warp(int S, int t0, int nblk, const ScanSmem &v, const uint32_t *ids_v0,
+                                                     uint32_t *pid, float *pd, int &sz, int topk, float &dk,
+                                                     unsigned long long &c_rr) {
+    const int lane = threadIdx.x & 31;
+    uint32_t cm = 0;
+    float smax = 0.0f;
+    if (lane < nblk) {
+        cm = v.cmask[lane];
+        if (S > 1 && cm) smax = stage_max(v.stage + lane * (S + 1), v.nstage[lane]);
+    }
+    uint32_t live = __ballot_sync(kFull, cm != 0 && !(S > 1 && smax > dk));
+    while (live) {
+        const int ww = __ffs(live) - 1;
+        live &= live - 1;
+        replay_block_warp(S, t0 + ww, v.cur + ww * 32, __shfl_sync(kFull, smax, ww),
+                          S == 1 ? v.part + ww * 32 : v.part + ww * S * 32, __shfl_sync(kFull, cm, ww), ids_v0, pid, pd,
+                          sz, topk, dk, c_rr);
+    }
+    return __reduce_add_sync(kFull, __popc(cm));
+}
+
 // Whether k_scan builds the next cluster's LUT during the last replay of the
 // current one (double-buffered cluster state).  Off: the overlap's extra
 // registers cost more occupancy than the overlap gains.
@@ -1373,22 +1431,19 @@ __device__ void scan_probes(const DevIndexView &ix, const uint32_t *__restrict__
         const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
         const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
         const bool ahead = dbuf && p + 1 < p_end;  // build the next cluster's state during the last replay
+        if (p + 1 < p_end) prefetch_centroid(ix, (int)probe[p + 1], tid, blockDim.x);
         tl.blocks += nb;
         tl.vecs += n;
         for (int t0 = 0; t0 < nb; t0 += kTileB) {
             tile_candidates(ix, v, b0, v0, nb, n, t0, nb, distk);
             const bool last = t0 + kTileB >= nb;
             if (tid < 32) {
-                if (tid == 0)
-                    for (int i = 0; i < kTileB; ++i) tl.spec += __popc(sm.cmask[i]);
                 float dk = distk;
                 int sz = pool_size;
-                for (int ww = 0; ww < kTileB && t0 + ww < nb; ++ww)
-                    replay_block_warp(S, t0 + ww, sm.cur + ww * 32,
-                                      S == 1 ? 0.0f : stage_max(sm.stage + ww * (S + 1), sm.nstage[ww]),
-                                      S == 1 ? sm.part + ww * 32 : sm.part + ww * S * 32, sm.cmask[ww], ix.ids + v0,
-                                      sm.pool_id, sm.pool_d, sz, topk, dk, tl.rr);
+                const unsigned nc = replay_tile_warp(S, t0, min(kTileB, nb - t0), sm, ix.ids + v0, sm.pool_id, sm.pool_d,
+                                                     sz, topk, dk, tl.rr);
                 if (tid == 0) {
+                    tl.spec += nc;
                     distk = dk;
                     pool_size = sz;
                 }
@@ -1490,14 +1545,15 @@ __device__ __forceinline__ void named_arrive(int id, int n) {
     asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_ws(DevIndexView ix, const uint32_t *__restrict__ probe,
+__global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_ws(DevIndexView ix, const uint32_t *__restrict__ probe,
                                                           QueryShape qsh, const float *__restrict__ qrot_all,
                                                           const float *__restrict__ prune_all,
                                                           uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
                                                           unsigned long long *__restrict__ counters, int xstride,
-                                                          const uint8_t *__restrict__ deferred) {
+                                                          const uint8_t *__restrict__ deferred,
+                                                          const int *__restrict__ order) {
     extern __shared__ __align__(16) char smem_raw[];
-    const int qi = blockIdx.x;
+    const int qi = order ? order[blockIdx.x] : (int)blockIdx.x;
     if (deferred && deferred[qi]) return;  // answered by the split pass
     const int np = qsh.np_of(qi), topk = qsh.k_of(qi), S = ix.S, tid = threadIdx.x;
     ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, qsh.k_max, xstride, false);
@@ -1550,15 +1606,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_ws(DevIndexView ix, const
                 named_sync(2 + b, kScanThreads);  // tile ntiles written
                 const ScanSmem v = ws_view(sm, extra, S, b);
                 const WsTile mt = meta[b];
-                const int cnt = min(kWsSlots, nb - mt.t0);
-                if (tid == 0)
-                    for (int i = 0; i < cnt; ++i) spec += __popc(v.cmask[i]);
-                for (int ww = 0; ww < cnt; ++ww)
-                    replay_block_warp(S, mt.t0 + ww, v.cur + ww * 32,
-                                      S == 1 ? 0.0f : stage_max(v.stage + ww * (S + 1), v.nstage[ww]),
-                                      S == 1 ? v.part + ww * 32 : v.part + ww * S * 32, v.cmask[ww], ix.ids + mt.v0,
-                                      sm.pool_id, sm.pool_d, sz, topk, dk, rr);
+                const unsigned nc = replay_tile_warp(S, mt.t0, min(kWsSlots, nb - mt.t0), v, ix.ids + mt.v0,
+                                                     sm.pool_id, sm.pool_d, sz, topk, dk, rr);
                 if (tid == 0) {
+                    spec += nc;
                     *vdistk = dk;
                     pool_size = sz;
                 }
@@ -1816,6 +1867,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_scan_warp(DevIndexView ix
 // reference's decisions on the records.  Blocks without a record cannot insert
 // anything (none of their lanes is below tau1 >= distk), so the replay is exact.
 constexpr int kTileBlocks = 16;
+constexpr int kSpecChunk = 8;  // speculative tiles per work chunk of k_scan_spec
 constexpr int kFirstBlocks = 16;  // exact prefix of a deferred query (its distk bounds the first level)
 // Levels of the speculation for deferred queries, in tiles after the split
 // point: [0, 8), [8, 64), [64, end) by default; the autotuner may pick another
@@ -1835,6 +1887,7 @@ constexpr int kDeferBlocks = 1024;  // a query scanning more blocks than this ta
 
 struct SplitState {
     int *nlist;          // number of queries on the list (device)
+    int *work_next;      // next chunk of the level's speculative tiles (reset by k_tile_prefix)
     int *qlist;          // [cap] slot -> query id
     int cap;             // slots
     uint32_t *pool_id;   // [cap][topk]
@@ -1881,7 +1934,7 @@ __host__ __device__ inline int rec_words_of(int S) { return (8 + (S + 1) + 32 + 
 
 __device__ __forceinline__ int list_len(const SplitState &st) { return min(*st.nlist, st.cap); }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, const uint32_t *__restrict__ probe,
+__global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_first(DevIndexView ix, const uint32_t *__restrict__ probe,
                                                              const float *__restrict__ qrot_all,
                                                              const float *__restrict__ prune_all, SplitState st, int *__restrict__ err,
                                                              unsigned long long *__restrict__ counters, int xstride) {
@@ -1922,16 +1975,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
             tl.vecs += min(n, te * 32) - t0 * 32;
             tile_candidates(ix, sm, b0, v0, nb, n, t0, nb, distk);
             if (tid < 32) {
-                if (tid == 0)
-                    for (int i = 0; i < kTileB; ++i) tl.spec += __popc(sm.cmask[i]);
                 float dk = distk;
                 int sz = pool_size;
-                for (int ww = 0; ww < kTileB && t0 + ww < nb; ++ww)
-                    replay_block_warp(S, t0 + ww, sm.cur + ww * 32,
-                                      S == 1 ? 0.0f : stage_max(sm.stage + ww * (S + 1), sm.nstage[ww]),
-                                      S == 1 ? sm.part + ww * 32 : sm.part + ww * S * 32, sm.cmask[ww], ix.ids + v0,
-                                      sm.pool_id, sm.pool_d, sz, topk, dk, tl.rr);
+                const unsigned nc = replay_tile_warp(S, t0, te - t0, sm, ix.ids + v0, sm.pool_id, sm.pool_d, sz, topk, dk,
+                                                     tl.rr);
                 if (tid == 0) {
+                    tl.spec += nc;
                     distk = dk;
                     pool_size = sz;
                 }
@@ -1966,20 +2015,50 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_first(DevIndexView ix, co
 }
 
 // Work offsets of the level's tiles: slot q holds tiles [t_lo, t_hi) of its own.
-__global__ void k_tile_prefix(SplitState st) {
-    const int nprobe = st.qsh.np_max;
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// One CTA of kPrefixThreads: each thread sums a contiguous run of slots, a
+// block-wide exclusive scan of the run sums, then each run is written.
+constexpr int kPrefixThreads = 1024;
+__global__ void __launch_bounds__(kPrefixThreads) k_tile_prefix(SplitState st) {
+    __shared__ int wsum[kPrefixThreads / 32];
+    const int nprobe = st.qsh.np_max, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int n = list_len(st);
-    int acc = 0;
-    for (int q = 0; q < n; ++q) {
-        st.q_tile_off[q] = acc;
+    const int per = (n + kPrefixThreads - 1) / kPrefixThreads, q0 = min(n, tid * per), q1 = min(n, q0 + per);
+    auto count = [&](int q) {
         const int nt = st.tile_off[(size_t)q * (nprobe + 1) + nprobe];
-        acc += max(0, min(nt, st.t_hi) - min(nt, st.t_lo));
+        return max(0, min(nt, st.t_hi) - min(nt, st.t_lo));
+    };
+    int run = 0;
+    for (int q = q0; q < q1; ++q) run += count(q);
+    int x = run;  // inclusive scan within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
-    st.q_tile_off[n] = acc;
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int v = wsum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        wsum[lane] = v;  // inclusive over warps
+    }
+    __syncthreads();
+    int acc = x - run + (w ? wsum[w - 1] : 0);
+    for (int q = q0; q < q1; ++q) {
+        st.q_tile_off[q] = acc;
+        acc += count(q);
+    }
+    if (tid == kPrefixThreads - 1) {
+        st.q_tile_off[n] = wsum[kPrefixThreads / 32 - 1];
+        *st.work_next = 0;
+    }
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, const uint32_t *__restrict__ probe,
+__global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_spec(DevIndexView ix, const uint32_t *__restrict__ probe,
                                                             int nprobe, const float *__restrict__ qrot_all,
                                                             const float *__restrict__ prune_all, SplitState st,
                                                             unsigned long long *__restrict__ counters, int xstride) {
@@ -1989,83 +2068,91 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_spec(DevIndexView ix, con
     ScanTally tl;
     const int nl = list_len(st);
     const int total = st.q_tile_off[nl];
-    // contiguous work ranges per CTA keep the tiles of one cluster together (LUT reuse)
-    const int per = (total + gridDim.x - 1) / gridDim.x;
-    const int w_begin = blockIdx.x * per, w_end = min(total, w_begin + per);
+    // chunks of kSpecChunk consecutive tiles (mostly of one cluster: one LUT)
+    // taken from a shared counter: tiles differ widely in cost (candidates,
+    // pruning stages), so equal shares per CTA leave a long tail
+    __shared__ int chunk;
     int last_slot = -1, last_c = -1;
-    for (int wi = w_begin; wi < w_end; ++wi) {
-        int lo = 0, hi = nl;  // slot: last with q_tile_off[slot] <= wi
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (st.q_tile_off[mid] <= wi) lo = mid;
-            else hi = mid;
-        }
-        const int slot = lo, q = st.qlist[slot];
-        const int local = st.t_lo + (wi - st.q_tile_off[slot]);
-        const int *to = st.tile_off + (size_t)slot * (nprobe + 1);
-        int plo = 0, phi = nprobe;  // probe: last p with to[p] <= local
-        while (phi - plo > 1) {
-            const int mid = (plo + phi) >> 1;
-            if (to[mid] <= local) plo = mid;
-            else phi = mid;
-        }
-        const int p = plo, tile = local - to[p];
-        const int c = (int)probe[(size_t)q * nprobe + p];
-        if (slot != last_slot || c != last_c) {  // LUTs survive across tiles of one cluster
-            prepare_cluster(ix, qrot_all + (size_t)q * ix.Dtot, prune_all + (size_t)q * S, c, sm);
-            last_slot = slot;
-            last_c = c;
-        }
-        const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
-        const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
-        const int first = p == st.split_p[slot] ? st.split_b[slot] : 0;
-        const int bstart = first + tile * kTileBlocks, bend = min(nb, bstart + kTileBlocks);
-        if (tid == 0) {
-            tl.blocks += bend - bstart;
-            tl.vecs += min(n, bend * 32) - bstart * 32;
-        }
-        const float tau = st.tau[slot];
-        const int64_t base = st.blk_base[(size_t)slot * nprobe + p];
-        for (int t0 = bstart; t0 < bend; t0 += kTileB) {
-            tile_candidates(ix, sm, b0, v0, nb, n, t0, bend, tau);
-            const int lane = tid & 31;
-            for (int k = 0; k < kBlocksPerWarp; ++k) {
-                const int w = (tid >> 5) + k * kScanWarps, b = t0 + w;
-                if (b < bend) {
-                    const uint32_t cm = sm.cmask[w];
-                    const int64_t pos = base + b;
-                    if (cm && pos < st.npos[slot]) {
-                        float *r = st.rec + (size_t)(st.pos_off[slot] + pos) * st.rec_words;
-                        uint32_t *ri = reinterpret_cast<uint32_t *>(r);
-                        // summary: a later distk below the minimum estimate, or below a stage minimum,
-                        // leaves the block without effect
-                        float mn = ((cm >> lane) & 1u) ? sm.cur[w * 32 + lane] : __int_as_float(0x7fffffff);
-                        float mx = (S > 1 && lane < sm.nstage[w]) ? sm.stage[w * (S + 1) + lane] : __int_as_float(0x7fffffff);
-#pragma unroll
-                        for (int o = 16; o; o >>= 1) {
-                            mn = fminf(mn, __shfl_xor_sync(kFull, mn, o));
-                            mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+    for (;;) {
+        if (tid == 0) chunk = atomicAdd(st.work_next, 1);
+        __syncthreads();
+        const int w_begin = chunk * kSpecChunk, w_end = min(total, w_begin + kSpecChunk);
+        __syncthreads();  // every thread has read `chunk` before thread 0 takes the next
+        if (w_begin >= total) break;
+        for (int wi = w_begin; wi < w_end; ++wi) {
+            int lo = 0, hi = nl;  // slot: last with q_tile_off[slot] <= wi
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (st.q_tile_off[mid] <= wi) lo = mid;
+                else hi = mid;
+            }
+            const int slot = lo, q = st.qlist[slot];
+            const int local = st.t_lo + (wi - st.q_tile_off[slot]);
+            const int *to = st.tile_off + (size_t)slot * (nprobe + 1);
+            int plo = 0, phi = nprobe;  // probe: last p with to[p] <= local
+            while (phi - plo > 1) {
+                const int mid = (plo + phi) >> 1;
+                if (to[mid] <= local) plo = mid;
+                else phi = mid;
+            }
+            const int p = plo, tile = local - to[p];
+            const int c = (int)probe[(size_t)q * nprobe + p];
+            if (slot != last_slot || c != last_c) {  // LUTs survive across tiles of one cluster
+                prepare_cluster(ix, qrot_all + (size_t)q * ix.Dtot, prune_all + (size_t)q * S, c, sm);
+                last_slot = slot;
+                last_c = c;
+            }
+            const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
+            const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
+            const int first = p == st.split_p[slot] ? st.split_b[slot] : 0;
+            const int bstart = first + tile * kTileBlocks, bend = min(nb, bstart + kTileBlocks);
+            if (tid == 0) {
+                tl.blocks += bend - bstart;
+                tl.vecs += min(n, bend * 32) - bstart * 32;
+            }
+            const float tau = st.tau[slot];
+            const int64_t base = st.blk_base[(size_t)slot * nprobe + p];
+            for (int t0 = bstart; t0 < bend; t0 += kTileB) {
+                tile_candidates(ix, sm, b0, v0, nb, n, t0, bend, tau);
+                const int lane = tid & 31;
+                for (int k = 0; k < kBlocksPerWarp; ++k) {
+                    const int w = (tid >> 5) + k * kScanWarps, b = t0 + w;
+                    if (b < bend) {
+                        const uint32_t cm = sm.cmask[w];
+                        const int64_t pos = base + b;
+                        if (cm && pos < st.npos[slot]) {
+                            float *r = st.rec + (size_t)(st.pos_off[slot] + pos) * st.rec_words;
+                            uint32_t *ri = reinterpret_cast<uint32_t *>(r);
+                            // summary: a later distk below the minimum estimate, or below a stage minimum,
+                            // leaves the block without effect
+                            float mn = ((cm >> lane) & 1u) ? sm.cur[w * 32 + lane] : __int_as_float(0x7fffffff);
+                            float mx = (S > 1 && lane < sm.nstage[w]) ? sm.stage[w * (S + 1) + lane] : __int_as_float(0x7fffffff);
+    #pragma unroll
+                            for (int o = 16; o; o >>= 1) {
+                                mn = fminf(mn, __shfl_xor_sync(kFull, mn, o));
+                                mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+                            }
+                            if (lane == 0) {
+                                ri[0] = (uint32_t)pos;
+                                ri[1] = cm;
+                                ri[2] = (uint32_t)(S == 1 ? 0 : sm.nstage[w]);
+                                ri[3] = (uint32_t)c;
+                                ri[4] = (uint32_t)b;
+                                ri[5] = (uint32_t)(uint64_t)v0;
+                                ri[6] = (uint32_t)((uint64_t)v0 >> 32);
+                                ri[7] = __float_as_uint(mx);
+                                st.summ[st.pos_off[slot] + pos] = make_float2(mn, mx);
+                                if (counters) atomicAdd(counters + 3, (unsigned long long)__popc(cm));
+                            }
+                            if (S > 1 && lane <= S) r[8 + lane] = sm.stage[w * (S + 1) + lane];
+                            r[8 + (S + 1) + lane] = sm.cur[w * 32 + lane];
+                            for (int s = 0; s < S; ++s)
+                                r[8 + (S + 1) + 32 + s * 32 + lane] = sm.part[(w * S + s) * 32 + lane];
                         }
-                        if (lane == 0) {
-                            ri[0] = (uint32_t)pos;
-                            ri[1] = cm;
-                            ri[2] = (uint32_t)(S == 1 ? 0 : sm.nstage[w]);
-                            ri[3] = (uint32_t)c;
-                            ri[4] = (uint32_t)b;
-                            ri[5] = (uint32_t)(uint64_t)v0;
-                            ri[6] = (uint32_t)((uint64_t)v0 >> 32);
-                            ri[7] = __float_as_uint(mx);
-                            st.summ[st.pos_off[slot] + pos] = make_float2(mn, mx);
-                            if (counters) atomicAdd(counters + 3, (unsigned long long)__popc(cm));
-                        }
-                        if (S > 1 && lane <= S) r[8 + lane] = sm.stage[w * (S + 1) + lane];
-                        r[8 + (S + 1) + lane] = sm.cur[w * 32 + lane];
-                        for (int s = 0; s < S; ++s)
-                            r[8 + (S + 1) + 32 + s * 32 + lane] = sm.part[(w * S + s) * 32 + lane];
                     }
                 }
+                __syncthreads();
             }
-            __syncthreads();
         }
     }
     if (tid == 0 && counters) {
@@ -2271,14 +2358,15 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, S
 
 // One CTA per query: the whole probe list sequentially (queries deferred to
 // the split pass are skipped).
-__global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const uint32_t *__restrict__ probe,
+__global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan(DevIndexView ix, const uint32_t *__restrict__ probe,
                                                        QueryShape qsh, const float *__restrict__ qrot_all,
                                                        const float *__restrict__ prune_all,
                                                        uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
                                                        int *__restrict__ err, unsigned long long *__restrict__ counters,
-                                                       int xstride, const uint8_t *__restrict__ deferred) {
+                                                       int xstride, const uint8_t *__restrict__ deferred,
+                                                       const int *__restrict__ order) {
     extern __shared__ __align__(16) char smem_raw[];
-    const int qi = blockIdx.x;
+    const int qi = order ? order[blockIdx.x] : (int)blockIdx.x;
     if (deferred && deferred[qi]) return;  // answered by the split pass
     const int np = qsh.np_of(qi), topk = qsh.k_of(qi);
     ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, qsh.k_max, xstride, kScanOverlap);
@@ -2291,6 +2379,39 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DevIndexView ix, const ui
     flush_tally(tl, counters);
     write_results(sm, pool_size, topk, qsh.k_max, out_ids + (size_t)qi * qsh.k_max,
                   out_d ? out_d + (size_t)qi * qsh.k_max : nullptr);
+}
+
+// Launch order of the CTA scan, heaviest queries first (blocks of their probes,
+// in power-of-two classes; the order inside a class is arbitrary), so that a
+// long query does not start in the last wave.  One CTA of kOrderThreads.
+constexpr int kOrderThreads = 1024;
+constexpr int kOrderMinQueries = 1024;  // batches from which the CTA scan is launched heaviest first
+__global__ void __launch_bounds__(kOrderThreads) k_order(DevIndexView ix, const uint32_t *__restrict__ probe, QueryShape qsh,
+                                                         int nq, int *__restrict__ order) {
+    __shared__ int cnt[32], cur[32];
+    const int tid = threadIdx.x;
+    if (tid < 32) cnt[tid] = 0;
+    __syncthreads();
+    auto cls = [&](int qi) {
+        int64_t total = 0;
+        const int np = qsh.np_of(qi);
+        for (int p = 0; p < np; ++p) {
+            const int c = (int)probe[(size_t)qi * qsh.np_max + p];
+            total += ix.blk_off[c + 1] - ix.blk_off[c];
+        }
+        return 31 - min(31, 63 - __clzll((long long)total + 1));  // heavier: smaller class
+    };
+    for (int qi = tid; qi < nq; qi += kOrderThreads) atomicAdd(&cnt[cls(qi)], 1);
+    __syncthreads();
+    if (tid == 0) {
+        int acc = 0;
+        for (int k = 0; k < 32; ++k) {
+            cur[k] = acc;
+            acc += cnt[k];
+        }
+    }
+    __syncthreads();
+    for (int qi = tid; qi < nq; qi += kOrderThreads) order[atomicAdd(&cur[cls(qi)], 1)] = qi;
 }
 
 // Puts every query whose probes hold more than `defer_blocks` blocks (a giant
@@ -2405,6 +2526,7 @@ size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t np
     add(2 * (size_t)nq * I.D);                 // BF16 queries (probe GEMM)
     add((size_t)nq);                           // shortlist: queries on the full exact path
     add(4 * (size_t)nq);                       // ... and their list
+    add(4 * (size_t)nq);                       // CTA scan launch order
     add(4 * (size_t)nq * topk * 2);            // outputs (host io)
     add(4 * (size_t)nq * 2);                   // per-query nprobe / k
     add(64);                                   // flags
@@ -2416,7 +2538,7 @@ size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t np
 size_t split_scratch_bytes(const Index &I, int64_t cap, int64_t topk, int64_t nprobe, int64_t pos_cap) {
     size_t b = 0;
     auto add = [&](size_t x) { b += align16(x); };
-    add(4 * 16);                                 // nlist, pos_used
+    add(4 * 16);                                 // nlist, pos_used, work_next
     add(4 * (size_t)cap);                        // qlist
     add(4 * (size_t)cap * topk);
     add(4 * (size_t)cap * topk);
@@ -2515,19 +2637,24 @@ void ensure_smem(const void *fn, size_t bytes) {
 // its warp-specialised form k_scan_ws, which gives the same answers.
 void launch_cta_scan(bool ws, const DevIndexView &ix, const uint32_t *probe, const QueryShape &qsh, const float *qrot,
                      const float *prune, uint32_t *ids, float *d, int *err, unsigned long long *cnt, int xs,
-                     const uint8_t *deferred, int64_t nq, cudaStream_t st) {
+                     const uint8_t *deferred, int64_t nq, int *order, cudaStream_t st) {
+    if (order) {
+        k_order<<<1, kOrderThreads, 0, st>>>(ix, probe, qsh, (int)nq, order);
+        check_launch("k_order");
+    }
     if (ws) {
         const size_t smem = ws_smem_bytes(ix.Dtot, ix.S, qsh.k_max, xs);
         SAQG_REQUIRE(smem <= 220 * 1024, "dimension / topk too large for the scan kernel's shared memory");
         ensure_smem((const void *)k_scan_ws, smem);
-        k_scan_ws<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, qsh, qrot, prune, ids, d, cnt, xs, deferred);
+        k_scan_ws<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, qsh, qrot, prune, ids, d, cnt, xs, deferred,
+                                                             order);
         check_launch("k_scan_ws");
         return;
     }
     const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, qsh.k_max, xs, kScanOverlap);
     SAQG_REQUIRE(smem <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
     ensure_smem((const void *)k_scan, smem);
-    k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, qsh, qrot, prune, ids, d, err, cnt, xs, deferred);
+    k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, qsh, qrot, prune, ids, d, err, cnt, xs, deferred, order);
     check_launch("k_scan");
 }
 
@@ -2711,6 +2838,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
     void *qbf = bp.take<uint16_t>((size_t)nq * I.D);
     uint8_t *full = bp.take<uint8_t>((size_t)nq);
     int *fb_list = bp.take<int>((size_t)nq);
+    // heaviest queries first once the CTA scan runs in several waves
+    int *order = nq >= kOrderMinQueries ? bp.take<int>((size_t)nq) : nullptr;
     uint32_t *oid = bp.take<uint32_t>((size_t)nq * topk);
     float *od = bp.take<float>((size_t)nq * topk);
     int *flags = bp.take<int>(16);
@@ -2796,7 +2925,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             // no query of this call can probe more blocks than the deferral
             // threshold: the CTA scan answers every query, no split pass
             launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, flags + 1, cnt, xs, nullptr, nq,
-                            st);
+                            order, st);
             count_launch(4);
         } else {
             // split-pass state: every query (mode 1), or the deferred giant-cluster queries (mode 0)
@@ -2808,6 +2937,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             SplitState ss;
             ss.nlist = sb.take<int>(16);
             ss.pos_used = reinterpret_cast<unsigned long long *>(ss.nlist + 2);
+            ss.work_next = ss.nlist + 4;
             ss.qlist = sb.take<int>(cap);
             ss.cap = (int)cap;
             ss.pool_id = sb.take<uint32_t>((size_t)cap * topk);
@@ -2835,7 +2965,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             if (const char *e = std::getenv("SAQG_FIRST_BLOCKS")) ss.first_blocks = std::max(1, std::atoi(e));
             uint8_t *deferred = sb.take<uint8_t>(nq);
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.summ, 0xff, 8 * (size_t)pos_cap, st));  // NaN: no record
-            SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 16, st));
+            SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 32, st));
             int defer = -1;  // mode 1: every query
             if (mode == 0) defer = defer_threshold(tune);
             k_defer<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(ix, probe, (int)nq, defer, ss, deferred);
@@ -2850,7 +2980,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                     SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, C.fork_event(), 0));
                 }
                 launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, flags + 1, cnt, xs,
-                                deferred, nq, st);
+                                deferred, nq, order, st);
             }
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
             const size_t smem_r = smem + 2 * 4 * (size_t)kReplayRecs * ss.rec_words;
@@ -2874,7 +3004,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                 sl.t_lo = mode == 0 ? levels[L] : 0;
                 sl.t_hi = L + 1 < nlev ? levels[L + 1] : INT_MAX;
                 sl.final_level = L + 1 == nlev;
-                k_tile_prefix<<<1, 32, 0, sp>>>(sl);
+                k_tile_prefix<<<1, kPrefixThreads, 0, sp>>>(sl);
                 check_launch("k_tile_prefix");
                 k_scan_spec<<<grid, kScanThreads, smem1, sp>>>(ix, probe, (int)nprobe, qrot, prune, sl, cnt, xs);
                 check_launch("k_scan_spec");
@@ -3131,7 +3261,7 @@ void run_search_static(const Index &I, const float *q, int64_t nq, int64_t topk,
     qsh.np_max = (int)nprobe;
     qsh.k_max = (int)topk;
     k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, qsh, qrot, prune, ids, dists,
-                                                      flags + 1, nullptr, xstride_of(ix), nullptr);
+                                                      flags + 1, nullptr, xstride_of(ix), nullptr, nullptr);
     check_launch("k_scan");
     count_launch(4);
 }

@@ -46,3 +46,27 @@ def test_mixed_nprobe_and_k(built, mode, defer, nq, monkeypatch):
         assert np.array_equal(ids[i, :ks[i]], oids[0]), i
         assert np.array_equal(d[i, :ks[i]].view(np.uint32), od[0].view(np.uint32)), i
         assert np.all(ids[i, ks[i]:] == 0) and np.all(np.isinf(d[i, ks[i]:]) | (d[i, ks[i]:] == np.float32(3.4028235e38)))
+
+
+@pytest.mark.parametrize("mode,defer", [(None, None), ("seq", "1"), ("seq", "0"), ("ws", "0")])
+def test_large_batch_heaviest_first(built, mode, defer, monkeypatch):
+    """Batches of 1,024 queries and more launch the CTA scan heaviest query
+    first; every answer must still be the oracle's, uniform and uneven shapes."""
+    index, oi, q = built
+    if mode:
+        monkeypatch.setenv("SAQG_SCAN_MODE", mode)
+    if defer:
+        monkeypatch.setenv("SAQG_DEFER_BLOCKS", defer)
+    rng = np.random.default_rng(11)
+    nq = 1500
+    qq = (q[rng.integers(0, q.shape[0], size=nq)] + rng.normal(0, 0.05, size=(nq, q.shape[1]))).astype(np.float32)
+    ids, d = index.search(qq, 10, 24, return_dists=True)
+    oids, od = oi.search(qq, 10, 24, with_dists=True)
+    assert np.array_equal(ids, oids)
+    assert np.array_equal(d.view(np.uint32), od.view(np.uint32))
+    nps = rng.integers(4, 41, size=nq).astype(np.int32)
+    ids, d = index.search(qq, 10, nps, return_dists=True)
+    for i in range(0, nq, 7):
+        oids, od = oi.search(qq[i:i + 1], 10, int(nps[i]), with_dists=True)
+        assert np.array_equal(ids[i], oids[0]), i
+        assert np.array_equal(d[i].view(np.uint32), od[0].view(np.uint32)), i
