@@ -864,33 +864,12 @@ struct ScanSmem {
     uint32_t *mm;     // per segment LUT min / max keys
     uint8_t *xbuf;    // per half-warp ex-code staging
     int xstride;
-    // second cluster state (LUT, residual query, scalars) for building the next
-    // cluster's while the current one finishes; null unless laid out with dbuf
-    uint16_t *lut2;
-    float *qres2;
-    SegScal *scal2;
 };
-
-// The cluster state `buf` (0 or 1) of a double-buffered layout.
-__device__ __forceinline__ ScanSmem cluster_view(const ScanSmem &sm, int buf) {
-    ScanSmem v = sm;
-    if (buf) {
-        v.lut = sm.lut2;
-        v.qres = sm.qres2;
-        v.scal = sm.scal2;
-    }
-    return v;
-}
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
-__host__ __device__ inline size_t scan_smem_bytes(int Dtot, int S, int topk, int xstride, bool dbuf = false) {
+__host__ __device__ inline size_t scan_smem_bytes(int Dtot, int S, int topk, int xstride) {
     size_t b = 0;
-    if (dbuf) {
-        b += align16(sizeof(uint16_t) * 4 * (size_t)Dtot);
-        b += align16(sizeof(float) * Dtot);
-        b += align16(sizeof(SegScal) * S);
-    }
     b += align16(sizeof(uint32_t) * 2 * S);
     b += align16((size_t)2 * kScanWarps * xstride);
     b += align16(sizeof(uint16_t) * 4 * (size_t)Dtot);
@@ -906,20 +885,9 @@ __host__ __device__ inline size_t scan_smem_bytes(int Dtot, int S, int topk, int
     return b;
 }
 
-__device__ ScanSmem scan_smem_layout(char *base, int Dtot, int S, int topk, int xstride, bool dbuf = false) {
+__device__ ScanSmem scan_smem_layout(char *base, int Dtot, int S, int topk, int xstride) {
     ScanSmem s;
     size_t o = 0;
-    s.lut2 = nullptr;
-    s.qres2 = nullptr;
-    s.scal2 = nullptr;
-    if (dbuf) {
-        s.lut2 = (uint16_t *)(base + o);
-        o += align16(sizeof(uint16_t) * 4 * (size_t)Dtot);
-        s.qres2 = (float *)(base + o);
-        o += align16(sizeof(float) * Dtot);
-        s.scal2 = (SegScal *)(base + o);
-        o += align16(sizeof(SegScal) * S);
-    }
     s.mm = (uint32_t *)(base + o);
     o += align16(sizeof(uint32_t) * 2 * S);
     s.xbuf = (uint8_t *)(base + o);
@@ -949,6 +917,57 @@ __device__ ScanSmem scan_smem_layout(char *base, int Dtot, int S, int topk, int 
     o += align16(sizeof(uint32_t) * (topk + 1));
     s.pool_d = (float *)(base + o);
     return s;
+}
+
+// ---- pieces of Lut::prepare (lut.hpp:60-87) shared by the in-CTA preparation
+// (prepare_cluster) and the batched one (k_lut), so both give the same bits.
+// The quantizer's scale from the segment's LUT min / max keys.
+__device__ __forceinline__ void seg_quant_scalars(uint32_t kmin, uint32_t kmax, SegScal &sc) {
+    const float vl = key_to_float(kmin), vr = key_to_float(kmax);
+    const float delta = (float)__ddiv_rn((double)__fsub_rn(vr, vl), 65536.0 - 0.01);
+    sc.delta = delta;
+    sc.rdelta = __frcp_rn(delta);
+    sc.vl = vl;
+}
+
+// compFastIP's epilogue constants (sum_q, q_l2sqr, vl and delta already set).
+__device__ __forceinline__ void seg_epilogue_scalars(const SegDev &g, float prune_s, SegScal &sc) {
+    const int ncb = g.dim / 4;
+    sc.sum_vl = (float)__dmul_rn(__dadd_rn((double)sc.vl, __dmul_rn(0.5, (double)sc.delta)), (double)(float)ncb);
+    sc.q_l2norm = sqrtf(sc.q_l2sqr);
+    sc.c1 = (float)__dsub_rn(__dmul_rn(0.5, (double)sc.sum_q), (double)__fmul_rn(0.58f, sc.q_l2norm));
+    sc.c2 = g.c2;
+    sc.vfac = __fsub_rn(sc.q_l2sqr, __fmul_rn(2.0f, prune_s));
+}
+
+// The 16 u16 entries of one codebook (4 residual dims at qq), 32 bytes at dst.
+__device__ __forceinline__ void quant_codebook(const float *qq, float vl, float delta, float rd, uint16_t *dst) {
+    float t[16];
+    lut_entries(qq, t);
+    uint32_t packed[8];
+#pragma unroll
+    for (int j = 0; j < 16; j += 2) {
+        const uint32_t a = lut_quant(__fsub_rn(t[j], vl), rd, delta);
+        const uint32_t b = lut_quant(__fsub_rn(t[j + 1], vl), rd, delta);
+        packed[j / 2] = a | (b << 16);
+    }
+    uint4 *d = reinterpret_cast<uint4 *>(dst);
+    d[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+    d[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+}
+
+// Min and max keys of one codebook's float entries.
+__device__ __forceinline__ void codebook_keys(const float *qq, uint32_t &kmin, uint32_t &kmax) {
+    float t[16];
+    lut_entries(qq, t);
+    float lo = t[0], hi = t[0];
+#pragma unroll
+    for (int j = 1; j < 16; ++j) {
+        lo = fminf(lo, t[j]);
+        hi = fmaxf(hi, t[j]);
+    }
+    kmin = fkey(lo);
+    kmax = fkey(hi);
 }
 
 // Lut::prepare (lut.hpp:60-87) for every segment of cluster c, spread over the
@@ -994,16 +1013,7 @@ __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict_
         if (cb < ncb_all) {
             s = 0;
             while (s + 1 < S && cb * 4 >= ix.seg[s + 1].qoff) ++s;
-            float t[16];
-            lut_entries(sm.qres + cb * 4, t);
-            float lo = t[0], hi = t[0];
-#pragma unroll
-            for (int j = 1; j < 16; ++j) {
-                lo = fminf(lo, t[j]);
-                hi = fmaxf(hi, t[j]);
-            }
-            kmin = fkey(lo);
-            kmax = fkey(hi);
+            codebook_keys(sm.qres + cb * 4, kmin, kmax);
         }
         // one shared atomic per segment present in the warp
         const unsigned grp = __match_any_sync(kFull, s);
@@ -1015,43 +1025,104 @@ __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict_
         }
     }
     sync();
-    if (tid < S) {  // what the quantizer needs
-        SegScal &sc = sm.scal[tid];
-        const float vl = key_to_float(sm.mm[2 * tid]), vr = key_to_float(sm.mm[2 * tid + 1]);
-        const float delta = (float)__ddiv_rn((double)__fsub_rn(vr, vl), 65536.0 - 0.01);
-        sc.delta = delta;
-        sc.rdelta = __frcp_rn(delta);
-        sc.vl = vl;
-    }
+    if (tid < S) seg_quant_scalars(sm.mm[2 * tid], sm.mm[2 * tid + 1], sm.scal[tid]);  // what the quantizer needs
     sync();
     if (tid >= nt - S) {  // the epilogue constants, beside the quantization (the last warp's last lanes)
         const int s = tid - (nt - S);
-        SegScal &sc = sm.scal[s];
-        const int ncb = ix.seg[s].dim / 4;
-        sc.sum_vl = (float)__dmul_rn(__dadd_rn((double)sc.vl, __dmul_rn(0.5, (double)sc.delta)), (double)(float)ncb);
-        sc.q_l2norm = sqrtf(sc.q_l2sqr);
-        sc.c1 = (float)__dsub_rn(__dmul_rn(0.5, (double)sc.sum_q), (double)__fmul_rn(0.58f, sc.q_l2norm));
-        sc.c2 = ix.seg[s].c2;
-        sc.vfac = __fsub_rn(sc.q_l2sqr, __fmul_rn(2.0f, prune[s]));
+        seg_epilogue_scalars(ix.seg[s], prune[s], sm.scal[s]);
     }
     for (int cb = tid; cb < ncb_all; cb += nt) {
         int s = 0;
         while (s + 1 < S && cb * 4 >= ix.seg[s + 1].qoff) ++s;
-        const float vl = sm.scal[s].vl, delta = sm.scal[s].delta, rd = sm.scal[s].rdelta;
-        float t[16];
-        lut_entries(sm.qres + cb * 4, t);
-        uint32_t packed[8];
-#pragma unroll
-        for (int j = 0; j < 16; j += 2) {
-            const uint32_t a = lut_quant(__fsub_rn(t[j], vl), rd, delta);
-            const uint32_t b = lut_quant(__fsub_rn(t[j + 1], vl), rd, delta);
-            packed[j / 2] = a | (b << 16);
-        }
-        uint4 *dst = reinterpret_cast<uint4 *>(sm.lut + cb * 16);
-        dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-        dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+        const SegScal &sc = sm.scal[s];
+        quant_codebook(sm.qres + cb * 4, sc.vl, sc.delta, sc.rdelta, sm.lut + cb * 16);
     }
     sync();
+}
+
+// Output of the batched preparation (k_lut); null members: the scans build
+// each cluster's state themselves.
+struct Prepared {
+    const uint16_t *lut = nullptr;
+    const SegScal *scal = nullptr;
+    int np_max = 0;
+    __device__ __forceinline__ const uint16_t *lut_of(int qi, int p, int Dtot) const {
+        return lut + ((size_t)qi * np_max + p) * 4 * Dtot;
+    }
+    __device__ __forceinline__ const SegScal *scal_of(int qi, int p, int S) const {
+        return scal + ((size_t)qi * np_max + p) * S;
+    }
+};
+
+// ---- batched preparation: the LUT and scalars of every (query, probe) pair
+// of a call, one warp per pair, before the scan.  Pair i = query * np_max +
+// probe; its LUT is 4 * Dtot u16 at lut + i * 4 * Dtot (the layout of
+// ScanSmem::lut), its scalars S SegScal at scal + i * S.  Pairs past a query's
+// nprobe and pairs of empty clusters are not written (no scan reads them).
+constexpr int kLutWarps = 8;
+__global__ void __launch_bounds__(kLutWarps * 32) k_lut(DevIndexView ix, const uint32_t *__restrict__ probe,
+                                                        QueryShape qsh, int nq, const float *__restrict__ qrot_all,
+                                                        const float *__restrict__ prune_all, uint16_t *__restrict__ lut,
+                                                        SegScal *__restrict__ scal) {
+    extern __shared__ __align__(16) float k_lut_qres[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t pair = (int64_t)blockIdx.x * kLutWarps + warp;
+    const int qi = (int)(pair / qsh.np_max), p = (int)(pair - (int64_t)qi * qsh.np_max);
+    if (qi >= nq || p >= qsh.np_of(qi)) return;  // whole warp
+    const int c = (int)probe[pair];
+    if (ix.blk_off[c + 1] == ix.blk_off[c]) return;
+    float *qres = k_lut_qres + (size_t)warp * ix.Dtot;
+    const float *qrot = qrot_all + (size_t)qi * ix.Dtot;
+    for (int s = 0; s < ix.S; ++s) {
+        const SegDev &g = ix.seg[s];
+        const float *cent = g.cent + (size_t)c * g.dim;
+        for (int i = lane; i < g.dim; i += 32) qres[g.qoff + i] = __fsub_rn(qrot[g.qoff + i], cent[i]);
+    }
+    __syncwarp();
+    uint16_t *L = lut + pair * 4 * ix.Dtot;
+    for (int s = 0; s < ix.S; ++s) {
+        const SegDev &g = ix.seg[s];
+        const float *qr = qres + g.qoff;
+        SegScal sc;
+        sc.sum_q = warp_eigen_sum(g.dim, [&](int i) { return qr[i]; });
+        sc.q_l2sqr = warp_eigen_sum(g.dim, [&](int i) { return __fmul_rn(qr[i], qr[i]); });
+        const int cb0 = g.qoff / 4, ncb = g.dim / 4;
+        uint32_t kmin = 0xffffffffu, kmax = 0u;
+        for (int k = lane; k < ncb; k += 32) {
+            uint32_t a, b;
+            codebook_keys(qres + (cb0 + k) * 4, a, b);
+            kmin = min(kmin, a);
+            kmax = max(kmax, b);
+        }
+        kmin = __reduce_min_sync(kFull, kmin);
+        kmax = __reduce_max_sync(kFull, kmax);
+        if (lane == 0) seg_quant_scalars(kmin, kmax, sc);
+        sc.vl = __shfl_sync(kFull, sc.vl, 0);
+        sc.delta = __shfl_sync(kFull, sc.delta, 0);
+        sc.rdelta = __shfl_sync(kFull, sc.rdelta, 0);
+        for (int k = lane; k < ncb; k += 32) quant_codebook(qres + (cb0 + k) * 4, sc.vl, sc.delta, sc.rdelta, L + (cb0 + k) * 16);
+        if (lane == 0) {
+            seg_epilogue_scalars(g, prune_all[(size_t)qi * ix.S + s], sc);
+            scal[pair * ix.S + s] = sc;
+        }
+    }
+}
+
+// The prepared state of cluster c from k_lut's output (lut / scal: this
+// pair's), and the residual query, into the CTA's shared memory.
+__device__ void load_cluster(const DevIndexView &ix, const float *__restrict__ qrot, const uint16_t *__restrict__ lut,
+                             const SegScal *__restrict__ scal, int c, ScanSmem &sm) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const uint4 *src = reinterpret_cast<const uint4 *>(lut);
+    uint4 *dst = reinterpret_cast<uint4 *>(sm.lut);
+    for (int i = tid; i < ix.Dtot / 2; i += nt) dst[i] = src[i];  // 8 * Dtot bytes
+    if (tid < ix.S) sm.scal[tid] = scal[tid];
+    for (int s = 0; s < ix.S; ++s) {
+        const SegDev &g = ix.seg[s];
+        const float *cent = g.cent + (size_t)c * g.dim;
+        for (int i = tid; i < g.dim; i += nt) sm.qres[g.qoff + i] = __fsub_rn(qrot[g.qoff + i], cent[i]);
+    }
+    __syncthreads();
 }
 
 // The block's minimum estimate for a pruning stage.  Only its comparisons with
@@ -1399,44 +1470,32 @@ __device__ __forceinline__ unsigned replay_tile_warp(int S, int t0, int nblk, co
     return __reduce_add_sync(kFull, __popc(cm));
 }
 
-// Whether k_scan builds the next cluster's LUT during the last replay of the
-// current one (double-buffered cluster state).  Off: the overlap's extra
-// registers cost more occupancy than the overlap gains.
-constexpr bool kScanOverlap = false;
-
 struct ScanTally {
     unsigned long long blocks = 0, vecs = 0, rr = 0, spec = 0;
 };
 
 // Exact sequential scan of probes [p_begin, p_end) of one query, continuing
-// the pool held in shared memory (pool_size / distk in shared memory).  With
-// a double-buffered layout (sm.lut2 set) the next cluster's state is built by
-// warps 1.. while warp 0 replays the current cluster's last tile.
-template <bool kOverlap>
+// the pool held in shared memory (pool_size / distk in shared memory).  Each
+// nonempty probed cluster's LUT comes from the batched preparation when `lut`
+// is set (this query's pairs: probe p's at lut + p * 4 * Dtot, scal + p * S),
+// else it is built here.
 __device__ void scan_probes(const DevIndexView &ix, const uint32_t *__restrict__ probe, int p_begin, int p_end,
                             const float *__restrict__ qrot, const float *__restrict__ prune, int topk, ScanSmem &sm,
-                            int &pool_size, float &distk, int *err, ScanTally &tl) {
+                            int &pool_size, float &distk, ScanTally &tl, const uint16_t *__restrict__ lut,
+                            const SegScal *__restrict__ scal) {
     const int S = ix.S, tid = threadIdx.x;
-    const bool dbuf = kOverlap && sm.lut2 != nullptr;
-    if (p_begin >= p_end) return;
-    {
-        ScanSmem v0 = cluster_view(sm, 0);
-        prepare_cluster(ix, qrot, prune, (int)probe[p_begin], v0);
-    }
     for (int p = p_begin; p < p_end; ++p) {
-        const int buf = dbuf ? (p - p_begin) & 1 : 0;
-        ScanSmem v = cluster_view(sm, buf);
-        if (!dbuf && p > p_begin) prepare_cluster(ix, qrot, prune, (int)probe[p], v);
         const int c = (int)probe[p];
         const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
         const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
-        const bool ahead = dbuf && p + 1 < p_end;  // build the next cluster's state during the last replay
-        if (p + 1 < p_end) prefetch_centroid(ix, (int)probe[p + 1], tid, blockDim.x);
         tl.blocks += nb;
         tl.vecs += n;
+        if (nb == 0) continue;
+        if (lut) load_cluster(ix, qrot, lut + (size_t)p * 4 * ix.Dtot, scal + (size_t)p * S, c, sm);
+        else prepare_cluster(ix, qrot, prune, c, sm);
+        if (p + 1 < p_end) prefetch_centroid(ix, (int)probe[p + 1], tid, blockDim.x);
         for (int t0 = 0; t0 < nb; t0 += kTileB) {
-            tile_candidates(ix, v, b0, v0, nb, n, t0, nb, distk);
-            const bool last = t0 + kTileB >= nb;
+            tile_candidates(ix, sm, b0, v0, nb, n, t0, nb, distk);
             if (tid < 32) {
                 float dk = distk;
                 int sz = pool_size;
@@ -1447,15 +1506,8 @@ __device__ void scan_probes(const DevIndexView &ix, const uint32_t *__restrict__
                     distk = dk;
                     pool_size = sz;
                 }
-            } else if (kOverlap && last && ahead) {
-                ScanSmem vn = cluster_view(sm, buf ^ 1);
-                prepare_cluster(ix, qrot, prune, (int)probe[p + 1], vn, 32, 1);
             }
             __syncthreads();
-        }
-        if (kOverlap && ahead && nb == 0) {  // an empty cluster: nothing to overlap with
-            ScanSmem vn = cluster_view(sm, buf ^ 1);
-            prepare_cluster(ix, qrot, prune, (int)probe[p + 1], vn);
         }
     }
 }
@@ -1515,7 +1567,7 @@ __host__ __device__ inline size_t ws_tile_bytes(int S) {
 }
 
 __host__ __device__ inline size_t ws_smem_bytes(int Dtot, int S, int topk, int xstride) {
-    return scan_smem_bytes(Dtot, S, topk, xstride, false) + ws_tile_bytes(S);
+    return scan_smem_bytes(Dtot, S, topk, xstride) + ws_tile_bytes(S);
 }
 
 // The tile buffer `b` of a warp-specialised layout: buffer 0 is the base
@@ -1556,8 +1608,8 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_ws(DevIndex
     const int qi = order ? order[blockIdx.x] : (int)blockIdx.x;
     if (deferred && deferred[qi]) return;  // answered by the split pass
     const int np = qsh.np_of(qi), topk = qsh.k_of(qi), S = ix.S, tid = threadIdx.x;
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, qsh.k_max, xstride, false);
-    char *extra = smem_raw + scan_smem_bytes(ix.Dtot, S, qsh.k_max, xstride, false);
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, qsh.k_max, xstride);
+    char *extra = smem_raw + scan_smem_bytes(ix.Dtot, S, qsh.k_max, xstride);
     __shared__ WsTile meta[2];
     __shared__ int pool_size;
     __shared__ float distk;
@@ -1937,7 +1989,8 @@ __device__ __forceinline__ int list_len(const SplitState &st) { return min(*st.n
 __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_first(DevIndexView ix, const uint32_t *__restrict__ probe,
                                                              const float *__restrict__ qrot_all,
                                                              const float *__restrict__ prune_all, SplitState st, int *__restrict__ err,
-                                                             unsigned long long *__restrict__ counters, int xstride) {
+                                                             unsigned long long *__restrict__ counters, int xstride,
+                                                             Prepared prep) {
     extern __shared__ __align__(16) char smem_raw[];
     const int S = ix.S, tid = threadIdx.x, slot = blockIdx.x;
     if (slot >= list_len(st)) return;
@@ -1967,7 +2020,8 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_first(DevIn
                 break;
             }
             if (!prepared) {
-                prepare_cluster(ix, qrot, prune, c, sm);
+                if (prep.lut) load_cluster(ix, qrot, prep.lut_of(qi, p, ix.Dtot), prep.scal_of(qi, p, S), c, sm);
+                else prepare_cluster(ix, qrot, prune, c, sm);
                 prepared = true;
             }
             const int te = min(nb, t0 + kTileB);
@@ -2061,7 +2115,8 @@ __global__ void __launch_bounds__(kPrefixThreads) k_tile_prefix(SplitState st) {
 __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_spec(DevIndexView ix, const uint32_t *__restrict__ probe,
                                                             int nprobe, const float *__restrict__ qrot_all,
                                                             const float *__restrict__ prune_all, SplitState st,
-                                                            unsigned long long *__restrict__ counters, int xstride) {
+                                                            unsigned long long *__restrict__ counters, int xstride,
+                                                            Prepared prep) {
     extern __shared__ __align__(16) char smem_raw[];
     const int S = ix.S, tid = threadIdx.x;
     ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, 1, xstride);
@@ -2098,7 +2153,9 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_spec(DevInd
             const int p = plo, tile = local - to[p];
             const int c = (int)probe[(size_t)q * nprobe + p];
             if (slot != last_slot || c != last_c) {  // LUTs survive across tiles of one cluster
-                prepare_cluster(ix, qrot_all + (size_t)q * ix.Dtot, prune_all + (size_t)q * S, c, sm);
+                if (prep.lut) load_cluster(ix, qrot_all + (size_t)q * ix.Dtot, prep.lut_of(q, p, ix.Dtot),
+                                           prep.scal_of(q, p, S), c, sm);
+                else prepare_cluster(ix, qrot_all + (size_t)q * ix.Dtot, prune_all + (size_t)q * S, c, sm);
                 last_slot = slot;
                 last_c = c;
             }
@@ -2362,20 +2419,21 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan(DevIndexVie
                                                        QueryShape qsh, const float *__restrict__ qrot_all,
                                                        const float *__restrict__ prune_all,
                                                        uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
-                                                       int *__restrict__ err, unsigned long long *__restrict__ counters,
-                                                       int xstride, const uint8_t *__restrict__ deferred,
-                                                       const int *__restrict__ order) {
+                                                       unsigned long long *__restrict__ counters, int xstride,
+                                                       const uint8_t *__restrict__ deferred,
+                                                       const int *__restrict__ order, Prepared prep) {
     extern __shared__ __align__(16) char smem_raw[];
     const int qi = order ? order[blockIdx.x] : (int)blockIdx.x;
     if (deferred && deferred[qi]) return;  // answered by the split pass
     const int np = qsh.np_of(qi), topk = qsh.k_of(qi);
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, qsh.k_max, xstride, kScanOverlap);
+    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, ix.S, qsh.k_max, xstride);
     __shared__ int pool_size;
     __shared__ float distk;
     ScanTally tl;
     init_pool(sm, topk, pool_size, distk);
-    scan_probes<kScanOverlap>(ix, probe + (size_t)qi * qsh.np_max, 0, np, qrot_all + (size_t)qi * ix.Dtot,
-                prune_all + (size_t)qi * ix.S, topk, sm, pool_size, distk, err, tl);
+    scan_probes(ix, probe + (size_t)qi * qsh.np_max, 0, np, qrot_all + (size_t)qi * ix.Dtot,
+                prune_all + (size_t)qi * ix.S, topk, sm, pool_size, distk, tl,
+                prep.lut ? prep.lut_of(qi, 0, ix.Dtot) : nullptr, prep.lut ? prep.scal_of(qi, 0, ix.S) : nullptr);
     flush_tally(tl, counters);
     write_results(sm, pool_size, topk, qsh.k_max, out_ids + (size_t)qi * qsh.k_max,
                   out_d ? out_d + (size_t)qi * qsh.k_max : nullptr);
@@ -2514,6 +2572,15 @@ struct Bump {
     }
 };
 
+// Bytes of the batched preparation's output for nq x nprobe pairs (0 when it
+// would pass kPrepCap: the scans then build each cluster's state themselves).
+constexpr size_t kPrepCap = (size_t)2 << 30;
+size_t prep_bytes(const Index &I, int64_t nq, int64_t nprobe) {
+    const size_t pairs = (size_t)nq * nprobe;
+    const size_t b = align16(pairs * 8 * (size_t)I.view.Dtot) + align16(pairs * sizeof(SegScal) * I.view.S);
+    return b <= kPrepCap ? b : 0;
+}
+
 size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t nprobe, bool host_io) {
     size_t b = 0;
     auto add = [&](size_t x) { b += align16(x); };
@@ -2531,6 +2598,7 @@ size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t np
     add(4 * (size_t)nq * 2);                   // per-query nprobe / k
     add(64);                                   // flags
     add(64);                                   // counters
+    add(prep_bytes(I, nq, nprobe));            // prepared LUTs
     (void)host_io;
     return b + 256;
 }
@@ -2636,8 +2704,8 @@ void ensure_smem(const void *fn, size_t bytes) {
 // The CTA-per-query scan of `nq` queries (deferred ones skipped): k_scan, or
 // its warp-specialised form k_scan_ws, which gives the same answers.
 void launch_cta_scan(bool ws, const DevIndexView &ix, const uint32_t *probe, const QueryShape &qsh, const float *qrot,
-                     const float *prune, uint32_t *ids, float *d, int *err, unsigned long long *cnt, int xs,
-                     const uint8_t *deferred, int64_t nq, int *order, cudaStream_t st) {
+                     const float *prune, uint32_t *ids, float *d, unsigned long long *cnt, int xs,
+                     const uint8_t *deferred, int64_t nq, int *order, const Prepared &prep, cudaStream_t st) {
     if (order) {
         k_order<<<1, kOrderThreads, 0, st>>>(ix, probe, qsh, (int)nq, order);
         check_launch("k_order");
@@ -2651,10 +2719,11 @@ void launch_cta_scan(bool ws, const DevIndexView &ix, const uint32_t *probe, con
         check_launch("k_scan_ws");
         return;
     }
-    const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, qsh.k_max, xs, kScanOverlap);
+    const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, qsh.k_max, xs);
     SAQG_REQUIRE(smem <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
     ensure_smem((const void *)k_scan, smem);
-    k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, qsh, qrot, prune, ids, d, err, cnt, xs, deferred, order);
+    k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, qsh, qrot, prune, ids, d, cnt, xs, deferred, order,
+                                                      prep);
     check_launch("k_scan");
 }
 
@@ -2844,6 +2913,9 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
     float *od = bp.take<float>((size_t)nq * topk);
     int *flags = bp.take<int>(16);
     unsigned long long *counters = bp.take<unsigned long long>(8);
+    const size_t pb = prep_bytes(I, nq, nprobe);
+    uint16_t *prep_lut = pb ? bp.take<uint16_t>((size_t)nq * nprobe * 4 * ix.Dtot) : nullptr;
+    SegScal *prep_scal = pb ? bp.take<SegScal>((size_t)nq * nprobe * ix.S) : nullptr;
     cudaEvent_t ev[7] = {};
     bool shortlist = false;  // centroid ranking by the GEMM shortlist
     if (stats)
@@ -2913,6 +2985,20 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         unsigned long long *cnt = stats ? counters : nullptr;
         const int mode0 = scan_mode(nq, topk, tune);
         const int mode = (qsh.np || qsh.k) && mode0 == 2 ? 0 : mode0;
+        Prepared prep;  // every (query, probe) pair's LUT, built by one batched kernel
+        if (mode != 2 && prep_lut) {
+            const size_t lsm = 4 * (size_t)kLutWarps * ix.Dtot;
+            SAQG_REQUIRE(lsm <= 200 * 1024, "dimension too large for the batched LUT preparation");
+            ensure_smem((const void *)k_lut, lsm);
+            const int64_t pairs = nq * nprobe;
+            k_lut<<<(unsigned)((pairs + kLutWarps - 1) / kLutWarps), kLutWarps * 32, lsm, st>>>(
+                ix, probe, qsh, (int)nq, qrot, prune, prep_lut, prep_scal);
+            check_launch("k_lut");
+            count_launch(1);
+            prep.lut = prep_lut;
+            prep.scal = prep_scal;
+            prep.np_max = (int)nprobe;
+        }
         if (mode == 2) {
             const size_t per_warp = align16(warp_smem_bytes(ix.Dtot, ix.S, (int)topk));
             const size_t wsm = per_warp * kWarpsPerCta;
@@ -2924,8 +3010,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         } else if (mode == 0 && no_deferral(I, nprobe, tune)) {
             // no query of this call can probe more blocks than the deferral
             // threshold: the CTA scan answers every query, no split pass
-            launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, flags + 1, cnt, xs, nullptr, nq,
-                            order, st);
+            launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, nullptr, nq, order,
+                            prep, st);
             count_launch(4);
         } else {
             // split-pass state: every query (mode 1), or the deferred giant-cluster queries (mode 0)
@@ -2979,8 +3065,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                     SAQG_CUDA_TRY(cudaEventRecord(C.fork_event(), st));
                     SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, C.fork_event(), 0));
                 }
-                launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, flags + 1, cnt, xs,
-                                deferred, nq, order, st);
+                launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, deferred, nq,
+                                order, prep, st);
             }
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
             const size_t smem_r = smem + 2 * 4 * (size_t)kReplayRecs * ss.rec_words;
@@ -2988,7 +3074,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             ensure_smem((const void *)k_scan_first, (size_t)smem);
             ensure_smem((const void *)k_scan_spec, (size_t)smem1);
             ensure_smem((const void *)k_scan_replay, (size_t)smem_r);
-            k_scan_first<<<(unsigned)cap, kScanThreads, smem, sp>>>(ix, probe, qrot, prune, ss, flags + 1, cnt, xs);
+            k_scan_first<<<(unsigned)cap, kScanThreads, smem, sp>>>(ix, probe, qrot, prune, ss, flags + 1, cnt, xs,
+                                                                     prep);
             check_launch("k_scan_first");
             if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[5], sp));
             const unsigned grid = (unsigned)full_grid((const void *)k_scan_spec, kScanThreads, smem1);
@@ -3006,7 +3093,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                 sl.final_level = L + 1 == nlev;
                 k_tile_prefix<<<1, kPrefixThreads, 0, sp>>>(sl);
                 check_launch("k_tile_prefix");
-                k_scan_spec<<<grid, kScanThreads, smem1, sp>>>(ix, probe, (int)nprobe, qrot, prune, sl, cnt, xs);
+                k_scan_spec<<<grid, kScanThreads, smem1, sp>>>(ix, probe, (int)nprobe, qrot, prune, sl, cnt, xs, prep);
                 check_launch("k_scan_spec");
                 if (stats && sl.final_level) SAQG_CUDA_TRY(cudaEventRecord(ev[6], sp));
                 k_scan_replay<<<(unsigned)cap, kScanThreads, smem_r, sp>>>(ix, sl, ids_out, d_out, cnt, xs);
@@ -3254,14 +3341,14 @@ void run_search_static(const Index &I, const float *q, int64_t nq, int64_t topk,
     for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
     k_qprep<<<dim3((unsigned)ix.S, (unsigned)nq), 256, qsm, st>>>(ix, q, m, qrot, prune);
     check_launch("k_qprep");
-    const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xstride_of(ix), kScanOverlap);
+    const size_t smem_k = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xstride_of(ix));
     SAQG_REQUIRE(smem_k <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
     ensure_smem((const void *)k_scan, (size_t)smem_k);
     QueryShape qsh;
     qsh.np_max = (int)nprobe;
     qsh.k_max = (int)topk;
-    k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, qsh, qrot, prune, ids, dists,
-                                                      flags + 1, nullptr, xstride_of(ix), nullptr, nullptr);
+    k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, qsh, qrot, prune, ids, dists, nullptr,
+                                                      xstride_of(ix), nullptr, nullptr, Prepared{});
     check_launch("k_scan");
     count_launch(4);
 }
