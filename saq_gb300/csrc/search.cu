@@ -1054,21 +1054,28 @@ struct Prepared {
     }
 };
 
-// ---- batched preparation: the LUT and scalars of every (query, probe) pair
-// of a call, one warp per pair, before the scan.  Pair i = query * np_max +
-// probe; its LUT is 4 * Dtot u16 at lut + i * 4 * Dtot (the layout of
-// ScanSmem::lut), its scalars S SegScal at scal + i * S.  Pairs past a query's
-// nprobe and pairs of empty clusters are not written (no scan reads them).
+// ---- batched preparation: the LUT and scalars of the (query, probe) pairs of
+// the queries on a list (the split pass's), one warp per pair.  Pair i =
+// query * np_max + probe; its LUT is 4 * Dtot u16 at lut + i * 4 * Dtot (the
+// layout of ScanSmem::lut), its scalars S SegScal at scal + i * S.  Work item w
+// is list entry w / np_max (entries at or past *nlist are none) and probe
+// w % np_max.  Pairs past a query's nprobe and pairs of empty clusters are not
+// written (no scan reads them).
 constexpr int kLutWarps = 8;
 __global__ void __launch_bounds__(kLutWarps * 32) k_lut(DevIndexView ix, const uint32_t *__restrict__ probe,
-                                                        QueryShape qsh, int nq, const float *__restrict__ qrot_all,
+                                                        QueryShape qsh, const int *__restrict__ qlist,
+                                                        const int *__restrict__ nlist, int cap,
+                                                        const float *__restrict__ qrot_all,
                                                         const float *__restrict__ prune_all, uint16_t *__restrict__ lut,
                                                         SegScal *__restrict__ scal) {
     extern __shared__ __align__(16) float k_lut_qres[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t pair = (int64_t)blockIdx.x * kLutWarps + warp;
-    const int qi = (int)(pair / qsh.np_max), p = (int)(pair - (int64_t)qi * qsh.np_max);
-    if (qi >= nq || p >= qsh.np_of(qi)) return;  // whole warp
+    const int64_t w = (int64_t)blockIdx.x * kLutWarps + warp;
+    const int slot = (int)(w / qsh.np_max), p = (int)(w - (int64_t)slot * qsh.np_max);
+    if (slot >= min(*nlist, cap)) return;  // whole warp
+    const int qi = qlist[slot];
+    if (p >= qsh.np_of(qi)) return;
+    const int64_t pair = (int64_t)qi * qsh.np_max + p;
     const int c = (int)probe[pair];
     if (ix.blk_off[c + 1] == ix.blk_off[c]) return;
     float *qres = k_lut_qres + (size_t)warp * ix.Dtot;
@@ -1919,7 +1926,8 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_scan_warp(DevIndexView ix
 // reference's decisions on the records.  Blocks without a record cannot insert
 // anything (none of their lanes is below tau1 >= distk), so the replay is exact.
 constexpr int kTileBlocks = 16;
-constexpr int kSpecChunk = 8;  // speculative tiles per work chunk of k_scan_spec
+constexpr int kSpecChunk = 8;          // speculative tiles per work chunk of k_scan_spec
+constexpr int kSpecChunkPrepared = 2;  // ... when the LUTs come from the batched preparation
 constexpr int kFirstBlocks = 16;  // exact prefix of a deferred query (its distk bounds the first level)
 // Levels of the speculation for deferred queries, in tiles after the split
 // point: [0, 8), [8, 64), [64, end) by default; the autotuner may pick another
@@ -1954,7 +1962,11 @@ struct SplitState {
     int *npos;           // [cap] scan positions (blocks) of the query
     int64_t *pos_off;    // [cap] first record position reserved for the slot
     unsigned long long *pos_used;  // record positions handed out so far
-    float2 *summ;        // [pos_cap] per record: min candidate estimate, max stage minimum (NaN: none)
+    // [pos_cap] per record (NaN: none): x the smallest candidate estimate, y the
+    // largest stage minimum, z the smallest value a candidate lane's accept test
+    // can see (its accurate distance; several segments: every running sum),
+    // -inf when one of them is NaN
+    float4 *summ;
     float *rec;          // [pos_cap][rec_words]
     int64_t pos_cap;
     int rec_words;
@@ -1992,86 +2004,89 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_first(DevIn
                                                              unsigned long long *__restrict__ counters, int xstride,
                                                              Prepared prep) {
     extern __shared__ __align__(16) char smem_raw[];
-    const int S = ix.S, tid = threadIdx.x, slot = blockIdx.x;
-    if (slot >= list_len(st)) return;
-    const int qi = st.qlist[slot];
-    const int np_max = st.qsh.np_max, k_max = st.qsh.k_max;
-    const int nprobe = st.qsh.np_of(qi), topk = st.qsh.k_of(qi);
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, k_max, xstride);
-    __shared__ int pool_size;
-    __shared__ float distk;
-    ScanTally tl;
-    init_pool(sm, topk, pool_size, distk);
-    const uint32_t *pr = probe + (size_t)qi * np_max;
-    const float *qrot = qrot_all + (size_t)qi * ix.Dtot, *prune = prune_all + (size_t)qi * S;
-    // the exact prefix, as scan_probes does: whole tiles in scan order until at
-    // least kFirstBlocks blocks are done and the pool is full (its distk then
-    // bounds every later distk, so it can serve as the speculation bound)
-    int sp_p = nprobe, sp_b = 0;
-    for (int p = 0; p < nprobe && sp_p == nprobe; ++p) {
-        const int c = (int)pr[p];
-        const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
-        const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
-        bool prepared = false;
-        for (int t0 = 0; t0 < nb; t0 += kTileB) {
-            if (tl.blocks >= st.first_blocks && pool_size == topk) {
-                sp_p = p;
-                sp_b = t0;
-                break;
-            }
-            if (!prepared) {
-                if (prep.lut) load_cluster(ix, qrot, prep.lut_of(qi, p, ix.Dtot), prep.scal_of(qi, p, S), c, sm);
-                else prepare_cluster(ix, qrot, prune, c, sm);
-                prepared = true;
-            }
-            const int te = min(nb, t0 + kTileB);
-            tl.blocks += te - t0;
-            tl.vecs += min(n, te * 32) - t0 * 32;
-            tile_candidates(ix, sm, b0, v0, nb, n, t0, nb, distk);
-            if (tid < 32) {
-                float dk = distk;
-                int sz = pool_size;
-                const unsigned nc = replay_tile_warp(S, t0, te - t0, sm, ix.ids + v0, sm.pool_id, sm.pool_d, sz, topk, dk,
-                                                     tl.rr);
-                if (tid == 0) {
-                    tl.spec += nc;
-                    distk = dk;
-                    pool_size = sz;
-                }
-            }
-            __syncthreads();
-        }
-    }
-    flush_tally(tl, counters);
-    for (int i = tid; i < topk; i += blockDim.x) {
-        st.pool_id[(size_t)slot * k_max + i] = sm.pool_id[i];
-        st.pool_d[(size_t)slot * k_max + i] = sm.pool_d[i];
-    }
-    if (tid == 0) {
-        st.pool_size[slot] = pool_size;
-        st.tau[slot] = distk;
-        st.split_p[slot] = sp_p;
-        st.split_b[slot] = sp_b;
-        int tiles = 0;
-        int64_t pos = 0;
-        for (int p = 0; p < nprobe; ++p) {
+    const int S = ix.S, tid = threadIdx.x;
+    // slots round-robin over a grid sized to the machine (the list length is known on the device only)
+    for (int slot = blockIdx.x; slot < list_len(st); slot += gridDim.x) {
+        const int qi = st.qlist[slot];
+        const int np_max = st.qsh.np_max, k_max = st.qsh.k_max;
+        const int nprobe = st.qsh.np_of(qi), topk = st.qsh.k_of(qi);
+        ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, k_max, xstride);
+        __shared__ int pool_size;
+        __shared__ float distk;
+        ScanTally tl;
+        init_pool(sm, topk, pool_size, distk);
+        const uint32_t *pr = probe + (size_t)qi * np_max;
+        const float *qrot = qrot_all + (size_t)qi * ix.Dtot, *prune = prune_all + (size_t)qi * S;
+        // the exact prefix, as scan_probes does: whole tiles in scan order until at
+        // least kFirstBlocks blocks are done and the pool is full (its distk then
+        // bounds every later distk, so it can serve as the speculation bound)
+        int sp_p = nprobe, sp_b = 0;
+        for (int p = 0; p < nprobe && sp_p == nprobe; ++p) {
             const int c = (int)pr[p];
-            const int nb = (int)(ix.blk_off[c + 1] - ix.blk_off[c]);
-            st.tile_off[(size_t)slot * (np_max + 1) + p] = tiles;
-            st.blk_base[(size_t)slot * np_max + p] = (int)pos;
-            const int rest = p < sp_p ? 0 : p == sp_p ? nb - sp_b : nb;
-            tiles += (rest + kTileBlocks - 1) / kTileBlocks;
-            pos += nb;
+            const int64_t b0 = ix.blk_off[c], v0 = ix.vec_off[c];
+            const int nb = (int)(ix.blk_off[c + 1] - b0), n = (int)(ix.vec_off[c + 1] - v0);
+            bool prepared = false;
+            for (int t0 = 0; t0 < nb; t0 += kTileB) {
+                if (tl.blocks >= st.first_blocks && pool_size == topk) {
+                    sp_p = p;
+                    sp_b = t0;
+                    break;
+                }
+                if (!prepared) {
+                    if (prep.lut) load_cluster(ix, qrot, prep.lut_of(qi, p, ix.Dtot), prep.scal_of(qi, p, S), c, sm);
+                    else prepare_cluster(ix, qrot, prune, c, sm);
+                    prepared = true;
+                }
+                const int te = min(nb, t0 + kTileB);
+                tl.blocks += te - t0;
+                tl.vecs += min(n, te * 32) - t0 * 32;
+                tile_candidates(ix, sm, b0, v0, nb, n, t0, nb, distk);
+                if (tid < 32) {
+                    float dk = distk;
+                    int sz = pool_size;
+                    const unsigned nc = replay_tile_warp(S, t0, te - t0, sm, ix.ids + v0, sm.pool_id, sm.pool_d, sz, topk, dk,
+                                                         tl.rr);
+                    if (tid == 0) {
+                        tl.spec += nc;
+                        distk = dk;
+                        pool_size = sz;
+                    }
+                }
+                __syncthreads();
+            }
         }
-        for (int p = nprobe; p <= np_max; ++p) st.tile_off[(size_t)slot * (np_max + 1) + p] = tiles;
-        if (pos != st.npos[slot]) *err = 2;
+        flush_tally(tl, counters);
+        for (int i = tid; i < topk; i += blockDim.x) {
+            st.pool_id[(size_t)slot * k_max + i] = sm.pool_id[i];
+            st.pool_d[(size_t)slot * k_max + i] = sm.pool_d[i];
+        }
+        if (tid == 0) {
+            st.pool_size[slot] = pool_size;
+            st.tau[slot] = distk;
+            st.split_p[slot] = sp_p;
+            st.split_b[slot] = sp_b;
+            int tiles = 0;
+            int64_t pos = 0;
+            for (int p = 0; p < nprobe; ++p) {
+                const int c = (int)pr[p];
+                const int nb = (int)(ix.blk_off[c + 1] - ix.blk_off[c]);
+                st.tile_off[(size_t)slot * (np_max + 1) + p] = tiles;
+                st.blk_base[(size_t)slot * np_max + p] = (int)pos;
+                const int rest = p < sp_p ? 0 : p == sp_p ? nb - sp_b : nb;
+                tiles += (rest + kTileBlocks - 1) / kTileBlocks;
+                pos += nb;
+            }
+            for (int p = nprobe; p <= np_max; ++p) st.tile_off[(size_t)slot * (np_max + 1) + p] = tiles;
+            if (pos != st.npos[slot]) *err = 2;
+        }
+        __syncthreads();  // the next slot reuses the shared state
     }
 }
 
 // Work offsets of the level's tiles: slot q holds tiles [t_lo, t_hi) of its own.
 // One CTA of kPrefixThreads: each thread sums a contiguous run of slots, a
 // block-wide exclusive scan of the run sums, then each run is written.
-constexpr int kPrefixThreads = 1024;
+constexpr int kPrefixThreads = 256;
 __global__ void __launch_bounds__(kPrefixThreads) k_tile_prefix(SplitState st) {
     __shared__ int wsum[kPrefixThreads / 32];
     const int nprobe = st.qsh.np_max, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -2091,14 +2106,15 @@ __global__ void __launch_bounds__(kPrefixThreads) k_tile_prefix(SplitState st) {
     }
     if (lane == 31) wsum[w] = x;
     __syncthreads();
+    constexpr int kW = kPrefixThreads / 32;
     if (w == 0) {
-        int v = wsum[lane];
+        int v = lane < kW ? wsum[lane] : 0;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int y = __shfl_up_sync(0xffffffffu, v, o);
             if (lane >= o) v += y;
         }
-        wsum[lane] = v;  // inclusive over warps
+        if (lane < kW) wsum[lane] = v;  // inclusive over warps
     }
     __syncthreads();
     int acc = x - run + (w ? wsum[w - 1] : 0);
@@ -2123,15 +2139,19 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_spec(DevInd
     ScanTally tl;
     const int nl = list_len(st);
     const int total = st.q_tile_off[nl];
-    // chunks of kSpecChunk consecutive tiles (mostly of one cluster: one LUT)
-    // taken from a shared counter: tiles differ widely in cost (candidates,
-    // pruning stages), so equal shares per CTA leave a long tail
+    // chunks of consecutive tiles (mostly of one cluster: one LUT) taken from a
+    // shared counter: tiles differ widely in cost (candidates, pruning stages),
+    // so equal shares per CTA leave a long tail.  With prepared LUTs a cluster
+    // switch is a copy, and chunks are short.
+    // at least about four chunks per CTA, so that a small level (few queries)
+    // still spreads over the whole grid
+    const int ct = max(1, min(prep.lut ? kSpecChunkPrepared : kSpecChunk, total / (4 * (int)gridDim.x)));
     __shared__ int chunk;
     int last_slot = -1, last_c = -1;
     for (;;) {
         if (tid == 0) chunk = atomicAdd(st.work_next, 1);
         __syncthreads();
-        const int w_begin = chunk * kSpecChunk, w_end = min(total, w_begin + kSpecChunk);
+        const int w_begin = chunk * ct, w_end = min(total, w_begin + ct);
         __syncthreads();  // every thread has read `chunk` before thread 0 takes the next
         if (w_begin >= total) break;
         for (int wi = w_begin; wi < w_end; ++wi) {
@@ -2182,12 +2202,30 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_spec(DevInd
                             uint32_t *ri = reinterpret_cast<uint32_t *>(r);
                             // summary: a later distk below the minimum estimate, or below a stage minimum,
                             // leaves the block without effect
-                            float mn = ((cm >> lane) & 1u) ? sm.cur[w * 32 + lane] : __int_as_float(0x7fffffff);
+                            const bool in = (cm >> lane) & 1u;
+                            float mn = in ? sm.cur[w * 32 + lane] : __int_as_float(0x7fffffff);
                             float mx = (S > 1 && lane < sm.nstage[w]) ? sm.stage[w * (S + 1) + lane] : __int_as_float(0x7fffffff);
+                            // ... and a later distk below every value the lane's accept test can
+                            // compare (replay_block_warp: the accurate distance, or each running sum)
+                            float mz = __int_as_float(0x7f800000);
+                            if (in) {
+                                if (S == 1) {
+                                    mz = sm.part[w * 32 + lane];
+                                } else {
+                                    float acc = sm.cur[w * 32 + lane];
+                                    for (int s2 = 0; s2 < S; ++s2) {
+                                        acc = __fadd_rn(acc, sm.part[(w * S + s2) * 32 + lane]);
+                                        mz = fminf(mz, acc);
+                                        if (acc != acc) mz = -__int_as_float(0x7f800000);
+                                    }
+                                }
+                                if (mz != mz) mz = -__int_as_float(0x7f800000);
+                            }
     #pragma unroll
                             for (int o = 16; o; o >>= 1) {
                                 mn = fminf(mn, __shfl_xor_sync(kFull, mn, o));
                                 mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+                                mz = fminf(mz, __shfl_xor_sync(kFull, mz, o));
                             }
                             if (lane == 0) {
                                 ri[0] = (uint32_t)pos;
@@ -2198,7 +2236,7 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_spec(DevInd
                                 ri[5] = (uint32_t)(uint64_t)v0;
                                 ri[6] = (uint32_t)((uint64_t)v0 >> 32);
                                 ri[7] = __float_as_uint(mx);
-                                st.summ[st.pos_off[slot] + pos] = make_float2(mn, mx);
+                                st.summ[st.pos_off[slot] + pos] = make_float4(mn, mx, mz, 0.0f);
                                 if (counters) atomicAdd(counters + 3, (unsigned long long)__popc(cm));
                             }
                             if (S > 1 && lane <= S) r[8 + lane] = sm.stage[w * (S + 1) + lane];
@@ -2271,145 +2309,195 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_replay(DevIndexView ix, S
                                                               uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
                                                               unsigned long long *__restrict__ counters, int xstride) {
     extern __shared__ __align__(16) char smem_raw[];
-    const int S = ix.S, slot = blockIdx.x;
-    if (slot >= list_len(st)) return;
-    const int qi = st.qlist[slot];
-    const int k_max = st.qsh.k_max, topk = st.qsh.k_of(qi);
-    ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, k_max, xstride);
-    float *stage_buf = reinterpret_cast<float *>(smem_raw + scan_smem_bytes(ix.Dtot, S, k_max, xstride));
-    __shared__ int pool_size;
-    __shared__ float distk;
-    __shared__ int list[kScanThreads * kReplayPer];
-    __shared__ int warp_cnt[kScanWarps];
-    __shared__ int eff[kReplayRecs], cnt[kReplayRecs];
-    __shared__ int s_next, s_plo, s_phi;
-    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    for (int i = tid; i < topk; i += blockDim.x) {
-        sm.pool_id[i] = st.pool_id[(size_t)slot * k_max + i];
-        sm.pool_d[i] = st.pool_d[(size_t)slot * k_max + i];
-    }
-    if (tid == 0) {
-        pool_size = st.pool_size[slot];
-        distk = st.tau[slot];
-        s_plo = tile_pos(st, slot, st.t_lo);  // this level's scan positions
-        s_phi = tile_pos(st, slot, st.t_hi);
-    }
-    const int np = st.npos[slot];
-    const float2 *su = st.summ + st.pos_off[slot];
-    const float *rq = st.rec + (size_t)st.pos_off[slot] * st.rec_words;
-    const int RW = st.rec_words, R16 = RW / 4;
-    unsigned long long rr = 0;
-    __syncthreads();
-    const int pos_end = min(np, s_phi);
-    for (int base = s_plo; base < pos_end; base += kScanThreads * kReplayPer) {
-        // thread t tests positions base + kReplayPer t .. + kReplayPer - 1; a
-        // block-wide prefix of the counts keeps the list in position order
-        const int p0 = base + kReplayPer * tid;
-        const float dk0 = distk;
-        bool f[kReplayPer];
-        int mine = 0;
-#pragma unroll
-        for (int r = 0; r < kReplayPer; ++r) {
-            f[r] = false;
-            if (p0 + r < pos_end) {
-                const float2 v = su[p0 + r];
-                f[r] = v.x < dk0 && !(v.y > dk0);
-            }
-            mine += f[r];
-        }
-        int incl = mine;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(kFull, incl, o);
-            if (lane >= o) incl += v;
-        }
-        if (lane == 31) warp_cnt[w] = incl;
-        __syncthreads();
-        int off = incl - mine, total = 0;
-        for (int i = 0; i < kScanWarps; ++i) {
-            if (i < w) off += warp_cnt[i];
-            total += warp_cnt[i];
-        }
-#pragma unroll
-        for (int r = 0; r < kReplayPer; ++r)
-            if (f[r]) list[off++] = p0 + r;
-        __syncthreads();
-        const int nch = (total + kReplayRecs - 1) / kReplayRecs;
-        auto issue = [&](int k) {
-            const int c0 = k * kReplayRecs, cn = min(kReplayRecs, total - c0);
-            float *buf = stage_buf + (size_t)(k & 1) * kReplayRecs * RW;
-            for (int i = tid; i < cn * R16; i += kScanThreads) {
-                const int r = i / R16, e = i - r * R16;
-                cp_async16(buf + (size_t)r * RW + 4 * e, rq + (size_t)list[c0 + r] * RW + 4 * e);
-            }
-            cp_async_commit();
-        };
-        if (nch) issue(0);
-        for (int k = 0; k < nch; ++k) {
-            if (k + 1 < nch) {
-                issue(k + 1);
-                cp_async_wait<1>();
-            } else {
-                cp_async_wait<0>();
-            }
-            __syncthreads();
-            const float *buf = stage_buf + (size_t)(k & 1) * kReplayRecs * RW;
-            const int cn = min(kReplayRecs, total - k * kReplayRecs);
-            int r0 = 0;
-            while (r0 < cn) {
-                const float dk = distk;
-                const int sz = pool_size;
-                for (int r = r0 + w; r < cn; r += kScanWarps) {
-                    int c;
-                    const bool e = record_effect(S, buf + (size_t)r * RW, dk, sz, topk, c);
-                    if (lane == 0) {
-                        eff[r] = e;
-                        cnt[r] = c;
-                    }
-                }
-                __syncthreads();
-                if (w == 0) {
-                    const bool mine = lane >= r0 && lane < cn;
-                    const uint32_t hit = __ballot_sync(kFull, mine && eff[lane]);
-                    const int rs = hit ? __ffs(hit) - 1 : cn;  // first record that changes the pool
-                    int c = (lane >= r0 && lane < rs) ? cnt[lane] : 0;
-                    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
-                    rr += (unsigned long long)c;
-                    if (rs < cn) {
-                        const float *rec = buf + (size_t)rs * RW;
-                        const uint32_t *ri = reinterpret_cast<const uint32_t *>(rec);
-                        const int64_t v0 = (int64_t)(((uint64_t)ri[6] << 32) | ri[5]);
-                        float dkw = dk;
-                        int szw = sz;
-                        replay_block_warp(S, (int)ri[4], rec + 8 + (S + 1), __uint_as_float(ri[7]),
-                                          rec + 8 + (S + 1) + 32, ri[1], ix.ids + v0, sm.pool_id, sm.pool_d, szw, topk,
-                                          dkw, rr);
-                        if (lane == 0) {
-                            distk = dkw;
-                            pool_size = szw;
-                        }
-                    }
-                    if (lane == 0) s_next = rs + 1;
-                }
-                __syncthreads();
-                r0 = s_next;
-            }
-        }
-    }
-    __syncthreads();
-    if (tid == 0 && counters) atomicAdd(counters + 2, rr);
-    if (st.final_level) {
-        write_results(sm, pool_size, topk, k_max, out_ids + (size_t)qi * k_max,
-                      out_d ? out_d + (size_t)qi * k_max : nullptr);
-    } else {  // the pool and its distk carry over to the next level
+    const int S = ix.S;
+    // slots round-robin over a grid sized to the machine (the list length is known on the device only)
+    for (int slot = blockIdx.x; slot < list_len(st); slot += gridDim.x) {
+        const int qi = st.qlist[slot];
+        const int k_max = st.qsh.k_max, topk = st.qsh.k_of(qi);
+        ScanSmem sm = scan_smem_layout(smem_raw, ix.Dtot, S, k_max, xstride);
+        float *stage_buf = reinterpret_cast<float *>(smem_raw + scan_smem_bytes(ix.Dtot, S, k_max, xstride));
+        __shared__ int pool_size;
+        __shared__ float distk;
+        __shared__ int list[kScanThreads * kReplayPer];
+        __shared__ int warp_cnt[kScanWarps];
+        __shared__ int eff[kReplayRecs], cnt[kReplayRecs];
+        __shared__ int s_next, s_plo, s_phi;
+        __shared__ int eff_pos[kReplayRecs], n_eff;  // records replayed in the current chunk
+        __shared__ float eff_dk[kReplayRecs], c_dk0;
+        const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
         for (int i = tid; i < topk; i += blockDim.x) {
-            st.pool_id[(size_t)slot * k_max + i] = sm.pool_id[i];
-            st.pool_d[(size_t)slot * k_max + i] = sm.pool_d[i];
+            sm.pool_id[i] = st.pool_id[(size_t)slot * k_max + i];
+            sm.pool_d[i] = st.pool_d[(size_t)slot * k_max + i];
         }
         if (tid == 0) {
-            st.pool_size[slot] = pool_size;
-            st.tau[slot] = distk;
+            pool_size = st.pool_size[slot];
+            distk = st.tau[slot];
+            s_plo = tile_pos(st, slot, st.t_lo);  // this level's scan positions
+            s_phi = tile_pos(st, slot, st.t_hi);
         }
+        const int np = st.npos[slot];
+        const float4 *su = st.summ + st.pos_off[slot];
+        const float *rq = st.rec + (size_t)st.pos_off[slot] * st.rec_words;
+        const int RW = st.rec_words, R16 = RW / 4;
+        unsigned long long rr = 0;
+        __syncthreads();
+        const int pos_end = min(np, s_phi);
+        for (int base = s_plo; base < pos_end; base += kScanThreads * kReplayPer) {
+            // thread t tests positions base + kReplayPer t .. + kReplayPer - 1; a
+            // block-wide prefix of the counts keeps the list in position order
+            const int p0 = base + kReplayPer * tid;
+            const float dk0 = distk;
+            // with a full pool a lane is accepted only at a value <= distk: a record whose
+            // every such value exceeds distk (summary z) changes nothing and is not staged.
+            // With counters kept, the lanes the reference evaluates in such a record are
+            // counted after each chunk under the distk at its position (count_dropped).
+            const bool zf = pool_size == topk;
+            const int wend = min(pos_end, base + kScanThreads * kReplayPer);
+            bool f[kReplayPer];
+            int mine = 0;
+    #pragma unroll
+            for (int r = 0; r < kReplayPer; ++r) {
+                f[r] = false;
+                if (p0 + r < pos_end) {
+                    const float4 v = su[p0 + r];
+                    f[r] = v.x < dk0 && !(v.y > dk0) && !(zf && v.z > dk0);
+                }
+                mine += f[r];
+            }
+            int incl = mine;
+    #pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += v;
+            }
+            if (lane == 31) warp_cnt[w] = incl;
+            __syncthreads();
+            int off = incl - mine, total = 0;
+            for (int i = 0; i < kScanWarps; ++i) {
+                if (i < w) off += warp_cnt[i];
+                total += warp_cnt[i];
+            }
+    #pragma unroll
+            for (int r = 0; r < kReplayPer; ++r)
+                if (f[r]) list[off++] = p0 + r;
+            __syncthreads();
+            const int nch = (total + kReplayRecs - 1) / kReplayRecs;
+            // lanes with candidate estimate below the distk at their position in the
+            // records of [lo, hi) that the accept bound dropped (distk: c_dk0, then after
+            // each of the n_eff records replayed in this range, in position order)
+            auto count_dropped = [&](int lo, int hi) {
+                unsigned long long add = 0;
+                for (int p = lo + tid; p < hi; p += kScanThreads) {
+                    const float4 v = su[p];
+                    if (!(v.x < dk0 && !(v.y > dk0) && v.z > dk0)) continue;
+                    float dkp = c_dk0;
+                    for (int e = 0; e < n_eff; ++e)
+                        if (eff_pos[e] < p) dkp = eff_dk[e];
+                    if (S > 1 && v.y > dkp) continue;  // a stage minimum above distk: no lane evaluated
+                    const float *rec = rq + (size_t)p * RW;
+                    const float *cur = rec + 8 + (S + 1);
+                    for (uint32_t m = reinterpret_cast<const uint32_t *>(rec)[1]; m; m &= m - 1)
+                        add += cur[__ffs(m) - 1] < dkp;
+                }
+                if (add) atomicAdd(counters + 2, add);
+            };
+            if (nch == 0 && counters && zf) {
+                if (tid == 0) {
+                    c_dk0 = dk0;
+                    n_eff = 0;
+                }
+                __syncthreads();
+                count_dropped(base, wend);
+                __syncthreads();
+            }
+            auto issue = [&](int k) {
+                const int c0 = k * kReplayRecs, cn = min(kReplayRecs, total - c0);
+                float *buf = stage_buf + (size_t)(k & 1) * kReplayRecs * RW;
+                for (int i = tid; i < cn * R16; i += kScanThreads) {
+                    const int r = i / R16, e = i - r * R16;
+                    cp_async16(buf + (size_t)r * RW + 4 * e, rq + (size_t)list[c0 + r] * RW + 4 * e);
+                }
+                cp_async_commit();
+            };
+            if (nch) issue(0);
+            for (int k = 0; k < nch; ++k) {
+                if (k + 1 < nch) {
+                    issue(k + 1);
+                    cp_async_wait<1>();
+                } else {
+                    cp_async_wait<0>();
+                }
+                __syncthreads();
+                const float *buf = stage_buf + (size_t)(k & 1) * kReplayRecs * RW;
+                const int c0 = k * kReplayRecs, cn = min(kReplayRecs, total - c0);
+                if (tid == 0) {  // read by warp 0 (thread 0 first) and, after the chunk, by count_dropped
+                    c_dk0 = distk;
+                    n_eff = 0;
+                }
+                int r0 = 0;
+                while (r0 < cn) {
+                    const float dk = distk;
+                    const int sz = pool_size;
+                    for (int r = r0 + w; r < cn; r += kScanWarps) {
+                        int c;
+                        const bool e = record_effect(S, buf + (size_t)r * RW, dk, sz, topk, c);
+                        if (lane == 0) {
+                            eff[r] = e;
+                            cnt[r] = c;
+                        }
+                    }
+                    __syncthreads();
+                    if (w == 0) {
+                        const bool mine = lane >= r0 && lane < cn;
+                        const uint32_t hit = __ballot_sync(kFull, mine && eff[lane]);
+                        const int rs = hit ? __ffs(hit) - 1 : cn;  // first record that changes the pool
+                        int c = (lane >= r0 && lane < rs) ? cnt[lane] : 0;
+                        for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+                        rr += (unsigned long long)c;
+                        if (rs < cn) {
+                            const float *rec = buf + (size_t)rs * RW;
+                            const uint32_t *ri = reinterpret_cast<const uint32_t *>(rec);
+                            const int64_t v0 = (int64_t)(((uint64_t)ri[6] << 32) | ri[5]);
+                            float dkw = dk;
+                            int szw = sz;
+                            replay_block_warp(S, (int)ri[4], rec + 8 + (S + 1), __uint_as_float(ri[7]),
+                                              rec + 8 + (S + 1) + 32, ri[1], ix.ids + v0, sm.pool_id, sm.pool_d, szw, topk,
+                                              dkw, rr);
+                            if (lane == 0) {
+                                distk = dkw;
+                                pool_size = szw;
+                                eff_pos[n_eff] = list[c0 + rs];
+                                eff_dk[n_eff] = dkw;
+                                ++n_eff;
+                            }
+                        }
+                        if (lane == 0) s_next = rs + 1;
+                    }
+                    __syncthreads();
+                    r0 = s_next;
+                }
+                if (counters && zf) {
+                    count_dropped(k == 0 ? base : list[c0 - 1] + 1, k + 1 == nch ? wend : list[c0 + cn - 1] + 1);
+                    __syncthreads();
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == 0 && counters) atomicAdd(counters + 2, rr);
+        if (st.final_level) {
+            write_results(sm, pool_size, topk, k_max, out_ids + (size_t)qi * k_max,
+                          out_d ? out_d + (size_t)qi * k_max : nullptr);
+        } else {  // the pool and its distk carry over to the next level
+            for (int i = tid; i < topk; i += blockDim.x) {
+                st.pool_id[(size_t)slot * k_max + i] = sm.pool_id[i];
+                st.pool_d[(size_t)slot * k_max + i] = sm.pool_d[i];
+            }
+            if (tid == 0) {
+                st.pool_size[slot] = pool_size;
+                st.tau[slot] = distk;
+            }
+        }
+        __syncthreads();  // the next slot reuses the shared state
     }
 }
 
@@ -2575,7 +2663,11 @@ struct Bump {
 // Bytes of the batched preparation's output for nq x nprobe pairs (0 when it
 // would pass kPrepCap: the scans then build each cluster's state themselves).
 constexpr size_t kPrepCap = (size_t)2 << 30;
+// Calls of fewer queries build each cluster's state in the scan CTAs (256
+// threads per LUT), which is the shorter latency for a single query.
+constexpr int64_t kPrepMinQueries = 64;
 size_t prep_bytes(const Index &I, int64_t nq, int64_t nprobe) {
+    if (nq < kPrepMinQueries) return 0;
     const size_t pairs = (size_t)nq * nprobe;
     const size_t b = align16(pairs * 8 * (size_t)I.view.Dtot) + align16(pairs * sizeof(SegScal) * I.view.S);
     return b <= kPrepCap ? b : 0;
@@ -2618,7 +2710,7 @@ size_t split_scratch_bytes(const Index &I, int64_t cap, int64_t topk, int64_t np
     add(4 * (size_t)(cap + 1));
     add(4 * (size_t)cap);                        // npos
     add(8 * (size_t)cap);                        // pos_off
-    add(8 * (size_t)pos_cap);                    // record summaries
+    add(16 * (size_t)pos_cap);                   // record summaries
     add(4 * (size_t)pos_cap * rec_words_of(I.view.S));
     add((size_t)cap);                            // deferred flags, one per query
     return b + 256;
@@ -2627,7 +2719,7 @@ size_t split_scratch_bytes(const Index &I, int64_t cap, int64_t topk, int64_t np
 // Record positions of the split pass for a batch: every block of every query
 // (`want`), bounded by scratch memory.
 int64_t split_positions(const Index &I, int64_t want) {
-    const size_t per = 4 * (size_t)rec_words_of(I.view.S) + 8;
+    const size_t per = 4 * (size_t)rec_words_of(I.view.S) + 16;
     const int64_t by_mem = (int64_t)(((size_t)4 << 30) / per);
     return std::max<int64_t>(1, std::min(want, by_mem));
 }
@@ -2728,6 +2820,20 @@ void launch_cta_scan(bool ws, const DevIndexView &ix, const uint32_t *probe, con
 }
 
 // SMs x resident CTAs of a kernel (per device and shared-memory size), cached.
+// Streaming multiprocessors of the current device, cached.
+int sm_count() {
+    static std::mutex mu;
+    static std::map<int, int> have;
+    int dev = 0;
+    SAQG_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = have.find(dev);
+    if (it != have.end()) return it->second;
+    int sms = 0;
+    SAQG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    return have[dev] = std::max(1, sms);
+}
+
 int full_grid(const void *fn, int threads, size_t smem) {
     static std::mutex mu;
     static std::map<std::tuple<const void *, int, size_t>, int> have;
@@ -2938,6 +3044,30 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         const int wpb = 8;
         dim3 grid((unsigned)((I.K + wpb - 1) / wpb), (unsigned)nq);
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[0], st));
+        // query preparation (rotation, prune bounds) depends on the queries alone:
+        // it runs on the auxiliary stream beside the centroid ranking
+        {
+            cudaStream_t qs = C.aux_stream();
+            SAQG_CUDA_TRY(cudaEventRecord(C.fork_event(), st));
+            SAQG_CUDA_TRY(cudaStreamWaitEvent(qs, C.fork_event(), 0));
+            size_t qsm = 0;
+            for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
+            if (nq >= kQprepQT && kQprepQT * qsm <= 200 * 1024) {
+                ensure_smem((const void *)k_qprep_tiled, (size_t)(kQprepQT * qsm));
+                k_qprep_tiled<<<dim3((unsigned)ix.S, (unsigned)((nq + kQprepQT - 1) / kQprepQT),
+                                     (unsigned)((qsm / 4 + kQprepSlice - 1) / kQprepSlice)),
+                                kQprepSlice, kQprepQT * qsm, qs>>>(ix, qin, (int)nq, m, qrot, prune);
+                check_launch("k_qprep_tiled");
+            } else {
+                int dmax = 0;
+                for (int s = 0; s < ix.S; ++s) dmax = std::max(dmax, ix.seg[s].dim);
+                const size_t sm_small = 4 * ((size_t)dmax + (size_t)(dmax / 16 + 1) * kQprepOut);
+                k_qprep_small<<<dim3((unsigned)ix.S, (unsigned)nq, (unsigned)((dmax + kQprepOut - 1) / kQprepOut)),
+                                256, sm_small, qs>>>(ix, qin, m, qrot, prune);
+                check_launch("k_qprep_small");
+            }
+            SAQG_CUDA_TRY(cudaEventRecord(C.join_event(), qs));
+        }
         const char *pm = std::getenv("SAQG_PROBE");
         shortlist = nq >= kGemmMinQueries && nprobe <= kShortCap && !(pm && std::string(pm) == "exact");
         if (shortlist) {
@@ -2960,22 +3090,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             check_launch("k_probe_select");
         }
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[1], st));
-        size_t qsm = 0;
-        for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
-        if (nq >= kQprepQT && kQprepQT * qsm <= 200 * 1024) {
-            ensure_smem((const void *)k_qprep_tiled, (size_t)(kQprepQT * qsm));
-            k_qprep_tiled<<<dim3((unsigned)ix.S, (unsigned)((nq + kQprepQT - 1) / kQprepQT),
-                                 (unsigned)((qsm / 4 + kQprepSlice - 1) / kQprepSlice)),
-                            kQprepSlice, kQprepQT * qsm, st>>>(ix, qin, (int)nq, m, qrot, prune);
-            check_launch("k_qprep_tiled");
-        } else {
-            int dmax = 0;
-            for (int s = 0; s < ix.S; ++s) dmax = std::max(dmax, ix.seg[s].dim);
-            const size_t sm_small = 4 * ((size_t)dmax + (size_t)(dmax / 16 + 1) * kQprepOut);
-            k_qprep_small<<<dim3((unsigned)ix.S, (unsigned)nq, (unsigned)((dmax + kQprepOut - 1) / kQprepOut)), 256,
-                            sm_small, st>>>(ix, qin, m, qrot, prune);
-            check_launch("k_qprep_small");
-        }
+        SAQG_CUDA_TRY(cudaStreamWaitEvent(st, C.join_event(), 0));  // the rotated queries
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[2], st));
         const int xs = xstride_of(ix);
         const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs);
@@ -2985,20 +3100,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         unsigned long long *cnt = stats ? counters : nullptr;
         const int mode0 = scan_mode(nq, topk, tune);
         const int mode = (qsh.np || qsh.k) && mode0 == 2 ? 0 : mode0;
-        Prepared prep;  // every (query, probe) pair's LUT, built by one batched kernel
-        if (mode != 2 && prep_lut) {
-            const size_t lsm = 4 * (size_t)kLutWarps * ix.Dtot;
-            SAQG_REQUIRE(lsm <= 200 * 1024, "dimension too large for the batched LUT preparation");
-            ensure_smem((const void *)k_lut, lsm);
-            const int64_t pairs = nq * nprobe;
-            k_lut<<<(unsigned)((pairs + kLutWarps - 1) / kLutWarps), kLutWarps * 32, lsm, st>>>(
-                ix, probe, qsh, (int)nq, qrot, prune, prep_lut, prep_scal);
-            check_launch("k_lut");
-            count_launch(1);
-            prep.lut = prep_lut;
-            prep.scal = prep_scal;
-            prep.np_max = (int)nprobe;
-        }
+
         if (mode == 2) {
             const size_t per_warp = align16(warp_smem_bytes(ix.Dtot, ix.S, (int)topk));
             const size_t wsm = per_warp * kWarpsPerCta;
@@ -3011,7 +3113,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             // no query of this call can probe more blocks than the deferral
             // threshold: the CTA scan answers every query, no split pass
             launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, nullptr, nq, order,
-                            prep, st);
+                            Prepared{}, st);
             count_launch(4);
         } else {
             // split-pass state: every query (mode 1), or the deferred giant-cluster queries (mode 0)
@@ -3038,7 +3140,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             ss.npos = sb.take<int>(cap);
             ss.pos_off = sb.take<int64_t>(cap);
             ss.pos_cap = pos_cap;
-            ss.summ = sb.take<float2>((size_t)pos_cap);
+            ss.summ = sb.take<float4>((size_t)pos_cap);
             ss.rec_words = rec_words_of(ix.S);
             ss.rec = sb.take<float>((size_t)pos_cap * ss.rec_words);
             ss.qsh = qsh;
@@ -3050,7 +3152,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             ss.final_level = 1;
             if (const char *e = std::getenv("SAQG_FIRST_BLOCKS")) ss.first_blocks = std::max(1, std::atoi(e));
             uint8_t *deferred = sb.take<uint8_t>(nq);
-            SAQG_CUDA_TRY(cudaMemsetAsync(ss.summ, 0xff, 8 * (size_t)pos_cap, st));  // NaN: no record
+            SAQG_CUDA_TRY(cudaMemsetAsync(ss.summ, 0xff, 16 * (size_t)pos_cap, st));  // NaN: no record
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 32, st));
             int defer = -1;  // mode 1: every query
             if (mode == 0) defer = defer_threshold(tune);
@@ -3066,7 +3168,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                     SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, C.fork_event(), 0));
                 }
                 launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, deferred, nq,
-                                order, prep, st);
+                                order, Prepared{}, st);
             }
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
             const size_t smem_r = smem + 2 * 4 * (size_t)kReplayRecs * ss.rec_words;
@@ -3074,7 +3176,23 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             ensure_smem((const void *)k_scan_first, (size_t)smem);
             ensure_smem((const void *)k_scan_spec, (size_t)smem1);
             ensure_smem((const void *)k_scan_replay, (size_t)smem_r);
-            k_scan_first<<<(unsigned)cap, kScanThreads, smem, sp>>>(ix, probe, qrot, prune, ss, flags + 1, cnt, xs,
+            Prepared prep;  // the listed queries' LUTs, one batched kernel ahead of the split pass
+            if (prep_lut) {
+                const size_t lsm = 4 * (size_t)kLutWarps * ix.Dtot;
+                SAQG_REQUIRE(lsm <= 200 * 1024, "dimension too large for the batched LUT preparation");
+                ensure_smem((const void *)k_lut, lsm);
+                const int64_t items = cap * nprobe;
+                k_lut<<<(unsigned)((items + kLutWarps - 1) / kLutWarps), kLutWarps * 32, lsm, sp>>>(
+                    ix, probe, qsh, ss.qlist, ss.nlist, ss.cap, qrot, prune, prep_lut, prep_scal);
+                check_launch("k_lut");
+                count_launch(1);
+                prep.lut = prep_lut;
+                prep.scal = prep_scal;
+                prep.np_max = (int)nprobe;
+            }
+            // the list holds at most cap slots; the per-slot kernels loop over them
+            const unsigned slot_grid = (unsigned)std::min<int64_t>(cap, 4 * (int64_t)sm_count());
+            k_scan_first<<<slot_grid, kScanThreads, smem, sp>>>(ix, probe, qrot, prune, ss, flags + 1, cnt, xs,
                                                                      prep);
             check_launch("k_scan_first");
             if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[5], sp));
@@ -3096,7 +3214,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                 k_scan_spec<<<grid, kScanThreads, smem1, sp>>>(ix, probe, (int)nprobe, qrot, prune, sl, cnt, xs, prep);
                 check_launch("k_scan_spec");
                 if (stats && sl.final_level) SAQG_CUDA_TRY(cudaEventRecord(ev[6], sp));
-                k_scan_replay<<<(unsigned)cap, kScanThreads, smem_r, sp>>>(ix, sl, ids_out, d_out, cnt, xs);
+                k_scan_replay<<<slot_grid, kScanThreads, smem_r, sp>>>(ix, sl, ids_out, d_out, cnt, xs);
                 check_launch("k_scan_replay");
             }
             if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[4], sp));
