@@ -349,6 +349,141 @@ __device__ __forceinline__ float excode_ip_thread(const float *__restrict__ q, c
     return ip8_thread(q, y, D, exb);
 }
 
+// ---- the same inner products by four lanes: lane j of an aligned group of
+// four keeps the SIMD accumulators 4j .. 4j+3 of ip_thread_bits, reading the
+// same words, and the group combines them with tree16's pairing (i with i + 8
+// and i + 4 across lanes, then (0 + 2) + (1 + 3) in lane 0).  Bit-identical to
+// the one-thread form, a quarter of its chain; valid in the group's lane 0.
+__device__ __forceinline__ uint32_t pick4(uint32_t a, uint32_t b, uint32_t c, uint32_t d, int j) {
+    return j == 0 ? a : j == 1 ? b : j == 2 ? c : d;
+}
+
+template <int B>
+__device__ __forceinline__ float ip_quad_bits(const float *__restrict__ q, const uint8_t *__restrict__ y, int D, int j) {
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const int l0 = 4 * j;
+    if (B == 1) {
+        for (int g = 0; g < D; g += 16) {
+            const uint32_t m = (uint32_t)y[g / 8] | ((uint32_t)y[g / 8 + 1] << 8);
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) {
+                const int l = l0 + jj;
+                acc[jj] = __fadd_rn(acc[jj], ((m >> l) & 1u) ? q[g + l] : 0.0f);
+            }
+        }
+    } else if (B == 2 || B == 3) {
+        for (int g = 0; g < D; g += 64) {
+            const uint8_t *gp = y + (g / 64) * (B == 2 ? 16 : 24);
+            const uint2 w0 = *reinterpret_cast<const uint2 *>(gp), w1 = *reinterpret_cast<const uint2 *>(gp + 8);
+            const uint32_t w = pick4(w0.x, w0.y, w1.x, w1.y, j);
+            uint32_t tw = 0;
+            if (B == 3) {
+                const uint2 tt = *reinterpret_cast<const uint2 *>(gp + 16);
+                tw = (j & 1) ? tt.y : tt.x;  // word (l & 7) >> 2 of the top bits
+            }
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) {
+                const int l = l0 + jj;
+                const uint32_t b = (w >> (8 * jj)) & 255u;
+                const uint32_t t = (tw >> (8 * jj)) & 255u;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    uint32_t v = (b >> (2 * k)) & 3u;
+                    if (B == 3) v |= ((t >> (2 * k + (l >> 3))) & 1u) << 2;
+                    acc[jj] = fmaf((float)v, q[g + 16 * k + l], acc[jj]);
+                }
+            }
+        }
+    } else if (B == 4) {
+        for (int g = 0; g < D; g += 32) {
+            const uint4 w4 = *reinterpret_cast<const uint4 *>(y + (g / 32) * 16);
+            const uint32_t w = pick4(w4.x, w4.y, w4.z, w4.w, j);
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) {
+                const int l = l0 + jj;
+                const uint32_t b = (w >> (8 * jj)) & 255u;
+                acc[jj] = fmaf((float)(b & 15u), q[g + l], acc[jj]);
+                acc[jj] = fmaf((float)(b >> 4), q[g + 16 + l], acc[jj]);
+            }
+        }
+    } else if (B == 6 || B == 7) {
+        for (int g = 0; g < D; g += 64) {
+            const uint8_t *gp = y + (g / 64) * (B == 6 ? 48 : 56);
+            uint32_t tw = 0;
+            if (B == 7) {
+                const uint2 tt = *reinterpret_cast<const uint2 *>(gp + 48);
+                tw = (j & 1) ? tt.y : tt.x;
+            }
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) {
+                const int l = l0 + jj;
+                const uint32_t b0 = gp[l], b1 = gp[16 + l], b2 = gp[32 + l];
+                uint32_t v0 = b0 & 63u, v1 = b1 & 63u;
+                uint32_t v2 = ((b0 >> 6) << 4) | (b2 & 15u), v3 = ((b1 >> 6) << 4) | (b2 >> 4);
+                if (B == 7) {
+                    const uint32_t t = (tw >> (8 * jj)) & 255u;
+                    const int sh = l >> 3;
+                    v0 |= ((t >> (0 + sh)) & 1u) << 6;
+                    v1 |= ((t >> (2 + sh)) & 1u) << 6;
+                    v2 |= ((t >> (4 + sh)) & 1u) << 6;
+                    v3 |= ((t >> (6 + sh)) & 1u) << 6;
+                }
+                acc[jj] = fmaf((float)v0, q[g + l], acc[jj]);
+                acc[jj] = fmaf((float)v1, q[g + 16 + l], acc[jj]);
+                acc[jj] = fmaf((float)v2, q[g + 32 + l], acc[jj]);
+                acc[jj] = fmaf((float)v3, q[g + 48 + l], acc[jj]);
+            }
+        }
+    } else {  // 8
+        for (int g = 0; g < D; g += 16) {
+            const uint4 w4 = *reinterpret_cast<const uint4 *>(y + g);
+            const uint32_t w = pick4(w4.x, w4.y, w4.z, w4.w, j);
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) acc[jj] = fmaf((float)((w >> (8 * jj)) & 255u), q[g + l0 + jj], acc[jj]);
+        }
+    }
+    // tree16: x[i] = a[i] + a[i + 8] (lanes 0, 1 with lanes 2, 3), y[i] = x[i] + x[i + 4]
+    // (lane 0 with lane 1), then (y0 + y2) + (y1 + y3)
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) acc[jj] = __fadd_rn(acc[jj], __shfl_down_sync(kFull, acc[jj], 2, 4));
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) acc[jj] = __fadd_rn(acc[jj], __shfl_down_sync(kFull, acc[jj], 1, 4));
+    return __fadd_rn(__fadd_rn(acc[0], acc[2]), __fadd_rn(acc[1], acc[3]));
+}
+
+__device__ __forceinline__ float ip8_quad(const float *__restrict__ q, const uint8_t *__restrict__ y, int D, int bits,
+                                          int j) {
+    switch (bits) {
+    case 1:
+        return ip_quad_bits<1>(q, y, D, j);
+    case 2:
+        return ip_quad_bits<2>(q, y, D, j);
+    case 3:
+        return ip_quad_bits<3>(q, y, D, j);
+    case 4:
+        return ip_quad_bits<4>(q, y, D, j);
+    case 5:  // CodeHelper<5>::compute_ip = 2 * IP4(top 4 bits) + IP1(low bit)
+        return __fadd_rn(2.0f * ip_quad_bits<4>(q, y, D, j), ip_quad_bits<1>(q, y + D / 2, D, j));
+    case 6:
+        return ip_quad_bits<6>(q, y, D, j);
+    case 7:
+        return ip_quad_bits<7>(q, y, D, j);
+    case 8:
+        return ip_quad_bits<8>(q, y, D, j);
+    default:
+        return 0.0f;
+    }
+}
+
+// get_IP_FUNC(ex_bits)(q, y, D) by an aligned group of four lanes (j = lane & 3;
+// every lane of the warp takes part); valid in the group's lane 0.
+__device__ __forceinline__ float excode_ip_quad(const float *__restrict__ q, const uint8_t *__restrict__ y, int D,
+                                                int exb, int j) {
+    if (exb == 0) return 0.0f;
+    if (exb > 8) return __fadd_rn(ip8_quad(q, y, D, 8, j), 256.0f * ip8_quad(q, y + D, D, exb - 8, j));
+    return ip8_quad(q, y, D, exb, j);
+}
+
 // CaqCluEstimator::compAccurateDist + Lut::getExtIP, L2 (caq_estimator.hpp:190-217, lut.hpp:121-126)
 __device__ __forceinline__ float accurate_dist(float onorm, float ipx, float ex_ip, float rescale, int bits, float sum_q,
                                                float q_l2sqr) {

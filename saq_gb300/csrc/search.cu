@@ -22,6 +22,7 @@
 #include <climits>
 #include <cstdio>
 #include <cstdlib>
+#include <functional>
 #include <map>
 #include <memory>
 #include <string>
@@ -1289,19 +1290,44 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
             for (int o = 0; o < g.lstride; o += 128) asm volatile("prefetch.global.L1 [%0];" ::"l"(row + o));
         }
     }
-    for (int t = tid; t < total; t += nthr) {
-        const int s = t / P, r = t - s * P;
-        if (r >= ncand) continue;
-        int ww, j;
-        decode(r, ww, j);
+    auto finish = [&](int s, int ww, int j, float ex) {
         const int64_t gb = b0 + t0 + ww, gv = v0 + (int64_t)(t0 + ww) * 32 + j;
         const SegDev &g = ix.seg[s];
-        const float ex =
-            g.bits > 1 ? excode_ip_thread(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim, g.bits - 1) : 0.0f;
         const SegScal &sc = sm.scal[s];
         const float acc = accurate_dist(g.onorm[gb * 32 + j], sm.ipx[(ww * S + s) * 32 + j], ex, g.exfac[gv].x, g.bits,
                                         sc.sum_q, sc.q_l2sqr);
         sm.part[(ww * S + s) * 32 + j] = S == 1 ? acc : __fsub_rn(acc, sm.cd[(ww * S + s) * 32 + j]);
+    };
+    // few tasks: four lanes per task (excode_ip_quad), a quarter of the chain;
+    // else one thread per task
+    const int P4 = (ncand + 7) & ~7;
+    if (S * P4 * 4 <= nthr) {
+        // a warp holds 8 tasks of one segment (each segment's tasks padded to a
+        // multiple of 8); padding tasks compute on candidate 0 and are discarded
+        for (int gl = tid; gl < S * P4 * 4; gl += nthr) {  // warp-uniform: a multiple of 32 lanes
+            const int t = gl >> 2, q4 = gl & 3, s = t / P4, r = t - s * P4;
+            const bool valid = r < ncand;
+            int ww, j;
+            decode(valid ? r : 0, ww, j);
+            const SegDev &g = ix.seg[s];
+            const int64_t gv = v0 + (int64_t)(t0 + ww) * 32 + j;
+            const float ex = g.bits > 1 ? excode_ip_quad(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim,
+                                                         g.bits - 1, q4)
+                                        : 0.0f;
+            if (valid && q4 == 0) finish(s, ww, j, ex);
+        }
+    } else {
+        for (int t = tid; t < total; t += nthr) {
+            const int s = t / P, r = t - s * P;
+            if (r >= ncand) continue;
+            int ww, j;
+            decode(r, ww, j);
+            const SegDev &g = ix.seg[s];
+            const int64_t gv = v0 + (int64_t)(t0 + ww) * 32 + j;
+            finish(s, ww, j,
+                   g.bits > 1 ? excode_ip_thread(sm.qres + g.qoff, g.lcode + (size_t)gv * g.lstride, g.dim, g.bits - 1)
+                              : 0.0f);
+        }
     }
     sync();
 }
@@ -2533,17 +2559,22 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan(DevIndexVie
 constexpr int kOrderThreads = 1024;
 constexpr int kOrderMinQueries = 1024;  // batches from which the CTA scan is launched heaviest first
 __global__ void __launch_bounds__(kOrderThreads) k_order(DevIndexView ix, const uint32_t *__restrict__ probe, QueryShape qsh,
-                                                         int nq, int *__restrict__ order) {
+                                                         int nq, const int *__restrict__ qblocks,
+                                                         int *__restrict__ order) {
     __shared__ int cnt[32], cur[32];
     const int tid = threadIdx.x;
     if (tid < 32) cnt[tid] = 0;
     __syncthreads();
     auto cls = [&](int qi) {
         int64_t total = 0;
-        const int np = qsh.np_of(qi);
-        for (int p = 0; p < np; ++p) {
-            const int c = (int)probe[(size_t)qi * qsh.np_max + p];
-            total += ix.blk_off[c + 1] - ix.blk_off[c];
+        if (qblocks) {
+            total = qblocks[qi];
+        } else {
+            const int np = qsh.np_of(qi);
+            for (int p = 0; p < np; ++p) {
+                const int c = (int)probe[(size_t)qi * qsh.np_max + p];
+                total += ix.blk_off[c + 1] - ix.blk_off[c];
+            }
         }
         return 31 - min(31, 63 - __clzll((long long)total + 1));  // heavier: smaller class
     };
@@ -2564,7 +2595,7 @@ __global__ void __launch_bounds__(kOrderThreads) k_order(DevIndexView ix, const 
 // Zipf cluster; every query when defer_blocks < 0) on the split list, each
 // with record positions for all its blocks, while the record space lasts.
 __global__ void k_defer(DevIndexView ix, const uint32_t *__restrict__ probe, int nq, int defer_blocks, SplitState st,
-                        uint8_t *__restrict__ deferred) {
+                        uint8_t *__restrict__ deferred, int *__restrict__ qblocks) {
     const int qi = blockIdx.x * blockDim.x + threadIdx.x;
     if (qi >= nq) return;
     int64_t total = 0;
@@ -2573,6 +2604,7 @@ __global__ void k_defer(DevIndexView ix, const uint32_t *__restrict__ probe, int
         const int c = (int)probe[(size_t)qi * st.qsh.np_max + p];
         total += ix.blk_off[c + 1] - ix.blk_off[c];
     }
+    qblocks[qi] = total < (int64_t)INT_MAX ? (int)total : INT_MAX;  // the CTA scan's launch order
     uint8_t d = 0;
     if (defer_blocks < 0 || (defer_blocks > 0 && total > defer_blocks)) {
         // reserve [cur, cur + total) of the record space (lock-free; bounded retries)
@@ -2713,6 +2745,7 @@ size_t split_scratch_bytes(const Index &I, int64_t cap, int64_t topk, int64_t np
     add(16 * (size_t)pos_cap);                   // record summaries
     add(4 * (size_t)pos_cap * rec_words_of(I.view.S));
     add((size_t)cap);                            // deferred flags, one per query
+    add(4 * (size_t)cap);                        // blocks of each query's probes
     return b + 256;
 }
 
@@ -2797,9 +2830,10 @@ void ensure_smem(const void *fn, size_t bytes) {
 // its warp-specialised form k_scan_ws, which gives the same answers.
 void launch_cta_scan(bool ws, const DevIndexView &ix, const uint32_t *probe, const QueryShape &qsh, const float *qrot,
                      const float *prune, uint32_t *ids, float *d, unsigned long long *cnt, int xs,
-                     const uint8_t *deferred, int64_t nq, int *order, const Prepared &prep, cudaStream_t st) {
+                     const uint8_t *deferred, int64_t nq, int *order, const int *qblocks, const Prepared &prep,
+                     cudaStream_t st) {
     if (order) {
-        k_order<<<1, kOrderThreads, 0, st>>>(ix, probe, qsh, (int)nq, order);
+        k_order<<<1, kOrderThreads, 0, st>>>(ix, probe, qsh, (int)nq, qblocks, order);
         check_launch("k_order");
     }
     if (ws) {
@@ -2873,7 +2907,8 @@ namespace {
 // kernel, and the full exact path for the queries it hands back.
 void probe_shortlist(const Index &I, SearchCtx &C, const float *q, int64_t nq, int64_t nprobe, const int *qnp,
                      float *dist, uint32_t *probe, uint8_t *full, int *fb_list, int *flags, Cand *work,
-                     unsigned long long *cnt, void *qbf, cudaStream_t st) {
+                     unsigned long long *cnt, void *qbf, cudaStream_t st,
+                     const std::function<void()> &after_gemm = nullptr) {
     const DevIndexView &ix = I.view;
     {
         std::lock_guard<std::mutex> lk(I.init_mu);
@@ -2901,6 +2936,7 @@ void probe_shortlist(const Index &I, SearchCtx &C, const float *q, int64_t nq, i
     // to nearest, FP32 accumulation); flags[3] is set if a GEMM wait timed out
     to_bf16(q, nq * I.D, qbf, st);
     probe_ip_gemm(qbf, nq, I.cent_bf16, I.K, I.D, dist, flags + 3, st);
+    if (after_gemm) after_gemm();  // work that can run beside the shortlist and its select
     const double u = 1.0 / 16777216.0;
     ShortBound sb;
     // BF16 operands lie within 2^-9 of their values: |q.c error| <= (2^-8 + 2^-18) |q||c| + accumulation
@@ -3045,8 +3081,10 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         dim3 grid((unsigned)((I.K + wpb - 1) / wpb), (unsigned)nq);
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[0], st));
         // query preparation (rotation, prune bounds) depends on the queries alone:
-        // it runs on the auxiliary stream beside the centroid ranking
-        {
+        // it runs on the auxiliary stream beside the centroid ranking (beside the
+        // shortlist and its select when the GEMM ranks the centroids: the GEMM
+        // wants whole SMs)
+        auto launch_qprep = [&]() {
             cudaStream_t qs = C.aux_stream();
             SAQG_CUDA_TRY(cudaEventRecord(C.fork_event(), st));
             SAQG_CUDA_TRY(cudaStreamWaitEvent(qs, C.fork_event(), 0));
@@ -3067,12 +3105,13 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                 check_launch("k_qprep_small");
             }
             SAQG_CUDA_TRY(cudaEventRecord(C.join_event(), qs));
-        }
+        };
         const char *pm = std::getenv("SAQG_PROBE");
         shortlist = nq >= kGemmMinQueries && nprobe <= kShortCap && !(pm && std::string(pm) == "exact");
+        if (!shortlist) launch_qprep();
         if (shortlist) {
             probe_shortlist(I, C, qin, nq, nprobe, qsh.np, dist, probe, full, fb_list, flags, work,
-                            stats ? counters : nullptr, qbf, st);
+                            stats ? counters : nullptr, qbf, st, launch_qprep);
         } else if (nq >= 8 && I.D % 32 == 0 && I.D <= 32 * kProbeRegs) {
             const size_t qsm = 4 * (size_t)kProbeQT * I.D;
             ensure_smem((const void *)k_probe_dist_tiled, (size_t)qsm);
@@ -3113,7 +3152,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             // no query of this call can probe more blocks than the deferral
             // threshold: the CTA scan answers every query, no split pass
             launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, nullptr, nq, order,
-                            Prepared{}, st);
+                            nullptr, Prepared{}, st);
             count_launch(4);
         } else {
             // split-pass state: every query (mode 1), or the deferred giant-cluster queries (mode 0)
@@ -3152,11 +3191,12 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             ss.final_level = 1;
             if (const char *e = std::getenv("SAQG_FIRST_BLOCKS")) ss.first_blocks = std::max(1, std::atoi(e));
             uint8_t *deferred = sb.take<uint8_t>(nq);
+            int *qblocks = sb.take<int>(nq);
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.summ, 0xff, 16 * (size_t)pos_cap, st));  // NaN: no record
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 32, st));
             int defer = -1;  // mode 1: every query
             if (mode == 0) defer = defer_threshold(tune);
-            k_defer<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(ix, probe, (int)nq, defer, ss, deferred);
+            k_defer<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(ix, probe, (int)nq, defer, ss, deferred, qblocks);
             check_launch("k_defer");
             cudaStream_t sp = st;  // stream of the split pass
             // the CTA scan serves what the split list does not hold: always in mode 0,
@@ -3168,7 +3208,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                     SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, C.fork_event(), 0));
                 }
                 launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, deferred, nq,
-                                order, Prepared{}, st);
+                                order, qblocks, Prepared{}, st);
             }
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
             const size_t smem_r = smem + 2 * 4 * (size_t)kReplayRecs * ss.rec_words;
