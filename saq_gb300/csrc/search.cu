@@ -2591,39 +2591,129 @@ __global__ void __launch_bounds__(kOrderThreads) k_order(DevIndexView ix, const 
     for (int qi = tid; qi < nq; qi += kOrderThreads) order[atomicAdd(&cur[cls(qi)], 1)] = qi;
 }
 
-// Puts every query whose probes hold more than `defer_blocks` blocks (a giant
-// Zipf cluster; every query when defer_blocks < 0) on the split list, each
-// with record positions for all its blocks, while the record space lasts.
-__global__ void k_defer(DevIndexView ix, const uint32_t *__restrict__ probe, int nq, int defer_blocks, SplitState st,
-                        uint8_t *__restrict__ deferred, int *__restrict__ qblocks) {
+// Blocks of each query's probes (the deferral's weights and the CTA scan's
+// launch order), one thread per query.
+__global__ void k_qblocks(DevIndexView ix, const uint32_t *__restrict__ probe, QueryShape qsh, int nq,
+                          int *__restrict__ qblocks) {
     const int qi = blockIdx.x * blockDim.x + threadIdx.x;
     if (qi >= nq) return;
     int64_t total = 0;
-    const int nprobe = st.qsh.np_of(qi);
-    for (int p = 0; p < nprobe; ++p) {
-        const int c = (int)probe[(size_t)qi * st.qsh.np_max + p];
+    const int np = qsh.np_of(qi);
+    for (int p = 0; p < np; ++p) {
+        const int c = (int)probe[(size_t)qi * qsh.np_max + p];
         total += ix.blk_off[c + 1] - ix.blk_off[c];
     }
-    qblocks[qi] = total < (int64_t)INT_MAX ? (int)total : INT_MAX;  // the CTA scan's launch order
-    uint8_t d = 0;
-    if (defer_blocks < 0 || (defer_blocks > 0 && total > defer_blocks)) {
-        // reserve [cur, cur + total) of the record space (lock-free; bounded retries)
-        unsigned long long cur = atomicAdd(st.pos_used, 0ull);
-        for (int tries = 0; tries < (1 << 16); ++tries) {
-            if (cur + (unsigned long long)total > (unsigned long long)st.pos_cap) break;
-            const unsigned long long prev = atomicCAS(st.pos_used, cur, cur + (unsigned long long)total);
-            if (prev == cur) {
-                const int t = atomicAdd(st.nlist, 1);  // < cap: cap is the batch size
-                st.qlist[t] = qi;
-                st.pos_off[t] = (int64_t)cur;
-                st.npos[t] = (int)total;
-                d = 1;
-                break;
-            }
-            cur = prev;
-        }
+    qblocks[qi] = total < (int64_t)INT_MAX ? (int)total : INT_MAX;
+}
+
+// Puts the queries whose probes hold more than `defer_blocks` blocks (giant Zipf
+// clusters; every query when defer_blocks < 0) on the split list, each with
+// record positions for all its blocks, heaviest first while the record space
+// lasts: queries in power-of-two classes of their blocks, heavy classes first,
+// in query order inside a class.  What does not fit is left to the CTA scan,
+// which then holds the lighter queries.  One CTA of kDeferThreads; thread t owns
+// the queries [t * per, (t + 1) * per).
+constexpr int kDeferThreads = 1024;
+__global__ void __launch_bounds__(kDeferThreads) k_defer(int nq, int defer_blocks, SplitState st,
+                                                         const int *__restrict__ qblocks, uint8_t *__restrict__ deferred) {
+    __shared__ long long wsum_b[kDeferThreads / 32];
+    __shared__ int wsum_n[kDeferThreads / 32], hist[32];
+    __shared__ long long s_base;  // record positions handed out
+    __shared__ int s_slot;        // list entries handed out
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int per = (nq + kDeferThreads - 1) / kDeferThreads, q0 = min(nq, tid * per), q1 = min(nq, q0 + per);
+    auto eligible = [&](int qi) {
+        return defer_blocks < 0 || (defer_blocks > 0 && qblocks[qi] > defer_blocks);
+    };
+    auto cls = [&](int qi) { return 31 - min(31, 31 - __clz(qblocks[qi] + 1)); };  // heavier: smaller class
+    if (tid < 32) hist[tid] = 0;
+    if (tid == 0) {
+        s_base = 0;
+        s_slot = 0;
     }
-    deferred[qi] = d;
+    __syncthreads();
+    for (int qi = q0; qi < q1; ++qi) {
+        deferred[qi] = 0;
+        if (eligible(qi)) atomicAdd(&hist[cls(qi)], 1);
+    }
+    __syncthreads();
+    for (int c = 0; c < 32; ++c) {
+        if (hist[c] == 0) continue;  // uniform: read after a barrier
+        long long mine = 0;
+        int cnt = 0;
+        for (int qi = q0; qi < q1; ++qi)
+            if (eligible(qi) && cls(qi) == c) {
+                mine += qblocks[qi];
+                ++cnt;
+            }
+        // exclusive prefix of (blocks, count) over the threads, in thread order
+        long long xb = mine;
+        int xn = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long yb = __shfl_up_sync(0xffffffffu, xb, o);
+            const int yn = __shfl_up_sync(0xffffffffu, xn, o);
+            if (lane >= o) {
+                xb += yb;
+                xn += yn;
+            }
+        }
+        if (lane == 31) {
+            wsum_b[w] = xb;
+            wsum_n[w] = xn;
+        }
+        __syncthreads();
+        long long before_b = xb - mine;
+        int before_n = xn - cnt;
+        for (int i = 0; i < w; ++i) {
+            before_b += wsum_b[i];
+            before_n += wsum_n[i];
+        }
+        const long long base = s_base;
+        const int slot0 = s_slot;
+        __syncthreads();  // every thread has read s_base / s_slot and the warp sums
+        // the accepted queries of the class are a prefix of its order: positions grow along it
+        long long acc_b = 0;
+        int acc_n = 0;
+        long long pos = base + before_b;
+        int k = before_n;
+        for (int qi = q0; qi < q1; ++qi) {
+            if (!eligible(qi) || cls(qi) != c) continue;
+            const int t = qblocks[qi];
+            if (pos + t > st.pos_cap) break;
+            const int slot = slot0 + k;
+            st.qlist[slot] = qi;
+            st.pos_off[slot] = pos;
+            st.npos[slot] = t;
+            deferred[qi] = 1;
+            pos += t;
+            ++k;
+            acc_b += t;
+            ++acc_n;
+        }
+        // the class's accepted blocks and queries
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            acc_b += __shfl_xor_sync(0xffffffffu, acc_b, o);
+            acc_n += __shfl_xor_sync(0xffffffffu, acc_n, o);
+        }
+        if (lane == 0) {
+            wsum_b[w] = acc_b;
+            wsum_n[w] = acc_n;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (int i = 0; i < kDeferThreads / 32; ++i) {
+                s_base += wsum_b[i];
+                s_slot += wsum_n[i];
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        *st.nlist = s_slot;
+        *st.pos_used = (unsigned long long)s_base;
+    }
 }
 
 // ------------------------------------------------------------------ estimate
@@ -2753,7 +2843,7 @@ size_t split_scratch_bytes(const Index &I, int64_t cap, int64_t topk, int64_t np
 // (`want`), bounded by scratch memory.
 int64_t split_positions(const Index &I, int64_t want) {
     const size_t per = 4 * (size_t)rec_words_of(I.view.S) + 16;
-    const int64_t by_mem = (int64_t)(((size_t)4 << 30) / per);
+    const int64_t by_mem = (int64_t)(((size_t)8 << 30) / per);
     return std::max<int64_t>(1, std::min(want, by_mem));
 }
 
@@ -3196,7 +3286,9 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 32, st));
             int defer = -1;  // mode 1: every query
             if (mode == 0) defer = defer_threshold(tune);
-            k_defer<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(ix, probe, (int)nq, defer, ss, deferred, qblocks);
+            k_qblocks<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(ix, probe, qsh, (int)nq, qblocks);
+            check_launch("k_qblocks");
+            k_defer<<<1, kDeferThreads, 0, st>>>((int)nq, defer, ss, qblocks, deferred);
             check_launch("k_defer");
             cudaStream_t sp = st;  // stream of the split pass
             // the CTA scan serves what the split list does not hold: always in mode 0,
