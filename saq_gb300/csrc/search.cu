@@ -1041,27 +1041,30 @@ __device__ void prepare_cluster(const DevIndexView &ix, const float *__restrict_
     sync();
 }
 
-// Output of the batched preparation (k_lut); null members: the scans build
-// each cluster's state themselves.
+// Output of the batched preparation (k_lut) for the first `slots` entries of the
+// split list; other entries (and null members) build each cluster's state in
+// the scan CTA.
 struct Prepared {
     const uint16_t *lut = nullptr;
     const SegScal *scal = nullptr;
     int np_max = 0;
-    __device__ __forceinline__ const uint16_t *lut_of(int qi, int p, int Dtot) const {
-        return lut + ((size_t)qi * np_max + p) * 4 * Dtot;
+    int slots = 0;
+    __device__ __forceinline__ bool has(int slot) const { return lut != nullptr && slot < slots; }
+    __device__ __forceinline__ const uint16_t *lut_of(int slot, int p, int Dtot) const {
+        return lut + ((size_t)slot * np_max + p) * 4 * Dtot;
     }
-    __device__ __forceinline__ const SegScal *scal_of(int qi, int p, int S) const {
-        return scal + ((size_t)qi * np_max + p) * S;
+    __device__ __forceinline__ const SegScal *scal_of(int slot, int p, int S) const {
+        return scal + ((size_t)slot * np_max + p) * S;
     }
 };
 
 // ---- batched preparation: the LUT and scalars of the (query, probe) pairs of
-// the queries on a list (the split pass's), one warp per pair.  Pair i =
-// query * np_max + probe; its LUT is 4 * Dtot u16 at lut + i * 4 * Dtot (the
-// layout of ScanSmem::lut), its scalars S SegScal at scal + i * S.  Work item w
-// is list entry w / np_max (entries at or past *nlist are none) and probe
-// w % np_max.  Pairs past a query's nprobe and pairs of empty clusters are not
-// written (no scan reads them).
+// the first `slots` entries of a list (the split pass's), one warp per pair.
+// Pair i = slot * np_max + probe; its LUT is 4 * Dtot u16 at lut + i * 4 * Dtot
+// (the layout of ScanSmem::lut), its scalars S SegScal at scal + i * S.  Work
+// item w is list entry w / np_max (entries at or past *nlist are none) and
+// probe w % np_max.  Pairs past a query's nprobe and pairs of empty clusters
+// are not written (no scan reads them).
 constexpr int kLutWarps = 8;
 __global__ void __launch_bounds__(kLutWarps * 32) k_lut(DevIndexView ix, const uint32_t *__restrict__ probe,
                                                         QueryShape qsh, const int *__restrict__ qlist,
@@ -1076,8 +1079,8 @@ __global__ void __launch_bounds__(kLutWarps * 32) k_lut(DevIndexView ix, const u
     if (slot >= min(*nlist, cap)) return;  // whole warp
     const int qi = qlist[slot];
     if (p >= qsh.np_of(qi)) return;
-    const int64_t pair = (int64_t)qi * qsh.np_max + p;
-    const int c = (int)probe[pair];
+    const int64_t pair = (int64_t)slot * qsh.np_max + p;
+    const int c = (int)probe[(size_t)qi * qsh.np_max + p];
     if (ix.blk_off[c + 1] == ix.blk_off[c]) return;
     float *qres = k_lut_qres + (size_t)warp * ix.Dtot;
     const float *qrot = qrot_all + (size_t)qi * ix.Dtot;
@@ -2059,7 +2062,7 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_first(DevIn
                     break;
                 }
                 if (!prepared) {
-                    if (prep.lut) load_cluster(ix, qrot, prep.lut_of(qi, p, ix.Dtot), prep.scal_of(qi, p, S), c, sm);
+                    if (prep.has(slot)) load_cluster(ix, qrot, prep.lut_of(slot, p, ix.Dtot), prep.scal_of(slot, p, S), c, sm);
                     else prepare_cluster(ix, qrot, prune, c, sm);
                     prepared = true;
                 }
@@ -2167,11 +2170,12 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_spec(DevInd
     const int total = st.q_tile_off[nl];
     // chunks of consecutive tiles (mostly of one cluster: one LUT) taken from a
     // shared counter: tiles differ widely in cost (candidates, pruning stages),
-    // so equal shares per CTA leave a long tail.  With prepared LUTs a cluster
-    // switch is a copy, and chunks are short.
+    // so equal shares per CTA leave a long tail.  When every listed query has
+    // prepared LUTs a cluster switch is a copy, and chunks are short.
     // at least about four chunks per CTA, so that a small level (few queries)
     // still spreads over the whole grid
-    const int ct = max(1, min(prep.lut ? kSpecChunkPrepared : kSpecChunk, total / (4 * (int)gridDim.x)));
+    const bool all_prepared = prep.lut && prep.slots >= nl;
+    const int ct = max(1, min(all_prepared ? kSpecChunkPrepared : kSpecChunk, total / (4 * (int)gridDim.x)));
     __shared__ int chunk;
     int last_slot = -1, last_c = -1;
     for (;;) {
@@ -2199,8 +2203,8 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan_spec(DevInd
             const int p = plo, tile = local - to[p];
             const int c = (int)probe[(size_t)q * nprobe + p];
             if (slot != last_slot || c != last_c) {  // LUTs survive across tiles of one cluster
-                if (prep.lut) load_cluster(ix, qrot_all + (size_t)q * ix.Dtot, prep.lut_of(q, p, ix.Dtot),
-                                           prep.scal_of(q, p, S), c, sm);
+                if (prep.has(slot)) load_cluster(ix, qrot_all + (size_t)q * ix.Dtot, prep.lut_of(slot, p, ix.Dtot),
+                                                 prep.scal_of(slot, p, S), c, sm);
                 else prepare_cluster(ix, qrot_all + (size_t)q * ix.Dtot, prune_all + (size_t)q * S, c, sm);
                 last_slot = slot;
                 last_c = c;
@@ -2535,7 +2539,7 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan(DevIndexVie
                                                        uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
                                                        unsigned long long *__restrict__ counters, int xstride,
                                                        const uint8_t *__restrict__ deferred,
-                                                       const int *__restrict__ order, Prepared prep) {
+                                                       const int *__restrict__ order) {
     extern __shared__ __align__(16) char smem_raw[];
     const int qi = order ? order[blockIdx.x] : (int)blockIdx.x;
     if (deferred && deferred[qi]) return;  // answered by the split pass
@@ -2546,8 +2550,7 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan(DevIndexVie
     ScanTally tl;
     init_pool(sm, topk, pool_size, distk);
     scan_probes(ix, probe + (size_t)qi * qsh.np_max, 0, np, qrot_all + (size_t)qi * ix.Dtot,
-                prune_all + (size_t)qi * ix.S, topk, sm, pool_size, distk, tl,
-                prep.lut ? prep.lut_of(qi, 0, ix.Dtot) : nullptr, prep.lut ? prep.scal_of(qi, 0, ix.S) : nullptr);
+                prune_all + (size_t)qi * ix.S, topk, sm, pool_size, distk, tl, nullptr, nullptr);
     flush_tally(tl, counters);
     write_results(sm, pool_size, topk, qsh.k_max, out_ids + (size_t)qi * qsh.k_max,
                   out_d ? out_d + (size_t)qi * qsh.k_max : nullptr);
@@ -2782,17 +2785,20 @@ struct Bump {
     }
 };
 
-// Bytes of the batched preparation's output for nq x nprobe pairs (0 when it
-// would pass kPrepCap: the scans then build each cluster's state themselves).
-constexpr size_t kPrepCap = (size_t)2 << 30;
-// Calls of fewer queries build each cluster's state in the scan CTAs (256
-// threads per LUT), which is the shorter latency for a single query.
+// List entries of the split pass that get the batched preparation: as many as
+// kPrepCap holds (nprobe pairs each), at most nq; 0 below kPrepMinQueries
+// queries, where the scan CTAs build each cluster's state in the shorter latency
+// (256 threads per LUT).
+constexpr size_t kPrepCap = (size_t)4 << 30;
 constexpr int64_t kPrepMinQueries = 64;
-size_t prep_bytes(const Index &I, int64_t nq, int64_t nprobe) {
+size_t prep_pair_bytes(const Index &I) { return 8 * (size_t)I.view.Dtot + sizeof(SegScal) * I.view.S; }
+int64_t prep_slots(const Index &I, int64_t nq, int64_t nprobe) {
     if (nq < kPrepMinQueries) return 0;
-    const size_t pairs = (size_t)nq * nprobe;
-    const size_t b = align16(pairs * 8 * (size_t)I.view.Dtot) + align16(pairs * sizeof(SegScal) * I.view.S);
-    return b <= kPrepCap ? b : 0;
+    return std::min<int64_t>(nq, (int64_t)(kPrepCap / (prep_pair_bytes(I) * (size_t)nprobe)));
+}
+size_t prep_bytes(const Index &I, int64_t nq, int64_t nprobe) {
+    const size_t pairs = (size_t)prep_slots(I, nq, nprobe) * nprobe;
+    return pairs ? align16(pairs * 8 * (size_t)I.view.Dtot) + align16(pairs * sizeof(SegScal) * I.view.S) : 0;
 }
 
 size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t nprobe, bool host_io) {
@@ -2920,8 +2926,7 @@ void ensure_smem(const void *fn, size_t bytes) {
 // its warp-specialised form k_scan_ws, which gives the same answers.
 void launch_cta_scan(bool ws, const DevIndexView &ix, const uint32_t *probe, const QueryShape &qsh, const float *qrot,
                      const float *prune, uint32_t *ids, float *d, unsigned long long *cnt, int xs,
-                     const uint8_t *deferred, int64_t nq, int *order, const int *qblocks, const Prepared &prep,
-                     cudaStream_t st) {
+                     const uint8_t *deferred, int64_t nq, int *order, const int *qblocks, cudaStream_t st) {
     if (order) {
         k_order<<<1, kOrderThreads, 0, st>>>(ix, probe, qsh, (int)nq, qblocks, order);
         check_launch("k_order");
@@ -2938,8 +2943,7 @@ void launch_cta_scan(bool ws, const DevIndexView &ix, const uint32_t *probe, con
     const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, qsh.k_max, xs);
     SAQG_REQUIRE(smem <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
     ensure_smem((const void *)k_scan, smem);
-    k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, qsh, qrot, prune, ids, d, cnt, xs, deferred, order,
-                                                      prep);
+    k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, qsh, qrot, prune, ids, d, cnt, xs, deferred, order);
     check_launch("k_scan");
 }
 
@@ -3145,9 +3149,9 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
     float *od = bp.take<float>((size_t)nq * topk);
     int *flags = bp.take<int>(16);
     unsigned long long *counters = bp.take<unsigned long long>(8);
-    const size_t pb = prep_bytes(I, nq, nprobe);
-    uint16_t *prep_lut = pb ? bp.take<uint16_t>((size_t)nq * nprobe * 4 * ix.Dtot) : nullptr;
-    SegScal *prep_scal = pb ? bp.take<SegScal>((size_t)nq * nprobe * ix.S) : nullptr;
+    const int64_t pslots = prep_slots(I, nq, nprobe);
+    uint16_t *prep_lut = pslots ? bp.take<uint16_t>((size_t)pslots * nprobe * 4 * ix.Dtot) : nullptr;
+    SegScal *prep_scal = pslots ? bp.take<SegScal>((size_t)pslots * nprobe * ix.S) : nullptr;
     cudaEvent_t ev[7] = {};
     bool shortlist = false;  // centroid ranking by the GEMM shortlist
     if (stats)
@@ -3242,7 +3246,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             // no query of this call can probe more blocks than the deferral
             // threshold: the CTA scan answers every query, no split pass
             launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, nullptr, nq, order,
-                            nullptr, Prepared{}, st);
+                            nullptr, st);
             count_launch(4);
         } else {
             // split-pass state: every query (mode 1), or the deferred giant-cluster queries (mode 0)
@@ -3300,7 +3304,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                     SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, C.fork_event(), 0));
                 }
                 launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, deferred, nq,
-                                order, qblocks, Prepared{}, st);
+                                order, qblocks, st);
             }
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
             const size_t smem_r = smem + 2 * 4 * (size_t)kReplayRecs * ss.rec_words;
@@ -3313,14 +3317,15 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                 const size_t lsm = 4 * (size_t)kLutWarps * ix.Dtot;
                 SAQG_REQUIRE(lsm <= 200 * 1024, "dimension too large for the batched LUT preparation");
                 ensure_smem((const void *)k_lut, lsm);
-                const int64_t items = cap * nprobe;
+                const int64_t items = pslots * nprobe;
                 k_lut<<<(unsigned)((items + kLutWarps - 1) / kLutWarps), kLutWarps * 32, lsm, sp>>>(
-                    ix, probe, qsh, ss.qlist, ss.nlist, ss.cap, qrot, prune, prep_lut, prep_scal);
+                    ix, probe, qsh, ss.qlist, ss.nlist, (int)pslots, qrot, prune, prep_lut, prep_scal);
                 check_launch("k_lut");
                 count_launch(1);
                 prep.lut = prep_lut;
                 prep.scal = prep_scal;
                 prep.np_max = (int)nprobe;
+                prep.slots = (int)pslots;
             }
             // the list holds at most cap slots; the per-slot kernels loop over them
             const unsigned slot_grid = (unsigned)std::min<int64_t>(cap, 4 * (int64_t)sm_count());
@@ -3598,7 +3603,7 @@ void run_search_static(const Index &I, const float *q, int64_t nq, int64_t topk,
     qsh.np_max = (int)nprobe;
     qsh.k_max = (int)topk;
     k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, qsh, qrot, prune, ids, dists, nullptr,
-                                                      xstride_of(ix), nullptr, nullptr, Prepared{});
+                                                      xstride_of(ix), nullptr, nullptr);
     check_launch("k_scan");
     count_launch(4);
 }
