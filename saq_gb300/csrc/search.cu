@@ -2594,37 +2594,33 @@ __global__ void __launch_bounds__(kOrderThreads) k_order(DevIndexView ix, const 
     for (int qi = tid; qi < nq; qi += kOrderThreads) order[atomicAdd(&cur[cls(qi)], 1)] = qi;
 }
 
-// Blocks of each query's probes (the deferral's weights and the CTA scan's
-// launch order), one thread per query.
-__global__ void k_qblocks(DevIndexView ix, const uint32_t *__restrict__ probe, QueryShape qsh, int nq,
-                          int *__restrict__ qblocks) {
-    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (qi >= nq) return;
-    int64_t total = 0;
-    const int np = qsh.np_of(qi);
-    for (int p = 0; p < np; ++p) {
-        const int c = (int)probe[(size_t)qi * qsh.np_max + p];
-        total += ix.blk_off[c + 1] - ix.blk_off[c];
-    }
-    qblocks[qi] = total < (int64_t)INT_MAX ? (int)total : INT_MAX;
-}
-
 // Puts the queries whose probes hold more than `defer_blocks` blocks (giant Zipf
 // clusters; every query when defer_blocks < 0) on the split list, each with
 // record positions for all its blocks, heaviest first while the record space
 // lasts: queries in power-of-two classes of their blocks, heavy classes first,
 // in query order inside a class.  What does not fit is left to the CTA scan,
-// which then holds the lighter queries.  One CTA of kDeferThreads; thread t owns
-// the queries [t * per, (t + 1) * per).
+// which then holds the lighter queries.  Also writes every query's block count
+// (qblocks: the CTA scan's launch order).  One CTA of up to kDeferThreads (a
+// multiple of 32); thread t owns the queries [t * per, (t + 1) * per).
 constexpr int kDeferThreads = 1024;
-__global__ void __launch_bounds__(kDeferThreads) k_defer(int nq, int defer_blocks, SplitState st,
-                                                         const int *__restrict__ qblocks, uint8_t *__restrict__ deferred) {
+__global__ void __launch_bounds__(kDeferThreads) k_defer(DevIndexView ix, const uint32_t *__restrict__ probe, int nq,
+                                                         int defer_blocks, SplitState st, int *__restrict__ qblocks,
+                                                         uint8_t *__restrict__ deferred) {
     __shared__ long long wsum_b[kDeferThreads / 32];
     __shared__ int wsum_n[kDeferThreads / 32], hist[32];
     __shared__ long long s_base;  // record positions handed out
     __shared__ int s_slot;        // list entries handed out
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int per = (nq + kDeferThreads - 1) / kDeferThreads, q0 = min(nq, tid * per), q1 = min(nq, q0 + per);
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nt = blockDim.x, nw = nt >> 5;
+    const int per = (nq + nt - 1) / nt, q0 = min(nq, tid * per), q1 = min(nq, q0 + per);
+    for (int qi = q0; qi < q1; ++qi) {
+        int64_t total = 0;
+        const int np = st.qsh.np_of(qi);
+        for (int p = 0; p < np; ++p) {
+            const int c = (int)probe[(size_t)qi * st.qsh.np_max + p];
+            total += ix.blk_off[c + 1] - ix.blk_off[c];
+        }
+        qblocks[qi] = total < (int64_t)INT_MAX ? (int)total : INT_MAX;  // read back by this thread only
+    }
     auto eligible = [&](int qi) {
         return defer_blocks < 0 || (defer_blocks > 0 && qblocks[qi] > defer_blocks);
     };
@@ -2668,7 +2664,7 @@ __global__ void __launch_bounds__(kDeferThreads) k_defer(int nq, int defer_block
         __syncthreads();
         long long before_b = xb - mine;
         int before_n = xn - cnt;
-        for (int i = 0; i < w; ++i) {
+        for (int i = 0; i < w; ++i) {  // the warps before this one
             before_b += wsum_b[i];
             before_n += wsum_n[i];
         }
@@ -2706,7 +2702,7 @@ __global__ void __launch_bounds__(kDeferThreads) k_defer(int nq, int defer_block
         }
         __syncthreads();
         if (tid == 0) {
-            for (int i = 0; i < kDeferThreads / 32; ++i) {
+            for (int i = 0; i < nw; ++i) {
                 s_base += wsum_b[i];
                 s_slot += wsum_n[i];
             }
@@ -3290,9 +3286,8 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             SAQG_CUDA_TRY(cudaMemsetAsync(ss.nlist, 0, 32, st));
             int defer = -1;  // mode 1: every query
             if (mode == 0) defer = defer_threshold(tune);
-            k_qblocks<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(ix, probe, qsh, (int)nq, qblocks);
-            check_launch("k_qblocks");
-            k_defer<<<1, kDeferThreads, 0, st>>>((int)nq, defer, ss, qblocks, deferred);
+            const int dthreads = (int)std::min<int64_t>(kDeferThreads, (nq + 31) / 32 * 32);
+            k_defer<<<1, dthreads, 0, st>>>(ix, probe, (int)nq, defer, ss, qblocks, deferred);
             check_launch("k_defer");
             cudaStream_t sp = st;  // stream of the split pass
             // the CTA scan serves what the split list does not hold: always in mode 0,
