@@ -2845,7 +2845,10 @@ size_t split_scratch_bytes(const Index &I, int64_t cap, int64_t topk, int64_t np
 // (`want`), bounded by scratch memory.
 int64_t split_positions(const Index &I, int64_t want) {
     const size_t per = 4 * (size_t)rec_words_of(I.view.S) + 16;
-    const int64_t by_mem = (int64_t)(((size_t)8 << 30) / per);
+    size_t budget = (size_t)8 << 30;
+    if (const char *e = std::getenv("SAQG_SPLIT_RECORD_BYTES"))  // tests: a small budget forces the overflow path
+        budget = std::max<size_t>(per, (size_t)std::atoll(e));
+    const int64_t by_mem = (int64_t)(budget / per);
     return std::max<int64_t>(1, std::min(want, by_mem));
 }
 

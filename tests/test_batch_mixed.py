@@ -70,3 +70,34 @@ def test_large_batch_heaviest_first(built, mode, defer, monkeypatch):
         oids, od = oi.search(qq[i:i + 1], 10, int(nps[i]), with_dists=True)
         assert np.array_equal(ids[i], oids[0]), i
         assert np.array_equal(d[i].view(np.uint32), od[0].view(np.uint32)), i
+
+
+@pytest.mark.parametrize("mode,defer", [(None, None), ("seq", "1"), ("split", None)])
+@pytest.mark.parametrize("budget_positions", [1, 300, 3000])
+def test_record_space_exhausted(built, mode, defer, budget_positions, monkeypatch):
+    """The split pass's record space holds only some of the queries it would take:
+    the heaviest go first, the rest are answered by the CTA scan; every answer must
+    still be the oracle's (uniform and uneven shapes)."""
+    index, oi, q = built
+    if mode:
+        monkeypatch.setenv("SAQG_SCAN_MODE", mode)
+    if defer:
+        monkeypatch.setenv("SAQG_DEFER_BLOCKS", defer)
+    # bytes per record position for the index's segments: 4 x the record words + the summary
+    S = len(index.info()["plan"])
+    words = (8 + (S + 1) + 32 + 32 * S + 3) & ~3
+    monkeypatch.setenv("SAQG_SPLIT_RECORD_BYTES", str(budget_positions * (4 * words + 16)))
+    rng = np.random.default_rng(budget_positions)
+    nq = 90
+    qq = q[:nq]
+    ids, d = index.search(qq, 10, 20, return_dists=True)
+    oids, od = oi.search(qq, 10, 20, with_dists=True)
+    assert np.array_equal(ids, oids)
+    assert np.array_equal(d.view(np.uint32), od.view(np.uint32))
+    nps = rng.integers(4, 41, size=nq).astype(np.int32)
+    ks = rng.choice([10, 100], size=nq).astype(np.int32)
+    ids, d = index.search(qq, ks, nps, return_dists=True)
+    for i in range(nq):
+        oids, od = oi.search(qq[i:i + 1], int(ks[i]), int(nps[i]), with_dists=True)
+        assert np.array_equal(ids[i, :ks[i]], oids[0]), i
+        assert np.array_equal(d[i, :ks[i]].view(np.uint32), od[0].view(np.uint32)), i
