@@ -88,7 +88,7 @@ TuneReport autotune_exact(const Index &I, const float *q, int64_t nq, int64_t to
     std::vector<ScanTune> cands;
     ScanTune dflt;  // built-in
     cands.push_back(dflt);
-    for (int defer : {256, 1024, 4096})
+    for (int defer : {256, 512, 1024, 2048, 4096})
         for (int first : {16, 64}) cands.push_back(ScanTune{0, defer, first, -1});
     for (int lv = 1; lv < 5; ++lv) cands.push_back(ScanTune{0, 1024, 16, lv});  // the speculation level sets
     for (int defer : {-1, 4096}) cands.push_back(ScanTune{3, defer, -1, -1});  // warp-specialised CTA scan
