@@ -1076,8 +1076,8 @@ __global__ void __launch_bounds__(kLutWarps * 32) k_lut(DevIndexView ix, const u
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t w = (int64_t)blockIdx.x * kLutWarps + warp;
     const int slot = (int)(w / qsh.np_max), p = (int)(w - (int64_t)slot * qsh.np_max);
-    if (slot >= min(*nlist, cap)) return;  // whole warp
-    const int qi = qlist[slot];
+    if (slot >= (qlist ? min(*nlist, cap) : cap)) return;  // whole warp
+    const int qi = qlist ? qlist[slot] : slot;  // no list: every query, entry = query
     if (p >= qsh.np_of(qi)) return;
     const int64_t pair = (int64_t)slot * qsh.np_max + p;
     const int c = (int)probe[(size_t)qi * qsh.np_max + p];
@@ -2539,7 +2539,7 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan(DevIndexVie
                                                        uint32_t *__restrict__ out_ids, float *__restrict__ out_d,
                                                        unsigned long long *__restrict__ counters, int xstride,
                                                        const uint8_t *__restrict__ deferred,
-                                                       const int *__restrict__ order) {
+                                                       const int *__restrict__ order, Prepared prep) {
     extern __shared__ __align__(16) char smem_raw[];
     const int qi = order ? order[blockIdx.x] : (int)blockIdx.x;
     if (deferred && deferred[qi]) return;  // answered by the split pass
@@ -2550,7 +2550,8 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan(DevIndexVie
     ScanTally tl;
     init_pool(sm, topk, pool_size, distk);
     scan_probes(ix, probe + (size_t)qi * qsh.np_max, 0, np, qrot_all + (size_t)qi * ix.Dtot,
-                prune_all + (size_t)qi * ix.S, topk, sm, pool_size, distk, tl, nullptr, nullptr);
+                prune_all + (size_t)qi * ix.S, topk, sm, pool_size, distk, tl,
+                prep.has(qi) ? prep.lut_of(qi, 0, ix.Dtot) : nullptr, prep.has(qi) ? prep.scal_of(qi, 0, ix.S) : nullptr);
     flush_tally(tl, counters);
     write_results(sm, pool_size, topk, qsh.k_max, out_ids + (size_t)qi * qsh.k_max,
                   out_d ? out_d + (size_t)qi * qsh.k_max : nullptr);
@@ -2814,7 +2815,8 @@ size_t search_scratch_bytes(const Index &I, int64_t nq, int64_t topk, int64_t np
     add(4 * (size_t)nq * 2);                   // per-query nprobe / k
     add(64);                                   // flags
     add(64);                                   // counters
-    add(prep_bytes(I, nq, nprobe));            // prepared LUTs
+    add(prep_bytes(I, nq, nprobe));            // prepared LUTs of the split list
+    if (prep_slots(I, nq, nprobe) == nq) add(prep_bytes(I, nq, nprobe));  // ... and of the CTA scan's queries
     (void)host_io;
     return b + 256;
 }
@@ -2925,7 +2927,8 @@ void ensure_smem(const void *fn, size_t bytes) {
 // its warp-specialised form k_scan_ws, which gives the same answers.
 void launch_cta_scan(bool ws, const DevIndexView &ix, const uint32_t *probe, const QueryShape &qsh, const float *qrot,
                      const float *prune, uint32_t *ids, float *d, unsigned long long *cnt, int xs,
-                     const uint8_t *deferred, int64_t nq, int *order, const int *qblocks, cudaStream_t st) {
+                     const uint8_t *deferred, int64_t nq, int *order, const int *qblocks, const Prepared &prep,
+                     cudaStream_t st) {
     if (order) {
         k_order<<<1, kOrderThreads, 0, st>>>(ix, probe, qsh, (int)nq, qblocks, order);
         check_launch("k_order");
@@ -2942,7 +2945,8 @@ void launch_cta_scan(bool ws, const DevIndexView &ix, const uint32_t *probe, con
     const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, qsh.k_max, xs);
     SAQG_REQUIRE(smem <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
     ensure_smem((const void *)k_scan, smem);
-    k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, qsh, qrot, prune, ids, d, cnt, xs, deferred, order);
+    k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, qsh, qrot, prune, ids, d, cnt, xs, deferred, order,
+                                                      prep);
     check_launch("k_scan");
 }
 
@@ -3151,6 +3155,9 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
     const int64_t pslots = prep_slots(I, nq, nprobe);
     uint16_t *prep_lut = pslots ? bp.take<uint16_t>((size_t)pslots * nprobe * 4 * ix.Dtot) : nullptr;
     SegScal *prep_scal = pslots ? bp.take<SegScal>((size_t)pslots * nprobe * ix.S) : nullptr;
+    const bool scan_prep_fits = pslots > 0 && pslots == nq;
+    uint16_t *scan_lut = scan_prep_fits ? bp.take<uint16_t>((size_t)nq * nprobe * 4 * ix.Dtot) : nullptr;
+    SegScal *scan_scal = scan_prep_fits ? bp.take<SegScal>((size_t)nq * nprobe * ix.S) : nullptr;
     cudaEvent_t ev[7] = {};
     bool shortlist = false;  // centroid ranking by the GEMM shortlist
     if (stats)
@@ -3232,6 +3239,27 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         unsigned long long *cnt = stats ? counters : nullptr;
         const int mode0 = scan_mode(nq, topk, tune);
         const int mode = (qsh.np || qsh.k) && mode0 == 2 ? 0 : mode0;
+        // The CTA scan's queries get batched LUTs too (by query; on the caller's stream,
+        // after the split pass has forked, so it overlaps the split pass's start) when
+        // the budget holds every query's: one batched kernel builds them for less than
+        // the scan CTAs do (10M / 4,096 queries: 3.70 against 3.81 ms per batch).
+        auto scan_prep = [&]() {
+            Prepared pp;
+            if (!scan_lut || scan_ws(tune)) return pp;
+            const size_t lsm = 4 * (size_t)kLutWarps * ix.Dtot;
+            SAQG_REQUIRE(lsm <= 200 * 1024, "dimension too large for the batched LUT preparation");
+            ensure_smem((const void *)k_lut, lsm);
+            const int64_t items = nq * nprobe;
+            k_lut<<<(unsigned)((items + kLutWarps - 1) / kLutWarps), kLutWarps * 32, lsm, st>>>(
+                ix, probe, qsh, nullptr, nullptr, (int)nq, qrot, prune, scan_lut, scan_scal);
+            check_launch("k_lut");
+            count_launch(1);
+            pp.lut = scan_lut;
+            pp.scal = scan_scal;
+            pp.np_max = (int)nprobe;
+            pp.slots = (int)nq;
+            return pp;
+        };
 
         if (mode == 2) {
             const size_t per_warp = align16(warp_smem_bytes(ix.Dtot, ix.S, (int)topk));
@@ -3245,7 +3273,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             // no query of this call can probe more blocks than the deferral
             // threshold: the CTA scan answers every query, no split pass
             launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, nullptr, nq, order,
-                            nullptr, st);
+                            nullptr, scan_prep(), st);
             count_launch(4);
         } else {
             // split-pass state: every query (mode 1), or the deferred giant-cluster queries (mode 0)
@@ -3302,7 +3330,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                     SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, C.fork_event(), 0));
                 }
                 launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, deferred, nq,
-                                order, qblocks, st);
+                                order, qblocks, scan_prep(), st);
             }
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
             const size_t smem_r = smem + 2 * 4 * (size_t)kReplayRecs * ss.rec_words;
@@ -3601,7 +3629,7 @@ void run_search_static(const Index &I, const float *q, int64_t nq, int64_t topk,
     qsh.np_max = (int)nprobe;
     qsh.k_max = (int)topk;
     k_scan<<<(unsigned)nq, kScanThreads, smem_k, st>>>(ix, probe, qsh, qrot, prune, ids, dists, nullptr,
-                                                      xstride_of(ix), nullptr, nullptr);
+                                                      xstride_of(ix), nullptr, nullptr, Prepared{});
     check_launch("k_scan");
     count_launch(4);
 }
