@@ -141,6 +141,9 @@ SearchCtx::~SearchCtx() {
     if (scratch) cudaFree(scratch);
     if (split_scratch) cudaFree(split_scratch);
     if (aux) cudaStreamDestroy(aux);
+    if (low) cudaStreamDestroy(low);
+    if (ev_qfork) cudaEventDestroy(ev_qfork);
+    if (ev_qjoin) cudaEventDestroy(ev_qjoin);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
 }
@@ -186,6 +189,24 @@ cudaStream_t SearchCtx::aux_stream() {
         SAQG_CUDA_TRY(cudaStreamCreateWithPriority(&aux, cudaStreamNonBlocking, greatest));
     }
     return aux;
+}
+// The query preparation runs beside the centroid ranking and is needed only by
+// the scan: the device's lowest priority lets the ranking's CTAs go first.
+cudaStream_t SearchCtx::low_stream() {
+    if (!low) {
+        int least = 0, greatest = 0;
+        SAQG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        SAQG_CUDA_TRY(cudaStreamCreateWithPriority(&low, cudaStreamNonBlocking, least));
+    }
+    return low;
+}
+cudaEvent_t SearchCtx::qfork_event() {
+    if (!ev_qfork) SAQG_CUDA_TRY(cudaEventCreateWithFlags(&ev_qfork, cudaEventDisableTiming));
+    return ev_qfork;
+}
+cudaEvent_t SearchCtx::qjoin_event() {
+    if (!ev_qjoin) SAQG_CUDA_TRY(cudaEventCreateWithFlags(&ev_qjoin, cudaEventDisableTiming));
+    return ev_qjoin;
 }
 cudaEvent_t SearchCtx::fork_event() {
     if (!ev_fork) SAQG_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));

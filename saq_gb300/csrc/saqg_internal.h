@@ -89,6 +89,10 @@ struct SearchCtx {
     size_t split_scratch_bytes = 0;
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // the query preparation's stream (lowest priority: it has slack beside the
+    // centroid ranking) with its own fork / join events
+    cudaStream_t low = nullptr;
+    cudaEvent_t ev_qfork = nullptr, ev_qjoin = nullptr;
     // pooled contexts: the stream of the last call and an event recorded at its
     // end, so a call on another stream waits for that work before reusing the arenas
     cudaStream_t last_stream = nullptr;
@@ -103,6 +107,9 @@ struct SearchCtx {
     cudaStream_t aux_stream();
     cudaEvent_t fork_event();
     cudaEvent_t join_event();
+    cudaStream_t low_stream();
+    cudaEvent_t qfork_event();
+    cudaEvent_t qjoin_event();
     size_t held_bytes() const { return scratch_bytes + split_scratch_bytes; }
 };
 

@@ -1069,6 +1069,7 @@ constexpr int kLutWarps = 8;
 __global__ void __launch_bounds__(kLutWarps * 32) k_lut(DevIndexView ix, const uint32_t *__restrict__ probe,
                                                         QueryShape qsh, const int *__restrict__ qlist,
                                                         const int *__restrict__ nlist, int cap,
+                                                        const uint8_t *__restrict__ skip,
                                                         const float *__restrict__ qrot_all,
                                                         const float *__restrict__ prune_all, uint16_t *__restrict__ lut,
                                                         SegScal *__restrict__ scal) {
@@ -1078,7 +1079,7 @@ __global__ void __launch_bounds__(kLutWarps * 32) k_lut(DevIndexView ix, const u
     const int slot = (int)(w / qsh.np_max), p = (int)(w - (int64_t)slot * qsh.np_max);
     if (slot >= (qlist ? min(*nlist, cap) : cap)) return;  // whole warp
     const int qi = qlist ? qlist[slot] : slot;  // no list: every query, entry = query
-    if (p >= qsh.np_of(qi)) return;
+    if (p >= qsh.np_of(qi) || (skip && skip[qi])) return;
     const int64_t pair = (int64_t)slot * qsh.np_max + p;
     const int c = (int)probe[(size_t)qi * qsh.np_max + p];
     if (ix.blk_off[c + 1] == ix.blk_off[c]) return;
@@ -1091,12 +1092,15 @@ __global__ void __launch_bounds__(kLutWarps * 32) k_lut(DevIndexView ix, const u
     }
     __syncwarp();
     uint16_t *L = lut + pair * 4 * ix.Dtot;
+    // segment s's sums and LUT min / max keys end in lane s, so the scalar steps
+    // (FP64) of all segments run at once, one lane each
+    SegScal sc;
+    uint32_t my_min = 0xffffffffu, my_max = 0u;
     for (int s = 0; s < ix.S; ++s) {
         const SegDev &g = ix.seg[s];
         const float *qr = qres + g.qoff;
-        SegScal sc;
-        sc.sum_q = warp_eigen_sum(g.dim, [&](int i) { return qr[i]; });
-        sc.q_l2sqr = warp_eigen_sum(g.dim, [&](int i) { return __fmul_rn(qr[i], qr[i]); });
+        const float sq = warp_eigen_sum(g.dim, [&](int i) { return qr[i]; });
+        const float l2 = warp_eigen_sum(g.dim, [&](int i) { return __fmul_rn(qr[i], qr[i]); });
         const int cb0 = g.qoff / 4, ncb = g.dim / 4;
         uint32_t kmin = 0xffffffffu, kmax = 0u;
         for (int k = lane; k < ncb; k += 32) {
@@ -1107,15 +1111,24 @@ __global__ void __launch_bounds__(kLutWarps * 32) k_lut(DevIndexView ix, const u
         }
         kmin = __reduce_min_sync(kFull, kmin);
         kmax = __reduce_max_sync(kFull, kmax);
-        if (lane == 0) seg_quant_scalars(kmin, kmax, sc);
-        sc.vl = __shfl_sync(kFull, sc.vl, 0);
-        sc.delta = __shfl_sync(kFull, sc.delta, 0);
-        sc.rdelta = __shfl_sync(kFull, sc.rdelta, 0);
-        for (int k = lane; k < ncb; k += 32) quant_codebook(qres + (cb0 + k) * 4, sc.vl, sc.delta, sc.rdelta, L + (cb0 + k) * 16);
-        if (lane == 0) {
-            seg_epilogue_scalars(g, prune_all[(size_t)qi * ix.S + s], sc);
-            scal[pair * ix.S + s] = sc;
+        if (lane == s) {
+            sc.sum_q = sq;
+            sc.q_l2sqr = l2;
+            my_min = kmin;
+            my_max = kmax;
         }
+    }
+    if (lane < ix.S) seg_quant_scalars(my_min, my_max, sc);
+    for (int s = 0; s < ix.S; ++s) {
+        const SegDev &g = ix.seg[s];
+        const float vl = __shfl_sync(kFull, sc.vl, s), delta = __shfl_sync(kFull, sc.delta, s),
+                    rd = __shfl_sync(kFull, sc.rdelta, s);
+        const int cb0 = g.qoff / 4, ncb = g.dim / 4;
+        for (int k = lane; k < ncb; k += 32) quant_codebook(qres + (cb0 + k) * 4, vl, delta, rd, L + (cb0 + k) * 16);
+    }
+    if (lane < ix.S) {
+        seg_epilogue_scalars(ix.seg[lane], prune_all[(size_t)qi * ix.S + lane], sc);
+        scal[pair * ix.S + lane] = sc;
     }
 }
 
@@ -2600,28 +2613,47 @@ __global__ void __launch_bounds__(kOrderThreads) k_order(DevIndexView ix, const 
 // record positions for all its blocks, heaviest first while the record space
 // lasts: queries in power-of-two classes of their blocks, heavy classes first,
 // in query order inside a class.  What does not fit is left to the CTA scan,
-// which then holds the lighter queries.  Also writes every query's block count
-// (qblocks: the CTA scan's launch order).  One CTA of up to kDeferThreads (a
-// multiple of 32); thread t owns the queries [t * per, (t + 1) * per).
+// which then holds the lighter queries.  Writes every query's block count
+// (qblocks: the CTA scan's launch order) unless k_qblocks has (have_qblocks).
+// One CTA of up to kDeferThreads (a multiple of 32); thread t owns the queries
+// [t * per, (t + 1) * per).
 constexpr int kDeferThreads = 1024;
+constexpr int kQblocksMinQueries = 256;  // from this batch size the block counts come from k_qblocks
+
+// Blocks of each query's probes, one thread per query (k_defer's input for
+// large batches, where its single CTA would sum them serially).
+__global__ void k_qblocks(DevIndexView ix, const uint32_t *__restrict__ probe, QueryShape qsh, int nq,
+                          int *__restrict__ qblocks) {
+    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= nq) return;
+    int64_t total = 0;
+    const int np = qsh.np_of(qi);
+    for (int p = 0; p < np; ++p) {
+        const int c = (int)probe[(size_t)qi * qsh.np_max + p];
+        total += ix.blk_off[c + 1] - ix.blk_off[c];
+    }
+    qblocks[qi] = total < (int64_t)INT_MAX ? (int)total : INT_MAX;
+}
+
 __global__ void __launch_bounds__(kDeferThreads) k_defer(DevIndexView ix, const uint32_t *__restrict__ probe, int nq,
                                                          int defer_blocks, SplitState st, int *__restrict__ qblocks,
-                                                         uint8_t *__restrict__ deferred) {
+                                                         int have_qblocks, uint8_t *__restrict__ deferred) {
     __shared__ long long wsum_b[kDeferThreads / 32];
     __shared__ int wsum_n[kDeferThreads / 32], hist[32];
     __shared__ long long s_base;  // record positions handed out
     __shared__ int s_slot;        // list entries handed out
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nt = blockDim.x, nw = nt >> 5;
     const int per = (nq + nt - 1) / nt, q0 = min(nq, tid * per), q1 = min(nq, q0 + per);
-    for (int qi = q0; qi < q1; ++qi) {
-        int64_t total = 0;
-        const int np = st.qsh.np_of(qi);
-        for (int p = 0; p < np; ++p) {
-            const int c = (int)probe[(size_t)qi * st.qsh.np_max + p];
-            total += ix.blk_off[c + 1] - ix.blk_off[c];
+    if (!have_qblocks)
+        for (int qi = q0; qi < q1; ++qi) {
+            int64_t total = 0;
+            const int np = st.qsh.np_of(qi);
+            for (int p = 0; p < np; ++p) {
+                const int c = (int)probe[(size_t)qi * st.qsh.np_max + p];
+                total += ix.blk_off[c + 1] - ix.blk_off[c];
+            }
+            qblocks[qi] = total < (int64_t)INT_MAX ? (int)total : INT_MAX;  // read back by this thread only
         }
-        qblocks[qi] = total < (int64_t)INT_MAX ? (int)total : INT_MAX;  // read back by this thread only
-    }
     auto eligible = [&](int qi) {
         return defer_blocks < 0 || (defer_blocks > 0 && qblocks[qi] > defer_blocks);
     };
@@ -3065,6 +3097,9 @@ void presize_ctx(const Index &I, SearchCtx &C, int64_t nq, int64_t topk, int64_t
     C.aux_stream();
     C.fork_event();
     C.join_event();
+    C.low_stream();
+    C.qfork_event();
+    C.qjoin_event();
 }
 
 
@@ -3181,13 +3216,13 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         dim3 grid((unsigned)((I.K + wpb - 1) / wpb), (unsigned)nq);
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[0], st));
         // query preparation (rotation, prune bounds) depends on the queries alone:
-        // it runs on the auxiliary stream beside the centroid ranking (beside the
-        // shortlist and its select when the GEMM ranks the centroids: the GEMM
-        // wants whole SMs)
+        // it runs on the context's low-priority stream beside the centroid ranking
+        // (beside the shortlist and its select when the GEMM ranks the centroids:
+        // the GEMM wants whole SMs), whose CTAs go first
         auto launch_qprep = [&]() {
-            cudaStream_t qs = C.aux_stream();
-            SAQG_CUDA_TRY(cudaEventRecord(C.fork_event(), st));
-            SAQG_CUDA_TRY(cudaStreamWaitEvent(qs, C.fork_event(), 0));
+            cudaStream_t qs = C.low_stream();
+            SAQG_CUDA_TRY(cudaEventRecord(C.qfork_event(), st));
+            SAQG_CUDA_TRY(cudaStreamWaitEvent(qs, C.qfork_event(), 0));
             size_t qsm = 0;
             for (int s = 0; s < ix.S; ++s) qsm = std::max(qsm, (size_t)4 * ix.seg[s].dim);
             if (nq >= kQprepQT && kQprepQT * qsm <= 200 * 1024) {
@@ -3204,7 +3239,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                                 256, sm_small, qs>>>(ix, qin, m, qrot, prune);
                 check_launch("k_qprep_small");
             }
-            SAQG_CUDA_TRY(cudaEventRecord(C.join_event(), qs));
+            SAQG_CUDA_TRY(cudaEventRecord(C.qjoin_event(), qs));
         };
         const char *pm = std::getenv("SAQG_PROBE");
         shortlist = nq >= kGemmMinQueries && nprobe <= kShortCap && !(pm && std::string(pm) == "exact");
@@ -3229,7 +3264,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             check_launch("k_probe_select");
         }
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[1], st));
-        SAQG_CUDA_TRY(cudaStreamWaitEvent(st, C.join_event(), 0));  // the rotated queries
+        SAQG_CUDA_TRY(cudaStreamWaitEvent(st, C.qjoin_event(), 0));  // the rotated queries
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[2], st));
         const int xs = xstride_of(ix);
         const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, (int)topk, xs);
@@ -3243,7 +3278,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         // after the split pass has forked, so it overlaps the split pass's start) when
         // the budget holds every query's: one batched kernel builds them for less than
         // the scan CTAs do (10M / 4,096 queries: 3.70 against 3.81 ms per batch).
-        auto scan_prep = [&]() {
+        auto scan_prep = [&](const uint8_t *skip) {  // skip: queries the split pass answers
             Prepared pp;
             if (!scan_lut || scan_ws(tune)) return pp;
             const size_t lsm = 4 * (size_t)kLutWarps * ix.Dtot;
@@ -3251,7 +3286,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             ensure_smem((const void *)k_lut, lsm);
             const int64_t items = nq * nprobe;
             k_lut<<<(unsigned)((items + kLutWarps - 1) / kLutWarps), kLutWarps * 32, lsm, st>>>(
-                ix, probe, qsh, nullptr, nullptr, (int)nq, qrot, prune, scan_lut, scan_scal);
+                ix, probe, qsh, nullptr, nullptr, (int)nq, skip, qrot, prune, scan_lut, scan_scal);
             check_launch("k_lut");
             count_launch(1);
             pp.lut = scan_lut;
@@ -3273,7 +3308,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             // no query of this call can probe more blocks than the deferral
             // threshold: the CTA scan answers every query, no split pass
             launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, nullptr, nq, order,
-                            nullptr, scan_prep(), st);
+                            nullptr, scan_prep(nullptr), st);
             count_launch(4);
         } else {
             // split-pass state: every query (mode 1), or the deferred giant-cluster queries (mode 0)
@@ -3318,7 +3353,12 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             int defer = -1;  // mode 1: every query
             if (mode == 0) defer = defer_threshold(tune);
             const int dthreads = (int)std::min<int64_t>(kDeferThreads, (nq + 31) / 32 * 32);
-            k_defer<<<1, dthreads, 0, st>>>(ix, probe, (int)nq, defer, ss, qblocks, deferred);
+            const bool par = nq >= kQblocksMinQueries;
+            if (par) {
+                k_qblocks<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(ix, probe, qsh, (int)nq, qblocks);
+                check_launch("k_qblocks");
+            }
+            k_defer<<<1, dthreads, 0, st>>>(ix, probe, (int)nq, defer, ss, qblocks, par ? 1 : 0, deferred);
             check_launch("k_defer");
             cudaStream_t sp = st;  // stream of the split pass
             // the CTA scan serves what the split list does not hold: always in mode 0,
@@ -3330,7 +3370,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                     SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, C.fork_event(), 0));
                 }
                 launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, deferred, nq,
-                                order, qblocks, scan_prep(), st);
+                                order, qblocks, scan_prep(deferred), st);
             }
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
             const size_t smem_r = smem + 2 * 4 * (size_t)kReplayRecs * ss.rec_words;
@@ -3345,7 +3385,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                 ensure_smem((const void *)k_lut, lsm);
                 const int64_t items = pslots * nprobe;
                 k_lut<<<(unsigned)((items + kLutWarps - 1) / kLutWarps), kLutWarps * 32, lsm, sp>>>(
-                    ix, probe, qsh, ss.qlist, ss.nlist, (int)pslots, qrot, prune, prep_lut, prep_scal);
+                    ix, probe, qsh, ss.qlist, ss.nlist, (int)pslots, nullptr, qrot, prune, prep_lut, prep_scal);
                 check_launch("k_lut");
                 count_launch(1);
                 prep.lut = prep_lut;
