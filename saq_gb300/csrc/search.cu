@@ -2572,17 +2572,20 @@ __global__ void __launch_bounds__(kScanThreads, kScanMinCtas) k_scan(DevIndexVie
 
 // Launch order of the CTA scan, heaviest queries first (blocks of their probes,
 // in power-of-two classes; the order inside a class is arbitrary), so that a
-// long query does not start in the last wave.  One CTA of kOrderThreads.
+// long query does not start in the last wave; the split pass's queries (deferred)
+// last, as their CTAs only return.  One CTA of kOrderThreads.
 constexpr int kOrderThreads = 1024;
 constexpr int kOrderMinQueries = 1024;  // batches from which the CTA scan is launched heaviest first
 __global__ void __launch_bounds__(kOrderThreads) k_order(DevIndexView ix, const uint32_t *__restrict__ probe, QueryShape qsh,
                                                          int nq, const int *__restrict__ qblocks,
+                                                         const uint8_t *__restrict__ deferred,
                                                          int *__restrict__ order) {
-    __shared__ int cnt[32], cur[32];
+    __shared__ int cnt[33], cur[33];
     const int tid = threadIdx.x;
-    if (tid < 32) cnt[tid] = 0;
+    if (tid < 33) cnt[tid] = 0;
     __syncthreads();
     auto cls = [&](int qi) {
+        if (deferred && deferred[qi]) return 32;
         int64_t total = 0;
         if (qblocks) {
             total = qblocks[qi];
@@ -2599,7 +2602,7 @@ __global__ void __launch_bounds__(kOrderThreads) k_order(DevIndexView ix, const 
     __syncthreads();
     if (tid == 0) {
         int acc = 0;
-        for (int k = 0; k < 32; ++k) {
+        for (int k = 0; k < 33; ++k) {
             cur[k] = acc;
             acc += cnt[k];
         }
@@ -2955,14 +2958,15 @@ void ensure_smem(const void *fn, size_t bytes) {
     h = bytes;
 }
 
-// The CTA-per-query scan of `nq` queries (deferred ones skipped): k_scan, or
-// its warp-specialised form k_scan_ws, which gives the same answers.
+// The CTA-per-query scan of `nq` queries (deferred ones skipped): k_scan, with
+// the batched LUTs that prep_of(deferred) launches and returns (or none), or its
+// warp-specialised form k_scan_ws, which gives the same answers.
 void launch_cta_scan(bool ws, const DevIndexView &ix, const uint32_t *probe, const QueryShape &qsh, const float *qrot,
                      const float *prune, uint32_t *ids, float *d, unsigned long long *cnt, int xs,
-                     const uint8_t *deferred, int64_t nq, int *order, const int *qblocks, const Prepared &prep,
-                     cudaStream_t st) {
+                     const uint8_t *deferred, int64_t nq, int *order, const int *qblocks,
+                     const std::function<Prepared(const uint8_t *)> &prep_of, cudaStream_t st) {
     if (order) {
-        k_order<<<1, kOrderThreads, 0, st>>>(ix, probe, qsh, (int)nq, qblocks, order);
+        k_order<<<1, kOrderThreads, 0, st>>>(ix, probe, qsh, (int)nq, qblocks, deferred, order);
         check_launch("k_order");
     }
     if (ws) {
@@ -2977,6 +2981,7 @@ void launch_cta_scan(bool ws, const DevIndexView &ix, const uint32_t *probe, con
     const size_t smem = scan_smem_bytes(ix.Dtot, ix.S, qsh.k_max, xs);
     SAQG_REQUIRE(smem <= 200 * 1024, "dimension / topk too large for the scan kernel's shared memory");
     ensure_smem((const void *)k_scan, smem);
+    const Prepared prep = prep_of(deferred);
     k_scan<<<(unsigned)nq, kScanThreads, smem, st>>>(ix, probe, qsh, qrot, prune, ids, d, cnt, xs, deferred, order,
                                                       prep);
     check_launch("k_scan");
@@ -3050,7 +3055,6 @@ void probe_shortlist(const Index &I, SearchCtx &C, const float *q, int64_t nq, i
             I.cnorm2 = p;
         }
     }
-    (void)C;
     {
         std::lock_guard<std::mutex> lk(I.init_mu);
         if (!I.cent_bf16) {
@@ -3065,7 +3069,17 @@ void probe_shortlist(const Index &I, SearchCtx &C, const float *q, int64_t nq, i
     // to nearest, FP32 accumulation); flags[3] is set if a GEMM wait timed out
     to_bf16(q, nq * I.D, qbf, st);
     probe_ip_gemm(qbf, nq, I.cent_bf16, I.K, I.D, dist, flags + 3, st);
-    if (after_gemm) after_gemm();  // work that can run beside the shortlist and its select
+    // Work that can run beside the shortlist and its select.  The caller's stream
+    // has the device's least (default) priority, like that work's, so the shortlist
+    // and the select then move to the context's greatest-priority stream: their CTAs
+    // go first and the side work fills the gaps.
+    cudaStream_t ps = st;
+    if (after_gemm) {
+        after_gemm();
+        ps = C.aux_stream();
+        SAQG_CUDA_TRY(cudaEventRecord(C.fork_event(), st));
+        SAQG_CUDA_TRY(cudaStreamWaitEvent(ps, C.fork_event(), 0));
+    }
     const double u = 1.0 / 16777216.0;
     ShortBound sb;
     // BF16 operands lie within 2^-9 of their values: |q.c error| <= (2^-8 + 2^-18) |q||c| + accumulation
@@ -3077,14 +3091,18 @@ void probe_shortlist(const Index &I, SearchCtx &C, const float *q, int64_t nq, i
     const size_t smem = 12 * (size_t)kShortCap + 4 * (size_t)I.D + (keep ? 4 * (size_t)I.K : 0);
     SAQG_REQUIRE(smem <= 220 * 1024, "dimension too large for the probe shortlist's shared memory");
     ensure_smem((const void *)k_probe_shortlist, (size_t)smem);
-    k_probe_shortlist<<<(unsigned)nq, kShortThreads, smem, st>>>(ix, q, dist, reinterpret_cast<const float2 *>(I.cnorm2),
+    k_probe_shortlist<<<(unsigned)nq, kShortThreads, smem, ps>>>(ix, q, dist, reinterpret_cast<const float2 *>(I.cnorm2),
                                                                  sb, (int)nprobe, qnp, probe, full,
                                                                  fb_list, flags + 2, cnt, flags + 3, keep ? 1 : 0);
     check_launch("k_probe_shortlist");
-    k_probe_dist_list<<<608, 256, 0, st>>>(ix, q, dist, fb_list, flags + 2);
+    k_probe_dist_list<<<608, 256, 0, ps>>>(ix, q, dist, fb_list, flags + 2);
     check_launch("k_probe_dist_list");
-    k_probe_select<<<(unsigned)nq, kSelThreads, 0, st>>>(dist, (int)I.K, (int)nprobe, probe, work, flags, full, qnp);
+    k_probe_select<<<(unsigned)nq, kSelThreads, 0, ps>>>(dist, (int)I.K, (int)nprobe, probe, work, flags, full, qnp);
     check_launch("k_probe_select");
+    if (ps != st) {
+        SAQG_CUDA_TRY(cudaEventRecord(C.join_event(), ps));
+        SAQG_CUDA_TRY(cudaStreamWaitEvent(st, C.join_event(), 0));
+    }
 }
 
 }  // namespace
@@ -3278,7 +3296,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         // after the split pass has forked, so it overlaps the split pass's start) when
         // the budget holds every query's: one batched kernel builds them for less than
         // the scan CTAs do (10M / 4,096 queries: 3.70 against 3.81 ms per batch).
-        auto scan_prep = [&](const uint8_t *skip) {  // skip: queries the split pass answers
+        const std::function<Prepared(const uint8_t *)> scan_prep = [&](const uint8_t *skip) {  // skip: queries left out
             Prepared pp;
             if (!scan_lut || scan_ws(tune)) return pp;
             const size_t lsm = 4 * (size_t)kLutWarps * ix.Dtot;
@@ -3308,7 +3326,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
             // no query of this call can probe more blocks than the deferral
             // threshold: the CTA scan answers every query, no split pass
             launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, nullptr, nq, order,
-                            nullptr, scan_prep(nullptr), st);
+                            nullptr, scan_prep, st);
             count_launch(4);
         } else {
             // split-pass state: every query (mode 1), or the deferred giant-cluster queries (mode 0)
@@ -3370,7 +3388,7 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
                     SAQG_CUDA_TRY(cudaStreamWaitEvent(sp, C.fork_event(), 0));
                 }
                 launch_cta_scan(scan_ws(tune), ix, probe, qsh, qrot, prune, ids_out, d_out, cnt, xs, deferred, nq,
-                                order, qblocks, scan_prep(deferred), st);
+                                order, qblocks, scan_prep, st);
             }
             const size_t smem1 = scan_smem_bytes(ix.Dtot, ix.S, 1, xs);
             const size_t smem_r = smem + 2 * 4 * (size_t)kReplayRecs * ss.rec_words;
