@@ -50,12 +50,13 @@ struct SegScal {
 // A u16 LUT entry (uint16_t)(int)(x / d), x >= 0, with the division rounded to
 // nearest, mostly without dividing: y = RN(x * r), r = RN(1 / d), lies within
 // 3.02 * 2^-24 * y of RN(x / d), so when no integer lies within 2^-21 * y of y
-// both truncate to the same integer.  Otherwise (and for NaN / inf) divide.
-__device__ __forceinline__ uint32_t lut_quant(float x, float r, float d) {
+// both truncate to the same integer.  Otherwise (and for NaN / inf) `ok` is
+// false and the caller divides.
+__device__ __forceinline__ uint32_t lut_quant_fast(float x, float r, bool &ok) {
     const float y = __fmul_rn(x, r);
     const float e = __fmul_rn(y, 4.76837158203125e-07f);  // 2^-21
-    if (floorf(__fsub_rn(y, e)) == floorf(__fadd_rn(y, e))) return (uint16_t)(int)y;
-    return (uint16_t)(int)__fdiv_rn(x, d);
+    ok = floorf(__fsub_rn(y, e)) == floorf(__fadd_rn(y, e));
+    return (uint16_t)(int)y;
 }
 
 __device__ __forceinline__ uint32_t fkey(float f) {
@@ -941,20 +942,42 @@ __device__ __forceinline__ void seg_epilogue_scalars(const SegDev &g, float prun
     sc.vfac = __fsub_rn(sc.q_l2sqr, __fmul_rn(2.0f, prune_s));
 }
 
+// Float entry j of one codebook in lut_entries' order: entry j = entry[j -
+// lowbit(j)] + q[kPos[lowbit(j)]], so the dims of j's bits are added from the
+// highest bit down (kPos of bit b is 3 - b).
+__device__ __forceinline__ float lut_entry_at(const float *qq, int j) {
+    float t = 0.0f;
+    for (int b = 3; b >= 0; --b)
+        if ((j >> b) & 1) t = __fadd_rn(t, qq[3 - b]);
+    return t;
+}
+
 // The 16 u16 entries of one codebook (4 residual dims at qq), 32 bytes at dst.
+// Every entry takes the multiply first; the few that it cannot settle (about 3%)
+// are divided afterwards and stored over it, in a loop whose trip count is the
+// lane's own number of such entries, so a warp runs a handful of divisions per
+// codebook instead of one per entry that any lane needs.
 __device__ __forceinline__ void quant_codebook(const float *qq, float vl, float delta, float rd, uint16_t *dst) {
     float t[16];
     lut_entries(qq, t);
     uint32_t packed[8];
+    uint32_t slow = 0;
 #pragma unroll
     for (int j = 0; j < 16; j += 2) {
-        const uint32_t a = lut_quant(__fsub_rn(t[j], vl), rd, delta);
-        const uint32_t b = lut_quant(__fsub_rn(t[j + 1], vl), rd, delta);
+        bool oa, ob;
+        const uint32_t a = lut_quant_fast(__fsub_rn(t[j], vl), rd, oa);
+        const uint32_t b = lut_quant_fast(__fsub_rn(t[j + 1], vl), rd, ob);
+        slow |= (oa ? 0u : 1u << j) | (ob ? 0u : 2u << j);
         packed[j / 2] = a | (b << 16);
     }
     uint4 *d = reinterpret_cast<uint4 *>(dst);
     d[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
     d[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+    while (slow) {  // same thread, same address: the later store wins
+        const int j = __ffs(slow) - 1;
+        slow &= slow - 1;
+        dst[j] = (uint16_t)(int)__fdiv_rn(__fsub_rn(lut_entry_at(qq, j), vl), delta);
+    }
 }
 
 // Min and max keys of one codebook's float entries.
