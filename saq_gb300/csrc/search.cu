@@ -51,12 +51,15 @@ struct SegScal {
 // nearest, mostly without dividing: y = RN(x * r), r = RN(1 / d), lies within
 // 3.02 * 2^-24 * y of RN(x / d), so when no integer lies within 2^-21 * y of y
 // both truncate to the same integer.  Otherwise (and for NaN / inf) `ok` is
-// false and the caller divides.
+// false and the caller divides.  The floors come from adding 2^23 rounded
+// down (2^23 + floor(v) for 0 <= v < 2^23, the integer in the low mantissa
+// bits), so the check and the result take FP32 adds, not conversions.
 __device__ __forceinline__ uint32_t lut_quant_fast(float x, float r, bool &ok) {
     const float y = __fmul_rn(x, r);
     const float e = __fmul_rn(y, 4.76837158203125e-07f);  // 2^-21
-    ok = floorf(__fsub_rn(y, e)) == floorf(__fadd_rn(y, e));
-    return (uint16_t)(int)y;
+    const float lo = __fadd_rd(__fsub_rn(y, e), 8388608.0f), hi = __fadd_rd(__fadd_rn(y, e), 8388608.0f);
+    ok = lo == hi && y < 4194304.0f;  // y < 2^22 keeps both sums in the binade of 2^23
+    return __float_as_uint(lo) & 0xffffu;  // (uint16_t)(int)y: y >= 0, trunc = floor
 }
 
 __device__ __forceinline__ uint32_t fkey(float f) {
