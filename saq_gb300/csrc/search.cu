@@ -880,7 +880,7 @@ __host__ __device__ inline size_t scan_smem_bytes(int Dtot, int S, int topk, int
     b += align16(sizeof(uint16_t) * 4 * (size_t)Dtot);
     b += align16(sizeof(float) * Dtot);
     b += align16(sizeof(SegScal) * S);
-    b += 3 * align16(sizeof(float) * kTileB * S * 32);  // cd, ipx, part
+    b += 2 * align16(sizeof(float) * kTileB * S * 32);  // cd (= part), ipx
     b += align16(sizeof(float) * kTileB * 32);          // cur
     b += align16(sizeof(float) * kTileB * (S + 1));     // stage minima
     b += align16(sizeof(uint32_t) * kTileB);
@@ -908,8 +908,11 @@ __device__ ScanSmem scan_smem_layout(char *base, int Dtot, int S, int topk, int 
     o += align16(sizeof(float) * kTileB * S * 32);
     s.ipx = (float *)(base + o);
     o += align16(sizeof(float) * kTileB * S * 32);
-    s.part = (float *)(base + o);
-    o += align16(sizeof(float) * kTileB * S * 32);
+    // A candidate's partial replaces its estimate in place: the accurate pass
+    // reads cd[i] and writes part[i] in the same thread, and nothing reads a
+    // candidate's estimate afterwards (the replay and the split pass's records
+    // read partials of candidate lanes only).
+    s.part = s.cd;
     s.cur = (float *)(base + o);
     o += align16(sizeof(float) * kTileB * 32);
     s.stage = (float *)(base + o);
@@ -1282,7 +1285,9 @@ __device__ void tile_candidates(const DevIndexView &ix, ScanSmem &sm, int64_t b0
         const int slot = w + k * nwarps, b = t0 + slot;
         if (b < t_end) block_estimates(ix, b0 + b, sm, slot, lane, tau);
     }
-    sync();
+    // a slot's mask reads only what the same warp's estimates wrote (its cd,
+    // cur, stage and nstage rows): a warp barrier orders them
+    __syncwarp();
 #pragma unroll
     for (int k = 0; k < kBlocksPerWarp; ++k) {
         const int slot = w + k * nwarps, b = t0 + slot;
