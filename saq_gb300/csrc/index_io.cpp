@@ -191,7 +191,8 @@ cudaStream_t SearchCtx::aux_stream() {
     return aux;
 }
 // The query preparation runs beside the centroid ranking and is needed only by
-// the scan: the device's lowest priority lets the ranking's CTAs go first.
+// the scan: it takes the device's least priority (also the default one), and
+// the ranking's shortlist and select, beside it, the greatest (aux_stream).
 cudaStream_t SearchCtx::low_stream() {
     if (!low) {
         int least = 0, greatest = 0;

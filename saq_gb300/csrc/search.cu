@@ -3265,9 +3265,10 @@ void run_search(const Index &I, const float *q, int64_t nq, int64_t topk, int64_
         dim3 grid((unsigned)((I.K + wpb - 1) / wpb), (unsigned)nq);
         if (stats) SAQG_CUDA_TRY(cudaEventRecord(ev[0], st));
         // query preparation (rotation, prune bounds) depends on the queries alone:
-        // it runs on the context's low-priority stream beside the centroid ranking
+        // it runs on the context's least-priority stream beside the centroid ranking
         // (beside the shortlist and its select when the GEMM ranks the centroids:
-        // the GEMM wants whole SMs), whose CTAs go first
+        // the GEMM wants whole SMs; those two then run at the greatest priority,
+        // so their CTAs go first)
         auto launch_qprep = [&]() {
             cudaStream_t qs = C.low_stream();
             SAQG_CUDA_TRY(cudaEventRecord(C.qfork_event(), st));
