@@ -2851,8 +2851,10 @@ struct Bump {
 // List entries of the split pass that get the batched preparation: as many as
 // kPrepCap holds (nprobe pairs each), at most nq; 0 below kPrepMinQueries
 // queries, where the scan CTAs build each cluster's state in the shorter latency
-// (256 threads per LUT).
-constexpr size_t kPrepCap = (size_t)4 << 30;
+// (256 threads per LUT).  12 GB holds every query of a 4,096-query batch at
+// nprobe 256 with D = 1024 (8.8 GB; the CTA scan's copy is as large again), a
+// few percent of the device beside the index.
+constexpr size_t kPrepCap = (size_t)12 << 30;
 constexpr int64_t kPrepMinQueries = 64;
 size_t prep_pair_bytes(const Index &I) { return 8 * (size_t)I.view.Dtot + sizeof(SegScal) * I.view.S; }
 int64_t prep_slots(const Index &I, int64_t nq, int64_t nprobe) {
