@@ -1,6 +1,6 @@
 """The u16 LUT quantiser's fast path, checked on the CPU in IEEE float32.
 
-Lut::prepare (saqlib/quantization/lut.hpp:60-87) stores trunc(RN(x / delta)) for
+Lut::prepare (saqlib/quantization/fastscan/lut.hpp:60-87) stores trunc(RN(x / delta)) for
 each float entry x - vl >= 0 of a segment's LUT, with delta = RN((vr - vl) /
 (65536 - 0.01)) taken in double.  The GPU quantiser (search.cu lut_quant_fast /
 quant_codebook) multiplies instead: y = RN(x * RN(1 / delta)), and keeps trunc(y)
